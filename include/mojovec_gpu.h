@@ -1,0 +1,207 @@
+/*
+ * mojovec_gpu.h - C ABI of libmojovec_gpu.so, the GB300 (sm_103a) hot path
+ * for MojoVec's vector-query and index-training path.
+ *
+ * Every entry point uses plain C types: float / int64_t / uint8_t pointers
+ * and sizes. Host-pointer entry points take caller-owned host buffers (numpy
+ * arrays, Mojo Lists) exactly as the reference passes Spans; "_device"
+ * entry points take device pointers and a cudaStream_t passed as void*.
+ *
+ * Status convention: every function returns int32_t, MV_OK (0) on success or
+ * a negative MV_ERR_* code; mv_last_error() returns the calling thread's last
+ * message. The reference's index-level search/add cannot raise
+ * (core/index.mojo:5-32); its collection layer raises. A Mojo shim therefore
+ * raises on a non-zero status at the collection layer.
+ *
+ * Forms:
+ *   MV_FORM_PLAIN - FP32 form that reproduces the reference CPU path: codes,
+ *                   coarse assignments and ids bit-exact, ties broken by the
+ *                   smaller id, distances equal to the FP32 reference order.
+ *   MV_FORM_FAST  - tensor-core coarse/base GEMMs (BF16, FP32 accumulate),
+ *                   per-query LUTs with per-vector precomputed terms and an
+ *                   exact FP32 rerank of a shortlist; judged on recall.
+ *
+ * Ids: the GPU index stores ids in [0, 2^32 - 2]; add rejects others with
+ * MV_ERR_ARG. The canonical result order is (distance asc, id asc).
+ */
+#ifndef MOJOVEC_GPU_H
+#define MOJOVEC_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MV_OK 0
+#define MV_ERR_ARG (-1)
+#define MV_ERR_OOM (-2)
+#define MV_ERR_CUDA (-3)
+#define MV_ERR_TIMEOUT (-4)
+#define MV_ERR_STATE (-5)
+#define MV_ERR_UNSUPPORTED (-6)
+#define MV_ERR_INTERNAL (-7)
+
+/* core/types.mojo:5-7 */
+#define MV_METRIC_L2 0
+#define MV_METRIC_IP 1
+
+#define MV_FORM_PLAIN 0
+#define MV_FORM_FAST 1
+
+typedef struct mv_ctx mv_ctx;
+typedef struct mv_ivfpq mv_ivfpq;
+typedef struct mv_flat mv_flat;
+typedef struct mv_sq8 mv_sq8;
+
+/* Search options for the IVF-PQ and Flat searches. Zero-initialised means
+ * the plain form with the index's own nprobe. */
+typedef struct mv_search_params {
+  int32_t form;        /* MV_FORM_PLAIN or MV_FORM_FAST */
+  int32_t nprobe;      /* 0 = the index's nprobe (index_ivf_pq.mojo:253) */
+  int32_t rerank;      /* fast form: shortlist depth for the exact FP32 rerank
+                          (0 = no rerank) */
+  int32_t coarse_fp32; /* fast form: 1 = FP32 SIMT coarse instead of BF16 */
+  int32_t lut_fp16;    /* fast form: 1 = FP16 lookup tables */
+  int32_t reserved[3];
+} mv_search_params;
+
+/* ---- library / context ---------------------------------------------- */
+
+/* Copies the calling thread's last error message (NUL-terminated). */
+int32_t mv_last_error(char* buf, size_t len);
+/* Library version string, e.g. "mojovec-gb300 0.1 sm_103a". */
+const char* mv_version(void);
+/* Creates a context bound to one CUDA device. */
+int32_t mv_ctx_create(int32_t device, mv_ctx** out);
+int32_t mv_ctx_destroy(mv_ctx* ctx);
+/* Waits for all work issued through ctx. */
+int32_t mv_ctx_synchronize(mv_ctx* ctx);
+/* Number of kernels this context launched since creation (for reports). */
+int64_t mv_ctx_kernel_launches(mv_ctx* ctx);
+
+/* Stage profiling: when enabled, each search stage is bracketed by CUDA
+ * events on the stream it runs on. Stage ids (MV_STAGE_*) index the arrays
+ * read by mv_ctx_stage_times (total milliseconds and launch counts since the
+ * last enable). Enabling resets the totals. */
+#define MV_STAGE_COARSE 0   /* query x centroid distances */
+#define MV_STAGE_SELECT 1   /* top-nprobe / top-k selection passes */
+#define MV_STAGE_SCAN 2     /* IVF-PQ LUT + ADC scan */
+#define MV_STAGE_LUT 3      /* per-query lookup tables (fast form) */
+#define MV_STAGE_RERANK 4   /* exact FP32 rerank */
+#define MV_STAGE_FLAT 5     /* Flat / SQ8 distance tiles */
+#define MV_STAGE_COUNT 8
+int32_t mv_ctx_profile(mv_ctx* ctx, int32_t enable);
+int32_t mv_ctx_stage_times(mv_ctx* ctx, double* ms, int64_t* counts, int32_t nstages);
+
+/* ---- IVF-PQ index: replaces IndexIVFPQ[IndexFlat]
+ *      (index/index_ivf_pq.mojo:12-360) -------------------------------- */
+
+/* IndexIVFPQ.__init__ (index_ivf_pq.mojo:35-71): M divides d, nlist in
+ * [1, 1e6], metric L2 or IP. ksub is 256 (pq.mojo:93). nprobe starts at 1. */
+int32_t mv_ivfpq_create(mv_ctx* ctx, int32_t d, int32_t nlist, int32_t M, int32_t metric,
+                        mv_ivfpq** out);
+int32_t mv_ivfpq_destroy(mv_ivfpq* index);
+/* Field nprobe (index_ivf_pq.mojo:22). */
+int32_t mv_ivfpq_set_nprobe(mv_ivfpq* index, int32_t nprobe);
+/* Reads d, nlist, M, nprobe, ntotal, metric, is_trained (index_ivf_pq.mojo:19-33). */
+int32_t mv_ivfpq_info(mv_ivfpq* index, int64_t* out7);
+/* Loads trained codebooks (host): centroids nlist x d, pq M x 256 x (d/M).
+ * Marks the index trained. The path that takes the reference's own trained
+ * codebooks. */
+int32_t mv_ivfpq_set_codebooks(mv_ivfpq* index, const float* centroids, const float* pq);
+int32_t mv_ivfpq_get_codebooks(mv_ivfpq* index, float* centroids, float* pq);
+/* IndexIVFPQ.train (index_ivf_pq.mojo:87-136): coarse k-means (niter_coarse,
+ * the reference uses 15), index-metric assignment, residual PQ k-means
+ * (niter_pq, reference 15) on the GPU in the plain exact form. */
+int32_t mv_ivfpq_train(mv_ivfpq* index, const float* x, int64_t n, int32_t niter_coarse,
+                       int32_t niter_pq);
+/* IndexIVFPQ.add (index_ivf_pq.mojo:138-148): sequential ids from ntotal. */
+int32_t mv_ivfpq_add(mv_ivfpq* index, const float* x, int64_t n);
+/* IndexIVFPQ.add_with_ids (index_ivf_pq.mojo:150-213). */
+int32_t mv_ivfpq_add_with_ids(mv_ivfpq* index, const float* x, const int64_t* ids, int64_t n);
+/* Exports the inverted lists as CSR: offsets[nlist+1], ids[ntotal],
+ * codes[ntotal*M] (storage/inverted_lists.mojo:93-117 per list). */
+int32_t mv_ivfpq_get_lists(mv_ivfpq* index, int64_t* offsets, int64_t* ids, uint8_t* codes);
+/* IndexIVFPQ.search (index_ivf_pq.mojo:215-360), host buffers. filter may be
+ * NULL; filter[id] != 0 excludes id (:328-334). Results distances[nq*k],
+ * labels[nq*k]; unfilled slots are 1e38 / -1 (:284-286). params may be NULL
+ * (plain form, index nprobe). */
+int32_t mv_ivfpq_search(mv_ivfpq* index, const float* x, int64_t nq, int32_t k,
+                        const uint8_t* filter, int64_t filter_len,
+                        const mv_search_params* params, float* distances, int64_t* labels);
+/* Same with device buffers on `stream` (cudaStream_t; NULL = the context's
+ * own stream). Returns after enqueueing; results are ready when the stream
+ * is. */
+int32_t mv_ivfpq_search_device(mv_ivfpq* index, const float* d_x, int64_t nq, int32_t k,
+                               const uint8_t* d_filter, int64_t filter_len,
+                               const mv_search_params* params, float* d_distances,
+                               int64_t* d_labels, void* stream);
+
+/* ---- Flat index: replaces IndexFlat (index/index_flat.mojo:117-330) ---- */
+int32_t mv_flat_create(mv_ctx* ctx, int32_t d, int32_t metric, mv_flat** out);
+int32_t mv_flat_destroy(mv_flat* index);
+/* IndexFlat.add (index_flat.mojo:185-210). */
+int32_t mv_flat_add(mv_flat* index, const float* x, int64_t n);
+int64_t mv_flat_ntotal(mv_flat* index);
+/* IndexFlat.search (index_flat.mojo:229-325); filter[j] > 0 excludes row j
+ * (:286-288). Unfilled slots (k > rows) are 0.0 / -1 (:232-238). */
+int32_t mv_flat_search(mv_flat* index, const float* x, int64_t nq, int32_t k,
+                       const uint8_t* filter, const mv_search_params* params,
+                       float* distances, int64_t* labels);
+int32_t mv_flat_search_device(mv_flat* index, const float* d_x, int64_t nq, int32_t k,
+                              const uint8_t* d_filter, const mv_search_params* params,
+                              float* d_distances, int64_t* d_labels, void* stream);
+
+/* ---- Flat SQ8 index: replaces IndexFlatSQ8
+ *      (index/index_flat_sq8.mojo:271-661) ------------------------------ */
+int32_t mv_sq8_create(mv_ctx* ctx, int32_t d, int32_t metric, mv_sq8** out);
+int32_t mv_sq8_destroy(mv_sq8* index);
+/* IndexFlatSQ8.add (index_flat_sq8.mojo:365-476): global min/max, affine
+ * UInt8 (L2) or symmetric Int8 (IP) codes, requantize on bound growth. */
+int32_t mv_sq8_add(mv_sq8* index, const float* x, int64_t n);
+/* out3 = {global_min, global_max, scale}. */
+int32_t mv_sq8_params(mv_sq8* index, float* out3);
+int64_t mv_sq8_ntotal(mv_sq8* index);
+/* Codes (ntotal*d bytes) and norms (ntotal uint32). */
+int32_t mv_sq8_get_codes(mv_sq8* index, uint8_t* codes, uint32_t* norms);
+/* IndexFlatSQ8.search (index_flat_sq8.mojo:478-605): tail 0.0 / -1. */
+int32_t mv_sq8_search(mv_sq8* index, const float* x, int64_t nq, int32_t k,
+                      const uint8_t* filter, float* distances, int64_t* labels);
+/* SQ8 shortlist of rerank_factor*k candidates reranked with exact FP32
+ * distances on the retained rows (index/index_hnsw.mojo:433-497 semantics). */
+int32_t mv_sq8_search_rerank(mv_sq8* index, const float* x, int64_t nq, int32_t k,
+                             int32_t rerank_factor, float* distances, int64_t* labels);
+
+/* ---- Training and encoding primitives --------------------------------- */
+
+/* KMeans(d, k, niter).train (clustering/kmeans.mojo:60-220), plain exact
+ * form: Philox init, 32-chunk FP32 accumulation in row order, ordered
+ * chunk reduce, reciprocal-multiply update, deterministic reseed.
+ * assignments (may be NULL) receive the last iteration's clusters. */
+int32_t mv_kmeans_train(mv_ctx* ctx, const float* x, int64_t n, int32_t d, int32_t k,
+                        int32_t niter, float* centroids, int64_t* assignments);
+/* ProductQuantizer.train (quantization/pq.mojo:125-176): M subspace
+ * k-means of 256 centroids each. out: M x 256 x (d/M). */
+int32_t mv_pq_train(mv_ctx* ctx, const float* x, int64_t n, int32_t d, int32_t M,
+                    int32_t niter, float* pq);
+/* ProductQuantizer.compute_codes (pq.mojo:178-219). codes: n x M. */
+int32_t mv_pq_encode(mv_ctx* ctx, const float* pq, int32_t d, int32_t M, const float* x,
+                     int64_t n, uint8_t* codes);
+/* ProductQuantizer.compute_distance_table (pq.mojo:252-292) for nq vectors:
+ * tables nq x M x 256. */
+int32_t mv_pq_distance_tables(mv_ctx* ctx, const float* pq, int32_t d, int32_t M,
+                              const float* x, int64_t nq, int32_t metric, float* tables);
+/* _encode_sq8_batch (quantization/sq8.mojo:41-59). */
+int32_t mv_sq8_encode(mv_ctx* ctx, const float* x, int64_t n, int32_t d, float minimum,
+                      float inverse_scale, int32_t symmetric, uint8_t* codes, uint32_t* norms);
+/* _normalize_vectors (api/collection_vector_query.mojo:24-46): FP64 sum of
+ * squares, 1/sqrt in FP64. Returns MV_ERR_ARG for non-finite or zero rows. */
+int32_t mv_normalize(mv_ctx* ctx, const float* x, int64_t n, int32_t d, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MOJOVEC_GPU_H */

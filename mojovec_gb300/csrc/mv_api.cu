@@ -1,0 +1,1228 @@
+// C ABI of libmojovec_gpu.so (include/mojovec_gpu.h): contexts, the IVF-PQ,
+// Flat and SQ8 indexes, k-means / PQ training and encoding primitives.
+//
+// Every entry point converts C++ exceptions into MV_ERR_* status codes and
+// records the message for mv_last_error(). Host-pointer entry points copy
+// their inputs to the device on a per-call stream, run, copy the results
+// back and synchronise that stream before returning.
+#include <algorithm>
+#include <cmath>
+#include <limits>
+#include <memory>
+#include <new>
+
+#include "mv_internal.h"
+#include "mv_kernels.h"
+
+namespace mv {
+
+static thread_local std::string g_last_error;
+static thread_local mv_ctx* g_cur_ctx = nullptr;
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+void count_launch() {
+  if (g_cur_ctx) g_cur_ctx->launches.fetch_add(1, std::memory_order_relaxed);
+}
+
+struct CtxScope {
+  mv_ctx* prev;
+  explicit CtxScope(mv_ctx* c) : prev(g_cur_ctx) {
+    g_cur_ctx = c;
+    if (c) c->set_device();
+  }
+  ~CtxScope() { g_cur_ctx = prev; }
+};
+
+template <class F>
+int32_t guard(mv_ctx* ctx, F&& f) {
+  try {
+    CtxScope scope(ctx);
+    f();
+    return MV_OK;
+  } catch (const Error& e) {
+    set_last_error(e.what());
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    set_last_error("host allocation failed");
+    return MV_ERR_OOM;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return MV_ERR_INTERNAL;
+  }
+}
+
+void h2d(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (bytes) MV_CHECK_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+}
+void d2h(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (bytes) MV_CHECK_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+}
+void d2d(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (bytes) MV_CHECK_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, s));
+}
+void sync(cudaStream_t s) { MV_CHECK_CUDA(cudaStreamSynchronize(s)); }
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11) for the k-means initialisation
+// (clustering/kmeans.mojo:70-82): key = seed, counter from zero, +1 per step.
+// ---------------------------------------------------------------------------
+struct Philox {
+  uint32_t key[2];
+  uint32_t ctr[4] = {0, 0, 0, 0};
+  explicit Philox(uint64_t seed) {
+    key[0] = (uint32_t)seed;
+    key[1] = (uint32_t)(seed >> 32);
+  }
+  void step(uint32_t* out) {
+    uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+      if (r) {
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+      }
+      uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+      uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+      uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0;
+      uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+      c[1] = (uint32_t)p1;
+      c[3] = (uint32_t)p0;
+      c[0] = n0;
+      c[2] = n2;
+    }
+    for (int i = 0; i < 4; ++i) out[i] = c[i];
+    for (int i = 0; i < 4; ++i)
+      if (++ctr[i] != 0) break;
+  }
+};
+constexpr uint64_t KMEANS_SEED = 0x4D4F4A4F564543ull;
+
+// Batched plain k-means over `batch` independent problems that share n, d
+// and k: x[b] at x + b*n*d, centroids[b] at cent + b*k*d, assign[b] at
+// assign + b*n.
+void kmeans_train_device(const float* x, int64_t n, int d, int k, int niter, int batch,
+                         float* cent, int32_t* assign, DevBuf& scratch, cudaStream_t s) {
+  if (n == 0 || k <= 0) return;
+  MV_REQUIRE(n <= 0xffffffffll, MV_ERR_UNSUPPORTED, "k-means: too many rows");
+  // :70-82 initial rows
+  Philox gen(KMEANS_SEED);
+  uint32_t words[4];
+  gen.step(words);
+  const int64_t sample_offset = (int64_t)(words[0] % (uint32_t)n);
+  std::vector<int64_t> idx(k);
+  for (int i = 0; i < k; ++i) {
+    if (i != 0 && i % 4 == 0) gen.step(words);
+    idx[i] = (int64_t)(words[i % 4] % (uint32_t)n);
+  }
+  const size_t sums = (size_t)32 * k * d * batch;
+  const size_t counts = (size_t)32 * k * batch;
+  scratch.ensure(ws_bytes(sums, 4) + ws_bytes(counts, 4) + ws_bytes(k, 8));
+  Arena ar(scratch);
+  float* local_sums = ar.take<float>(sums);
+  int32_t* local_counts = ar.take<int32_t>(counts);
+  int64_t* d_idx = ar.take<int64_t>(k);
+  h2d(d_idx, idx.data(), sizeof(int64_t) * k, s);
+  launch_gather_rows(x, d, d_idx, k, cent, batch, n * d, (int64_t)k * d, s);
+  const int kind = d <= 4 ? KIND_L2_SHORT4 : KIND_L2_SIMD8;  // kmeans.mojo:131-139
+  for (int it = 0; it < niter; ++it) {
+    launch_exact_argmin(kind, 1, x, n, d, cent, k, d, d, assign, nullptr, batch, n * d,
+                        (int64_t)k * d, n, s);
+    launch_kmeans_accumulate(x, n, d, k, assign, local_sums, local_counts, batch, n * d, n,
+                             (int64_t)32 * k * d, (int64_t)32 * k, s);
+    launch_kmeans_update(x, n, d, k, local_sums, local_counts, sample_offset, it, cent, batch,
+                         n * d, (int64_t)32 * k * d, (int64_t)32 * k, (int64_t)k * d, s);
+  }
+  sync(s);  // the host-side idx vector and scratch must outlive the kernels
+}
+
+// PQ training: subspace extraction then M batched k-means of 256 centroids
+// (quantization/pq.mojo:45-69,125-176).
+void pq_train_device(const float* x, int64_t n, int d, int M, int niter, float* pq_out,
+                     DevBuf& work, DevBuf& scratch, cudaStream_t s) {
+  const int dsub = d / M;
+  work.ensure(ws_bytes((size_t)n * d, 4) + ws_bytes((size_t)M * n, 4));
+  Arena ar(work);
+  float* sub = ar.take<float>((size_t)n * d);
+  int32_t* assign = ar.take<int32_t>((size_t)M * n);
+  launch_split_subspaces(x, n, d, M, sub, s);
+  kmeans_train_device(sub, n, dsub, 256, niter, M, pq_out, assign, scratch, s);
+}
+
+}  // namespace mv
+
+using namespace mv;
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+void mv_ctx::set_device() const { cudaSetDevice(device); }
+
+mv::Slot* mv_ctx::acquire() {
+  Slot* pick = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    // Prefer an idle slot whose last call has drained.
+    for (size_t i = 0; i < free_slots.size(); ++i) {
+      if (cudaEventQuery(free_slots[i]->done) == cudaSuccess) {
+        pick = free_slots[i];
+        free_slots.erase(free_slots.begin() + i);
+        break;
+      }
+    }
+    if (!pick && (free_slots.empty() || all_slots.size() < 8)) {
+      auto* s = new Slot();
+      MV_CHECK_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+      MV_CHECK_CUDA(cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming));
+      all_slots.push_back(s);
+      pick = s;
+    }
+    if (!pick) {
+      pick = free_slots.front();
+      free_slots.erase(free_slots.begin());
+    }
+  }
+  MV_CHECK_CUDA(cudaEventSynchronize(pick->done));
+  return pick;
+}
+
+void mv_ctx::release(mv::Slot* s, cudaStream_t used) {
+  cudaEventRecord(s->done, used);
+  std::lock_guard<std::mutex> lk(mu);
+  free_slots.push_back(s);
+}
+
+extern "C" {
+
+int32_t mv_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return MV_ERR_ARG;
+  size_t n = std::min(len - 1, g_last_error.size());
+  std::memcpy(buf, g_last_error.data(), n);
+  buf[n] = 0;
+  return MV_OK;
+}
+
+const char* mv_version(void) { return "mojovec-gb300 0.1 sm_103a"; }
+
+int32_t mv_ctx_create(int32_t device, mv_ctx** out) {
+  if (!out) return MV_ERR_ARG;
+  *out = nullptr;
+  return guard(nullptr, [&] {
+    int count = 0;
+    MV_CHECK_CUDA(cudaGetDeviceCount(&count));
+    MV_REQUIRE(device >= 0 && device < count, MV_ERR_ARG, "no such CUDA device");
+    auto ctx = std::make_unique<mv_ctx>();
+    ctx->device = device;
+    MV_CHECK_CUDA(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    MV_CHECK_CUDA(cudaGetDeviceProperties(&prop, device));
+    MV_REQUIRE(prop.major >= 10, MV_ERR_UNSUPPORTED,
+               std::string("libmojovec_gpu targets sm_103a; device is ") + prop.name);
+    ctx->num_sms = prop.multiProcessorCount;
+    ctx->smem_optin = prop.sharedMemPerBlockOptin;
+    MV_CHECK_CUDA(cudaStreamCreateWithFlags(&ctx->main_stream, cudaStreamNonBlocking));
+    *out = ctx.release();
+  });
+}
+
+int32_t mv_ctx_destroy(mv_ctx* ctx) {
+  if (!ctx) return MV_ERR_ARG;
+  return guard(ctx, [&] {
+    cudaDeviceSynchronize();
+    for (auto* s : ctx->all_slots) {
+      if (s->stream) cudaStreamDestroy(s->stream);
+      if (s->done) cudaEventDestroy(s->done);
+      delete s;
+    }
+    if (ctx->main_stream) cudaStreamDestroy(ctx->main_stream);
+    g_cur_ctx = nullptr;
+    delete ctx;
+  });
+}
+
+int32_t mv_ctx_synchronize(mv_ctx* ctx) {
+  if (!ctx) return MV_ERR_ARG;
+  return guard(ctx, [&] { MV_CHECK_CUDA(cudaDeviceSynchronize()); });
+}
+
+int64_t mv_ctx_kernel_launches(mv_ctx* ctx) { return ctx ? ctx->launches.load() : -1; }
+
+int32_t mv_ctx_profile(mv_ctx* ctx, int32_t enable) {
+  if (!ctx) return MV_ERR_ARG;
+  return guard(ctx, [&] {
+    std::lock_guard<std::mutex> lk(ctx->prof_mu);
+    for (auto& r : ctx->prof_pending) {
+      cudaEventSynchronize(r.b);
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+    }
+    ctx->prof_pending.clear();
+    for (int i = 0; i < MV_STAGE_COUNT; ++i) {
+      ctx->stage_ms[i] = 0.0;
+      ctx->stage_n[i] = 0;
+    }
+    ctx->profile.store(enable != 0);
+  });
+}
+
+int32_t mv_ctx_stage_times(mv_ctx* ctx, double* ms, int64_t* counts, int32_t nstages) {
+  if (!ctx || nstages < 0) return MV_ERR_ARG;
+  return guard(ctx, [&] {
+    std::lock_guard<std::mutex> lk(ctx->prof_mu);
+    for (auto& r : ctx->prof_pending) {
+      MV_CHECK_CUDA(cudaEventSynchronize(r.b));
+      float t = 0.0f;
+      MV_CHECK_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
+      ctx->stage_ms[r.stage] += t;
+      ctx->stage_n[r.stage] += 1;
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+    }
+    ctx->prof_pending.clear();
+    for (int i = 0; i < nstages && i < MV_STAGE_COUNT; ++i) {
+      if (ms) ms[i] = ctx->stage_ms[i];
+      if (counts) counts[i] = ctx->stage_n[i];
+    }
+  });
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// IVF-PQ
+// ---------------------------------------------------------------------------
+namespace mv {
+
+int effective_nprobe(const mv_ivfpq* ix, const mv_search_params* p) {
+  int np = (p && p->nprobe > 0) ? p->nprobe : ix->nprobe;
+  return std::min(np, ix->nlist);  // index_ivf_pq.mojo:253-254
+}
+
+void check_search_args(int64_t nq, int32_t k) {
+  MV_REQUIRE(nq >= 0, MV_ERR_ARG, "query count must be non-negative");
+  MV_REQUIRE(k >= 1 && k <= 2048, MV_ERR_ARG, "n_results must be between 1 and 2048.");
+}
+
+// Fills distances/labels with a constant (device).
+__global__ void k_fill(float* d, int64_t* l, int64_t n, float dv) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    d[i] = dv;
+    l[i] = -1;
+  }
+}
+void launch_fill(float* d, int64_t* l, int64_t n, float dv, cudaStream_t s) {
+  if (n == 0) return;
+  k_fill<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, l, n, dv);
+  count_launch();
+  MV_CHECK_CUDA(cudaGetLastError());
+}
+
+// Plain IVF-PQ search on device buffers (index_ivf_pq.mojo:225-360).
+void ivfpq_search_plain(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int nprobe,
+                        const uint8_t* d_filter, int64_t filter_len, float* d_out,
+                        int64_t* d_lab, DevBuf& ws, cudaStream_t s) {
+  if (nq == 0) return;
+  if (!ix->trained || ix->ntotal == 0) {  // :247-251
+    launch_fill(d_out, d_lab, nq * k, 1e38f, s);
+    return;
+  }
+  MV_REQUIRE(nprobe <= 8192, MV_ERR_UNSUPPORTED, "nprobe above 8192 is not supported on the GPU");
+  // Query batches bound the coarse distance matrix to ~1.5 GB.
+  int64_t qb = std::max<int64_t>(64, (int64_t)(1536ll * 1024 * 1024 / ((int64_t)ix->nlist * 4)));
+  qb = std::min<int64_t>({qb, nq, 65535ll * 64});
+  ws.ensure(ws_bytes((size_t)qb * ix->nlist, 4) + ws_bytes((size_t)qb * nprobe, 8) +
+            ws_bytes((size_t)qb * nprobe, 4));
+  Arena ar(ws);
+  float* dmat = ar.take<float>((size_t)qb * ix->nlist);
+  uint64_t* ckeys = ar.take<uint64_t>((size_t)qb * nprobe);
+  int32_t* probes = ar.take<int32_t>((size_t)qb * nprobe);
+  const int kind = ix->metric == MV_METRIC_L2 ? KIND_L2_SIMD8 : KIND_IP_SIMD8;
+  for (int64_t q0 = 0; q0 < nq; q0 += qb) {
+    const int64_t nb = std::min(qb, nq - q0);
+    const float* xq = d_x + q0 * ix->d;
+    // :264 coarse quantizer search with k = nprobe
+    {
+      StageTimer t(ix->ctx, MV_STAGE_COARSE, s);
+      launch_exact_matrix(kind, xq, nb, ix->d, ix->centroids.as<float>(), ix->nlist, ix->d, ix->d,
+                          dmat, ix->nlist, s);
+    }
+    {
+      StageTimer t(ix->ctx, MV_STAGE_SELECT, s);
+      launch_select_rows(dmat, nb, ix->nlist, ix->nlist, 0, nprobe, nullptr, ckeys, nullptr, s);
+      launch_keys_to_ids(ckeys, nb * nprobe, probes, s);
+    }
+    IvfpqScanArgs a;
+    a.q = xq;
+    a.nq = nb;
+    a.d = ix->d;
+    a.M = ix->M;
+    a.dsub = ix->dsub;
+    a.metric = ix->metric;
+    a.centroids = ix->centroids.as<float>();
+    a.pq = ix->pq.as<float>();
+    a.list_off = ix->d_off.as<int64_t>();
+    a.ids = ix->d_ids.as<uint32_t>();
+    a.codes = ix->d_codes.as<uint8_t>();
+    a.probes = probes;
+    a.nprobe = nprobe;
+    a.filter = d_filter;
+    a.filter_len = d_filter ? filter_len : 0;
+    a.k = k;
+    a.out_d = d_out + q0 * k;
+    a.out_l = d_lab + q0 * k;
+    StageTimer t(ix->ctx, MV_STAGE_SCAN, s);
+    launch_ivfpq_scan_plain(a, s);
+  }
+}
+
+// Scatter of fixed-width rows: dst[pos[i]] = src[i] (width in 4-byte words).
+__global__ void k_scatter_words(const uint32_t* __restrict__ src, int64_t n, int w,
+                                const int64_t* __restrict__ pos, uint32_t* __restrict__ dst) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * w) return;
+  int64_t i = e / w;
+  int j = (int)(e - i * w);
+  dst[pos[i] * w + j] = src[e];
+}
+__global__ void k_scatter_bytes(const uint8_t* __restrict__ src, int64_t n, int w,
+                                const int64_t* __restrict__ pos, uint8_t* __restrict__ dst) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * w) return;
+  int64_t i = e / w;
+  int j = (int)(e - i * w);
+  dst[pos[i] * w + j] = src[e];
+}
+void scatter_rows(const void* src, int64_t n, int width_bytes, const int64_t* pos, void* dst,
+                  cudaStream_t s) {
+  int64_t total;
+  if (n == 0) return;
+  if (width_bytes % 4 == 0) {
+    int w = width_bytes / 4;
+    total = n * w;
+    k_scatter_words<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(
+        static_cast<const uint32_t*>(src), n, w, pos, static_cast<uint32_t*>(dst));
+  } else {
+    total = n * width_bytes;
+    k_scatter_bytes<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(
+        static_cast<const uint8_t*>(src), n, width_bytes, pos, static_cast<uint8_t*>(dst));
+  }
+  count_launch();
+  MV_CHECK_CUDA(cudaGetLastError());
+}
+
+// IndexIVFPQ.add_with_ids (index_ivf_pq.mojo:150-213): assign with the
+// index-metric quantizer, residual PQ codes, append to the lists in input
+// order (storage/inverted_lists.mojo:162-186). Lists are kept as CSR on the
+// device; an append rebuilds it with one scatter per array.
+void ivfpq_add(mv_ivfpq* ix, const float* x, const int64_t* ids, int64_t n) {
+  if (!ix->trained || n == 0) return;  // :161
+  for (int64_t i = 0; i < n; ++i)
+    MV_REQUIRE(ids[i] >= 0 && ids[i] <= 0xfffffffell, MV_ERR_ARG,
+               "ids must be in [0, 2^32 - 2] for the GPU index");
+  SlotLease lease(ix->ctx);
+  cudaStream_t s = lease.stream();
+  const int d = ix->d, M = ix->M;
+  std::vector<int32_t> h_assign(n);
+  DevBuf new_codes, new_raw;
+  new_codes.ensure((size_t)n * M + 16);
+  new_raw.ensure((size_t)n * d * 4 + 16);
+  const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(n, (1ll << 28) / d));
+  {
+    DevBuf& ws = lease.slot->ws;
+    ws.ensure(ws_bytes((size_t)chunk * d, 4) * 2 + ws_bytes(chunk, 4));
+    Arena ar(ws);
+    float* dx = ar.take<float>((size_t)chunk * d);
+    float* res = ar.take<float>((size_t)chunk * d);
+    int32_t* assign = ar.take<int32_t>(chunk);
+    const int kind = ix->metric == MV_METRIC_L2 ? KIND_L2_SIMD8 : KIND_IP_SIMD8;
+    for (int64_t r0 = 0; r0 < n; r0 += chunk) {
+      const int64_t nb = std::min(chunk, n - r0);
+      h2d(dx, x + r0 * d, sizeof(float) * nb * d, s);
+      // :172 quantizer.search(x, 1)
+      launch_exact_argmin(kind, 2, dx, nb, d, ix->centroids.as<float>(), ix->nlist, d, d, assign,
+                          nullptr, 1, 0, 0, 0, s);
+      launch_residuals(dx, nb, d, ix->centroids.as<float>(), ix->nlist, assign, res, s);
+      launch_pq_encode(res, nb, d, M, ix->pq.as<float>(), new_codes.as<uint8_t>() + r0 * M, s);
+      d2d(new_raw.as<float>() + r0 * d, dx, sizeof(float) * nb * d, s);
+      d2h(h_assign.data() + r0, assign, sizeof(int32_t) * nb, s);
+      sync(s);
+    }
+  }
+  // New CSR layout: old entries of list l keep their order, new ones follow
+  // in input order (:199-211 appends one at a time).
+  const int nlist = ix->nlist;
+  std::vector<int64_t> old_off = ix->h_off;
+  std::vector<int64_t> add_cnt(nlist, 0);
+  int64_t kept = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    int l = h_assign[i];
+    if (l < 0 || l >= nlist) continue;  // :201
+    add_cnt[l]++;
+    kept++;
+  }
+  std::vector<int64_t> new_off(nlist + 1, 0);
+  for (int l = 0; l < nlist; ++l)
+    new_off[l + 1] = new_off[l] + (old_off[l + 1] - old_off[l]) + add_cnt[l];
+  const int64_t old_total = old_off[nlist];
+  const int64_t new_total = old_total + kept;
+  std::vector<int64_t> pos_old(old_total), pos_new(n);
+  for (int l = 0; l < nlist; ++l)
+    for (int64_t p = old_off[l]; p < old_off[l + 1]; ++p) pos_old[p] = p - old_off[l] + new_off[l];
+  std::vector<int64_t> fill(nlist);
+  for (int l = 0; l < nlist; ++l) fill[l] = new_off[l] + (old_off[l + 1] - old_off[l]);
+  std::vector<uint32_t> ids32(n);
+  int64_t dropped = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    int l = h_assign[i];
+    ids32[i] = (uint32_t)ids[i];
+    if (l < 0 || l >= nlist) {
+      pos_new[i] = new_total + dropped++;  // parked past the end, never read
+      continue;
+    }
+    pos_new[i] = fill[l]++;
+  }
+  const int64_t cap = new_total + dropped;
+  DevBuf off_d, ids_d, codes_d, raw_d, pos_d, ids_new;
+  off_d.ensure(sizeof(int64_t) * (nlist + 1));
+  ids_d.ensure(sizeof(uint32_t) * cap + 16);
+  codes_d.ensure((size_t)cap * M + 16);
+  raw_d.ensure(sizeof(float) * cap * d + 16);
+  pos_d.ensure(sizeof(int64_t) * (old_total + n) + 16);
+  ids_new.ensure(sizeof(uint32_t) * n + 16);
+  h2d(off_d.p, new_off.data(), sizeof(int64_t) * (nlist + 1), s);
+  h2d(pos_d.p, pos_old.data(), sizeof(int64_t) * old_total, s);
+  h2d(pos_d.as<int64_t>() + old_total, pos_new.data(), sizeof(int64_t) * n, s);
+  h2d(ids_new.p, ids32.data(), sizeof(uint32_t) * n, s);
+  if (old_total) {
+    scatter_rows(ix->d_ids.p, old_total, 4, pos_d.as<int64_t>(), ids_d.p, s);
+    scatter_rows(ix->d_codes.p, old_total, M, pos_d.as<int64_t>(), codes_d.p, s);
+    scatter_rows(ix->d_raw.p, old_total, 4 * d, pos_d.as<int64_t>(), raw_d.p, s);
+  }
+  scatter_rows(ids_new.p, n, 4, pos_d.as<int64_t>() + old_total, ids_d.p, s);
+  scatter_rows(new_codes.p, n, M, pos_d.as<int64_t>() + old_total, codes_d.p, s);
+  scatter_rows(new_raw.p, n, 4 * d, pos_d.as<int64_t>() + old_total, raw_d.p, s);
+  sync(s);
+  std::swap(ix->d_off.p, off_d.p);
+  std::swap(ix->d_off.bytes, off_d.bytes);
+  std::swap(ix->d_ids.p, ids_d.p);
+  std::swap(ix->d_ids.bytes, ids_d.bytes);
+  std::swap(ix->d_codes.p, codes_d.p);
+  std::swap(ix->d_codes.bytes, codes_d.bytes);
+  std::swap(ix->d_raw.p, raw_d.p);
+  std::swap(ix->d_raw.bytes, raw_d.bytes);
+  ix->h_off = new_off;
+  ix->ntotal += n;  // :213 counts every input row
+  ix->fast_ready = false;
+}
+
+}  // namespace mv
+
+extern "C" {
+
+int32_t mv_ivfpq_create(mv_ctx* ctx, int32_t d, int32_t nlist, int32_t M, int32_t metric,
+                        mv_ivfpq** out) {
+  if (!ctx || !out) return MV_ERR_ARG;
+  *out = nullptr;
+  return guard(ctx, [&] {
+    // index_ivf_pq.mojo:52-59 and core/validation.mojo:11-13
+    MV_REQUIRE(d > 0 && d <= 65536, MV_ERR_ARG, "dimension must be between 1 and 65536.");
+    MV_REQUIRE(nlist > 0 && nlist <= 1000000, MV_ERR_ARG, "IVF-PQ nlist must be between 1 and 1000000.");
+    MV_REQUIRE(M > 0 && M <= d && d % M == 0, MV_ERR_ARG,
+               "IVF-PQ M must divide dimension and be between 1 and dimension.");
+    MV_REQUIRE(metric == MV_METRIC_L2 || metric == MV_METRIC_IP, MV_ERR_ARG, "unknown metric");
+    auto ix = std::make_unique<mv_ivfpq>();
+    ix->ctx = ctx;
+    ix->d = d;
+    ix->nlist = nlist;
+    ix->M = M;
+    ix->dsub = d / M;
+    ix->metric = metric;
+    ix->centroids.ensure(sizeof(float) * nlist * d);
+    ix->pq.ensure(sizeof(float) * 256 * d);
+    ix->h_off.assign(nlist + 1, 0);
+    ix->d_off.ensure(sizeof(int64_t) * (nlist + 1));
+    MV_CHECK_CUDA(cudaMemset(ix->d_off.p, 0, sizeof(int64_t) * (nlist + 1)));
+    MV_CHECK_CUDA(cudaMemset(ix->centroids.p, 0, sizeof(float) * nlist * d));
+    MV_CHECK_CUDA(cudaMemset(ix->pq.p, 0, sizeof(float) * 256 * d));
+    *out = ix.release();
+  });
+}
+
+int32_t mv_ivfpq_destroy(mv_ivfpq* ix) {
+  if (!ix) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    cudaDeviceSynchronize();
+    delete ix;
+  });
+}
+
+int32_t mv_ivfpq_set_nprobe(mv_ivfpq* ix, int32_t nprobe) {
+  if (!ix) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    MV_REQUIRE(nprobe >= 1 && nprobe <= 65536, MV_ERR_ARG, "nprobe must be between 1 and nlist.");
+    ix->nprobe = nprobe;
+  });
+}
+
+int32_t mv_ivfpq_info(mv_ivfpq* ix, int64_t* out7) {
+  if (!ix || !out7) return MV_ERR_ARG;
+  out7[0] = ix->d;
+  out7[1] = ix->nlist;
+  out7[2] = ix->M;
+  out7[3] = ix->nprobe;
+  out7[4] = ix->ntotal;
+  out7[5] = ix->metric;
+  out7[6] = ix->trained ? 1 : 0;
+  return MV_OK;
+}
+
+int32_t mv_ivfpq_set_codebooks(mv_ivfpq* ix, const float* centroids, const float* pq) {
+  if (!ix || !centroids || !pq) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    std::lock_guard<std::mutex> lk(ix->mu);
+    MV_CHECK_CUDA(cudaMemcpy(ix->centroids.p, centroids, sizeof(float) * ix->nlist * ix->d,
+                             cudaMemcpyHostToDevice));
+    MV_CHECK_CUDA(cudaMemcpy(ix->pq.p, pq, sizeof(float) * 256 * ix->d, cudaMemcpyHostToDevice));
+    ix->trained = true;
+    ix->fast_ready = false;
+  });
+}
+
+int32_t mv_ivfpq_get_codebooks(mv_ivfpq* ix, float* centroids, float* pq) {
+  if (!ix) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    if (centroids)
+      MV_CHECK_CUDA(cudaMemcpy(centroids, ix->centroids.p, sizeof(float) * ix->nlist * ix->d,
+                               cudaMemcpyDeviceToHost));
+    if (pq)
+      MV_CHECK_CUDA(cudaMemcpy(pq, ix->pq.p, sizeof(float) * 256 * ix->d, cudaMemcpyDeviceToHost));
+  });
+}
+
+int32_t mv_ivfpq_train(mv_ivfpq* ix, const float* x, int64_t n, int32_t niter_coarse,
+                       int32_t niter_pq) {
+  if (!ix || (!x && n > 0)) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    std::lock_guard<std::mutex> lk(ix->mu);
+    if (ix->trained) return;  // :93
+    MV_REQUIRE(n > 0, MV_ERR_ARG, "training needs at least one vector");
+    MV_REQUIRE(niter_coarse >= 0 && niter_pq >= 0, MV_ERR_ARG, "niter must be non-negative");
+    SlotLease lease(ix->ctx);
+    cudaStream_t s = lease.stream();
+    const int d = ix->d;
+    DevBuf dx, res, assign, work, scratch;
+    dx.ensure(sizeof(float) * n * d);
+    h2d(dx.p, x, sizeof(float) * n * d, s);
+    // 1. coarse k-means (:98-103)
+    assign.ensure(sizeof(int32_t) * n);
+    kmeans_train_device(dx.as<float>(), n, d, ix->nlist, niter_coarse, 1, ix->centroids.as<float>(),
+                        assign.as<int32_t>(), scratch, s);
+    // 2. index-metric assignment and residuals (:113-128)
+    const int kind = ix->metric == MV_METRIC_L2 ? KIND_L2_SIMD8 : KIND_IP_SIMD8;
+    launch_exact_argmin(kind, 2, dx.as<float>(), n, d, ix->centroids.as<float>(), ix->nlist, d, d,
+                        assign.as<int32_t>(), nullptr, 1, 0, 0, 0, s);
+    res.ensure(sizeof(float) * n * d);
+    launch_residuals(dx.as<float>(), n, d, ix->centroids.as<float>(), ix->nlist,
+                     assign.as<int32_t>(), res.as<float>(), s);
+    dx.release();
+    // 3. PQ on residuals (:130-132)
+    pq_train_device(res.as<float>(), n, d, ix->M, niter_pq, ix->pq.as<float>(), work, scratch, s);
+    sync(s);
+    ix->trained = true;
+    ix->fast_ready = false;
+  });
+}
+
+int32_t mv_ivfpq_add_with_ids(mv_ivfpq* ix, const float* x, const int64_t* ids, int64_t n) {
+  if (!ix || n < 0 || (n > 0 && (!x || !ids))) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    std::lock_guard<std::mutex> lk(ix->mu);
+    ivfpq_add(ix, x, ids, n);
+  });
+}
+
+int32_t mv_ivfpq_add(mv_ivfpq* ix, const float* x, int64_t n) {
+  if (!ix || n < 0 || (n > 0 && !x)) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    std::lock_guard<std::mutex> lk(ix->mu);
+    std::vector<int64_t> ids(n);
+    for (int64_t i = 0; i < n; ++i) ids[i] = ix->ntotal + i;  // :144-148
+    ivfpq_add(ix, x, ids.data(), n);
+  });
+}
+
+int32_t mv_ivfpq_get_lists(mv_ivfpq* ix, int64_t* offsets, int64_t* ids, uint8_t* codes) {
+  if (!ix) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    std::lock_guard<std::mutex> lk(ix->mu);
+    const int64_t total = ix->h_off[ix->nlist];
+    if (offsets) std::memcpy(offsets, ix->h_off.data(), sizeof(int64_t) * (ix->nlist + 1));
+    if (ids && total) {
+      std::vector<uint32_t> tmp(total);
+      MV_CHECK_CUDA(cudaMemcpy(tmp.data(), ix->d_ids.p, sizeof(uint32_t) * total, cudaMemcpyDeviceToHost));
+      for (int64_t i = 0; i < total; ++i) ids[i] = tmp[i];
+    }
+    if (codes && total)
+      MV_CHECK_CUDA(cudaMemcpy(codes, ix->d_codes.p, (size_t)total * ix->M, cudaMemcpyDeviceToHost));
+  });
+}
+
+int32_t mv_ivfpq_search_device(mv_ivfpq* ix, const float* d_x, int64_t nq, int32_t k,
+                               const uint8_t* d_filter, int64_t filter_len,
+                               const mv_search_params* params, float* d_distances,
+                               int64_t* d_labels, void* stream) {
+  if (!ix || (nq > 0 && (!d_x || !d_distances || !d_labels))) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    check_search_args(nq, k);
+    const int form = params ? params->form : MV_FORM_PLAIN;
+    MV_REQUIRE(form == MV_FORM_PLAIN, MV_ERR_UNSUPPORTED, "fast form not built in this library");
+    SlotLease lease(ix->ctx);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : lease.stream();
+    lease.use(s);
+    ivfpq_search_plain(ix, d_x, nq, k, effective_nprobe(ix, params), d_filter, filter_len,
+                       d_distances, d_labels, lease.slot->ws, s);
+    if (!stream) sync(s);
+  });
+}
+
+int32_t mv_ivfpq_search(mv_ivfpq* ix, const float* x, int64_t nq, int32_t k,
+                        const uint8_t* filter, int64_t filter_len,
+                        const mv_search_params* params, float* distances, int64_t* labels) {
+  if (!ix || (nq > 0 && (!x || !distances || !labels))) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    check_search_args(nq, k);
+    if (nq == 0) return;
+    const int form = params ? params->form : MV_FORM_PLAIN;
+    MV_REQUIRE(form == MV_FORM_PLAIN, MV_ERR_UNSUPPORTED, "fast form not built in this library");
+    SlotLease lease(ix->ctx);
+    cudaStream_t s = lease.stream();
+    DevBuf& io = lease.slot->io;
+    const size_t fl = filter ? (size_t)filter_len : 0;
+    io.ensure(ws_bytes((size_t)nq * ix->d, 4) + ws_bytes((size_t)nq * k, 4) +
+              ws_bytes((size_t)nq * k, 8) + ws_bytes(fl + 1, 1));
+    Arena ar(io);
+    float* dx = ar.take<float>((size_t)nq * ix->d);
+    float* dd = ar.take<float>((size_t)nq * k);
+    int64_t* dl = ar.take<int64_t>((size_t)nq * k);
+    uint8_t* df = ar.take<uint8_t>(fl + 1);
+    h2d(dx, x, sizeof(float) * nq * ix->d, s);
+    if (fl) h2d(df, filter, fl, s);
+    ivfpq_search_plain(ix, dx, nq, k, effective_nprobe(ix, params), fl ? df : nullptr,
+                       (int64_t)fl, dd, dl, lease.slot->ws, s);
+    d2h(distances, dd, sizeof(float) * nq * k, s);
+    d2h(labels, dl, sizeof(int64_t) * nq * k, s);
+    sync(s);
+  });
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Flat
+// ---------------------------------------------------------------------------
+namespace mv {
+
+void flat_search_plain(mv_flat* ix, const float* d_x, int64_t nq, int k, const uint8_t* d_filter,
+                       float* d_out, int64_t* d_lab, DevBuf& ws, cudaStream_t s) {
+  if (nq == 0) return;
+  const int64_t nb = ix->ntotal;
+  if (nb == 0) {
+    launch_fill(d_out, d_lab, nq * k, 0.0f, s);
+    return;
+  }
+  int64_t qb = std::min<int64_t>(nq, 65535ll * 64);
+  int64_t cb = (int64_t)(1024ll * 1024 * 1024 / 4) / std::max<int64_t>(qb, 1);
+  cb = std::max<int64_t>(64, (cb / 64) * 64);
+  cb = std::min(cb, nb);
+  ws.ensure(ws_bytes((size_t)qb * cb, 4) + 2 * ws_bytes((size_t)qb * k, 8));
+  Arena ar(ws);
+  float* dmat = ar.take<float>((size_t)qb * cb);
+  uint64_t* ka = ar.take<uint64_t>((size_t)qb * k);
+  uint64_t* kb = ar.take<uint64_t>((size_t)qb * k);
+  const int kind = ix->metric == MV_METRIC_L2 ? KIND_L2_SIMD8 : KIND_IP_SIMD8;
+  for (int64_t q0 = 0; q0 < nq; q0 += qb) {
+    const int64_t nqb = std::min(qb, nq - q0);
+    uint64_t* cur = ka;
+    uint64_t* nxt = kb;
+    bool first = true;
+    for (int64_t c0 = 0; c0 < nb; c0 += cb) {
+      const int64_t nc = std::min(cb, nb - c0);
+      {
+        StageTimer t(ix->ctx, MV_STAGE_FLAT, s);
+        launch_exact_matrix(kind, d_x + q0 * ix->d, nqb, ix->d, ix->rows.as<float>() + c0 * ix->d,
+                            nc, ix->d, ix->d, dmat, nc, s);
+      }
+      StageTimer t(ix->ctx, MV_STAGE_SELECT, s);
+      launch_select_rows(dmat, nqb, nc, nc, c0, k, first ? nullptr : cur, nxt, d_filter, s);
+      std::swap(cur, nxt);
+      first = false;
+    }
+    // index_flat.mojo:305-316; rows beyond ntotal read 0.0 / -1.
+    launch_keys_to_results(cur, nqb, k, 0.0f, ix->metric == MV_METRIC_IP, d_out + q0 * k,
+                           d_lab + q0 * k, s);
+  }
+}
+
+}  // namespace mv
+
+extern "C" {
+
+int32_t mv_flat_create(mv_ctx* ctx, int32_t d, int32_t metric, mv_flat** out) {
+  if (!ctx || !out) return MV_ERR_ARG;
+  *out = nullptr;
+  return guard(ctx, [&] {
+    MV_REQUIRE(d > 0 && d <= 65536, MV_ERR_ARG, "dimension must be between 1 and 65536.");
+    MV_REQUIRE(metric == MV_METRIC_L2 || metric == MV_METRIC_IP, MV_ERR_ARG, "unknown metric");
+    auto ix = std::make_unique<mv_flat>();
+    ix->ctx = ctx;
+    ix->d = d;
+    ix->metric = metric;
+    *out = ix.release();
+  });
+}
+
+int32_t mv_flat_destroy(mv_flat* ix) {
+  if (!ix) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    cudaDeviceSynchronize();
+    delete ix;
+  });
+}
+
+int32_t mv_flat_add(mv_flat* ix, const float* x, int64_t n) {
+  if (!ix || n < 0 || (n > 0 && !x)) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    std::lock_guard<std::mutex> lk(ix->mu);
+    if (n == 0) return;
+    MV_REQUIRE(ix->ntotal + n <= 0xfffffffell, MV_ERR_ARG, "Flat index limited to 2^32 - 2 rows");
+    SlotLease lease(ix->ctx);
+    cudaStream_t s = lease.stream();
+    const int64_t need = ix->ntotal + n;
+    if (need > ix->capacity) {  // index_flat.mojo:198-206 capacity doubling
+      int64_t cap = std::max<int64_t>(ix->capacity * 2, need);
+      DevBuf nb;
+      nb.ensure(sizeof(float) * cap * ix->d);
+      d2d(nb.p, ix->rows.p, sizeof(float) * ix->ntotal * ix->d, s);
+      sync(s);
+      std::swap(nb.p, ix->rows.p);
+      std::swap(nb.bytes, ix->rows.bytes);
+      ix->capacity = cap;
+    }
+    h2d(ix->rows.as<float>() + ix->ntotal * ix->d, x, sizeof(float) * n * ix->d, s);
+    sync(s);
+    ix->ntotal = need;
+    ix->fast_ready = false;
+  });
+}
+
+int64_t mv_flat_ntotal(mv_flat* ix) { return ix ? ix->ntotal : -1; }
+
+int32_t mv_flat_search_device(mv_flat* ix, const float* d_x, int64_t nq, int32_t k,
+                              const uint8_t* d_filter, const mv_search_params* params,
+                              float* d_distances, int64_t* d_labels, void* stream) {
+  if (!ix || (nq > 0 && (!d_x || !d_distances || !d_labels))) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    check_search_args(nq, k);
+    const int form = params ? params->form : MV_FORM_PLAIN;
+    MV_REQUIRE(form == MV_FORM_PLAIN, MV_ERR_UNSUPPORTED, "fast form not built in this library");
+    SlotLease lease(ix->ctx);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : lease.stream();
+    lease.use(s);
+    flat_search_plain(ix, d_x, nq, k, d_filter, d_distances, d_labels, lease.slot->ws, s);
+    if (!stream) sync(s);
+  });
+}
+
+int32_t mv_flat_search(mv_flat* ix, const float* x, int64_t nq, int32_t k, const uint8_t* filter,
+                       const mv_search_params* params, float* distances, int64_t* labels) {
+  if (!ix || (nq > 0 && (!x || !distances || !labels))) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    check_search_args(nq, k);
+    if (nq == 0) return;
+    const int form = params ? params->form : MV_FORM_PLAIN;
+    MV_REQUIRE(form == MV_FORM_PLAIN, MV_ERR_UNSUPPORTED, "fast form not built in this library");
+    SlotLease lease(ix->ctx);
+    cudaStream_t s = lease.stream();
+    DevBuf& io = lease.slot->io;
+    const size_t fl = filter ? (size_t)ix->ntotal : 0;
+    io.ensure(ws_bytes((size_t)nq * ix->d, 4) + ws_bytes((size_t)nq * k, 4) +
+              ws_bytes((size_t)nq * k, 8) + ws_bytes(fl + 1, 1));
+    Arena ar(io);
+    float* dx = ar.take<float>((size_t)nq * ix->d);
+    float* dd = ar.take<float>((size_t)nq * k);
+    int64_t* dl = ar.take<int64_t>((size_t)nq * k);
+    uint8_t* df = ar.take<uint8_t>(fl + 1);
+    h2d(dx, x, sizeof(float) * nq * ix->d, s);
+    if (fl) h2d(df, filter, fl, s);
+    flat_search_plain(ix, dx, nq, k, fl ? df : nullptr, dd, dl, lease.slot->ws, s);
+    d2h(distances, dd, sizeof(float) * nq * k, s);
+    d2h(labels, dl, sizeof(int64_t) * nq * k, s);
+    sync(s);
+  });
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// SQ8
+// ---------------------------------------------------------------------------
+namespace mv {
+
+// Encodes nq queries with the index codec and writes the nq x k shortlist
+// keys of the SQ8 scan (index_flat_sq8.mojo:526-583).
+void sq8_scan_keys(mv_sq8* ix, const float* d_x, int64_t nq, int kk, const uint8_t* d_filter,
+                   uint64_t* out_keys, DevBuf& ws, cudaStream_t s) {
+  const bool ip = ix->metric != MV_METRIC_L2;
+  const float inv = 1.0f / ix->scale;
+  const float scale_sq = ix->scale * ix->scale;
+  const int64_t nb = ix->ntotal;
+  int64_t cb = (int64_t)(1024ll * 1024 * 1024 / 4) / std::max<int64_t>(nq, 1);
+  cb = std::max<int64_t>(64, (cb / 64) * 64);
+  cb = std::min(cb, std::max<int64_t>(nb, 1));
+  ws.ensure(ws_bytes((size_t)nq * ix->dpad, 1) + ws_bytes(nq, 4) + ws_bytes((size_t)nq * cb, 4) +
+            ws_bytes((size_t)nq * kk, 8));
+  Arena ar(ws);
+  uint8_t* qc = ar.take<uint8_t>((size_t)nq * ix->dpad);
+  uint32_t* qn = ar.take<uint32_t>(nq);
+  float* dmat = ar.take<float>((size_t)nq * cb);
+  uint64_t* tmp = ar.take<uint64_t>((size_t)nq * kk);
+  launch_sq8_encode(d_x, nq, ix->d, ix->dpad, ip ? 0.0f : ix->gmin, inv, ip, qc, qn, s);
+  uint64_t* cur = out_keys;
+  uint64_t* nxt = tmp;
+  // Chunks alternate between the two key buffers; pick the start so that
+  // the last chunk writes out_keys.
+  int64_t nchunks = (nb + cb - 1) / cb;
+  if (nchunks % 2 == 1) std::swap(cur, nxt);
+  bool first = true;
+  for (int64_t c0 = 0; c0 < nb; c0 += cb) {
+    const int64_t nc = std::min(cb, nb - c0);
+    launch_sq8_matrix(qc, qn, nq, ix->codes.as<uint8_t>() + c0 * ix->dpad,
+                      ix->norms.as<uint32_t>() + c0, nc, ix->dpad, ip, scale_sq, dmat, nc, s);
+    launch_select_rows(dmat, nq, nc, nc, c0, kk, first ? nullptr : cur, nxt, d_filter, s);
+    std::swap(cur, nxt);
+    first = false;
+  }
+}
+
+__global__ void k_keys_to_cand(const uint64_t* __restrict__ keys, int64_t n, int64_t* __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = keys[i] == ~0ull ? -1 : (int64_t)(uint32_t)keys[i];
+}
+
+void sq8_search_impl(mv_sq8* ix, const float* d_x, int64_t nq, int k, int rerank_factor,
+                     const uint8_t* d_filter, float* d_out, int64_t* d_lab, DevBuf& ws,
+                     cudaStream_t s) {
+  if (nq == 0) return;
+  const bool ip = ix->metric != MV_METRIC_L2;
+  if (ix->ntotal == 0) {
+    launch_fill(d_out, d_lab, nq * k, 0.0f, s);
+    return;
+  }
+  if (rerank_factor <= 0) {
+    DevBuf keys;
+    keys.ensure(sizeof(uint64_t) * nq * k);
+    sq8_scan_keys(ix, d_x, nq, k, d_filter, keys.as<uint64_t>(), ws, s);
+    launch_keys_to_results(keys.as<uint64_t>(), nq, k, 0.0f, ip, d_out, d_lab, s);  // :595-602
+    sync(s);
+    return;
+  }
+  const int kk = (int)std::min<int64_t>((int64_t)k * rerank_factor, 2048);
+  DevBuf keys, cand, fk;
+  keys.ensure(sizeof(uint64_t) * nq * kk);
+  cand.ensure(sizeof(int64_t) * nq * kk);
+  fk.ensure(sizeof(uint64_t) * nq * k);
+  sq8_scan_keys(ix, d_x, nq, kk, d_filter, keys.as<uint64_t>(), ws, s);
+  k_keys_to_cand<<<(unsigned)((nq * kk + 255) / 256), 256, 0, s>>>(keys.as<uint64_t>(), nq * kk,
+                                                                  cand.as<int64_t>());
+  count_launch();
+  launch_rerank_simd64(d_x, nq, ix->d, ix->f32.as<float>(), ix->metric, cand.as<int64_t>(), kk, k,
+                       fk.as<uint64_t>(), s);
+  launch_keys_to_results(fk.as<uint64_t>(), nq, k, 0.0f, ip, d_out, d_lab, s);
+  sync(s);
+}
+
+}  // namespace mv
+
+extern "C" {
+
+int32_t mv_sq8_create(mv_ctx* ctx, int32_t d, int32_t metric, mv_sq8** out) {
+  if (!ctx || !out) return MV_ERR_ARG;
+  *out = nullptr;
+  return guard(ctx, [&] {
+    MV_REQUIRE(d > 0 && d <= 65536, MV_ERR_ARG, "dimension must be between 1 and 65536.");
+    MV_REQUIRE(metric == MV_METRIC_L2 || metric == MV_METRIC_IP, MV_ERR_ARG, "unknown metric");
+    auto ix = std::make_unique<mv_sq8>();
+    ix->ctx = ctx;
+    ix->d = d;
+    ix->dpad = (d + 15) / 16 * 16;
+    ix->metric = metric;
+    ix->gmin = std::numeric_limits<float>::max();   // index_flat_sq8.mojo:311-313
+    ix->gmax = -std::numeric_limits<float>::max();
+    ix->scale = 1.0f;
+    *out = ix.release();
+  });
+}
+
+int32_t mv_sq8_destroy(mv_sq8* ix) {
+  if (!ix) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    cudaDeviceSynchronize();
+    delete ix;
+  });
+}
+
+int32_t mv_sq8_add(mv_sq8* ix, const float* x, int64_t n) {
+  if (!ix || n < 0 || (n > 0 && !x)) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    std::lock_guard<std::mutex> lk(ix->mu);
+    if (n == 0) return;  // :373-374
+    MV_REQUIRE(ix->ntotal + n <= 0xfffffffell, MV_ERR_ARG, "SQ8 index limited to 2^32 - 2 rows");
+    SlotLease lease(ix->ctx);
+    cudaStream_t s = lease.stream();
+    const int d = ix->d, dp = ix->dpad;
+    const int64_t need = ix->ntotal + n;
+    if (need > ix->capacity) {  // :376-394
+      int64_t cap = std::max<int64_t>(ix->capacity * 2, need);
+      DevBuf f, c, nm;
+      f.ensure(sizeof(float) * cap * d);
+      c.ensure((size_t)cap * dp);
+      nm.ensure(sizeof(uint32_t) * cap);
+      d2d(f.p, ix->f32.p, sizeof(float) * ix->ntotal * d, s);
+      d2d(c.p, ix->codes.p, (size_t)ix->ntotal * dp, s);
+      d2d(nm.p, ix->norms.p, sizeof(uint32_t) * ix->ntotal, s);
+      sync(s);
+      std::swap(f.p, ix->f32.p);
+      std::swap(f.bytes, ix->f32.bytes);
+      std::swap(c.p, ix->codes.p);
+      std::swap(c.bytes, ix->codes.bytes);
+      std::swap(nm.p, ix->norms.p);
+      std::swap(nm.bytes, ix->norms.bytes);
+      ix->capacity = cap;
+    }
+    float* newrows = ix->f32.as<float>() + ix->ntotal * d;
+    h2d(newrows, x, sizeof(float) * n * d, s);
+    DevBuf mm;
+    mm.ensure(8);
+    launch_minmax(newrows, n * d, mm.as<float>(), s);  // :397-402
+    float bminmax[2];
+    d2h(bminmax, mm.p, 8, s);
+    sync(s);
+    bool requant = false;  // :404-410
+    if (bminmax[0] < ix->gmin) {
+      ix->gmin = bminmax[0];
+      requant = true;
+    }
+    if (bminmax[1] > ix->gmax) {
+      ix->gmax = bminmax[1];
+      requant = true;
+    }
+    const bool sym = ix->metric != MV_METRIC_L2;
+    if (!sym) {  // :412-421
+      ix->scale = (ix->gmax == ix->gmin) ? 1.0f : (ix->gmax - ix->gmin) / 255.0f;
+    } else {
+      float max_abs = std::max(std::fabs(ix->gmin), std::fabs(ix->gmax));
+      ix->scale = max_abs > 0.0f ? max_abs / 127.0f : 1.0f;
+    }
+    const float inv = 1.0f / ix->scale;  // :423
+    const float mn = sym ? 0.0f : ix->gmin;
+    if (requant && ix->ntotal > 0)  // :426-446
+      launch_sq8_encode(ix->f32.as<float>(), ix->ntotal, d, dp, mn, inv, sym, ix->codes.as<uint8_t>(),
+                        ix->norms.as<uint32_t>(), s);
+    launch_sq8_encode(newrows, n, d, dp, mn, inv, sym, ix->codes.as<uint8_t>() + ix->ntotal * dp,
+                      ix->norms.as<uint32_t>() + ix->ntotal, s);
+    sync(s);
+    ix->ntotal = need;
+  });
+}
+
+int32_t mv_sq8_params(mv_sq8* ix, float* out3) {
+  if (!ix || !out3) return MV_ERR_ARG;
+  out3[0] = ix->gmin;
+  out3[1] = ix->gmax;
+  out3[2] = ix->scale;
+  return MV_OK;
+}
+
+int64_t mv_sq8_ntotal(mv_sq8* ix) { return ix ? ix->ntotal : -1; }
+
+int32_t mv_sq8_get_codes(mv_sq8* ix, uint8_t* codes, uint32_t* norms) {
+  if (!ix) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    std::lock_guard<std::mutex> lk(ix->mu);
+    if (ix->ntotal == 0) return;
+    if (codes)
+      MV_CHECK_CUDA(cudaMemcpy2D(codes, ix->d, ix->codes.p, ix->dpad, ix->d, ix->ntotal,
+                                 cudaMemcpyDeviceToHost));
+    if (norms)
+      MV_CHECK_CUDA(cudaMemcpy(norms, ix->norms.p, sizeof(uint32_t) * ix->ntotal, cudaMemcpyDeviceToHost));
+  });
+}
+
+static int32_t sq8_search_host(mv_sq8* ix, const float* x, int64_t nq, int32_t k,
+                               const uint8_t* filter, int rerank_factor, float* distances,
+                               int64_t* labels) {
+  if (!ix || (nq > 0 && (!x || !distances || !labels))) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    check_search_args(nq, k);
+    if (nq == 0) return;
+    SlotLease lease(ix->ctx);
+    cudaStream_t s = lease.stream();
+    DevBuf& io = lease.slot->io;
+    const size_t fl = filter ? (size_t)ix->ntotal : 0;
+    io.ensure(ws_bytes((size_t)nq * ix->d, 4) + ws_bytes((size_t)nq * k, 4) +
+              ws_bytes((size_t)nq * k, 8) + ws_bytes(fl + 1, 1));
+    Arena ar(io);
+    float* dx = ar.take<float>((size_t)nq * ix->d);
+    float* dd = ar.take<float>((size_t)nq * k);
+    int64_t* dl = ar.take<int64_t>((size_t)nq * k);
+    uint8_t* df = ar.take<uint8_t>(fl + 1);
+    h2d(dx, x, sizeof(float) * nq * ix->d, s);
+    if (fl) h2d(df, filter, fl, s);
+    sq8_search_impl(ix, dx, nq, k, rerank_factor, fl ? df : nullptr, dd, dl, lease.slot->ws, s);
+    d2h(distances, dd, sizeof(float) * nq * k, s);
+    d2h(labels, dl, sizeof(int64_t) * nq * k, s);
+    sync(s);
+  });
+}
+
+int32_t mv_sq8_search(mv_sq8* ix, const float* x, int64_t nq, int32_t k, const uint8_t* filter,
+                      float* distances, int64_t* labels) {
+  return sq8_search_host(ix, x, nq, k, filter, 0, distances, labels);
+}
+
+int32_t mv_sq8_search_rerank(mv_sq8* ix, const float* x, int64_t nq, int32_t k,
+                             int32_t rerank_factor, float* distances, int64_t* labels) {
+  if (rerank_factor < 1) return MV_ERR_ARG;
+  return sq8_search_host(ix, x, nq, k, nullptr, rerank_factor, distances, labels);
+}
+
+// ---------------------------------------------------------------------------
+// primitives
+// ---------------------------------------------------------------------------
+int32_t mv_kmeans_train(mv_ctx* ctx, const float* x, int64_t n, int32_t d, int32_t k,
+                        int32_t niter, float* centroids, int64_t* assignments) {
+  if (!ctx || n < 0 || (n > 0 && (!x || !centroids)) || d <= 0 || k <= 0) return MV_ERR_ARG;
+  return guard(ctx, [&] {
+    if (n == 0) return;  // kmeans.mojo:62
+    SlotLease lease(ctx);
+    cudaStream_t s = lease.stream();
+    DevBuf dx, dc, da, scratch;
+    dx.ensure(sizeof(float) * n * d);
+    dc.ensure(sizeof(float) * k * d);
+    da.ensure(sizeof(int32_t) * n);
+    h2d(dx.p, x, sizeof(float) * n * d, s);
+    kmeans_train_device(dx.as<float>(), n, d, k, niter, 1, dc.as<float>(), da.as<int32_t>(),
+                        scratch, s);
+    d2h(centroids, dc.p, sizeof(float) * k * d, s);
+    if (assignments) {
+      DevBuf a64;
+      a64.ensure(sizeof(int64_t) * n);
+      launch_i32_to_i64(da.as<int32_t>(), n, a64.as<int64_t>(), s);
+      d2h(assignments, a64.p, sizeof(int64_t) * n, s);
+      sync(s);
+    }
+    sync(s);
+  });
+}
+
+int32_t mv_pq_train(mv_ctx* ctx, const float* x, int64_t n, int32_t d, int32_t M, int32_t niter,
+                    float* pq) {
+  if (!ctx || n <= 0 || !x || !pq || d <= 0 || M <= 0 || d % M != 0) return MV_ERR_ARG;
+  return guard(ctx, [&] {
+    SlotLease lease(ctx);
+    cudaStream_t s = lease.stream();
+    DevBuf dx, dp, work, scratch;
+    dx.ensure(sizeof(float) * n * d);
+    dp.ensure(sizeof(float) * 256 * d);
+    h2d(dx.p, x, sizeof(float) * n * d, s);
+    pq_train_device(dx.as<float>(), n, d, M, niter, dp.as<float>(), work, scratch, s);
+    d2h(pq, dp.p, sizeof(float) * 256 * d, s);
+    sync(s);
+  });
+}
+
+int32_t mv_pq_encode(mv_ctx* ctx, const float* pq, int32_t d, int32_t M, const float* x, int64_t n,
+                     uint8_t* codes) {
+  if (!ctx || !pq || d <= 0 || M <= 0 || d % M != 0 || n < 0 || (n > 0 && (!x || !codes)))
+    return MV_ERR_ARG;
+  return guard(ctx, [&] {
+    if (n == 0) return;
+    SlotLease lease(ctx);
+    cudaStream_t s = lease.stream();
+    DevBuf dx, dp, dc;
+    dx.ensure(sizeof(float) * n * d);
+    dp.ensure(sizeof(float) * 256 * d);
+    dc.ensure((size_t)n * M);
+    h2d(dx.p, x, sizeof(float) * n * d, s);
+    h2d(dp.p, pq, sizeof(float) * 256 * d, s);
+    launch_pq_encode(dx.as<float>(), n, d, M, dp.as<float>(), dc.as<uint8_t>(), s);
+    d2h(codes, dc.p, (size_t)n * M, s);
+    sync(s);
+  });
+}
+
+int32_t mv_pq_distance_tables(mv_ctx* ctx, const float* pq, int32_t d, int32_t M, const float* x,
+                              int64_t nq, int32_t metric, float* tables) {
+  if (!ctx || !pq || d <= 0 || M <= 0 || d % M != 0 || nq < 0 || (nq > 0 && (!x || !tables)))
+    return MV_ERR_ARG;
+  return guard(ctx, [&] {
+    if (nq == 0) return;
+    SlotLease lease(ctx);
+    cudaStream_t s = lease.stream();
+    DevBuf dx, dp, dt;
+    dx.ensure(sizeof(float) * nq * d);
+    dp.ensure(sizeof(float) * 256 * d);
+    dt.ensure(sizeof(float) * nq * M * 256);
+    h2d(dx.p, x, sizeof(float) * nq * d, s);
+    h2d(dp.p, pq, sizeof(float) * 256 * d, s);
+    launch_pq_tables(dx.as<float>(), nq, d, M, dp.as<float>(), metric, dt.as<float>(), s);
+    d2h(tables, dt.p, sizeof(float) * nq * M * 256, s);
+    sync(s);
+  });
+}
+
+int32_t mv_sq8_encode(mv_ctx* ctx, const float* x, int64_t n, int32_t d, float minimum,
+                      float inverse_scale, int32_t symmetric, uint8_t* codes, uint32_t* norms) {
+  if (!ctx || d <= 0 || n < 0 || (n > 0 && (!x || !codes || !norms))) return MV_ERR_ARG;
+  return guard(ctx, [&] {
+    if (n == 0) return;
+    SlotLease lease(ctx);
+    cudaStream_t s = lease.stream();
+    const int dp = (d + 15) / 16 * 16;
+    DevBuf dx, dc, dn;
+    dx.ensure(sizeof(float) * n * d);
+    dc.ensure((size_t)n * dp);
+    dn.ensure(sizeof(uint32_t) * n);
+    h2d(dx.p, x, sizeof(float) * n * d, s);
+    launch_sq8_encode(dx.as<float>(), n, d, dp, minimum, inverse_scale, symmetric != 0,
+                      dc.as<uint8_t>(), dn.as<uint32_t>(), s);
+    MV_CHECK_CUDA(cudaMemcpy2DAsync(codes, d, dc.p, dp, d, n, cudaMemcpyDeviceToHost, s));
+    d2h(norms, dn.p, sizeof(uint32_t) * n, s);
+    sync(s);
+  });
+}
+
+int32_t mv_normalize(mv_ctx* ctx, const float* x, int64_t n, int32_t d, float* out) {
+  if (!ctx || d <= 0 || n < 0 || (n > 0 && (!x || !out))) return MV_ERR_ARG;
+  return guard(ctx, [&] {
+    if (n == 0) return;
+    SlotLease lease(ctx);
+    cudaStream_t s = lease.stream();
+    DevBuf dx, dy, bad;
+    dx.ensure(sizeof(float) * n * d);
+    dy.ensure(sizeof(float) * n * d);
+    bad.ensure(4);
+    MV_CHECK_CUDA(cudaMemsetAsync(bad.p, 0, 4, s));
+    h2d(dx.p, x, sizeof(float) * n * d, s);
+    launch_normalize(dx.as<float>(), n, d, dy.as<float>(), bad.as<int32_t>(), s);
+    int32_t hb = 0;
+    d2h(&hb, bad.p, 4, s);
+    sync(s);
+    MV_REQUIRE(hb != 1, MV_ERR_ARG, "Vector components must be finite.");
+    MV_REQUIRE(hb != 2, MV_ERR_ARG, "Cosine embeddings must be non-zero vectors.");
+    d2h(out, dy.p, sizeof(float) * n * d, s);
+    sync(s);
+  });
+}
+
+}  // extern "C"

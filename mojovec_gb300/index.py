@@ -1,0 +1,385 @@
+"""Host-side mirror of MojoVec's index and quantizer interfaces, backed by
+libmojovec_gpu.so.
+
+Class and method names follow the reference so code (and tests) written
+against it read the same:
+
+* IndexIVFPQ      -> mojovec/index/index_ivf_pq.mojo:12 (train, add,
+                     add_with_ids, search, nprobe)
+* IndexFlat       -> mojovec/index/index_flat.mojo:117 (add, search)
+* IndexFlatSQ8    -> mojovec/index/index_flat_sq8.mojo:271 (add, search,
+                     scale / global_min / global_max)
+* KMeans          -> mojovec/clustering/kmeans.mojo:8 (train, centroids)
+* ProductQuantizer-> mojovec/quantization/pq.mojo:80 (train, compute_codes,
+                     decode, compute_distance_table)
+
+Search results come back as numpy arrays (distances float32 (n, k), labels
+int64 (n, k)) instead of filling caller Spans.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+import numpy as np
+
+from . import _lib
+from ._lib import METRIC_IP, METRIC_L2, SearchParams, check
+
+
+def _f32(a, d=None):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if d is not None:
+        a = a.reshape(-1, d)
+    return a
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class Context:
+    """One CUDA device (mv_ctx)."""
+
+    _default = None
+    _default_lock = threading.Lock()
+
+    def __init__(self, device: int = 0):
+        lib = _lib.load()
+        h = C.c_void_p()
+        check(lib.mv_ctx_create(device, C.byref(h)))
+        self._h = h
+        self.device = device
+
+    @classmethod
+    def default(cls) -> "Context":
+        with cls._default_lock:
+            if cls._default is None:
+                cls._default = Context(0)
+            return cls._default
+
+    @property
+    def handle(self):
+        return self._h
+
+    def synchronize(self):
+        check(_lib.load().mv_ctx_synchronize(self._h))
+
+    def kernel_launches(self) -> int:
+        return int(_lib.load().mv_ctx_kernel_launches(self._h))
+
+    def profile(self, enable: bool = True):
+        """Enables (and resets) per-stage CUDA-event timing."""
+        check(_lib.load().mv_ctx_profile(self._h, 1 if enable else 0))
+
+    def stage_times(self) -> dict:
+        """{stage: (total_ms, launches)} since the last profile(True)."""
+        n = len(_lib.STAGES)
+        ms = np.zeros(n, np.float64)
+        cnt = np.zeros(n, np.int64)
+        check(_lib.load().mv_ctx_stage_times(self._h, _p(ms), _p(cnt), n))
+        return {name: (float(ms[i]), int(cnt[i])) for i, name in enumerate(_lib.STAGES) if cnt[i]}
+
+
+def _params(form=None, nprobe=0, rerank=0, coarse_fp32=False, lut_fp16=False):
+    p = SearchParams()
+    p.form = _lib.FORM_PLAIN if form is None else int(form)
+    p.nprobe = int(nprobe)
+    p.rerank = int(rerank)
+    p.coarse_fp32 = 1 if coarse_fp32 else 0
+    p.lut_fp16 = 1 if lut_fp16 else 0
+    return p
+
+
+class IndexIVFPQ:
+    """IVF-PQ index on the GPU (index/index_ivf_pq.mojo:12)."""
+
+    def __init__(self, d: int, nlist: int, M: int, metric: int = METRIC_L2, ctx: Context | None = None):
+        self.ctx = ctx or Context.default()
+        h = C.c_void_p()
+        check(_lib.load().mv_ivfpq_create(self.ctx.handle, d, nlist, M, metric, C.byref(h)))
+        self._h = h
+        self.d, self.nlist, self.M, self.metric_type = d, nlist, M, metric
+        self.ksub = 256
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib._lib is not None:
+            _lib._lib.mv_ivfpq_destroy(h)
+            self._h = None
+
+    def _info(self):
+        out = np.zeros(7, np.int64)
+        check(_lib.load().mv_ivfpq_info(self._h, _p(out)))
+        return out
+
+    @property
+    def nprobe(self) -> int:
+        return int(self._info()[3])
+
+    @nprobe.setter
+    def nprobe(self, v: int):
+        check(_lib.load().mv_ivfpq_set_nprobe(self._h, int(v)))
+
+    @property
+    def ntotal(self) -> int:
+        return int(self._info()[4])
+
+    @property
+    def is_trained(self) -> bool:
+        return bool(self._info()[6])
+
+    def set_codebooks(self, centroids, pq_centroids):
+        """Loads trained coarse centroids (nlist, d) and PQ codebooks
+        (M, 256, d/M), e.g. the reference's own, and marks the index trained."""
+        c = _f32(centroids)
+        p = _f32(pq_centroids)
+        assert c.size == self.nlist * self.d and p.size == 256 * self.d
+        check(_lib.load().mv_ivfpq_set_codebooks(self._h, _p(c), _p(p)))
+
+    def codebooks(self):
+        c = np.zeros((self.nlist, self.d), np.float32)
+        p = np.zeros((self.M, 256, self.d // self.M), np.float32)
+        check(_lib.load().mv_ivfpq_get_codebooks(self._h, _p(c), _p(p)))
+        return c, p
+
+    def train(self, x, niter_coarse: int = 15, niter_pq: int = 15):
+        """IndexIVFPQ.train; the reference hard-codes 15 iterations for both
+        k-means runs (index_ivf_pq.mojo:98, pq.mojo:64)."""
+        x = _f32(x, self.d)
+        check(_lib.load().mv_ivfpq_train(self._h, _p(x), x.shape[0], niter_coarse, niter_pq))
+
+    def add(self, x):
+        x = _f32(x, self.d)
+        check(_lib.load().mv_ivfpq_add(self._h, _p(x), x.shape[0]))
+
+    def add_with_ids(self, x, ids):
+        x = _f32(x, self.d)
+        ids = np.ascontiguousarray(ids, dtype=np.int64)
+        assert ids.shape[0] == x.shape[0]
+        check(_lib.load().mv_ivfpq_add_with_ids(self._h, _p(x), _p(ids), x.shape[0]))
+
+    def lists(self):
+        """CSR export: (offsets (nlist+1,), ids (ntotal,), codes (ntotal, M))."""
+        off = np.zeros(self.nlist + 1, np.int64)
+        check(_lib.load().mv_ivfpq_get_lists(self._h, _p(off), None, None))
+        n = int(off[-1])
+        ids = np.zeros(max(n, 1), np.int64)
+        codes = np.zeros((max(n, 1), self.M), np.uint8)
+        check(_lib.load().mv_ivfpq_get_lists(self._h, None, _p(ids), _p(codes)))
+        return off, ids[:n], codes[:n]
+
+    def search(self, x, k: int, filter=None, form=None, nprobe: int = 0, rerank: int = 0,
+               coarse_fp32: bool = False, lut_fp16: bool = False):
+        x = _f32(x, self.d)
+        n = x.shape[0]
+        dist = np.empty((n, k), np.float32)
+        lab = np.empty((n, k), np.int64)
+        flt = None if filter is None else np.ascontiguousarray(filter, dtype=np.uint8)
+        p = _params(form, nprobe, rerank, coarse_fp32, lut_fp16)
+        check(_lib.load().mv_ivfpq_search(self._h, _p(x), n, k, _p(flt),
+                                          0 if flt is None else flt.size, C.byref(p), _p(dist),
+                                          _p(lab)))
+        return dist, lab
+
+    def search_device(self, x_ptr: int, n: int, k: int, dist_ptr: int, lab_ptr: int,
+                      stream: int = 0, form=None, nprobe: int = 0, rerank: int = 0,
+                      coarse_fp32: bool = False, lut_fp16: bool = False):
+        """Device-pointer search (e.g. torch tensors' data_ptr())."""
+        p = _params(form, nprobe, rerank, coarse_fp32, lut_fp16)
+        check(_lib.load().mv_ivfpq_search_device(self._h, x_ptr, n, k, None, 0, C.byref(p),
+                                                 dist_ptr, lab_ptr, stream or None))
+
+
+class IndexFlat:
+    """Exact index over raw FP32 rows (index/index_flat.mojo:117)."""
+
+    def __init__(self, d: int, metric: int = METRIC_L2, ctx: Context | None = None):
+        self.ctx = ctx or Context.default()
+        h = C.c_void_p()
+        check(_lib.load().mv_flat_create(self.ctx.handle, d, metric, C.byref(h)))
+        self._h = h
+        self.d, self.metric_type = d, metric
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib._lib is not None:
+            _lib._lib.mv_flat_destroy(h)
+            self._h = None
+
+    @property
+    def ntotal(self) -> int:
+        return int(_lib.load().mv_flat_ntotal(self._h))
+
+    def add(self, x):
+        x = _f32(x, self.d)
+        check(_lib.load().mv_flat_add(self._h, _p(x), x.shape[0]))
+
+    def search(self, x, k: int, filter=None, form=None, rerank: int = 0):
+        x = _f32(x, self.d)
+        n = x.shape[0]
+        dist = np.empty((n, k), np.float32)
+        lab = np.empty((n, k), np.int64)
+        flt = None if filter is None else np.ascontiguousarray(filter, dtype=np.uint8)
+        p = _params(form, 0, rerank)
+        check(_lib.load().mv_flat_search(self._h, _p(x), n, k, _p(flt), C.byref(p), _p(dist),
+                                         _p(lab)))
+        return dist, lab
+
+    def search_device(self, x_ptr: int, n: int, k: int, dist_ptr: int, lab_ptr: int,
+                      stream: int = 0, form=None, rerank: int = 0):
+        p = _params(form, 0, rerank)
+        check(_lib.load().mv_flat_search_device(self._h, x_ptr, n, k, None, C.byref(p), dist_ptr,
+                                                lab_ptr, stream or None))
+
+
+class IndexFlatSQ8:
+    """SQ8 brute-force index (index/index_flat_sq8.mojo:271)."""
+
+    def __init__(self, d: int, metric: int = METRIC_L2, ctx: Context | None = None):
+        self.ctx = ctx or Context.default()
+        h = C.c_void_p()
+        check(_lib.load().mv_sq8_create(self.ctx.handle, d, metric, C.byref(h)))
+        self._h = h
+        self.d, self.metric_type = d, metric
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib._lib is not None:
+            _lib._lib.mv_sq8_destroy(h)
+            self._h = None
+
+    def _params(self):
+        out = np.zeros(3, np.float32)
+        check(_lib.load().mv_sq8_params(self._h, _p(out)))
+        return out
+
+    @property
+    def global_min(self) -> float:
+        return float(self._params()[0])
+
+    @property
+    def global_max(self) -> float:
+        return float(self._params()[1])
+
+    @property
+    def scale(self) -> float:
+        return float(self._params()[2])
+
+    @property
+    def ntotal(self) -> int:
+        return int(_lib.load().mv_sq8_ntotal(self._h))
+
+    def add(self, x):
+        x = _f32(x, self.d)
+        check(_lib.load().mv_sq8_add(self._h, _p(x), x.shape[0]))
+
+    def codes(self):
+        n = self.ntotal
+        c = np.zeros((max(n, 1), self.d), np.uint8)
+        nm = np.zeros(max(n, 1), np.uint32)
+        check(_lib.load().mv_sq8_get_codes(self._h, _p(c), _p(nm)))
+        return c[:n], nm[:n]
+
+    def search(self, x, k: int, filter=None):
+        x = _f32(x, self.d)
+        n = x.shape[0]
+        dist = np.empty((n, k), np.float32)
+        lab = np.empty((n, k), np.int64)
+        flt = None if filter is None else np.ascontiguousarray(filter, dtype=np.uint8)
+        check(_lib.load().mv_sq8_search(self._h, _p(x), n, k, _p(flt), _p(dist), _p(lab)))
+        return dist, lab
+
+    def search_rerank(self, x, k: int, rerank_factor: int = 2):
+        x = _f32(x, self.d)
+        n = x.shape[0]
+        dist = np.empty((n, k), np.float32)
+        lab = np.empty((n, k), np.int64)
+        check(_lib.load().mv_sq8_search_rerank(self._h, _p(x), n, k, rerank_factor, _p(dist),
+                                               _p(lab)))
+        return dist, lab
+
+
+class KMeans:
+    """KMeans(d, k, niter) (clustering/kmeans.mojo:8), plain exact form."""
+
+    def __init__(self, d: int, k: int, niter: int = 15, ctx: Context | None = None):
+        self.ctx = ctx or Context.default()
+        self.d, self.k, self.niter = d, k, niter
+        self.centroids = np.zeros((k, d), np.float32)
+        self.assignments = np.zeros(0, np.int64)
+
+    def train(self, x):
+        x = _f32(x, self.d)
+        n = x.shape[0]
+        self.assignments = np.zeros(n, np.int64)
+        check(_lib.load().mv_kmeans_train(self.ctx.handle, _p(x), n, self.d, self.k, self.niter,
+                                          _p(self.centroids), _p(self.assignments)))
+        return self.centroids
+
+
+class ProductQuantizer:
+    """ProductQuantizer(d, M, 256) (quantization/pq.mojo:80)."""
+
+    def __init__(self, d: int, M: int, ksub: int = 256, ctx: Context | None = None):
+        if ksub != 256:
+            raise ValueError("the GPU product quantizer uses 256 centroids per subspace")
+        if M <= 0 or M > d or d % M != 0:
+            raise ValueError("PQ M must divide dimension and be between 1 and dimension.")
+        self.ctx = ctx or Context.default()
+        self.d, self.M, self.ksub, self.dsub = d, M, ksub, d // M
+        self.centroids = np.zeros((M, ksub, d // M), np.float32)
+        self.is_trained = False
+
+    def train(self, x, niter: int = 15):
+        x = _f32(x, self.d)
+        check(_lib.load().mv_pq_train(self.ctx.handle, _p(x), x.shape[0], self.d, self.M, niter,
+                                      _p(self.centroids)))
+        self.is_trained = True
+
+    def compute_codes(self, x):
+        x = _f32(x, self.d)
+        n = x.shape[0]
+        codes = np.zeros((n, self.M), np.uint8)
+        check(_lib.load().mv_pq_encode(self.ctx.handle, _p(self.centroids), self.d, self.M, _p(x),
+                                       n, _p(codes)))
+        return codes
+
+    def decode(self, codes):
+        codes = np.asarray(codes, np.uint8).reshape(-1, self.M)
+        out = np.empty((codes.shape[0], self.M, self.dsub), np.float32)
+        for m in range(self.M):
+            out[:, m, :] = self.centroids[m][codes[:, m]]
+        return out.reshape(codes.shape[0], self.d)
+
+    def compute_distance_table(self, x, metric: int = METRIC_L2):
+        x = _f32(x, self.d)
+        n = x.shape[0]
+        t = np.zeros((n, self.M, self.ksub), np.float32)
+        check(_lib.load().mv_pq_distance_tables(self.ctx.handle, _p(self.centroids), self.d,
+                                                self.M, _p(x), n, metric, _p(t)))
+        return t
+
+
+def sq8_encode(x, minimum: float, inverse_scale: float, symmetric: bool, ctx: Context | None = None):
+    """_encode_sq8_batch (quantization/sq8.mojo:41-59) on the GPU."""
+    ctx = ctx or Context.default()
+    x = _f32(x)
+    n, d = x.shape
+    codes = np.zeros((n, d), np.uint8)
+    norms = np.zeros(n, np.uint32)
+    check(_lib.load().mv_sq8_encode(ctx.handle, _p(x), n, d, minimum, inverse_scale,
+                                    1 if symmetric else 0, _p(codes), _p(norms)))
+    return codes, norms
+
+
+def normalize(x, ctx: Context | None = None):
+    """_normalize_vectors (api/collection_vector_query.mojo:24-46) on the GPU."""
+    ctx = ctx or Context.default()
+    x = _f32(x)
+    out = np.empty_like(x)
+    st = _lib.load().mv_normalize(ctx.handle, _p(x), x.shape[0], x.shape[1], _p(out))
+    if st != 0:
+        raise ValueError(_lib.last_error())
+    return out
