@@ -71,11 +71,17 @@ __host__ __device__ __forceinline__ int next_pow2(int v) {
 //
 // Protocol per round: every thread calls push() with at most one key, then
 // the whole block calls end_round(). finish() leaves keys[0, k) sorted.
+// The flush decision uses a per-thread copy of the pending count that is
+// advanced by __syncthreads_count, so it is the same in every thread: a
+// thread that has already started the next round cannot change another
+// thread's decision through the shared counter.
 struct BlockTopK {
   uint64_t* keys;
-  int* count;          // shared counter
+  int* count;          // shared slot allocator
   uint64_t* thresh;    // shared: k-th best so far (KEY_NONE until k found)
   int k, bufcap, P;
+  int pending;         // keys in the buffer (uniform across the block)
+  bool pushed;         // this thread pushed in the current round
 
   static __host__ __device__ int smem_keys(int k, int bufcap) { return next_pow2(k + bufcap); }
 
@@ -86,6 +92,8 @@ struct BlockTopK {
     k = k_;
     bufcap = bufcap_;
     P = next_pow2(k + bufcap);
+    pending = 0;
+    pushed = false;
     for (int i = threadIdx.x; i < P; i += blockDim.x) keys[i] = KEY_NONE;
     if (threadIdx.x == 0) {
       *count = 0;
@@ -106,6 +114,7 @@ struct BlockTopK {
     if (key < *thresh) {
       int pos = atomicAdd(count, 1);
       keys[k + pos] = key;
+      pushed = true;
     }
   }
 
@@ -116,18 +125,21 @@ struct BlockTopK {
       *count = 0;
       *thresh = keys[k - 1];
     }
+    pending = 0;
     __syncthreads();
   }
 
   // Call after every round; guarantees room for one key per thread next round.
   __device__ void end_round() {
-    __syncthreads();
-    if (*count > bufcap - (int)blockDim.x) flush();
+    pending += __syncthreads_count(pushed ? 1 : 0);
+    pushed = false;
+    if (pending > bufcap - (int)blockDim.x) flush();
   }
 
   __device__ void finish() {
-    __syncthreads();
-    if (*count > 0) flush();
+    pending += __syncthreads_count(pushed ? 1 : 0);
+    pushed = false;
+    if (pending > 0) flush();
   }
 };
 

@@ -985,6 +985,17 @@ void orc_ivfpq_add(void* h, const float* x, int64_t n, int nthreads) {
   ivfpq_add_with_ids(ix, x, n, ids.data(), nthreads);
 }
 int64_t orc_ivfpq_ntotal(void* h) { return static_cast<IVFPQ*>(h)->ntotal; }
+// Loads CSR lists (offsets[nlist+1], ids, codes) in place of adds; ntotal
+// becomes offsets[nlist]. Used to search an index built elsewhere.
+void orc_ivfpq_set_lists(void* h, const int64_t* offsets, const int64_t* ids,
+                         const uint8_t* codes) {
+  auto& ix = *static_cast<IVFPQ*>(h);
+  for (int l = 0; l < ix.nlist; ++l) {
+    ix.list_ids[l].assign(ids + offsets[l], ids + offsets[l + 1]);
+    ix.list_codes[l].assign(codes + offsets[l] * ix.M, codes + offsets[l + 1] * ix.M);
+  }
+  ix.ntotal = offsets[ix.nlist];
+}
 // Exports the lists as CSR: offsets[nlist+1], ids[ntotal], codes[ntotal*M].
 void orc_ivfpq_get_lists(void* h, int64_t* offsets, int64_t* ids, uint8_t* codes) {
   auto& ix = *static_cast<IVFPQ*>(h);

@@ -73,6 +73,7 @@ def lib():
     _sig(L, "orc_ivfpq_add", None, [_vp, _f32p, _i64, _int])
     _sig(L, "orc_ivfpq_ntotal", _i64, [_vp])
     _sig(L, "orc_ivfpq_get_lists", None, [_vp, _i64p, _i64p, _u8p])
+    _sig(L, "orc_ivfpq_set_lists", None, [_vp, _i64p, _i64p, _u8p])
     _sig(L, "orc_ivfpq_search", None,
          [_vp, _f32p, _i64, _i64, _i64, _vp, _i64, _int, _f32p, _i64p, _int, _int])
     _sig(L, "orc_sq8_create", _vp, [_int, _int])
@@ -270,6 +271,11 @@ class IVFPQ:
         codes = np.zeros((max(n, 1), self.M), np.uint8)
         lib().orc_ivfpq_get_lists(self._h, off, ids, codes)
         return off, ids[:n], codes[:n]
+
+    def set_lists(self, offsets, ids, codes):
+        lib().orc_ivfpq_set_lists(self._h, np.ascontiguousarray(offsets, np.int64),
+                                  np.ascontiguousarray(ids, np.int64),
+                                  np.ascontiguousarray(codes, np.uint8))
 
     def search(self, q, k, nprobe, filter=None, mode=MODE_CANONICAL, nthreads=0, lut_threads=1):
         q = _f32(q)
