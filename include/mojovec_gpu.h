@@ -196,6 +196,13 @@ int32_t mv_pq_distance_tables(mv_ctx* ctx, const float* pq, int32_t d, int32_t M
 /* _encode_sq8_batch (quantization/sq8.mojo:41-59). */
 int32_t mv_sq8_encode(mv_ctx* ctx, const float* x, int64_t n, int32_t d, float minimum,
                       float inverse_scale, int32_t symmetric, uint8_t* codes, uint32_t* norms);
+/* Distance matrix out[nx*ny] between rows of x and y (host buffers).
+ * precision 0: exact FP32 in the reference's l2_distance_simd[8] /
+ * -inner_product_simd[8] order (distances.mojo:43-228);
+ * precision 1: BF16 tensor cores (tcgen05) with FP32 accumulation,
+ * ||x||^2 + ||y||^2 - 2 x.y over the BF16-rounded rows (d <= 256). */
+int32_t mv_distance_matrix(mv_ctx* ctx, const float* x, int64_t nx, const float* y, int64_t ny,
+                           int32_t d, int32_t metric, int32_t precision, float* out);
 /* _normalize_vectors (api/collection_vector_query.mojo:24-46): FP64 sum of
  * squares, 1/sqrt in FP64. Returns MV_ERR_ARG for non-finite or zero rows. */
 int32_t mv_normalize(mv_ctx* ctx, const float* x, int64_t n, int32_t d, float* out);

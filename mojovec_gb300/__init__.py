@@ -21,6 +21,7 @@ from .index import (  # noqa: F401
     IndexFlatSQ8,
     IndexIVFPQ,
     KMeans,
+    distance_matrix,
     ProductQuantizer,
     normalize,
     sq8_encode,

@@ -109,6 +109,7 @@ SIGNATURES = {
     "mv_pq_distance_tables": (_i32, [_vp, _vp, _i32, _i32, _vp, _i64, _i32, _vp]),
     "mv_sq8_encode": (_i32, [_vp, _vp, _i64, _i32, _f32, _f32, _i32, _vp, _vp]),
     "mv_normalize": (_i32, [_vp, _vp, _i64, _i32, _vp]),
+    "mv_distance_matrix": (_i32, [_vp, _vp, _i64, _vp, _i64, _i32, _i32, _i32, _vp]),
 }
 
 _lib = None

@@ -1,0 +1,375 @@
+// BF16 tensor-core distance GEMM for sm_103a (tcgen05 + TMA + TMEM).
+//
+// Computes the dense query x base (or query x centroid) inner products that
+// dominate the coarse quantizer (index/index_flat.mojo:260-325 used with
+// k = nprobe), the flat scan and the k-means assign step
+// (clustering/kmeans.mojo:114-161), and turns them into distances in the
+// epilogue: L2 ||x||^2 + ||y||^2 - 2 x.y, IP -x.y.
+//
+// Layout: X (rows) and Y (cols) are BF16, row-major, rows padded with zeros
+// to Kp = 64 * nkb elements. One work item is a 128 x BN output tile; CTAs
+// are persistent (one per SM) and walk the items column-tile-major, so the
+// CTAs running at the same time share the same Y tile through L2 while the
+// small X row blocks stay L2-resident.
+//
+// Warp roles (192 threads):
+//   warp 0      TMA producer: per item, the 128-row X tile and BN-row Y tile
+//               (nkb k-blocks of 64 BF16 = one 128-byte swizzle row each)
+//               into a 2-stage ring, completion on full[s].
+//   warp 1      allocates 2*BN TMEM columns; lane 0 issues the UMMAs
+//               (tcgen05.mma kind::f16, M = 128, N = BN, K = 16 per
+//               instruction) into accumulator (item & 1) and commits
+//               empty[s] / tfull[acc].
+//   warps 2-5   epilogue: tcgen05.ld 32 columns at a time from their TMEM
+//               lane quarter, apply the distance formula, then store the
+//               distance matrix (EPI_MATRIX) or fold a per-row argmin into a
+//               64-bit (distance, column) key with atomicMin (EPI_ARGMIN).
+// Every mbarrier wait is bounded (2 s); on timeout the kernel records an
+// error flag, drains what it issued and frees its TMEM.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include <mutex>
+
+#include "mv_internal.h"
+#include "mv_kernels.h"
+#include "mv_select.cuh"
+#include "mv_sm100.cuh"
+#include "mv_umma.h"
+
+namespace mv {
+namespace {
+
+using namespace sm100;
+
+constexpr int BM = 128;
+constexpr int STAGES = 2;
+constexpr int NUM_THREADS = 192;
+
+template <int BN>
+struct Smem {
+  static constexpr uint32_t a_bytes_kb = BM * 128;  // one k-block of the X tile
+  static constexpr uint32_t b_bytes_kb = BN * 128;
+  static __host__ __device__ uint32_t stage_bytes(int nkb) { return (uint32_t)nkb * (a_bytes_kb + b_bytes_kb); }
+  static __host__ __device__ size_t total(int nkb) { return 1024 + (size_t)STAGES * stage_bytes(nkb) + 256; }
+};
+
+template <int BN, int EPI>
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+    k_umma_dist(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUtensorMap ty,
+                UmmaArgs g) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  const int nkb = g.nkb;
+  const uint32_t stage_bytes = Smem<BN>::stage_bytes(nkb);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * stage_bytes);
+  uint32_t* holder = reinterpret_cast<uint32_t*>(bars + 12);
+  __shared__ int s_err;
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const uint32_t bar0 = smem_u32(bars);
+  // bars[0..1] full, [2..3] empty, [4..5] tfull, [6..7] tempty, [8] done
+  auto b_full = [&](int s) { return bar0 + 8u * s; };
+  auto b_empty = [&](int s) { return bar0 + 8u * (2 + s); };
+  auto b_tfull = [&](int a) { return bar0 + 8u * (4 + a); };
+  auto b_tempty = [&](int a) { return bar0 + 8u * (6 + a); };
+  const uint32_t b_done = bar0 + 8u * 8;
+
+  if (threadIdx.x == 0) {
+    s_err = 0;
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(b_full(s), 1);
+      mbar_init(b_empty(s), 1);
+    }
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(b_tfull(a), 1);
+      mbar_init(b_tempty(a), 128);
+    }
+    mbar_init(b_done, 1);
+    fence_mbar_init();
+  }
+  if (warp == 0 && lane == 0) {
+    prefetch_tmap(&tx);
+    prefetch_tmap(&ty);
+  }
+  if (warp == 1) tmem_alloc(smem_u32(holder), 2 * BN);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(holder);
+
+  const int nrb = (g.nrows + BM - 1) / BM;
+  const int nct = (g.ncols + BN - 1) / BN;
+  const int64_t total = (int64_t)nrb * nct;
+  const int64_t first = blockIdx.x;
+  const int64_t step = gridDim.x;
+  const int my_count = first < total ? (int)((total - 1 - first) / step + 1) : 0;
+  volatile int* verr = &s_err;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int i = 0;
+      for (; i < my_count; ++i) {
+        const int s = i % STAGES;
+        const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
+        if (*verr || !mbar_wait(b_empty(s), ph ^ 1u)) {
+          *verr = 1;
+          break;
+        }
+        const int64_t w = first + (int64_t)i * step;
+        const int ct = (int)(w / nrb);
+        const int rb = (int)(w - (int64_t)ct * nrb);
+        uint8_t* st = smem + (size_t)s * stage_bytes;
+        mbar_arrive_expect_tx(b_full(s), stage_bytes);
+        for (int kb = 0; kb < nkb; ++kb) {
+          tma_load_2d(smem_u32(st + kb * Smem<BN>::a_bytes_kb), &tx, kb * 64, rb * BM, b_full(s));
+          tma_load_2d(smem_u32(st + nkb * Smem<BN>::a_bytes_kb + kb * Smem<BN>::b_bytes_kb), &ty,
+                      kb * 64, ct * BN, b_full(s));
+        }
+      }
+      // Drain: every issued load must land before the CTA exits.
+      for (int j = (i > STAGES ? i - STAGES : 0); j < i; ++j)
+        if (!mbar_wait(b_full(j % STAGES), (uint32_t)(j / STAGES) & 1u)) *verr = 1;
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_f32(BM, BN);
+      for (int i = 0; i < my_count; ++i) {
+        const int s = i % STAGES;
+        const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
+        const int acc = i & 1;
+        const uint32_t aph = (uint32_t)(i >> 1) & 1u;
+        if (*verr || !mbar_wait(b_tempty(acc), aph ^ 1u) || !mbar_wait(b_full(s), ph)) {
+          *verr = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint8_t* st = smem + (size_t)s * stage_bytes;
+        const uint32_t d = tmem + (uint32_t)(acc * BN);
+        for (int kb = 0; kb < nkb; ++kb) {
+          const uint64_t ad = desc_k_sw128(smem_u32(st + kb * Smem<BN>::a_bytes_kb));
+          const uint64_t bd =
+              desc_k_sw128(smem_u32(st + nkb * Smem<BN>::a_bytes_kb + kb * Smem<BN>::b_bytes_kb));
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk)  // 4 x K16 per 64-element k-block (+32 B each)
+            umma_bf16(d, ad + 2u * kk, bd + 2u * kk, idesc, (kb | kk) ? 1u : 0u);
+        }
+        umma_commit(b_empty(s));
+        umma_commit(b_tfull(acc));
+      }
+      umma_commit(b_done);
+    }
+  } else {
+    const int q = warp & 3;  // TMEM lane quarter of this warp
+    const int rloc = q * 32 + lane;
+    for (int i = 0; i < my_count; ++i) {
+      const int acc = i & 1;
+      const uint32_t aph = (uint32_t)(i >> 1) & 1u;
+      bool ok = !*verr && mbar_wait(b_tfull(acc), aph);
+      if (!__all_sync(0xffffffffu, ok)) {
+        *verr = 1;
+        break;
+      }
+      tc_fence_after();
+      const int64_t w = first + (int64_t)i * step;
+      const int ct = (int)(w / nrb);
+      const int rb = (int)(w - (int64_t)ct * nrb);
+      const int64_t row = (int64_t)rb * BM + rloc;
+      const bool row_ok = row < g.nrows;
+      const float rn = (row_ok && g.rnorm) ? g.rnorm[row] : 0.0f;
+      uint64_t best = KEY_NONE;
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        float v[32];
+        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + c0), v);
+        const int64_t col0 = (int64_t)ct * BN + c0;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int64_t col = col0 + j;
+          float dist;
+          if (g.metric == MV_METRIC_L2) {
+            const float cn = (col < g.ncols) ? __ldg(g.cnorm + col) : 0.0f;
+            dist = rn + cn - 2.0f * v[j];
+          } else {
+            dist = -v[j];
+          }
+          v[j] = dist;
+        }
+        if (EPI == EPI_MATRIX) {
+          if (row_ok) {
+            float* o = g.out + row * g.ldo + col0;
+            if (col0 + 32 <= g.ncols && (g.ldo & 3) == 0) {
+#pragma unroll
+              for (int j = 0; j < 32; j += 4)
+                *reinterpret_cast<float4*>(o + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+            } else {
+              for (int j = 0; j < 32; ++j)
+                if (col0 + j < g.ncols) o[j] = v[j];
+            }
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            if (col0 + j < g.ncols) {
+              uint64_t key = make_key(v[j], (uint32_t)(col0 + j));
+              best = key < best ? key : best;
+            }
+          }
+        }
+      }
+      if (EPI == EPI_ARGMIN && row_ok && best != KEY_NONE)
+        atomicMin(reinterpret_cast<unsigned long long*>(g.keys + row), (unsigned long long)best);
+      tc_fence_before();
+      mbar_arrive(b_tempty(acc));
+    }
+  }
+  __syncthreads();
+  if (warp == 1) {
+    bool done = true;
+    if (lane == 0) done = mbar_wait(b_done, 0);
+    done = __shfl_sync(0xffffffffu, done, 0);
+    if (!done && lane == 0) *verr = 1;
+    tc_fence_after();
+    tmem_dealloc(tmem, 2 * BN);
+  }
+  if (threadIdx.x == 0 && *verr && g.err) atomicExch(g.err, 1);
+}
+
+__global__ void k_to_bf16(const float* __restrict__ x, int64_t n, int d, int kp,
+                          __nv_bfloat16* __restrict__ out, float* __restrict__ norms) {
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= n) return;
+  float acc = 0.0f;
+  for (int j = lane; j < kp; j += 32) {
+    float v = j < d ? x[row * d + j] : 0.0f;
+    __nv_bfloat16 b = __float2bfloat16_rn(v);
+    out[row * kp + j] = b;
+    float r = __bfloat162float(b);
+    acc = fmaf(r, r, acc);
+  }
+  for (int s = 16; s > 0; s >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, s);
+  if (norms && lane == 0) norms[row] = acc;
+}
+
+__global__ void k_fill_keys(uint64_t* keys, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) keys[i] = KEY_NONE;
+}
+
+__global__ void k_keys_argmin(const uint64_t* __restrict__ keys, int64_t n, int32_t* __restrict__ out,
+                              float* __restrict__ dist) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t k = keys[i];
+  out[i] = k == KEY_NONE ? 0 : (int32_t)key_id(k);
+  if (dist) dist[i] = k == KEY_NONE ? 0.0f : key_dist(k);
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  MV_REQUIRE(fn != nullptr, MV_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+  return fn;
+}
+
+CUtensorMap make_tmap(const void* base, int64_t rows, int kp, int box_rows) {
+  MV_REQUIRE((reinterpret_cast<uintptr_t>(base) & 15) == 0, MV_ERR_INTERNAL, "TMA base not 16-byte aligned");
+  MV_REQUIRE(kp % 64 == 0, MV_ERR_INTERNAL, "TMA rows must be padded to 64 elements");
+  CUtensorMap tm;
+  cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)kp * 2};
+  cuuint32_t box[2] = {64, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode_fn()(&tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims,
+                           strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  MV_REQUIRE(r == CUDA_SUCCESS, MV_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return tm;
+}
+
+template <int BN, int EPI>
+void launch_bn(const UmmaArgs& g, const CUtensorMap& tx, const CUtensorMap& ty, int num_sms,
+               cudaStream_t s) {
+  const size_t smem = Smem<BN>::total(g.nkb);
+  MV_REQUIRE(smem <= 227 * 1024, MV_ERR_UNSUPPORTED, "BF16 GEMM: dimension too large");
+  MV_CHECK_CUDA(cudaFuncSetAttribute(k_umma_dist<BN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+  const int64_t items = (int64_t)((g.nrows + BM - 1) / BM) * ((g.ncols + BN - 1) / BN);
+  const int grid = (int)std::min<int64_t>(items, num_sms);
+  k_umma_dist<BN, EPI><<<grid, NUM_THREADS, smem, s>>>(tx, ty, g);
+  count_launch();
+  MV_CHECK_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+int umma_kpad(int d) { return (d + 63) / 64 * 64; }
+
+void launch_to_bf16(const float* x, int64_t n, int d, __nv_bfloat16* out, float* norms,
+                    cudaStream_t s) {
+  if (n == 0) return;
+  k_to_bf16<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(x, n, d, umma_kpad(d), out, norms);
+  count_launch();
+  MV_CHECK_CUDA(cudaGetLastError());
+}
+
+void launch_umma_dist(int epi, const __nv_bfloat16* X, int64_t nx, const __nv_bfloat16* Y,
+                      int64_t ny, int d, int metric, const float* xnorm, const float* ynorm,
+                      float* out, int64_t ldo, uint64_t* keys, int* err, int num_sms,
+                      cudaStream_t s) {
+  if (nx == 0 || ny == 0) return;
+  const int kp = umma_kpad(d);
+  MV_REQUIRE(kp <= 256, MV_ERR_UNSUPPORTED, "BF16 GEMM supports d <= 256");
+  MV_REQUIRE(nx < (1ll << 31) && ny < (1ll << 31), MV_ERR_UNSUPPORTED, "GEMM too large");
+  UmmaArgs g;
+  g.nrows = nx;
+  g.ncols = ny;
+  g.nkb = kp / 64;
+  g.metric = metric;
+  g.rnorm = xnorm;
+  g.cnorm = ynorm;
+  g.out = out;
+  g.ldo = ldo;
+  g.keys = keys;
+  g.err = err;
+  // Widest Y tile whose 2-stage ring fits in shared memory: BN = 256 up to
+  // d = 128, 128 up to d = 192, 64 up to d = 256.
+  const int bn = g.nkb <= 2 ? 256 : (g.nkb == 3 ? 128 : 64);
+  const CUtensorMap tx = make_tmap(X, nx, kp, BM);
+  const CUtensorMap ty = make_tmap(Y, ny, kp, bn);
+  if (epi == EPI_ARGMIN) {
+    k_fill_keys<<<(unsigned)((nx + 255) / 256), 256, 0, s>>>(keys, nx);
+    count_launch();
+  }
+  if (bn == 256) {
+    if (epi == EPI_MATRIX) launch_bn<256, EPI_MATRIX>(g, tx, ty, num_sms, s);
+    else launch_bn<256, EPI_ARGMIN>(g, tx, ty, num_sms, s);
+  } else if (bn == 128) {
+    if (epi == EPI_MATRIX) launch_bn<128, EPI_MATRIX>(g, tx, ty, num_sms, s);
+    else launch_bn<128, EPI_ARGMIN>(g, tx, ty, num_sms, s);
+  } else {
+    if (epi == EPI_MATRIX) launch_bn<64, EPI_MATRIX>(g, tx, ty, num_sms, s);
+    else launch_bn<64, EPI_ARGMIN>(g, tx, ty, num_sms, s);
+  }
+}
+
+void launch_keys_argmin(const uint64_t* keys, int64_t n, int32_t* out, float* dist, cudaStream_t s) {
+  if (n == 0) return;
+  k_keys_argmin<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(keys, n, out, dist);
+  count_launch();
+  MV_CHECK_CUDA(cudaGetLastError());
+}
+
+}  // namespace mv

@@ -11,8 +11,10 @@
 #include <memory>
 #include <new>
 
+#include "mv_fast.h"
 #include "mv_internal.h"
 #include "mv_kernels.h"
+#include "mv_umma.h"
 
 namespace mv {
 
@@ -220,6 +222,8 @@ int32_t mv_ctx_create(int32_t device, mv_ctx** out) {
     ctx->num_sms = prop.multiProcessorCount;
     ctx->smem_optin = prop.sharedMemPerBlockOptin;
     MV_CHECK_CUDA(cudaStreamCreateWithFlags(&ctx->main_stream, cudaStreamNonBlocking));
+    ctx->d_err.ensure(sizeof(int));
+    MV_CHECK_CUDA(cudaMemset(ctx->d_err.p, 0, sizeof(int)));
     *out = ctx.release();
   });
 }
@@ -372,6 +376,145 @@ void ivfpq_search_plain(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int n
     a.out_l = d_lab + q0 * k;
     StageTimer t(ix->ctx, MV_STAGE_SCAN, s);
     launch_ivfpq_scan_plain(a, s);
+  }
+}
+
+// Reads and clears the context's kernel error flag (after a stream sync).
+void check_kernel_errors(mv_ctx* ctx, cudaStream_t s) {
+  int e = 0;
+  d2h(&e, ctx->d_err.p, sizeof(int), s);
+  sync(s);
+  if (e) {
+    MV_CHECK_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, sizeof(int), s));
+    sync(s);
+    throw Error(MV_ERR_TIMEOUT, "a tensor-core kernel gave up waiting (bounded wait expired)");
+  }
+}
+
+// Builds the fast-form side structures once per index state: BF16
+// centroids and their norms, and the per-vector term ||y||^2 + 2<c, y>.
+void ensure_fast(mv_ivfpq* ix, cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(ix->fast_mu);
+  if (ix->fast_ready) return;
+  const int kp = umma_kpad(ix->d);
+  ix->d_cent_bf16.ensure((size_t)ix->nlist * kp * 2);
+  ix->d_cnorm.ensure((size_t)ix->nlist * 4);
+  launch_to_bf16(ix->centroids.as<float>(), ix->nlist, ix->d, ix->d_cent_bf16.as<__nv_bfloat16>(),
+                 ix->d_cnorm.as<float>(), s);
+  const int64_t total = ix->h_off[ix->nlist];
+  if (ix->metric == MV_METRIC_L2 && total > 0) {
+    ix->d_vec_term.ensure((size_t)total * 4);
+    launch_vec_terms(ix->d_off.as<int64_t>(), ix->nlist, ix->d_codes.as<uint8_t>(),
+                     ix->pq.as<float>(), ix->centroids.as<float>(), ix->d, ix->M,
+                     ix->d_vec_term.as<float>(), s);
+  }
+  sync(s);
+  ix->fast_ready = true;
+}
+
+// Fast-form IVF-PQ search (BF16 coarse GEMM + exact FP32 recheck, one LUT
+// per query with precomputed per-vector terms, exact FP32 rerank).
+void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int nprobe,
+                       const mv_search_params* p, float* d_out, int64_t* d_lab, DevBuf& ws,
+                       cudaStream_t s) {
+  if (nq == 0) return;
+  if (!ix->trained || ix->ntotal == 0) {
+    launch_fill(d_out, d_lab, nq * k, 1e38f, s);
+    return;
+  }
+  ensure_fast(ix, s);
+  const bool fp32_coarse = p && p->coarse_fp32;
+  const int R = std::max(k, (p && p->rerank > 0) ? (int)p->rerank : k);
+  MV_REQUIRE(R <= 4096, MV_ERR_ARG, "rerank depth must be at most 4096");
+  MV_REQUIRE(nprobe <= 8192, MV_ERR_UNSUPPORTED, "nprobe above 8192 is not supported on the GPU");
+  const int nc = fp32_coarse ? nprobe : std::min(ix->nlist, nprobe + std::max(8, nprobe / 4));
+  const int kp = umma_kpad(ix->d);
+  int64_t qb = std::max<int64_t>(128, (int64_t)(1536ll * 1024 * 1024 / ((int64_t)ix->nlist * 4)));
+  qb = std::min<int64_t>({qb, nq, 65535ll * 64});
+  ws.ensure(ws_bytes((size_t)qb * kp, 2) + ws_bytes((size_t)qb * ix->nlist, 4) +
+            ws_bytes((size_t)qb * nc, 8) + ws_bytes((size_t)qb * nprobe, 4) * 2 +
+            ws_bytes((size_t)qb * R, 8));
+  Arena ar(ws);
+  __nv_bfloat16* xq = ar.take<__nv_bfloat16>((size_t)qb * kp);
+  float* dmat = ar.take<float>((size_t)qb * ix->nlist);
+  uint64_t* ckeys = ar.take<uint64_t>((size_t)qb * nc);
+  int32_t* probes = ar.take<int32_t>((size_t)qb * nprobe);
+  float* term = ar.take<float>((size_t)qb * nprobe);
+  uint64_t* skeys = ar.take<uint64_t>((size_t)qb * R);
+  for (int64_t q0 = 0; q0 < nq; q0 += qb) {
+    const int64_t nb = std::min(qb, nq - q0);
+    const float* xb = d_x + q0 * ix->d;
+    {
+      StageTimer t(ix->ctx, MV_STAGE_COARSE, s);
+      if (fp32_coarse) {
+        launch_exact_matrix(ix->metric == MV_METRIC_L2 ? KIND_L2_SIMD8 : KIND_IP_SIMD8, xb, nb,
+                            ix->d, ix->centroids.as<float>(), ix->nlist, ix->d, ix->d, dmat,
+                            ix->nlist, s);
+      } else {
+        launch_to_bf16(xb, nb, ix->d, xq, nullptr, s);
+        launch_umma_dist(EPI_MATRIX, xq, nb, ix->d_cent_bf16.as<__nv_bfloat16>(), ix->nlist, ix->d,
+                         ix->metric, nullptr, ix->d_cnorm.as<float>(), dmat, ix->nlist, nullptr,
+                         ix->ctx->d_err.as<int>(), ix->ctx->num_sms, s);
+      }
+    }
+    {
+      StageTimer t(ix->ctx, MV_STAGE_SELECT, s);
+      launch_select_rows(dmat, nb, ix->nlist, ix->nlist, 0, nc, nullptr, ckeys, nullptr, s);
+      launch_coarse_recheck(xb, nb, ix->d, ix->centroids.as<float>(), ix->metric, ckeys, nc, nprobe,
+                            probes, term, s);
+    }
+    {
+      StageTimer t(ix->ctx, MV_STAGE_SCAN, s);
+      FastScanArgs a;
+      a.q = xb;
+      a.nq = nb;
+      a.d = ix->d;
+      a.M = ix->M;
+      a.metric = ix->metric;
+      a.pq = ix->pq.as<float>();
+      a.list_off = ix->d_off.as<int64_t>();
+      a.codes = ix->d_codes.as<uint8_t>();
+      a.vterm = ix->metric == MV_METRIC_L2 ? ix->d_vec_term.as<float>() : nullptr;
+      a.probes = probes;
+      a.term = term;
+      a.nprobe = nprobe;
+      a.R = R;
+      a.out_keys = skeys;
+      launch_ivfpq_scan_fast(a, s);
+    }
+    if (p && p->rerank > 0) {
+      StageTimer t(ix->ctx, MV_STAGE_RERANK, s);
+      RerankArgs r;
+      r.q = xb;
+      r.nq = nb;
+      r.d = ix->d;
+      r.metric = ix->metric;
+      r.raw = ix->d_raw.as<float>();
+      r.ids = ix->d_ids.as<uint32_t>();
+      r.cand = skeys;
+      r.R = R;
+      r.k = k;
+      r.out_d = d_out + q0 * k;
+      r.out_l = d_lab + q0 * k;
+      launch_rerank_fast(r, s);
+    } else {
+      launch_short_to_results(skeys, nb, R, k, ix->d_ids.as<uint32_t>(), ix->metric,
+                              d_out + q0 * k, d_lab + q0 * k, s);
+    }
+  }
+}
+
+void ivfpq_search_any(mv_ivfpq* ix, const float* d_x, int64_t nq, int k,
+                      const uint8_t* d_filter, int64_t filter_len, const mv_search_params* p,
+                      float* d_out, int64_t* d_lab, DevBuf& ws, cudaStream_t s) {
+  const int form = p ? p->form : MV_FORM_PLAIN;
+  const int nprobe = effective_nprobe(ix, p);
+  if (form == MV_FORM_FAST) {
+    MV_REQUIRE(d_filter == nullptr, MV_ERR_UNSUPPORTED, "the fast form takes no filter");
+    ivfpq_search_fast(ix, d_x, nq, k, nprobe, p, d_out, d_lab, ws, s);
+  } else {
+    MV_REQUIRE(form == MV_FORM_PLAIN, MV_ERR_ARG, "unknown search form");
+    ivfpq_search_plain(ix, d_x, nq, k, nprobe, d_filter, filter_len, d_out, d_lab, ws, s);
   }
 }
 
@@ -674,14 +817,12 @@ int32_t mv_ivfpq_search_device(mv_ivfpq* ix, const float* d_x, int64_t nq, int32
   if (!ix || (nq > 0 && (!d_x || !d_distances || !d_labels))) return MV_ERR_ARG;
   return guard(ix->ctx, [&] {
     check_search_args(nq, k);
-    const int form = params ? params->form : MV_FORM_PLAIN;
-    MV_REQUIRE(form == MV_FORM_PLAIN, MV_ERR_UNSUPPORTED, "fast form not built in this library");
     SlotLease lease(ix->ctx);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : lease.stream();
     lease.use(s);
-    ivfpq_search_plain(ix, d_x, nq, k, effective_nprobe(ix, params), d_filter, filter_len,
-                       d_distances, d_labels, lease.slot->ws, s);
-    if (!stream) sync(s);
+    ivfpq_search_any(ix, d_x, nq, k, d_filter, filter_len, params, d_distances, d_labels,
+                     lease.slot->ws, s);
+    if (!stream) check_kernel_errors(ix->ctx, s);
   });
 }
 
@@ -692,8 +833,6 @@ int32_t mv_ivfpq_search(mv_ivfpq* ix, const float* x, int64_t nq, int32_t k,
   return guard(ix->ctx, [&] {
     check_search_args(nq, k);
     if (nq == 0) return;
-    const int form = params ? params->form : MV_FORM_PLAIN;
-    MV_REQUIRE(form == MV_FORM_PLAIN, MV_ERR_UNSUPPORTED, "fast form not built in this library");
     SlotLease lease(ix->ctx);
     cudaStream_t s = lease.stream();
     DevBuf& io = lease.slot->io;
@@ -707,11 +846,11 @@ int32_t mv_ivfpq_search(mv_ivfpq* ix, const float* x, int64_t nq, int32_t k,
     uint8_t* df = ar.take<uint8_t>(fl + 1);
     h2d(dx, x, sizeof(float) * nq * ix->d, s);
     if (fl) h2d(df, filter, fl, s);
-    ivfpq_search_plain(ix, dx, nq, k, effective_nprobe(ix, params), fl ? df : nullptr,
-                       (int64_t)fl, dd, dl, lease.slot->ws, s);
+    ivfpq_search_any(ix, dx, nq, k, fl ? df : nullptr, (int64_t)fl, params, dd, dl,
+                     lease.slot->ws, s);
     d2h(distances, dd, sizeof(float) * nq * k, s);
     d2h(labels, dl, sizeof(int64_t) * nq * k, s);
-    sync(s);
+    check_kernel_errors(ix->ctx, s);
   });
 }
 
@@ -1199,6 +1338,42 @@ int32_t mv_sq8_encode(mv_ctx* ctx, const float* x, int64_t n, int32_t d, float m
     MV_CHECK_CUDA(cudaMemcpy2DAsync(codes, d, dc.p, dp, d, n, cudaMemcpyDeviceToHost, s));
     d2h(norms, dn.p, sizeof(uint32_t) * n, s);
     sync(s);
+  });
+}
+
+int32_t mv_distance_matrix(mv_ctx* ctx, const float* x, int64_t nx, const float* y, int64_t ny,
+                           int32_t d, int32_t metric, int32_t precision, float* out) {
+  if (!ctx || d <= 0 || nx < 0 || ny < 0 || (nx > 0 && ny > 0 && (!x || !y || !out)))
+    return MV_ERR_ARG;
+  return guard(ctx, [&] {
+    MV_REQUIRE(metric == MV_METRIC_L2 || metric == MV_METRIC_IP, MV_ERR_ARG, "unknown metric");
+    MV_REQUIRE(precision == 0 || precision == 1, MV_ERR_ARG, "precision must be 0 or 1");
+    if (nx == 0 || ny == 0) return;
+    SlotLease lease(ctx);
+    cudaStream_t s = lease.stream();
+    DevBuf dx, dy, dout, bx, by, nxb, nyb;
+    dx.ensure(sizeof(float) * nx * d);
+    dy.ensure(sizeof(float) * ny * d);
+    dout.ensure(sizeof(float) * nx * ny);
+    h2d(dx.p, x, sizeof(float) * nx * d, s);
+    h2d(dy.p, y, sizeof(float) * ny * d, s);
+    if (precision == 0) {
+      launch_exact_matrix(metric == MV_METRIC_L2 ? KIND_L2_SIMD8 : KIND_IP_SIMD8, dx.as<float>(), nx,
+                          d, dy.as<float>(), ny, d, d, dout.as<float>(), ny, s);
+    } else {
+      const int kp = umma_kpad(d);
+      bx.ensure(sizeof(uint16_t) * nx * kp);
+      by.ensure(sizeof(uint16_t) * ny * kp);
+      nxb.ensure(sizeof(float) * nx);
+      nyb.ensure(sizeof(float) * ny);
+      launch_to_bf16(dx.as<float>(), nx, d, bx.as<__nv_bfloat16>(), nxb.as<float>(), s);
+      launch_to_bf16(dy.as<float>(), ny, d, by.as<__nv_bfloat16>(), nyb.as<float>(), s);
+      launch_umma_dist(EPI_MATRIX, bx.as<__nv_bfloat16>(), nx, by.as<__nv_bfloat16>(), ny, d, metric,
+                       nxb.as<float>(), nyb.as<float>(), dout.as<float>(), ny, nullptr,
+                       ctx->d_err.as<int>(), ctx->num_sms, s);
+    }
+    d2h(out, dout.p, sizeof(float) * nx * ny, s);
+    check_kernel_errors(ctx, s);
   });
 }
 

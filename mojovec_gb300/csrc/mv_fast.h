@@ -1,0 +1,47 @@
+// Host interface of the fast-form IVF-PQ kernels (k_ivfpq_fast.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace mv {
+
+struct FastScanArgs {
+  const float* q;
+  int64_t nq;
+  int d, M, metric;
+  const float* pq;
+  const int64_t* list_off;
+  const uint8_t* codes;
+  const float* vterm;     // per CSR entry, null for IP
+  const int32_t* probes;  // nq x nprobe, ascending coarse distance
+  const float* term;      // nq x nprobe coarse distances (exact FP32)
+  int nprobe;
+  int R;                  // shortlist length
+  uint64_t* out_keys;     // nq x R (distance, CSR position)
+};
+
+struct RerankArgs {
+  const float* q;
+  int64_t nq;
+  int d, metric;
+  const float* raw;       // FP32 rows in CSR order
+  const uint32_t* ids;    // id per CSR entry
+  const uint64_t* cand;   // nq x R shortlist keys
+  int R, k;
+  float* out_d;
+  int64_t* out_l;
+};
+
+void launch_vec_terms(const int64_t* off, int nlist, const uint8_t* codes, const float* pq,
+                      const float* cent, int d, int M, float* out, cudaStream_t s);
+void launch_coarse_recheck(const float* q, int64_t nq, int d, const float* cent, int metric,
+                           const uint64_t* cand, int nc, int nprobe, int32_t* probes, float* term,
+                           cudaStream_t s);
+void launch_ivfpq_scan_fast(const FastScanArgs& a, cudaStream_t s);
+void launch_rerank_fast(const RerankArgs& a, cudaStream_t s);
+void launch_short_to_results(const uint64_t* keys, int64_t nq, int R, int k, const uint32_t* ids,
+                             int metric, float* out_d, int64_t* out_l, cudaStream_t s);
+
+}  // namespace mv

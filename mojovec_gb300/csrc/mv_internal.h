@@ -102,6 +102,7 @@ struct mv_ctx {
   std::vector<mv::Slot*> all_slots;
   std::atomic<int64_t> launches{0};
   cudaStream_t main_stream = nullptr;
+  mv::DevBuf d_err;  // int: set by kernels whose bounded waits gave up
   // stage profiling (mv_ctx_profile)
   std::atomic<bool> profile{false};
   std::mutex prof_mu;
@@ -174,6 +175,7 @@ struct mv_ivfpq {
   mv::DevBuf d_codes;   // M bytes per entry
   mv::DevBuf d_raw;     // FP32 rows per entry (exact rerank in the fast form)
   // Fast-form state (built lazily from the above).
+  std::mutex fast_mu;
   bool fast_ready = false;
   mv::DevBuf d_vec_term;    // FP32 per vector: ||y||^2 + 2<c, y> (y = PQ reconstruction)
   mv::DevBuf d_cnorm;       // FP32 per centroid ||c||^2

@@ -1,0 +1,42 @@
+// Host interface of the BF16 tensor-core distance GEMM (k_umma.cu).
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace mv {
+
+enum UmmaEpilogue : int {
+  EPI_MATRIX = 0,  // write the distance matrix
+  EPI_ARGMIN = 1,  // per-row min (distance, column) key via atomicMin
+};
+
+struct UmmaArgs {
+  int64_t nrows, ncols;
+  int nkb;           // 64-element k-blocks
+  int metric;        // MV_METRIC_L2 / MV_METRIC_IP
+  const float* rnorm;  // ||x||^2 per row (may be null: row-constant term dropped)
+  const float* cnorm;  // ||y||^2 per column (L2)
+  float* out;
+  int64_t ldo;
+  uint64_t* keys;    // EPI_ARGMIN output, one per row
+  int* err;          // set to 1 when a bounded wait gave up
+};
+
+// Rows are padded to this many BF16 elements (a multiple of 64).
+int umma_kpad(int d);
+// FP32 rows -> zero-padded BF16 rows (kpad wide) and FP32 norms of the
+// rounded rows (norms may be null).
+void launch_to_bf16(const float* x, int64_t n, int d, __nv_bfloat16* out, float* norms,
+                    cudaStream_t s);
+// Distances between BF16 rows X (nx) and Y (ny) on the tensor cores.
+void launch_umma_dist(int epi, const __nv_bfloat16* X, int64_t nx, const __nv_bfloat16* Y,
+                      int64_t ny, int d, int metric, const float* xnorm, const float* ynorm,
+                      float* out, int64_t ldo, uint64_t* keys, int* err, int num_sms,
+                      cudaStream_t s);
+// keys -> argmin columns (and distances).
+void launch_keys_argmin(const uint64_t* keys, int64_t n, int32_t* out, float* dist, cudaStream_t s);
+
+}  // namespace mv

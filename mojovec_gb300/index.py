@@ -374,6 +374,20 @@ def sq8_encode(x, minimum: float, inverse_scale: float, symmetric: bool, ctx: Co
     return codes, norms
 
 
+def distance_matrix(x, y, metric: int = METRIC_L2, precision: int = 0,
+                    ctx: Context | None = None):
+    """Distances between the rows of x and y: precision 0 = exact FP32 in the
+    reference order, 1 = BF16 tensor cores with FP32 accumulation."""
+    ctx = ctx or Context.default()
+    x = _f32(x)
+    y = _f32(y)
+    assert x.shape[1] == y.shape[1]
+    out = np.empty((x.shape[0], y.shape[0]), np.float32)
+    check(_lib.load().mv_distance_matrix(ctx.handle, _p(x), x.shape[0], _p(y), y.shape[0],
+                                         x.shape[1], metric, precision, _p(out)))
+    return out
+
+
 def normalize(x, ctx: Context | None = None):
     """_normalize_vectors (api/collection_vector_query.mojo:24-46) on the GPU."""
     ctx = ctx or Context.default()

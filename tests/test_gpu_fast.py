@@ -1,0 +1,114 @@
+"""Fast-form (tensor-core) checks.
+
+* The BF16 tcgen05 distance GEMM is exact when every input is an integer of
+  small magnitude (BF16 represents it exactly and every FP32 partial sum is
+  an integer below 2^24), so it is compared bit for bit with int64 numpy.
+* On real-valued data it is compared with an FP64 reference within the BF16
+  rounding bound.
+* The fast IVF-PQ search becomes exact when every list is probed and the
+  rerank shortlist holds every candidate: it must then return the exact
+  Flat answer. Recall floors and determinism are checked at realistic sizes.
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RNG = np.random.default_rng(777)
+
+
+def _int_rows(n, d, lo=-8, hi=8):
+    return RNG.integers(lo, hi + 1, size=(n, d)).astype(np.float32)
+
+
+@pytest.mark.parametrize("d", [8, 32, 64, 96, 128, 200, 256])
+@pytest.mark.parametrize("nx,ny", [(1, 1), (130, 77), (300, 600)])
+def test_umma_exact_on_integers(mv, d, nx, ny):
+    x = _int_rows(nx, d)
+    y = _int_rows(ny, d)
+    xi = x.astype(np.int64)
+    yi = y.astype(np.int64)
+    dot = xi @ yi.T
+    l2 = (xi * xi).sum(1)[:, None] + (yi * yi).sum(1)[None, :] - 2 * dot
+    got_l2 = mv.distance_matrix(x, y, metric=0, precision=1)
+    got_ip = mv.distance_matrix(x, y, metric=1, precision=1)
+    assert np.array_equal(got_l2, l2.astype(np.float32))
+    assert np.array_equal(got_ip, (-dot).astype(np.float32))
+
+
+def test_umma_real_valued_within_bf16_bound(mv):
+    x = RNG.standard_normal((513, 128)).astype(np.float32)
+    y = RNG.standard_normal((1031, 128)).astype(np.float32)
+    ref = -(x.astype(np.float64) @ y.T.astype(np.float64))
+    got = mv.distance_matrix(x, y, metric=1, precision=1)
+    bound = 2.0 ** -7 * np.abs(x).astype(np.float64) @ np.abs(y).T.astype(np.float64) + 1e-4
+    assert (np.abs(got - ref) <= bound).all()
+
+
+def test_exact_matrix_matches_oracle_order(mv, orc):
+    x = RNG.standard_normal((70, 100)).astype(np.float32)
+    y = RNG.standard_normal((90, 100)).astype(np.float32)
+    got = mv.distance_matrix(x, y, metric=0, precision=0)
+    for i in range(0, 70, 7):
+        for j in range(0, 90, 11):
+            assert got[i, j] == np.float32(orc.l2_simd(x[i], y[j]))
+
+
+def _index(mv, base, d, nlist, M, metric=0):
+    g = mv.IndexIVFPQ(d, nlist, M, metric)
+    g.train(base[: min(len(base), 20000)], niter_coarse=6, niter_pq=6)
+    g.add(base)
+    return g
+
+
+@pytest.mark.parametrize("metric", [0, 1])
+def test_fast_exhaustive_equals_flat(mv, metric):
+    base = RNG.standard_normal((3000, 64)).astype(np.float32)
+    q = RNG.standard_normal((40, 64)).astype(np.float32)
+    g = _index(mv, base, 64, 16, 8, metric)
+    d, l = g.search(q, 10, form=mv.FORM_FAST, nprobe=16, rerank=3000)
+    flat = mv.IndexFlat(64, metric)
+    flat.add(base)
+    fd, fl = flat.search(q, 10)
+    assert np.array_equal(l, fl)
+    assert np.allclose(d, fd, rtol=1e-5, atol=1e-4)
+
+
+def test_fast_recall_and_determinism(mv):
+    from mojovec_gb300 import synth
+
+    base, q = synth.sift_like(100000, d=128, n_centers=256, nq=500, seed=21)
+    g = _index(mv, base, 128, 256, 16)
+    flat = mv.IndexFlat(128, 0)
+    flat.add(base)
+    _, gt = flat.search(q, 10)
+
+    def recall(lab):
+        return np.mean([len(set(gt[i]) & set(lab[i])) / 10 for i in range(len(q))])
+
+    g.nprobe = 32
+    _, lp = g.search(q, 10)
+    r_plain = recall(lp)
+    _, lf = g.search(q, 10, form=mv.FORM_FAST, nprobe=32)
+    r_fast = recall(lf)
+    assert abs(r_fast - r_plain) < 0.05  # same PQ quantisation, different rounding
+    runs = [g.search(q, 10, form=mv.FORM_FAST, nprobe=32, rerank=400) for _ in range(3)]
+    for d, l in runs[1:]:
+        assert np.array_equal(l, runs[0][1]) and np.array_equal(d, runs[0][0])
+    r_rerank = recall(runs[0][1])
+    assert r_rerank > r_plain + 0.2
+    _, lc = g.search(q, 10, form=mv.FORM_FAST, nprobe=32, rerank=400, coarse_fp32=True)
+    assert abs(recall(lc) - r_rerank) < 0.02
+
+
+def test_fast_untrained_and_small_lists(mv):
+    g = mv.IndexIVFPQ(16, 8, 4)
+    d, l = g.search(np.zeros((2, 16), np.float32), 5, form=mv.FORM_FAST, nprobe=4)
+    assert (l == -1).all()
+    base = RNG.standard_normal((300, 16)).astype(np.float32)
+    g.train(base, niter_coarse=3, niter_pq=3)
+    g.add(base[:20])
+    d, l = g.search(base[:3], 50, form=mv.FORM_FAST, nprobe=8, rerank=100)
+    assert (l[:, 20:] == -1).all() and set(l[0, :20].tolist()) == set(range(20))
+    assert l[0, 0] == 0 and d[0, 0] == 0.0
