@@ -7,6 +7,12 @@ k-means) from a 131,072-row sample, 10 iterations each for the coarse and
 the PQ codebooks, then all rows added. A step is one search of the whole
 10,000-query batch.
 
+The headline form is the fast form (BF16 tensor-core coarse GEMM with an
+exact FP32 recheck, per-query LUT, exact FP32 rerank of a shortlist) at the
+operating point that reaches recall@10 >= 0.95; the plain FP32 form (the
+reference's own algorithm, bit-exact) is timed in the same run at the same
+nprobe and reported beside it.
+
 `value` times steps with the queries and results resident in HBM (CUDA
 events on the launching stream, L2 flushed with a 256 MiB write before each
 step, outside the timed interval); `e2e` times the public host-buffer C-ABI
@@ -33,10 +39,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-NB = 1_000_000
 D = 128
 N_CENTERS = 1024
-NQ = 10_000
 NLIST = 4096
 M = 16
 K = 10
@@ -109,10 +113,14 @@ class ClockSampler:
         }
 
 
-def build_workload():
+NB = 1_000_000
+NQ = 10_000
+
+
+def build_workload(nb=None, nq=None):
     from mojovec_gb300 import synth
 
-    base, queries = synth.sift_like(NB, d=D, n_centers=N_CENTERS, nq=NQ)
+    base, queries = synth.sift_like(nb or NB, d=D, n_centers=N_CENTERS, nq=nq or NQ)
     return base, queries
 
 
@@ -157,16 +165,39 @@ def cpu_baseline(index, queries, nprobe, threads, sample):
     return sample / dt, lab
 
 
+def _timed_steps(torch, step, steps, stream, flush):
+    """Times `steps` calls with CUDA events on the launching stream; L2 is
+    flushed (256 MiB write) before each step, outside the events."""
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(steps)]
+    for a, b in evs:
+        flush.fill_(1.0)
+        a.record(stream)
+        step()
+        b.record(stream)
+    torch.cuda.synchronize()
+    return float(sum(a.elapsed_time(b) for a, b in evs))
+
+
+def _max_over_ranks(torch, world, v):
+    if world == 1:
+        return v
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_gpu(args, rank, world):
     import torch
 
     import mojovec_gb300 as mv
 
+    nb, nq = args.nb, args.nq
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
     ctx = mv.Context(dev)
     t_setup = time.perf_counter()
-    base, queries = build_workload()
+    base, queries = build_workload(nb, nq)
     index = mv.IndexIVFPQ(D, NLIST, M, mv.METRIC_L2, ctx=ctx)
     index.train(base[:TRAIN_N], niter_coarse=NITER, niter_pq=NITER)
     index.add(base)
@@ -182,71 +213,66 @@ def run_gpu(args, rank, world):
     del flat
     setup_s = time.perf_counter() - t_setup
 
-    form = mv.FORM_FAST if args.form == "fast" else mv.FORM_PLAIN
-    sopts = dict(form=form, nprobe=nprobe, rerank=args.rerank)
+    fast = dict(form=mv.FORM_FAST, nprobe=nprobe, rerank=args.rerank)
+    plain = dict(form=mv.FORM_PLAIN, nprobe=nprobe)
+    headline = fast if args.form == "fast" else plain
     d_q = torch.from_numpy(queries).cuda()
-    d_dist = torch.empty((NQ, K), dtype=torch.float32, device="cuda")
-    d_lab = torch.empty((NQ, K), dtype=torch.int64, device="cuda")
+    d_dist = torch.empty((nq, K), dtype=torch.float32, device="cuda")
+    d_lab = torch.empty((nq, K), dtype=torch.int64, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
 
-    def step():
-        index.search_device(d_q.data_ptr(), NQ, K, d_dist.data_ptr(), d_lab.data_ptr(),
-                            stream=stream.cuda_stream, **sopts)
+    def make_step(opts):
+        def step():
+            index.search_device(d_q.data_ptr(), nq, K, d_dist.data_ptr(), d_lab.data_ptr(),
+                                stream=stream.cuda_stream, **opts)
+        return step
 
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    labels = d_lab.cpu().numpy()
-    rec = recall_at(gt, labels, K)
+    results = {}
+    for name, opts in (("plain", plain), ("headline", headline)):
+        step = make_step(opts)
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        labels = d_lab.cpu().numpy()
+        results[name] = {"recall": recall_at(gt, labels, K), "labels": labels}
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        if name == "headline":
+            clocks = ClockSampler(dev)
+            clocks.start()
+            ctx.profile(True)
+            launches0 = ctx.kernel_launches()
+        torch.cuda.nvtx.range_push(f"timed_{name}")
+        ms = _timed_steps(torch, step, args.steps, stream, flush)
+        torch.cuda.nvtx.range_pop()
+        if name == "headline":
+            launches = ctx.kernel_launches() - launches0
+            stage = ctx.stage_times()
+            ctx.profile(False)
+            clk = clocks.stop()
+        results[name]["ms"] = _max_over_ranks(torch, world, ms)
+    total_ms = results["headline"]["ms"]
+    value = world * nq * args.steps / (total_ms / 1e3)
+    plain_qps = world * nq * args.steps / (results["plain"]["ms"] / 1e3)
+    labels = results["headline"]["labels"]
 
-    # ---- timed region (device-resident) ----
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    clocks = ClockSampler(dev)
-    clocks.start()
-    ctx.profile(True)
-    launches0 = ctx.kernel_launches()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(args.steps)]
-    for a, b in evs:
-        flush.fill_(1.0)
-        a.record(stream)
-        step()
-        b.record(stream)
-    torch.cuda.synchronize()
-    launches = ctx.kernel_launches() - launches0
-    stage = ctx.stage_times()
-    ctx.profile(False)
-    clk = clocks.stop()
-    step_ms = [a.elapsed_time(b) for a, b in evs]
-    total_ms = float(sum(step_ms))
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * NQ * args.steps / (total_ms / 1e3)
-
-    # ---- e2e through the host-buffer C ABI, pinned queries ----
-    pinned = torch.empty((NQ, D), dtype=torch.float32).pin_memory()
+    # ---- e2e through the host-buffer C ABI, queries in pinned memory ----
+    pinned = torch.empty((nq, D), dtype=torch.float32).pin_memory()
     pinned.copy_(torch.from_numpy(queries))
     hq = pinned.numpy()
-    index.search(hq, K, **sopts)
+    index.search(hq, K, **headline)
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        _, elab = index.search(hq, K, **sopts)
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_qps = world * NQ * args.steps / e2e_s
+        _, elab = index.search(hq, K, **headline)
+    e2e_s = _max_over_ranks(torch, world, time.perf_counter() - t0)
+    e2e_qps = world * nq * args.steps / e2e_s
     assert np.array_equal(elab, labels), "host-buffer and device-buffer searches disagree"
 
-    # ---- roofline of the dominant kernel ----
+    # ---- roofline of the dominant kernel (the ADC scan) ----
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -258,6 +284,7 @@ def run_gpu(args, rank, world):
     code_bytes = probed_code_bytes(index, queries, nprobe)
     per_launch_ms = scan_ms / max(scan_n, 1)
     achieved = code_bytes / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
+    fast_form = args.form == "fast"
 
     out = {
         "metric": METRIC,
@@ -270,16 +297,20 @@ def run_gpu(args, rank, world):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32" if form == mv.FORM_PLAIN else "bf16+f32",
+        "dtype": "bf16+f32" if fast_form else "f32",
         "data": "synthetic SIFT-like (seeded Gaussian mixture, integer-valued), not SIFT1M",
         "config": {
-            "workload": "ivfpq_1Mx128_nlist4096_M16_nq10000_k10",
-            "form": args.form,
+            "workload": f"ivfpq_{nb}x128_nlist4096_M16_nq{nq}_k10",
+            "form": "fast: BF16 tcgen05 coarse + FP32 recheck, per-query LUT, exact FP32 rerank"
+                    if fast_form else "plain FP32 (reference algorithm, bit-exact)",
             "nprobe": nprobe,
-            "rerank": args.rerank,
-            "nb": NB, "d": D, "nlist": NLIST, "M": M, "nq": NQ, "k": K,
+            "rerank": args.rerank if fast_form else 0,
+            "nb": nb, "d": D, "nlist": NLIST, "M": M, "nq": nq, "k": K,
             "train_rows": TRAIN_N, "train_niter": NITER,
-            "recall_at_10": round(rec, 4),
+            "recall_at_10": round(results["headline"]["recall"], 4),
+            "plain_fp32_qps_same_nprobe": round(plain_qps, 1),
+            "plain_fp32_recall_at_10": round(results["plain"]["recall"], 4),
+            "speedup_vs_plain_fp32": round(value / plain_qps, 2),
             "l2_policy": "flush: 256 MiB device write before every timed step (outside the events)",
             "parallelism": f"replicas x{world}",
             "setup_s": round(setup_s, 1),
@@ -287,13 +318,13 @@ def run_gpu(args, rank, world):
         "e2e": {
             "value": round(e2e_qps, 1),
             "unit": "queries/s",
-            "h2d_bytes_per_step": NQ * D * 4,
-            "d2h_bytes_per_step": NQ * K * (4 + 8),
+            "h2d_bytes_per_step": nq * D * 4,
+            "d2h_bytes_per_step": nq * K * (4 + 8),
         },
         "gpu_launches": int(launches),
         "roofline": {
             "bound": "hbm",
-            "kernel": "k_ivfpq_scan_plain" if form == mv.FORM_PLAIN else "ivfpq fast ADC scan",
+            "kernel": "k_ivfpq_scan_fast" if fast_form else "k_ivfpq_scan_plain",
             "achieved": round(achieved, 1),
             "peak": hbm_peak,
             "peak_source": peak_src,
@@ -307,21 +338,18 @@ def run_gpu(args, rank, world):
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu:
-        sample = args.cpu_sample
+        sample = min(args.cpu_sample, nq)
         threads = os.cpu_count() or 1
         qps, clab = cpu_baseline(index, queries, nprobe, threads, sample)
-        plain_match = None
-        if form == mv.FORM_PLAIN:
-            plain_match = bool(np.array_equal(clab, labels[:sample]))
         out["cpu_baseline"] = {
             "value": round(qps, 1),
             "unit": "queries/s",
             "cores": threads,
             "kind": "port",
-            "sample": f"{sample} of the {NQ} queries, same index (codebooks + lists loaded "
-                      f"from the GPU index), nprobe {nprobe}, coarse and LUT+ADC query-parallel "
-                      f"on {threads} threads",
-            "ids_equal_to_gpu": plain_match,
+            "sample": f"{sample} of the {nq} queries, same index (codebooks + lists loaded "
+                      f"from the GPU index), nprobe {nprobe}, reference algorithm (plain form), "
+                      f"coarse and LUT+ADC query-parallel on {threads} threads",
+            "ids_equal_to_gpu_plain": bool(np.array_equal(clab, results["plain"]["labels"][:sample])),
         }
     return out
 
@@ -333,12 +361,12 @@ def run_reference(args):
 
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
-    base, queries = build_workload()
+    base, queries = build_workload(args.nb, args.nq)
     ref = orc.IVFPQ(D, NLIST, M)
     ref.train(base[:TRAIN_N], niter_coarse=NITER, niter_pq=NITER, nthreads=threads)
     ref.add(base, nthreads=threads)
     setup_s = time.perf_counter() - t0
-    sample = args.cpu_sample
+    sample = min(args.cpu_sample, args.nq)
     q = queries[:sample]
     for _ in range(max(args.warmup, 0)):
         ref.search(q[:32], K, args.nprobe, nthreads=threads, lut_threads=threads)
@@ -364,10 +392,10 @@ def run_reference(args):
         "dtype": "f32",
         "data": "synthetic SIFT-like (seeded Gaussian mixture, integer-valued), not SIFT1M",
         "config": {
-            "workload": "ivfpq_1Mx128_nlist4096_M16_nq10000_k10",
+            "workload": f"ivfpq_{args.nb}x128_nlist4096_M16_nq{args.nq}_k10",
             "form": "reference CPU path (oracle port)",
             "nprobe": args.nprobe,
-            "nb": NB, "d": D, "nlist": NLIST, "M": M, "nq": NQ, "k": K,
+            "nb": args.nb, "d": D, "nlist": NLIST, "M": M, "nq": args.nq, "k": K,
             "train_rows": TRAIN_N, "train_niter": NITER,
             "setup_s": round(setup_s, 1),
         },
@@ -376,7 +404,7 @@ def run_reference(args):
             "unit": "queries/s",
             "cores": threads,
             "kind": "port",
-            "sample": f"{sample} queries per step of the {NQ}; index trained and filled by the "
+            "sample": f"{sample} queries per step of the {args.nq}; index trained and filled by the "
                       f"oracle on the CPU; coarse and LUT+ADC query-parallel on {threads} threads",
         },
         "e2e": {"value": round(qps, 1), "unit": "queries/s", "h2d_bytes_per_step": 0,
@@ -390,9 +418,11 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--form", default="plain", choices=["plain", "fast"])
-    ap.add_argument("--nprobe", type=int, default=64)
-    ap.add_argument("--rerank", type=int, default=0)
+    ap.add_argument("--form", default="fast", choices=["plain", "fast"])
+    ap.add_argument("--nprobe", type=int, default=16)
+    ap.add_argument("--rerank", type=int, default=256)
+    ap.add_argument("--nb", type=int, default=NB, help="base rows (profiling runs use fewer)")
+    ap.add_argument("--nq", type=int, default=NQ, help="queries per step")
     ap.add_argument("--cpu-sample", type=int, default=500)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

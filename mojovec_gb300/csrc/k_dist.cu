@@ -322,8 +322,7 @@ size_t tile_smem(int d) { return (size_t)2 * TB * d * sizeof(float); }
 
 template <typename K>
 void set_smem(K kernel, size_t bytes) {
-  if (bytes > 48 * 1024)
-    MV_CHECK_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  smem_limit(kernel, bytes);
 }
 
 }  // namespace

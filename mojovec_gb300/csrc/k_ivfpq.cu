@@ -199,9 +199,7 @@ void launch_ivfpq_scan_plain(const IvfpqScanArgs& a, cudaStream_t s) {
                 (size_t)BlockTopK::smem_keys(a.k, SCAN_BUF) * 8;
   MV_REQUIRE(smem <= 220 * 1024, MV_ERR_UNSUPPORTED, "IVF-PQ scan: M, d or k too large");
   MV_REQUIRE(a.nq <= 0x7fffffff, MV_ERR_UNSUPPORTED, "too many queries");
-  if (smem > 48 * 1024)
-    MV_CHECK_CUDA(cudaFuncSetAttribute(k_ivfpq_scan_plain,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  smem_limit(k_ivfpq_scan_plain, smem);
   k_ivfpq_scan_plain<<<(unsigned)a.nq, SCAN_THREADS, smem, s>>>(a);
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());

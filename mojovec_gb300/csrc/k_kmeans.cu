@@ -148,17 +148,13 @@ void launch_kmeans_accumulate(const float* x, int64_t n, int d, int k, const int
   dim3 grid(NUM_CHUNKS, (unsigned)((d + 31) / 32), (unsigned)batch);
   size_t smem_acc = (size_t)k * 32 * sizeof(float) + (size_t)k * sizeof(int);
   if (smem_acc <= 200 * 1024) {
-    if (smem_acc > 48 * 1024)
-      MV_CHECK_CUDA(cudaFuncSetAttribute(k_kmeans_accumulate<true>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_acc));
+    smem_limit(k_kmeans_accumulate<true>, smem_acc);
     k_kmeans_accumulate<true><<<grid, 32, smem_acc, s>>>(x, n, d, k, assign, local_sums,
                                                          local_counts, bx, ba, bs, bc);
   } else {
     size_t smem = (size_t)k * sizeof(int);
     MV_REQUIRE(smem <= 200 * 1024, MV_ERR_UNSUPPORTED, "k-means: k too large");
-    if (smem > 48 * 1024)
-      MV_CHECK_CUDA(cudaFuncSetAttribute(k_kmeans_accumulate<false>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    smem_limit(k_kmeans_accumulate<false>, smem);
     k_kmeans_accumulate<false><<<grid, 32, smem, s>>>(x, n, d, k, assign, local_sums,
                                                       local_counts, bx, ba, bs, bc);
   }

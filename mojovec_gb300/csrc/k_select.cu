@@ -73,9 +73,7 @@ void launch_select_rows(const float* D, int64_t rows, int64_t ldd, int64_t ncols
   MV_REQUIRE(rows <= 0x7fffffff, MV_ERR_UNSUPPORTED, "too many rows");
   size_t smem = (size_t)BlockTopK::smem_keys(k, SEL_BUF) * sizeof(uint64_t);
   MV_REQUIRE(smem <= 200 * 1024, MV_ERR_UNSUPPORTED, "k too large for the select kernel");
-  if (smem > 48 * 1024)
-    MV_CHECK_CUDA(cudaFuncSetAttribute(k_select_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
+  smem_limit(k_select_rows, smem);
   k_select_rows<<<(unsigned)rows, SEL_THREADS, smem, s>>>(D, ldd, ncols, col_base, k, prev, out,
                                                            filter);
   count_launch();

@@ -343,14 +343,10 @@ void launch_sq8_matrix(const uint8_t* qc, const uint32_t* qn, int64_t nq, const 
   MV_REQUIRE((nq + TB - 1) / TB <= 65535, MV_ERR_UNSUPPORTED, "too many queries in one call");
   dim3 grid((unsigned)((nb + TB - 1) / TB), (unsigned)((nq + TB - 1) / TB));
   if (ip) {
-    if (smem > 48 * 1024)
-      MV_CHECK_CUDA(cudaFuncSetAttribute(k_sq8_matrix<true>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    smem_limit(k_sq8_matrix<true>, smem);
     k_sq8_matrix<true><<<grid, NT, smem, s>>>(qc, qn, nq, bc, bn, nb, dpad, scale_sq, D, ldd);
   } else {
-    if (smem > 48 * 1024)
-      MV_CHECK_CUDA(cudaFuncSetAttribute(k_sq8_matrix<false>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    smem_limit(k_sq8_matrix<false>, smem);
     k_sq8_matrix<false><<<grid, NT, smem, s>>>(qc, qn, nq, bc, bn, nb, dpad, scale_sq, D, ldd);
   }
   count_launch();
@@ -364,9 +360,7 @@ void launch_rerank_simd64(const float* q, int64_t nq, int d, const float* base, 
   const int bufcap = 512;
   size_t smem = (size_t)BlockTopK::smem_keys(k, bufcap) * 8;
   MV_REQUIRE(smem <= 200 * 1024, MV_ERR_UNSUPPORTED, "rerank: k too large");
-  if (smem > 48 * 1024)
-    MV_CHECK_CUDA(cudaFuncSetAttribute(k_rerank_simd64, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
+  smem_limit(k_rerank_simd64, smem);
   k_rerank_simd64<<<(unsigned)nq, RR_THREADS, smem, s>>>(q, d, base, metric, cand, ncand, k, bufcap,
                                                           out_keys);
   count_launch();

@@ -304,8 +304,7 @@ void launch_bn(const UmmaArgs& g, const CUtensorMap& tx, const CUtensorMap& ty, 
                cudaStream_t s) {
   const size_t smem = Smem<BN>::total(g.nkb);
   MV_REQUIRE(smem <= 227 * 1024, MV_ERR_UNSUPPORTED, "BF16 GEMM: dimension too large");
-  MV_CHECK_CUDA(cudaFuncSetAttribute(k_umma_dist<BN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
+  smem_limit(k_umma_dist<BN, EPI>, smem);
   const int64_t items = (int64_t)((g.nrows + BM - 1) / BM) * ((g.ncols + BN - 1) / BN);
   const int grid = (int)std::min<int64_t>(items, num_sms);
   k_umma_dist<BN, EPI><<<grid, NUM_THREADS, smem, s>>>(tx, ty, g);

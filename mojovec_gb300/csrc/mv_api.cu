@@ -10,6 +10,7 @@
 #include <limits>
 #include <memory>
 #include <new>
+#include <unordered_map>
 
 #include "mv_fast.h"
 #include "mv_internal.h"
@@ -22,6 +23,17 @@ static thread_local std::string g_last_error;
 static thread_local mv_ctx* g_cur_ctx = nullptr;
 
 void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+void raise_smem_limit(const void* kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::unordered_map<const void*, size_t> high;
+  std::lock_guard<std::mutex> lk(mu);
+  size_t& h = high[kernel];
+  if (bytes <= h) return;
+  MV_CHECK_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  h = bytes;
+}
+
 void count_launch() {
   if (g_cur_ctx) g_cur_ctx->launches.fetch_add(1, std::memory_order_relaxed);
 }
@@ -432,12 +444,11 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
   int64_t qb = std::max<int64_t>(128, (int64_t)(1536ll * 1024 * 1024 / ((int64_t)ix->nlist * 4)));
   qb = std::min<int64_t>({qb, nq, 65535ll * 64});
   ws.ensure(ws_bytes((size_t)qb * kp, 2) + ws_bytes((size_t)qb * ix->nlist, 4) +
-            ws_bytes((size_t)qb * nc, 8) + ws_bytes((size_t)qb * nprobe, 4) * 2 +
+            ws_bytes((size_t)qb * nprobe, 4) * 2 +
             ws_bytes((size_t)qb * R, 8));
   Arena ar(ws);
   __nv_bfloat16* xq = ar.take<__nv_bfloat16>((size_t)qb * kp);
   float* dmat = ar.take<float>((size_t)qb * ix->nlist);
-  uint64_t* ckeys = ar.take<uint64_t>((size_t)qb * nc);
   int32_t* probes = ar.take<int32_t>((size_t)qb * nprobe);
   float* term = ar.take<float>((size_t)qb * nprobe);
   uint64_t* skeys = ar.take<uint64_t>((size_t)qb * R);
@@ -459,9 +470,8 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
     }
     {
       StageTimer t(ix->ctx, MV_STAGE_SELECT, s);
-      launch_select_rows(dmat, nb, ix->nlist, ix->nlist, 0, nc, nullptr, ckeys, nullptr, s);
-      launch_coarse_recheck(xb, nb, ix->d, ix->centroids.as<float>(), ix->metric, ckeys, nc, nprobe,
-                            probes, term, s);
+      launch_coarse_fast(dmat, nb, ix->nlist, xb, ix->d, ix->centroids.as<float>(), ix->metric, nc,
+                         nprobe, probes, term, s);
     }
     {
       StageTimer t(ix->ctx, MV_STAGE_SCAN, s);
@@ -479,6 +489,7 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
       a.term = term;
       a.nprobe = nprobe;
       a.R = R;
+      a.sorted = (p && p->rerank > 0) ? 0 : 1;
       a.out_keys = skeys;
       launch_ivfpq_scan_fast(a, s);
     }

@@ -19,7 +19,9 @@ struct FastScanArgs {
   const float* term;      // nq x nprobe coarse distances (exact FP32)
   int nprobe;
   int R;                  // shortlist length
+  int sorted;             // 1: shortlist sorted ascending (it is the answer)
   uint64_t* out_keys;     // nq x R (distance, CSR position)
+  int cap, Rp;            // set by the launcher
 };
 
 struct RerankArgs {
@@ -32,15 +34,17 @@ struct RerankArgs {
   int R, k;
   float* out_d;
   int64_t* out_l;
+  int kp;                 // set by the launcher
 };
 
 void launch_vec_terms(const int64_t* off, int nlist, const uint8_t* codes, const float* pq,
                       const float* cent, int d, int M, float* out, cudaStream_t s);
-void launch_coarse_recheck(const float* q, int64_t nq, int d, const float* cent, int metric,
-                           const uint64_t* cand, int nc, int nprobe, int32_t* probes, float* term,
-                           cudaStream_t s);
-void launch_ivfpq_scan_fast(const FastScanArgs& a, cudaStream_t s);
-void launch_rerank_fast(const RerankArgs& a, cudaStream_t s);
+// Top-nc of the approximate coarse distances, exact FP32 recheck, top-nprobe.
+void launch_coarse_fast(const float* approx, int64_t nq, int nlist, const float* q, int d,
+                        const float* cent, int metric, int nc, int nprobe, int32_t* probes,
+                        float* term, cudaStream_t s);
+void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s);
+void launch_rerank_fast(RerankArgs a, cudaStream_t s);
 void launch_short_to_results(const uint64_t* keys, int64_t nq, int R, int k, const uint32_t* ids,
                              int metric, float* out_d, int64_t* out_l, cudaStream_t s);
 

@@ -81,6 +81,16 @@ struct Arena {
 };
 inline size_t ws_bytes(size_t count, size_t elem) { return (count * elem + 255) & ~size_t(255); }
 
+// Raises a kernel's dynamic shared-memory limit to at least `bytes`. The
+// limit only ever grows (a per-kernel high-water mark), so a concurrent
+// launch that needs more is never undercut by one that needs less. Needed
+// whenever static + dynamic shared memory exceeds 48 KB.
+void raise_smem_limit(const void* kernel, size_t bytes);
+template <typename K>
+inline void smem_limit(K kernel, size_t bytes) {
+  raise_smem_limit(reinterpret_cast<const void*>(kernel), bytes);
+}
+
 // One per concurrent call: its own stream and scratch, so concurrent
 // read-only searches (the reference releases the GIL around search,
 // python/mojovec_python.mojo:1074) never share mutable state.

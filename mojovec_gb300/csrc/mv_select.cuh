@@ -143,4 +143,129 @@ struct BlockTopK {
   }
 };
 
+// ---------------------------------------------------------------------------
+// Block radix select: the R smallest of n distinct 64-bit keys held in
+// shared memory, in O(passes * n) shared-memory accesses instead of the
+// O(n log^2 n) of a sort.
+//
+// The keys between the block's min and max share their high bits; digits of
+// 11 bits are taken from the first bit where min and max differ. Each pass
+// histograms the digit of the keys still matching the chosen prefix, finds
+// the bucket holding the R-th key and extends the prefix; it stops as soon as
+// that bucket is taken whole. The result (all keys <= the final bound) is
+// exactly the R smallest; it is written unsorted to out[0, R) and does not
+// depend on the order of the input.
+// ---------------------------------------------------------------------------
+struct RadixScratch {
+  uint32_t hist[2048];
+  uint32_t wsum[32];
+  unsigned long long lo, hi;
+  uint32_t bucket, before;
+  int out_n;
+};
+
+// Returns min(n, R). All threads of the block must call it with the same
+// arguments. keys[0, n) are not modified; out must not alias keys. Keys are
+// expected to be distinct; equal keys at the boundary are cut at R.
+template <int NT>
+__device__ int block_radix_select(const uint64_t* keys, int n, int R, uint64_t* out,
+                                  RadixScratch& s) {
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  constexpr int NW = NT / 32;
+  if (n <= R) {
+    for (int i = tid; i < n; i += NT) out[i] = keys[i];
+    __syncthreads();
+    return n;
+  }
+  // min / max of the keys
+  unsigned long long lo = ~0ull, hi = 0ull;
+  for (int i = tid; i < n; i += NT) {
+    const unsigned long long v = keys[i];
+    lo = v < lo ? v : lo;
+    hi = v > hi ? v : hi;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long a = __shfl_xor_sync(0xffffffffu, lo, o);
+    const unsigned long long b = __shfl_xor_sync(0xffffffffu, hi, o);
+    lo = a < lo ? a : lo;
+    hi = b > hi ? b : hi;
+  }
+  if (tid == 0) {
+    s.lo = ~0ull;
+    s.hi = 0ull;
+    s.out_n = 0;
+  }
+  __syncthreads();
+  if (lane == 0) {
+    atomicMin(&s.lo, lo);
+    atomicMax(&s.hi, hi);
+  }
+  __syncthreads();
+  lo = s.lo;
+  hi = s.hi;
+  // shift = number of low bits still undetermined
+  int shift = 64 - __clzll((long long)(lo ^ hi));
+  unsigned long long prefix = shift >= 64 ? 0ull : (lo >> shift) << shift;
+  int need = R;
+  while (shift > 0) {
+    const int bits = shift < 11 ? shift : 11;
+    const int nb = 1 << bits;
+    shift -= bits;
+    const int top = shift + bits;  // bits at or above `top` must match the prefix
+    for (int b = tid; b < nb; b += NT) s.hist[b] = 0;
+    __syncthreads();
+    for (int i = tid; i < n; i += NT) {
+      const unsigned long long v = keys[i];
+      const bool match = top >= 64 || ((v >> top) == (prefix >> top));
+      if (match) atomicAdd(&s.hist[(uint32_t)(v >> shift) & (uint32_t)(nb - 1)], 1u);
+    }
+    __syncthreads();
+    // exclusive scan over nb bins: each thread owns a contiguous run
+    const int per = (nb + NT - 1) / NT;
+    const int b0 = tid * per;
+    uint32_t local = 0;
+    for (int b = b0; b < b0 + per && b < nb; ++b) local += s.hist[b];
+    uint32_t incl = local;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    if (lane == 31) s.wsum[warp] = incl;
+    __syncthreads();
+    uint32_t wbase = 0;
+    for (int w = 0; w < warp; ++w) wbase += s.wsum[w];
+    uint32_t run = wbase + incl - local;  // bins before b0
+    for (int b = b0; b < b0 + per && b < nb; ++b) {
+      const uint32_t h = s.hist[b];
+      if (run < (uint32_t)need && (uint32_t)need <= run + h) {
+        s.bucket = (uint32_t)b;
+        s.before = run;
+      }
+      run += h;
+    }
+    __syncthreads();
+    const uint32_t b = s.bucket;
+    need -= (int)s.before;
+    prefix |= (unsigned long long)b << shift;
+    const bool whole = s.hist[b] == (uint32_t)need;
+    __syncthreads();
+    if (whole) break;
+  }
+  // keys <= bound are exactly the R smallest
+  const unsigned long long bound = shift >= 64 ? ~0ull : (prefix | ((1ull << shift) - 1ull));
+  for (int i0 = 0; i0 < n; i0 += NT) {
+    const int i = i0 + tid;
+    const bool take = i < n && keys[i] <= bound;
+    const unsigned mask = __ballot_sync(0xffffffffu, take);
+    int base = 0;
+    if (lane == 0 && mask) base = atomicAdd(&s.out_n, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    const int slot = base + __popc(mask & ((1u << lane) - 1u));
+    if (take && slot < R) out[slot] = keys[i];  // equal keys (duplicate ids) never overflow
+  }
+  __syncthreads();
+  return R;
+}
+
 }  // namespace mv

@@ -112,3 +112,26 @@ def test_fast_untrained_and_small_lists(mv):
     d, l = g.search(base[:3], 50, form=mv.FORM_FAST, nprobe=8, rerank=100)
     assert (l[:, 20:] == -1).all() and set(l[0, :20].tolist()) == set(range(20))
     assert l[0, 0] == 0 and d[0, 0] == 0.0
+
+
+def test_fast_search_in_fresh_process():
+    """Each kernel's shared-memory limit is raised on first use; a search in
+    a fresh process must not depend on an earlier call having raised it."""
+    import os
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    script = (
+        "import numpy as np, mojovec_gb300 as mv\n"
+        "from mojovec_gb300 import synth\n"
+        "b, q = synth.sift_like(20000, d=128, n_centers=64, nq=300, seed=5)\n"
+        "g = mv.IndexIVFPQ(128, 64, 16); g.train(b, niter_coarse=3, niter_pq=3); g.add(b)\n"
+        "d, l = g.search(q, 10, form=mv.FORM_FAST, nprobe=16, rerank=256)\n"
+        "d2, l2 = g.search(q, 10, form=mv.FORM_FAST, nprobe=16)\n"
+        "assert (l >= 0).all() and (l2 >= 0).all()\n"
+        "print('ok')\n"
+    )
+    r = subprocess.run([sys.executable, "-c", script], cwd=root, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0 and "ok" in r.stdout, r.stderr[-2000:]
