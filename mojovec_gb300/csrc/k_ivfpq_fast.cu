@@ -106,7 +106,10 @@ __global__ void __launch_bounds__(FT)
   }
 }
 
+// Sum of the M table entries of one code; four partial sums break the
+// dependency chain (the fast form does not reproduce the reference's order).
 __device__ __forceinline__ float adc_fast(const float* lut, const uint8_t* code, int M, float acc) {
+  float p[4] = {acc, 0.0f, 0.0f, 0.0f};
   if ((M & 15) == 0) {
     for (int m0 = 0; m0 < M; m0 += 16) {
       const uint4 v = *reinterpret_cast<const uint4*>(code + m0);
@@ -114,7 +117,7 @@ __device__ __forceinline__ float adc_fast(const float* lut, const uint8_t* code,
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int b = 0; b < 4; ++b) acc += lut[((m0 + 4 * i + b) << 8) + ((w[i] >> (8 * b)) & 255u)];
+        for (int b = 0; b < 4; ++b) p[b] += lut[((m0 + 4 * i + b) << 8) + ((w[i] >> (8 * b)) & 255u)];
     }
   } else if ((M & 7) == 0) {
     for (int m0 = 0; m0 < M; m0 += 8) {
@@ -123,68 +126,201 @@ __device__ __forceinline__ float adc_fast(const float* lut, const uint8_t* code,
 #pragma unroll
       for (int i = 0; i < 2; ++i)
 #pragma unroll
-        for (int b = 0; b < 4; ++b) acc += lut[((m0 + 4 * i + b) << 8) + ((w[i] >> (8 * b)) & 255u)];
+        for (int b = 0; b < 4; ++b) p[b] += lut[((m0 + 4 * i + b) << 8) + ((w[i] >> (8 * b)) & 255u)];
     }
   } else {
-    for (int m = 0; m < M; ++m) acc += lut[(m << 8) + code[m]];
+    for (int m = 0; m < M; ++m) p[m & 3] += lut[(m << 8) + code[m]];
   }
-  return acc;
+  return (p[0] + p[1]) + (p[2] + p[3]);
 }
 
-// ADC scan, one CTA per query. Candidate keys (distance, CSR position)
-// are staged contiguously in shared memory; whenever the next chunk would
-// overflow the staging area, and once at the end, a radix select keeps the R
-// smallest. The shortlist is written unsorted (the rerank orders it), or
-// sorted when it is the final answer.
+// Per-query table lut[m][k] = scale * <q_m, C[m][k]>: warp w builds
+// subspaces w, w + 8, ...; each lane owns 8 codewords and keeps q_m in
+// registers, with the codeword rows read as float4 when dsub is 4 or 8.
+__device__ __forceinline__ void build_lut(float* lut, const float* qv, const float* pq, int M,
+                                          int dsub, float scale) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int mm = warp; mm < M; mm += FT / 32) {
+    const float* cm = pq + (int64_t)mm * 256 * dsub;
+    const float* xm = qv + mm * dsub;
+    if (dsub == 8) {
+      const float4 qa = *reinterpret_cast<const float4*>(xm);
+      const float4 qb = *reinterpret_cast<const float4*>(xm + 4);
+      float4 ca[8], cb[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const float* c = cm + (lane + 32 * u) * 8;
+        ca[u] = __ldg(reinterpret_cast<const float4*>(c));
+        cb[u] = __ldg(reinterpret_cast<const float4*>(c + 4));
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        float dot = qa.x * ca[u].x;
+        dot = fmaf(qa.y, ca[u].y, dot);
+        dot = fmaf(qa.z, ca[u].z, dot);
+        dot = fmaf(qa.w, ca[u].w, dot);
+        dot = fmaf(qb.x, cb[u].x, dot);
+        dot = fmaf(qb.y, cb[u].y, dot);
+        dot = fmaf(qb.z, cb[u].z, dot);
+        dot = fmaf(qb.w, cb[u].w, dot);
+        lut[(mm << 8) + lane + 32 * u] = scale * dot;
+      }
+    } else if (dsub == 4) {
+      const float4 qa = *reinterpret_cast<const float4*>(xm);
+      float4 ca[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) ca[u] = __ldg(reinterpret_cast<const float4*>(cm + (lane + 32 * u) * 4));
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        float dot = qa.x * ca[u].x;
+        dot = fmaf(qa.y, ca[u].y, dot);
+        dot = fmaf(qa.z, ca[u].z, dot);
+        dot = fmaf(qa.w, ca[u].w, dot);
+        lut[(mm << 8) + lane + 32 * u] = scale * dot;
+      }
+    } else {
+      for (int u = 0; u < 8; ++u) {
+        const float* c = cm + (lane + 32 * u) * dsub;
+        float dot = 0.0f;
+        for (int t = 0; t < dsub; ++t) dot = fmaf(xm[t], c[t], dot);
+        lut[(mm << 8) + lane + 32 * u] = scale * dot;
+      }
+    }
+  }
+}
+
+// ADC scan, one CTA per query. The probed lists are laid end to end in one
+// candidate index space (prefix sums of their lengths in shared memory), so
+// every thread has work whatever the list lengths. Candidate keys are staged
+// as (ordered distance, CSR position) word pairs; whenever the next chunk
+// would overflow the staging area, and once at the end, a radix select keeps
+// the R smallest. The shortlist is written unsorted (the rerank orders it),
+// or sorted when it is the final answer.
 __global__ void __launch_bounds__(FT) k_ivfpq_scan_fast(FastScanArgs a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int M = a.M, d = a.d, dsub = d / M;
   float* lut = reinterpret_cast<float*>(smraw);
   float* qv = lut + M * 256;
-  uint64_t* cand =
+  uint64_t* outb =
       reinterpret_cast<uint64_t*>(smraw + (((size_t)(M * 256 + d) * 4 + 15) & ~size_t(15)));
-  uint64_t* outb = cand + a.cap;  // R (padded to a power of two when sorting)
+  uint32_t* khi = reinterpret_cast<uint32_t*>(outb + a.Rp);
+  uint32_t* klo = khi + a.cap;
+  int64_t* poff = reinterpret_cast<int64_t*>(klo + a.cap);  // nprobe list offsets
+  int* pbeg = reinterpret_cast<int*>(poff + a.nprobe);      // nprobe + 1 prefix sums
+  float* pterm = reinterpret_cast<float*>(pbeg + a.nprobe + 1);
   __shared__ RadixScratch rs;
+  __shared__ int s_fill;
   const int64_t row = blockIdx.x;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) s_fill = 0;
   for (int j = threadIdx.x; j < d; j += FT) qv[j] = a.q[row * d + j];
+  // probe table: offsets, lengths -> prefix sums (warp 0)
+  if (threadIdx.x < 32) {
+    int carry = 0;
+    for (int p0 = 0; p0 < a.nprobe; p0 += 32) {
+      const int p = p0 + lane;
+      int len = 0;
+      if (p < a.nprobe) {
+        const int list = a.probes[row * a.nprobe + p];
+        int64_t off = 0;
+        if (list >= 0) {
+          off = a.list_off[list];
+          len = (int)(a.list_off[list + 1] - off);
+        }
+        poff[p] = off;
+        pterm[p] = a.term[row * a.nprobe + p];
+      }
+      int incl = len;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      if (p < a.nprobe) pbeg[p] = carry + incl - len;
+      carry += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (lane == 0) pbeg[a.nprobe] = carry;
+  }
   __syncthreads();
   const float scale = a.metric == MV_METRIC_L2 ? -2.0f : -1.0f;
-  for (int e = threadIdx.x; e < M * 256; e += FT) {
-    const int mm = e >> 8, kk = e & 255;
-    const float* c = a.pq + ((int64_t)mm * 256 + kk) * dsub;
-    const float* x = qv + mm * dsub;
-    float dot = 0.0f;
-    for (int t = 0; t < dsub; ++t) dot = fmaf(x[t], c[t], dot);
-    lut[e] = scale * dot;
-  }
+  build_lut(lut, qv, a.pq, M, dsub, scale);
   __syncthreads();
+  const int total = pbeg[a.nprobe];
   const int chunk = a.cap - a.R;
   int m = 0;
-  for (int p = 0; p < a.nprobe; ++p) {
-    const int list = a.probes[row * a.nprobe + p];
-    if (list < 0) continue;
-    const int64_t off = a.list_off[list];
-    const int64_t ls = a.list_off[list + 1] - off;
-    const float t1 = a.term[row * a.nprobe + p];
-    for (int64_t j0 = 0; j0 < ls; j0 += chunk) {
-      const int len = (int)min((int64_t)chunk, ls - j0);
-      if (m + len > a.cap) {
-        const int r = block_radix_select<FT>(cand, m, a.R, outb, rs);
-        for (int j = threadIdx.x; j < r; j += FT) cand[j] = outb[j];
-        __syncthreads();
-        m = r;
+  int p = 0;  // per-thread probe cursor (candidate indices only grow)
+  // Keys at or above `bound` cannot enter the shortlist once R keys below
+  // it have been seen; it tightens after every intermediate select.
+  unsigned long long bound = ~0ull;
+  for (int base = 0; base < total; base += chunk) {
+    const int len = min(chunk, total - base);
+    if (m + len > a.cap) {
+      const int r = block_radix_select_soa<FT>(khi, klo, m, a.R, outb, rs);
+      unsigned long long mx = 0ull;
+      for (int j = threadIdx.x; j < r; j += FT) {
+        const uint64_t k = outb[j];
+        khi[j] = (uint32_t)(k >> 32);
+        klo[j] = (uint32_t)k;
+        mx = k > mx ? k : mx;
       }
-      for (int j = threadIdx.x; j < len; j += FT) {
-        const int64_t pos = off + j0 + j;
-        float acc = t1 + (a.vterm ? a.vterm[pos] : 0.0f);
-        acc = adc_fast(lut, a.codes + pos * M, M, acc);
-        cand[m + j] = make_key(acc, (uint32_t)pos);
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xffffffffu, mx, o);
+        mx = t > mx ? t : mx;
       }
-      m += len;
+      if (threadIdx.x == 0) rs.lo = 0ull;
+      __syncthreads();
+      if (lane == 0) atomicMax(&rs.lo, mx);
+      __syncthreads();
+      if (r == a.R) bound = rs.lo;  // the R-th smallest key so far
+      m = r;
+      if (threadIdx.x == 0) s_fill = m;
       __syncthreads();
     }
+    // Two candidates per thread per step: both rows' loads are issued before
+    // either table walk.
+    for (int j0 = 0; j0 < len; j0 += 2 * FT) {
+      const int j = j0 + threadIdx.x;
+      const bool has0 = j < len;
+      const int c0 = base + (has0 ? j : 0), c1 = c0 + FT;
+      const bool has1 = j + FT < len;
+      while (pbeg[p + 1] <= c0) ++p;
+      const int64_t pos0 = poff[p] + (c0 - pbeg[p]);
+      const float t0 = pterm[p];
+      int p1 = p;
+      if (has1)
+        while (pbeg[p1 + 1] <= c1) ++p1;
+      const int64_t pos1 = has1 ? poff[p1] + (c1 - pbeg[p1]) : pos0;
+      const float t1 = pterm[p1];
+      const float v0 = a.vterm ? a.vterm[pos0] : 0.0f;
+      const float v1 = a.vterm ? a.vterm[pos1] : 0.0f;
+      const float d0 = adc_fast(lut, a.codes + pos0 * M, M, t0 + v0);
+      const float d1 = adc_fast(lut, a.codes + pos1 * M, M, t1 + v1);
+      const unsigned long long k0 = ((unsigned long long)float_to_ordered(d0) << 32) | (uint32_t)pos0;
+      const unsigned long long k1 = ((unsigned long long)float_to_ordered(d1) << 32) | (uint32_t)pos1;
+      const bool in0 = has0 && k0 < bound;
+      const bool in1 = has1 && k1 < bound;
+      const unsigned b0 = __ballot_sync(0xffffffffu, in0);
+      const unsigned b1 = __ballot_sync(0xffffffffu, in1);
+      int wbase = 0;
+      if (lane == 0 && (b0 | b1)) wbase = atomicAdd(&s_fill, __popc(b0) + __popc(b1));
+      wbase = __shfl_sync(0xffffffffu, wbase, 0);
+      const unsigned below = (1u << lane) - 1u;
+      if (in0) {
+        const int slot = wbase + __popc(b0 & below);
+        khi[slot] = (uint32_t)(k0 >> 32);
+        klo[slot] = (uint32_t)k0;
+      }
+      if (in1) {
+        const int slot = wbase + __popc(b0) + __popc(b1 & below);
+        khi[slot] = (uint32_t)(k1 >> 32);
+        klo[slot] = (uint32_t)k1;
+      }
+      if (has0) p = p1;
+    }
+    __syncthreads();
+    m = s_fill;
+    __syncthreads();
   }
-  const int r = block_radix_select<FT>(cand, m, a.R, outb, rs);
+  const int r = block_radix_select_soa<FT>(khi, klo, m, a.R, outb, rs);
   if (a.sorted) {
     for (int j = r + threadIdx.x; j < a.Rp; j += FT) outb[j] = KEY_NONE;
     __syncthreads();
@@ -208,44 +344,64 @@ __global__ void __launch_bounds__(FT) k_rerank_fast(RerankArgs a) {
   for (int j = threadIdx.x; j < d; j += FT) qv[j] = a.q[row * d + j];
   __syncthreads();
   const uint64_t* cand = a.cand + row * a.R;
-  for (int c = warp; c < a.R; c += FT / 32) {
-    const uint64_t key = cand[c];
-    uint64_t out = KEY_NONE - (uint64_t)c;  // distinct keys for empty slots
-    if (key != KEY_NONE) {
-      const uint32_t pos = key_id(key);
-      const float* x = a.raw + (int64_t)pos * d;
-      float acc = 0.0f;
-      if ((d & 3) == 0) {
-        for (int j = lane * 4; j < d; j += 128) {
-          const float4 v = *reinterpret_cast<const float4*>(x + j);
+  // Each warp takes U candidates at a time and issues all of their row loads
+  // before reducing, so U rows per warp are in flight.
+  constexpr int U = 4;
+  for (int c0 = warp * U; c0 < a.R; c0 += (FT / 32) * U) {
+    uint32_t pos[U];
+    float acc[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int c = c0 + u;
+      const uint64_t key = c < a.R ? cand[c] : KEY_NONE;
+      pos[u] = key == KEY_NONE ? 0xffffffffu : key_id(key);
+      acc[u] = 0.0f;
+    }
+    if ((d & 3) == 0) {
+      for (int j = lane * 4; j < d; j += 128) {
+        float4 v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          v[u] = pos[u] != 0xffffffffu
+                     ? *reinterpret_cast<const float4*>(a.raw + (int64_t)pos[u] * d + j)
+                     : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float q0 = qv[j], q1 = qv[j + 1], q2 = qv[j + 2], q3 = qv[j + 3];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
           if (a.metric == MV_METRIC_L2) {
-            const float d0 = qv[j] - v.x, d1 = qv[j + 1] - v.y, d2 = qv[j + 2] - v.z,
-                        d3 = qv[j + 3] - v.w;
-            acc = fmaf(d0, d0, acc);
-            acc = fmaf(d1, d1, acc);
-            acc = fmaf(d2, d2, acc);
-            acc = fmaf(d3, d3, acc);
+            const float d0 = q0 - v[u].x, d1 = q1 - v[u].y, d2 = q2 - v[u].z, d3 = q3 - v[u].w;
+            acc[u] = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, acc[u]))));
           } else {
-            acc = fmaf(qv[j], v.x, acc);
-            acc = fmaf(qv[j + 1], v.y, acc);
-            acc = fmaf(qv[j + 2], v.z, acc);
-            acc = fmaf(qv[j + 3], v.w, acc);
-          }
-        }
-      } else {
-        for (int j = lane; j < d; j += 32) {
-          if (a.metric == MV_METRIC_L2) {
-            const float df = qv[j] - x[j];
-            acc = fmaf(df, df, acc);
-          } else {
-            acc = fmaf(qv[j], x[j], acc);
+            acc[u] = fmaf(q0, v[u].x, fmaf(q1, v[u].y, fmaf(q2, v[u].z, fmaf(q3, v[u].w, acc[u]))));
           }
         }
       }
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      out = make_key(a.metric == MV_METRIC_L2 ? acc : -acc, a.ids[pos]);
+    } else {
+      for (int j = lane; j < d; j += 32) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          if (pos[u] == 0xffffffffu) continue;
+          const float x = a.raw[(int64_t)pos[u] * d + j];
+          if (a.metric == MV_METRIC_L2) {
+            const float df = qv[j] - x;
+            acc[u] = fmaf(df, df, acc[u]);
+          } else {
+            acc[u] = fmaf(qv[j], x, acc[u]);
+          }
+        }
+      }
     }
-    if (lane == 0) ck[c] = out;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      float t = acc[u];
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      const int c = c0 + u;
+      if (lane == 0 && c < a.R) {
+        ck[c] = pos[u] == 0xffffffffu
+                    ? KEY_NONE - (uint64_t)c  // distinct keys for empty slots
+                    : make_key(a.metric == MV_METRIC_L2 ? t : -t, a.ids[pos[u]]);
+      }
+    }
   }
   __syncthreads();
   const int r = block_radix_select<FT>(ck, a.R, a.k, outb, rs);
@@ -313,14 +469,15 @@ void launch_coarse_fast(const float* approx, int64_t nq, int nlist, const float*
   MV_CHECK_CUDA(cudaGetLastError());
 }
 
-int fast_scan_cap(int R) { return std::max(3072, 2 * R + 1024); }
+int fast_scan_cap(int R) { return std::max(2048, 2 * R + 1024); }
 
 void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s) {
   if (a.nq == 0) return;
   a.cap = fast_scan_cap(a.R);
   a.Rp = next_pow2(a.R);
   const size_t smem = (((size_t)(a.M * 256 + a.d) * 4 + 15) & ~size_t(15)) +
-                      (size_t)(a.cap + a.Rp) * 8;
+                      (size_t)a.Rp * 8 + (size_t)a.cap * 8 + (size_t)a.nprobe * 8 +
+                      (size_t)(a.nprobe + 1) * 4 + (size_t)a.nprobe * 4;
   MV_REQUIRE(smem <= 220 * 1024, MV_ERR_UNSUPPORTED, "fast IVF-PQ scan: M, d or shortlist too large");
   smem_attr(k_ivfpq_scan_fast, smem);
   k_ivfpq_scan_fast<<<(unsigned)a.nq, FT, smem, s>>>(a);

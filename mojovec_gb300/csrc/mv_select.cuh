@@ -268,4 +268,120 @@ __device__ int block_radix_select(const uint64_t* keys, int n, int R, uint64_t* 
   return R;
 }
 
+// Same selection over keys stored as two word arrays, key = (hi << 32) | lo
+// (hi: ordered distance, lo: payload). Histogram passes whose digit lies in
+// the high word read 4 bytes per key; the low word is read only when
+// distances tie down to the last bit. Histogram updates are aggregated per
+// warp (one atomic per distinct digit).
+template <int NT>
+__device__ int block_radix_select_soa(const uint32_t* khi, const uint32_t* klo, int n, int R,
+                                      uint64_t* out, RadixScratch& s) {
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  auto key_at = [&](int i) -> unsigned long long {
+    return ((unsigned long long)khi[i] << 32) | klo[i];
+  };
+  if (n <= R) {
+    for (int i = tid; i < n; i += NT) out[i] = key_at(i);
+    __syncthreads();
+    return n;
+  }
+  unsigned long long lo = ~0ull, hi = 0ull;
+  for (int i = tid; i < n; i += NT) {
+    const unsigned long long v = key_at(i);
+    lo = v < lo ? v : lo;
+    hi = v > hi ? v : hi;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long a = __shfl_xor_sync(0xffffffffu, lo, o);
+    const unsigned long long b = __shfl_xor_sync(0xffffffffu, hi, o);
+    lo = a < lo ? a : lo;
+    hi = b > hi ? b : hi;
+  }
+  if (tid == 0) {
+    s.lo = ~0ull;
+    s.hi = 0ull;
+    s.out_n = 0;
+  }
+  __syncthreads();
+  if (lane == 0) {
+    atomicMin(&s.lo, lo);
+    atomicMax(&s.hi, hi);
+  }
+  __syncthreads();
+  lo = s.lo;
+  hi = s.hi;
+  int shift = 64 - __clzll((long long)(lo ^ hi));
+  unsigned long long prefix = shift >= 64 ? 0ull : (lo >> shift) << shift;
+  int need = R;
+  while (shift > 0) {
+    const int bits = shift < 11 ? shift : 11;
+    const int nb = 1 << bits;
+    shift -= bits;
+    const int top = shift + bits;
+    for (int b = tid; b < nb; b += NT) s.hist[b] = 0;
+    __syncthreads();
+    const bool hi_only = shift >= 32;
+    for (int i0 = 0; i0 < n; i0 += NT) {
+      const int i = i0 + tid;
+      bool match = false;
+      uint32_t digit = 0;
+      if (i < n) {
+        const unsigned long long v = hi_only ? ((unsigned long long)khi[i] << 32) : key_at(i);
+        match = top >= 64 || ((v >> top) == (prefix >> top));
+        digit = (uint32_t)(v >> shift) & (uint32_t)(nb - 1);
+      }
+      const unsigned act = __ballot_sync(0xffffffffu, match);
+      if (match) {
+        const unsigned peers = __match_any_sync(act, digit);
+        if (lane == __ffs(peers) - 1) atomicAdd(&s.hist[digit], (uint32_t)__popc(peers));
+      }
+    }
+    __syncthreads();
+    const int per = (nb + NT - 1) / NT;
+    const int b0 = tid * per;
+    uint32_t local = 0;
+    for (int b = b0; b < b0 + per && b < nb; ++b) local += s.hist[b];
+    uint32_t incl = local;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    if (lane == 31) s.wsum[warp] = incl;
+    __syncthreads();
+    uint32_t wbase = 0;
+    for (int w = 0; w < warp; ++w) wbase += s.wsum[w];
+    uint32_t run = wbase + incl - local;
+    for (int b = b0; b < b0 + per && b < nb; ++b) {
+      const uint32_t h = s.hist[b];
+      if (run < (uint32_t)need && (uint32_t)need <= run + h) {
+        s.bucket = (uint32_t)b;
+        s.before = run;
+      }
+      run += h;
+    }
+    __syncthreads();
+    const uint32_t b = s.bucket;
+    need -= (int)s.before;
+    prefix |= (unsigned long long)b << shift;
+    const bool whole = s.hist[b] == (uint32_t)need;
+    __syncthreads();
+    if (whole) break;
+  }
+  const unsigned long long bound = shift >= 64 ? ~0ull : (prefix | ((1ull << shift) - 1ull));
+  for (int i0 = 0; i0 < n; i0 += NT) {
+    const int i = i0 + tid;
+    const unsigned long long v = i < n ? key_at(i) : ~0ull;
+    const bool take = i < n && v <= bound;
+    const unsigned mask = __ballot_sync(0xffffffffu, take);
+    int base = 0;
+    if (lane == 0 && mask) base = atomicAdd(&s.out_n, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    const int slot = base + __popc(mask & ((1u << lane) - 1u));
+    if (take && slot < R) out[slot] = v;
+  }
+  __syncthreads();
+  return R;
+}
+
 }  // namespace mv
