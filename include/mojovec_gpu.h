@@ -139,6 +139,25 @@ int32_t mv_ivfpq_search_device(mv_ivfpq* index, const float* d_x, int64_t nq, in
                                const mv_search_params* params, float* d_distances,
                                int64_t* d_labels, void* stream);
 
+/* Plain IVF-PQ search that allocates no device memory. No counterpart in
+ * the reference: it exists for callers that cannot allocate while they
+ * search, such as a serving process that gives all GPU memory to its own
+ * pool at start-up, or a host loop that must not absorb cudaFree's implicit
+ * device synchronisation. Inputs and outputs are device buffers owned by the
+ * caller (d_x nq*d, d_distances / d_labels nq*k); nprobe 0 means the
+ * index's nprobe; no filter. Its scratch is one fixed array of
+ * MV_NOALLOC_SCRATCH_BYTES inside the library, held by every GPU that loads
+ * it until the process exits; queries are processed in batches that fit,
+ * and a configuration whose single query needs more scratch is rejected with
+ * MV_ERR_ARG. The first call on a device resolves the array's address (make
+ * it before any stream capture). All calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller. Returns
+ * after enqueueing on `stream` (NULL = the legacy default stream). */
+#define MV_NOALLOC_SCRATCH_BYTES (8u * 1024u * 1024u)
+int32_t mv_ivfpq_search_noalloc(mv_ivfpq* index, const float* d_x, int64_t nq, int32_t k,
+                                int32_t nprobe, float* d_distances, int64_t* d_labels,
+                                void* stream);
+
 /* ---- Flat index: replaces IndexFlat (index/index_flat.mojo:117-330) ---- */
 int32_t mv_flat_create(mv_ctx* ctx, int32_t d, int32_t metric, mv_flat** out);
 int32_t mv_flat_destroy(mv_flat* index);

@@ -89,6 +89,7 @@ SIGNATURES = {
     "mv_ivfpq_get_lists": (_i32, [_vp, _vp, _vp, _vp]),
     "mv_ivfpq_search": (_i32, [_vp, _vp, _i64, _i32, _vp, _i64, _vp, _vp, _vp]),
     "mv_ivfpq_search_device": (_i32, [_vp, _vp, _i64, _i32, _vp, _i64, _vp, _vp, _vp, _vp]),
+    "mv_ivfpq_search_noalloc": (_i32, [_vp, _vp, _i64, _i32, _i32, _vp, _vp, _vp]),
     "mv_flat_create": (_i32, [_vp, _i32, _i32, C.POINTER(_vp)]),
     "mv_flat_destroy": (_i32, [_vp]),
     "mv_flat_add": (_i32, [_vp, _vp, _i64]),
