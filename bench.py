@@ -179,12 +179,19 @@ def _timed_steps(torch, step, steps, stream, flush):
     return float(sum(a.elapsed_time(b) for a, b in evs))
 
 
-def _max_over_ranks(torch, world, v):
+def _max_over_ranks(torch, world, v, device="cuda"):
+    """The slowest rank's time: all ranks' work counts as done only when the
+    last rank finishes."""
     if world == 1:
         return v
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device=device)
     torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
     return float(t.item())
+
+
+def aggregate_qps(world, nq, steps, max_ms):
+    """Whole-job throughput: every rank answered nq queries per step."""
+    return world * nq * steps / (max_ms / 1e3)
 
 
 def run_gpu(args, rank, world):
@@ -254,8 +261,8 @@ def run_gpu(args, rank, world):
             clk = clocks.stop()
         results[name]["ms"] = _max_over_ranks(torch, world, ms)
     total_ms = results["headline"]["ms"]
-    value = world * nq * args.steps / (total_ms / 1e3)
-    plain_qps = world * nq * args.steps / (results["plain"]["ms"] / 1e3)
+    value = aggregate_qps(world, nq, args.steps, total_ms)
+    plain_qps = aggregate_qps(world, nq, args.steps, results["plain"]["ms"])
     labels = results["headline"]["labels"]
 
     # ---- e2e through the host-buffer C ABI, queries in pinned memory ----

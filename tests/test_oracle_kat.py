@@ -1,0 +1,264 @@
+"""CPU tests of the oracle (the C++ restatement of the reference CPU path).
+
+* Known-answer tests ported from the reference's own test suite (each cites
+  the reference test it follows).
+* Published Philox4x32-10 known-answer vectors.
+* An independent numpy restatement of the SIMD operation order of
+  utils/distances.mojo, so the oracle's emulation is checked against a second
+  implementation, not only against itself.
+* The committed golden fixtures (tests/golden/make_golden.py).
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "oracle_golden.npz")
+
+
+def test_philox_published_known_answers(orc):
+    # Random123 kat_vectors for philox4x32_10
+    assert orc.philox_block([0, 0, 0, 0], [0, 0]).tolist() == [
+        0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    assert orc.philox_block([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2).tolist() == [
+        0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]
+    assert orc.philox_block([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344],
+                            [0xA4093822, 0x299F31D0]).tolist() == [
+        0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
+
+
+def _np_tree(v):
+    v = list(v)
+    while len(v) > 1:
+        h = len(v) // 2
+        v = [np.float32(v[i] + v[i + h]) for i in range(h)]
+    return v[0]
+
+
+def _np_l2_simd(x, y, W):
+    """utils/distances.mojo:43-143 restated with numpy float32 scalars."""
+    f = np.float32
+    d = len(x)
+    if d < W:
+        r = f(0)
+        for i in range(d):
+            df = f(x[i] - y[i])
+            r = f(r + f(df * df))
+        return r
+    acc = [[f(0)] * W for _ in range(4)]
+    i = 0
+    while i <= d - 4 * W:
+        for a in range(4):
+            for l in range(W):
+                df = f(x[i + a * W + l] - y[i + a * W + l])
+                acc[a][l] = f(np.float64(df) * np.float64(df) + np.float64(acc[a][l]))  # exact fma
+        i += 4 * W
+    s = [f(f(f(acc[0][l] + acc[1][l]) + acc[2][l]) + acc[3][l]) for l in range(W)]
+    while i <= d - W:
+        for l in range(W):
+            df = f(x[i + l] - y[i + l])
+            s[l] = f(np.float64(df) * np.float64(df) + np.float64(s[l]))
+        i += W
+    res = _np_tree(s)
+    for width, need in ((16, 32), (8, 16), (4, 8)):
+        if W >= need:
+            while i <= d - width:
+                r = [f(f(x[i + l] - y[i + l]) * f(x[i + l] - y[i + l])) for l in range(width)]
+                res = f(res + _np_tree(r))
+                i += width
+    while i < d:
+        df = f(x[i] - y[i])
+        res = f(res + f(df * df))
+        i += 1
+    return res
+
+
+@pytest.mark.parametrize("d", [1, 5, 8, 13, 32, 45, 96, 128, 131])
+@pytest.mark.parametrize("W", [4, 8])
+def test_l2_simd_order_matches_independent_restatement(orc, d, W):
+    # The numpy side forms fma as an exact float64 product plus a float64
+    # add, then rounds to float32: a double rounding that can differ from a
+    # single-rounded fma in rare halfway cases; these seeds do not hit one.
+    rng = np.random.default_rng(d * 10 + W)
+    x = rng.standard_normal(d).astype(np.float32)
+    y = rng.standard_normal(d).astype(np.float32)
+    assert np.float32(orc.l2_simd(x, y, W)) == _np_l2_simd(x, y, W)
+
+
+def test_index_flat_known_answers(orc):
+    # tests/test_index_flat.mojo:6-81
+    d, l = orc.flat_search(np.array([[0] * 4, [1] * 4, [2] * 4], np.float32),
+                           np.full((1, 4), 1.1, np.float32), 2)
+    assert set(l[0].tolist()) == {1, 2}
+    assert abs(d[0][0] - 0.04) < 1e-3 and abs(d[0][1] - 3.24) < 1e-3
+    d, l = orc.flat_search(np.array([[1] * 4, [2] * 4, [3] * 4], np.float32),
+                           np.ones((1, 4), np.float32), 2, metric=1)
+    assert sorted(d[0].tolist()) == [8.0, 12.0] and set(l[0].tolist()) == {1, 2}
+
+
+def test_signed_sq8_dot_exact(orc):
+    # tests/test_distances_simd.mojo:87-102
+    for dim in (1, 7, 16, 63, 64, 127, 128, 129):
+        idx = np.arange(dim)
+        x = ((idx * 37) % 255 - 127).astype(np.int8)
+        y = ((idx * 53 + 11) % 255 - 127).astype(np.int8)
+        assert orc.sq8_dot_s8(x, y) == int((x.astype(np.int64) * y.astype(np.int64)).sum())
+
+
+def test_pq_adc_identity(orc):
+    # tests/test_pq.mojo:57-114
+    x = orc.philox_uniform_matrix(191, 100, 16) * 2 - 1
+    pq = orc.pq_train(x, 4)
+    codes = orc.pq_compute_codes(pq, x)
+    dec = orc.pq_decode(pq, codes)
+    t = orc.pq_distance_table(pq, x[0])
+    adc = sum(float(t[m, codes[0, m]]) for m in range(4))
+    assert abs(adc - orc.l2_simd(x[0], dec[0], 4)) <= 1e-5
+
+
+def test_pq_reconstruction_error(orc):
+    # tests/test_pq.mojo:8-55
+    x = orc.philox_uniform_matrix(181, 1000, 16) * 2 - 1
+    pq = orc.pq_train(x, 4)
+    dec = orc.pq_decode(pq, orc.pq_compute_codes(pq, x))
+    assert ((x - dec) ** 2).sum(1).mean() < 1.0
+
+
+def test_kmeans_known_properties(orc):
+    # tests/test_kmeans.mojo:8-72
+    c, _ = orc.kmeans_train(np.ones((100, 16), np.float32), 5, niter=5)
+    assert np.isfinite(c).all()
+    c, _ = orc.kmeans_train(np.arange(80, dtype=np.float32).reshape(5, 16), 10, niter=5)
+    assert c.shape == (10, 16)
+    i = np.arange(257 * 8)
+    x = (((i * 37 + (i // 8) * 11) % 101) / 50.0 - 1.0).astype(np.float32).reshape(257, 8)
+    a, _ = orc.kmeans_train(x, 17, niter=5)
+    b, _ = orc.kmeans_train(x, 17, niter=5, nthreads=1)
+    assert np.array_equal(a, b)  # 32 fixed chunks: thread count does not matter
+
+
+def test_ivfpq_grid_known_answers(orc):
+    # tests/test_ivf_pq.mojo:48-77 and :209-232 (self-match, filter)
+    from mojovec_gb300 import synth
+
+    rows = synth.grid_vectors()
+    ix = orc.IVFPQ(8, 8, 2)
+    ix.train(rows)
+    ix.add(rows)
+    d, l = ix.search(rows[:1], 5, 4)
+    assert l[0][0] == 0 and d[0][0] < 1e-4
+    excl = np.zeros(256, np.uint8)
+    excl[0] = 1
+    _, l = ix.search(rows[:1], 1, 8, filter=excl)
+    assert l[0][0] != 0
+
+
+def test_ivfpq_sparse_tail_and_untrained(orc):
+    # index/index_ivf_pq.mojo:247-251, :284-286 (tests/test_ivf_flat.mojo:91-137)
+    ix = orc.IVFPQ(4, 1, 2)
+    d, l = ix.search(np.zeros((1, 4), np.float32), 3, 1)
+    assert (l == -1).all() and (d == np.float32(1e38)).all()
+    x = np.random.default_rng(0).standard_normal((300, 4)).astype(np.float32)
+    ix.train(x, 3, 3)
+    ix.add(x[:1], np.array([42], np.int64))
+    d, l = ix.search(x[:1], 5, 1)
+    assert l[0][0] == 42 and l[0][1:].tolist() == [-1] * 4
+    assert (d[0][1:] == np.float32(1e38)).all()
+
+
+def test_sq8_known_answers(orc):
+    # tests/test_metrics.mojo:56-96
+    s = orc.SQ8(3, 1)
+    s.add(np.array([[1, 0, 0], [-1, 0, 0], [0.5, 0, 0]], np.float32))
+    d, l = s.search(np.array([[1, 0, 0]], np.float32), 3)
+    assert l[0].tolist() == [0, 2, 1] and d[0][0] > d[0][1] > d[0][2]
+    t = orc.SQ8(2, 1)
+    t.add(np.array([[1.0, 0.25]], np.float32))
+    t.add(np.array([[-4.0, 0.0]], np.float32))
+    assert abs(t.params()[2] - 4.0 / 127.0) < 1e-6
+
+
+def test_accuracy_floors(orc):
+    # tests/test_accuracy.mojo:129-161 (IVF-PQ >= 0.50) and :190-230 (SQ8 IP >= 0.95)
+    db = orc.philox_uniform_matrix(42, 5000, 32) * 2 - 1
+    q = orc.philox_uniform_matrix(43, 100, 32) * 2 - 1
+    _, gt = orc.flat_search(db, q, 10)
+    ix = orc.IVFPQ(32, 64, 8)
+    ix.train(db)
+    ix.add(db)
+    _, l = ix.search(q, 10, 16)
+    assert orc.recall(gt, l) >= 0.50
+    _, gti = orc.flat_search(db, q, 10, metric=1)
+    s = orc.SQ8(32, 1)
+    s.add(db)
+    _, ls = s.search(q, 10)
+    assert orc.recall(gti, ls) >= 0.95
+
+
+def test_reference_heap_and_canonical_agree_without_ties(orc):
+    rng = np.random.default_rng(5)
+    base = rng.standard_normal((2000, 24)).astype(np.float32)
+    q = rng.standard_normal((20, 24)).astype(np.float32)
+    d0, l0 = orc.flat_search(base, q, 15, mode=orc.MODE_REFERENCE_HEAP)
+    d1, l1 = orc.flat_search(base, q, 15, mode=orc.MODE_CANONICAL)
+    assert np.array_equal(l0, l1) and np.array_equal(d0, d1)
+
+
+def test_normalize_errors(orc):
+    with pytest.raises(ValueError, match="finite"):
+        orc.normalize(np.array([[np.nan, 1.0]], np.float32))
+    with pytest.raises(ValueError, match="non-zero"):
+        orc.normalize(np.zeros((1, 3), np.float32))
+    x = np.array([[3.0, 4.0]], np.float32)
+    assert np.allclose(orc.normalize(x), [[0.6, 0.8]])
+
+
+def test_ground_truth_fp64(orc):
+    rng = np.random.default_rng(8)
+    base = rng.standard_normal((500, 16)).astype(np.float32)
+    q = rng.standard_normal((5, 16)).astype(np.float32)
+    d, l = orc.ground_truth(base, q, 5)
+    ref = ((q[:, None, :].astype(np.float64) - base[None].astype(np.float64)) ** 2).sum(-1)
+    assert np.array_equal(l, np.argsort(ref, axis=1, kind="stable")[:, :5])
+
+
+def test_golden_fixtures(orc):
+    """The oracle reproduces its committed fixtures bit for bit."""
+    from mojovec_gb300 import synth
+
+    g = np.load(GOLDEN)
+    assert np.array_equal(orc.philox_steps(0x4D4F4A4F564543, 16), g["philox_kmeans_seed_steps"])
+    for d in (1, 3, 4, 7, 8, 12, 31, 32, 33, 96, 128, 130, 257):
+        x, y = g[f"dist_d{d}_x"], g[f"dist_d{d}_y"]
+        got = np.array([orc.l2_simd(x, y, 8), orc.ip_simd(x, y, 8), orc.l2_simd(x, y, 4),
+                        orc.ip_simd(x, y, 4), orc.l2_simd(x, y, 64), orc.ip_simd(x, y, 64)],
+                       np.float32)
+        assert np.array_equal(got, g[f"dist_d{d}"]), d
+    rows = synth.grid_vectors()
+    ix = orc.IVFPQ(8, 8, 2)
+    ix.train(rows, niter_coarse=15, niter_pq=15)
+    ix.add(rows)
+    c, p = ix.codebooks()
+    assert np.array_equal(c, g["grid_centroids"]) and np.array_equal(p, g["grid_pq"])
+    off, ids, codes = ix.lists()
+    assert np.array_equal(off, g["grid_offsets"]) and np.array_equal(codes, g["grid_codes"])
+    d, l = ix.search(rows[:16], 5, 4)
+    assert np.array_equal(d, g["grid_dist"]) and np.array_equal(l, g["grid_labels"])
+    kc, ka = orc.kmeans_train(g["kmeans_x"], 17, niter=5)
+    assert np.array_equal(kc, g["kmeans_centroids"]) and np.array_equal(ka, g["kmeans_assign"])
+    ix2 = orc.IVFPQ(32, 16, 8)
+    ix2.set_codebooks(g["sift_centroids"], g["sift_pq"])
+    base, _ = synth.sift_like(4000, d=32, n_centers=40, nq=40, seed=3)
+    ix2.add(base)
+    d2, l2 = ix2.search(g["sift_queries"], 10, 3)
+    assert np.array_equal(d2, g["sift_dist"]) and np.array_equal(l2, g["sift_labels"])
+    for metric in (0, 1):
+        s = orc.SQ8(16, metric)
+        s.add(g["sq8_a"])
+        s.add(g["sq8_b"])
+        codes, norms = s.codes()
+        assert np.array_equal(codes, g[f"sq8_m{metric}_codes"])
+        assert np.array_equal(norms, g[f"sq8_m{metric}_norms"])
+        dd, ll = s.search(g["sq8_a"][:8], 5)
+        assert np.array_equal(dd, g[f"sq8_m{metric}_dist"]) and np.array_equal(ll, g[f"sq8_m{metric}_labels"])
