@@ -22,6 +22,11 @@ pinned memory and the device->host copy of distances and ids.
 `--impl reference` times the oracle (the C++ restatement of the reference's
 CPU path) on the host cores over a bounded query sample of the same
 workload, with an index it builds itself on the CPU.
+
+`--workload flat` measures the flat scan instead (1,000,000 x 128 of the
+same rows, 10,000 queries, k = 10 or 100, L2 or IP): the fast form (BF16
+tcgen05 GEMM with a per-row heap epilogue, exact FP32 rerank of a k * 4
+shortlist) against the plain FP32 form, with the GEMM's tensor roofline.
 """
 
 from __future__ import annotations
@@ -361,6 +366,153 @@ def run_gpu(args, rank, world):
     return out
 
 
+FLAT_METRIC = "Flat QPS (1Mx128 SIFT-like, 10k queries), BF16 tcgen05 + FP32 rerank of k*4 vs plain FP32"
+
+
+def run_flat(args, rank, world):
+    """Flat scan: plain FP32 (the reference's IndexFlat arithmetic) and the
+    fast form on the same rows; recall against the plain form, which equals
+    FP64 on these integer-valued rows."""
+    import torch
+
+    import mojovec_gb300 as mv
+
+    nb, nq, k = args.nb, args.nq, args.k
+    metric = mv.METRIC_L2 if args.metric == "l2" else mv.METRIC_IP
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    ctx = mv.Context(dev)
+    t_setup = time.perf_counter()
+    base, queries = build_workload(nb, nq)
+    flat = mv.IndexFlat(D, metric, ctx=ctx)
+    flat.add(base)
+    setup_s = time.perf_counter() - t_setup
+    rerank = args.rerank
+    fast = dict(form=mv.FORM_FAST, rerank=rerank)
+    plain = dict(form=mv.FORM_PLAIN)
+    d_q = torch.from_numpy(queries).cuda()
+    d_dist = torch.empty((nq, k), dtype=torch.float32, device="cuda")
+    d_lab = torch.empty((nq, k), dtype=torch.int64, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def make_step(opts):
+        def step():
+            flat.search_device(d_q.data_ptr(), nq, k, d_dist.data_ptr(), d_lab.data_ptr(),
+                               stream=stream.cuda_stream, **opts)
+        return step
+
+    results = {}
+    plain_steps = max(1, min(args.steps, 3))  # the FP32 scan is ~50x slower
+    for name, opts, steps in (("plain", plain, plain_steps), ("fast", fast, args.steps)):
+        step = make_step(opts)
+        for _ in range(args.warmup if name == "fast" else 1):
+            step()
+        torch.cuda.synchronize()
+        results[name] = {"labels": d_lab.cpu().numpy(), "dist": d_dist.cpu().numpy()}
+        if world > 1:
+            torch.distributed.barrier()
+        if name == "fast":
+            clocks = ClockSampler(dev)
+            clocks.start()
+            ctx.profile(True)
+            launches0 = ctx.kernel_launches()
+        ms = _timed_steps(torch, step, steps, stream, flush)
+        if name == "fast":
+            launches = ctx.kernel_launches() - launches0
+            stage = ctx.stage_times()
+            ctx.profile(False)
+            clk = clocks.stop()
+        results[name]["ms"] = _max_over_ranks(torch, world, ms) / steps
+    gt = results["plain"]["labels"]
+    rec = recall_at(gt, results["fast"]["labels"], k)
+    value = world * nq / (results["fast"]["ms"] / 1e3)
+    plain_qps = world * nq / (results["plain"]["ms"] / 1e3)
+
+    pinned = torch.empty((nq, D), dtype=torch.float32).pin_memory()
+    pinned.copy_(torch.from_numpy(queries))
+    hq = pinned.numpy()
+    flat.search(hq, k, **fast)
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _, elab = flat.search(hq, k, **fast)
+    e2e_s = _max_over_ranks(torch, world, time.perf_counter() - t0)
+    e2e_qps = world * nq * args.steps / e2e_s
+    assert np.array_equal(elab, results["fast"]["labels"]), "host and device searches disagree"
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    tc_peak = float(peaks.get("bf16_tflops", 1900.0))
+    gemm_ms, gemm_n = stage.get("flat", (0.0, 0))
+    per_launch_ms = gemm_ms / max(gemm_n, 1)
+    flops = 2.0 * nq * nb * D
+    achieved = flops / (per_launch_ms / 1e3) / 1e12 if per_launch_ms > 0 else 0.0
+    out = {
+        "metric": FLAT_METRIC,
+        "value": round(value, 1),
+        "unit": "queries/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(results["fast"]["ms"], 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "bf16+f32",
+        "data": "synthetic SIFT-like (seeded Gaussian mixture, integer-valued), not SIFT1M",
+        "config": {
+            "workload": f"flat_{nb}x128_{args.metric}_nq{nq}_k{k}",
+            "form": f"fast: BF16 tcgen05 GEMM + per-row heap top-{min(max(rerank, k), 64)} per "
+                    f"segment, exact FP32 rerank of {rerank}" if rerank else
+                    "fast: BF16 tcgen05 GEMM + per-row heap, BF16 distances (no rerank)",
+            "recall_at_k_vs_plain_fp32": round(rec, 5),
+            "plain_fp32_qps": round(plain_qps, 1),
+            "speedup_vs_plain_fp32": round(value / plain_qps, 2),
+            "l2_policy": "inputs larger than L2 (256 MB BF16 rows) and a 256 MiB flush per step",
+            "parallelism": f"replicas x{world}",
+            "setup_s": round(setup_s, 1),
+        },
+        "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s",
+                "h2d_bytes_per_step": nq * D * 4, "d2h_bytes_per_step": nq * k * 12},
+        "gpu_launches": int(launches),
+        "roofline": {
+            "bound": "tensor",
+            "kernel": "k_umma_topk (includes the query BF16 conversion)",
+            "achieved": round(achieved, 1),
+            "peak": tc_peak,
+            "peak_source": "measured" if "bf16_tflops" in peaks else "fallback",
+            "unit": "TFLOP/s",
+            "frac": round(achieved / tc_peak, 4),
+            "traffic": None,
+            "algorithmic_flops_per_launch": flops,
+            "launch_ms": round(per_launch_ms, 4),
+        },
+        "stages_ms_per_step": {kk: round(v[0] / args.steps, 4) for kk, v in stage.items()},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as orc
+
+        sample = min(args.cpu_sample // 10, nq)
+        threads = os.cpu_count() or 1
+        orc.flat_search(base, queries[:4], k, metric=metric, nthreads=threads)
+        t0 = time.perf_counter()
+        _, clab = orc.flat_search(base, queries[:sample], k, metric=metric, nthreads=threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {
+            "value": round(sample / dt, 1), "unit": "queries/s", "cores": threads, "kind": "port",
+            "sample": f"{sample} of the {nq} queries over all {nb} rows, reference IndexFlat "
+                      f"arithmetic, query-parallel on {threads} threads",
+            "ids_equal_to_gpu_plain": bool(np.array_equal(clab, gt[:sample])),
+        }
+    return out
+
+
 def run_reference(args):
     """The oracle (C++ restatement of the reference CPU path) builds the same
     index on the host and answers a bounded query sample."""
@@ -419,6 +571,39 @@ def run_reference(args):
     }
 
 
+def run_reference_flat(args):
+    """The oracle's IndexFlat search over all rows for a bounded query sample."""
+    from oracle import oracle as orc
+
+    threads = os.cpu_count() or 1
+    base, queries = build_workload(args.nb, args.nq)
+    metric = 0 if args.metric == "l2" else 1
+    sample = min(max(args.cpu_sample // 10, 1), args.nq)
+    q = queries[:sample]
+    for _ in range(max(args.warmup, 0)):
+        orc.flat_search(base, q[:2], args.k, metric=metric, nthreads=threads)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        orc.flat_search(base, q, args.k, metric=metric, nthreads=threads)
+    total = time.perf_counter() - t
+    qps = sample * args.steps / total
+    return {
+        "metric": FLAT_METRIC, "impl": "reference", "value": round(qps, 1), "unit": "queries/s",
+        "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * total / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic SIFT-like (seeded Gaussian mixture, integer-valued), not SIFT1M",
+        "config": {"workload": f"flat_{args.nb}x128_{args.metric}_nq{args.nq}_k{args.k}",
+                   "form": "reference CPU path (oracle port)"},
+        "cpu_baseline": {"value": round(qps, 1), "unit": "queries/s", "cores": threads,
+                         "kind": "port",
+                         "sample": f"{sample} queries per step over all {args.nb} rows, "
+                                   f"query-parallel on {threads} threads"},
+        "e2e": {"value": round(qps, 1), "unit": "queries/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -427,26 +612,33 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--form", default="fast", choices=["plain", "fast"])
     ap.add_argument("--nprobe", type=int, default=16)
-    ap.add_argument("--rerank", type=int, default=256)
+    ap.add_argument("--rerank", type=int, default=None,
+                    help="shortlist depth (IVF-PQ default 256, flat default k * 4)")
     ap.add_argument("--nb", type=int, default=NB, help="base rows (profiling runs use fewer)")
     ap.add_argument("--nq", type=int, default=NQ, help="queries per step")
     ap.add_argument("--cpu-sample", type=int, default=500)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="ivfpq", choices=["ivfpq", "flat"])
+    ap.add_argument("--k", type=int, default=K, help="flat workload: results per query")
+    ap.add_argument("--metric", default="l2", choices=["l2", "ip"], help="flat workload metric")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.rerank is None:
+        args.rerank = 256 if args.workload == "ivfpq" else 4 * args.k
     world = _env_int("WORLD_SIZE", 1)
     rank = _env_int("RANK", 0)
 
     if args.impl == "reference":
         if rank == 0:
-            print(json.dumps(run_reference(args)), flush=True)
+            ref = run_reference_flat(args) if args.workload == "flat" else run_reference(args)
+            print(json.dumps(ref), flush=True)
         return
 
     if world > 1:
         import torch
 
         torch.distributed.init_process_group("nccl")
-    out = run_gpu(args, rank, world)
+    out = run_flat(args, rank, world) if args.workload == "flat" else run_gpu(args, rank, world)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

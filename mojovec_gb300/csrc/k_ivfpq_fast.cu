@@ -56,7 +56,7 @@ constexpr int CC_CHUNK = 4096;
 __global__ void __launch_bounds__(FT)
     k_coarse_fast(const float* __restrict__ approx, int nlist, const float* __restrict__ q, int d,
                   const float* __restrict__ cent, int metric, int nc, int ncp, int nprobe,
-                  int32_t* __restrict__ probes, float* __restrict__ term) {
+                  int32_t* __restrict__ probes, float* __restrict__ term, int* __restrict__ err) {
   extern __shared__ __align__(16) unsigned char smraw[];
   uint64_t* keys = reinterpret_cast<uint64_t*>(smraw);  // CC_CHUNK + nc
   uint64_t* sel = keys + CC_CHUNK + nc;                 // ncp (power of two >= nc)
@@ -79,7 +79,9 @@ __global__ void __launch_bounds__(FT)
   // exact FP32 distances of the nc candidates
   for (int c = warp; c < ncp; c += FT / 32) {
     uint64_t out = KEY_NONE - (uint64_t)c;  // distinct padding keys sort last
-    if (c < m) {
+    const bool in_range = c < m && key_id(keys[c]) < (uint32_t)nlist;
+    if (c < m && !in_range && lane == 0) atomicExch(err, 102);
+    if (in_range) {
       const uint32_t list = key_id(keys[c]);
       const float* cp = cent + (int64_t)list * d;
       float acc = 0.0f;
@@ -132,6 +134,64 @@ __device__ __forceinline__ float adc_fast(const float* lut, const uint8_t* code,
     for (int m = 0; m < M; ++m) p[m & 3] += lut[(m << 8) + code[m]];
   }
   return (p[0] + p[1]) + (p[2] + p[3]);
+}
+
+// Coarse step from the fused GEMM's per-segment candidates: the nc
+// smallest of the ncand approximate keys, their exact FP32 distances, the
+// nprobe smallest sorted ascending by (distance, list). Padding keys are made
+// distinct (KEY_NONE - i) and never selected ahead of real ones.
+__global__ void __launch_bounds__(FT)
+    k_coarse_from_keys(const uint64_t* __restrict__ cand, int ncand, const float* __restrict__ q,
+                       int d, const float* __restrict__ cent, int nlist, int metric, int nc,
+                       int ncp, int nprobe, int32_t* __restrict__ probes, float* __restrict__ term,
+                       int* __restrict__ err) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  uint64_t* keys = reinterpret_cast<uint64_t*>(smraw);  // ncand
+  uint64_t* sel = keys + ncand;                         // ncp
+  float* qv = reinterpret_cast<float*>(sel + ncp);
+  __shared__ RadixScratch rs;
+  const int64_t row = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint64_t pad0 = KEY_NONE - (uint64_t)ncand;
+  for (int j = threadIdx.x; j < d; j += FT) qv[j] = q[row * d + j];
+  for (int j = threadIdx.x; j < ncand; j += FT) {
+    const uint64_t k = cand[row * ncand + j];
+    keys[j] = k == KEY_NONE ? KEY_NONE - (uint64_t)j : k;
+  }
+  __syncthreads();
+  const int r = block_radix_select<FT>(keys, ncand, nc, sel, rs);
+  for (int j = threadIdx.x; j < r; j += FT) keys[j] = sel[j];
+  __syncthreads();
+  for (int c = warp; c < ncp; c += FT / 32) {
+    uint64_t out = KEY_NONE - (uint64_t)c;
+    const bool real = c < r && keys[c] <= pad0;
+    const bool in_range = real && key_id(keys[c]) < (uint32_t)nlist;
+    if (real && !in_range && lane == 0) atomicExch(err, 101);
+    if (in_range) {
+      const uint32_t list = key_id(keys[c]);
+      const float* cp = cent + (int64_t)list * d;
+      float acc = 0.0f;
+      for (int j = lane; j < d; j += 32) {
+        if (metric == MV_METRIC_L2) {
+          const float df = qv[j] - cp[j];
+          acc = fmaf(df, df, acc);
+        } else {
+          acc = fmaf(qv[j], cp[j], acc);
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      out = make_key(metric == MV_METRIC_L2 ? acc : -acc, list);
+    }
+    if (lane == 0) sel[c] = out;
+  }
+  __syncthreads();
+  block_bitonic_sort(sel, ncp);
+  for (int p = threadIdx.x; p < nprobe; p += FT) {
+    const uint64_t key = sel[p];
+    const bool ok = key < KEY_NONE - (uint64_t)ncp;
+    probes[row * nprobe + p] = ok ? (int32_t)key_id(key) : -1;
+    term[row * nprobe + p] = ok ? key_dist(key) : 0.0f;
+  }
 }
 
 // Per-query table lut[m][k] = scale * <q_m, C[m][k]>: warp w builds
@@ -221,7 +281,11 @@ __global__ void __launch_bounds__(FT) k_ivfpq_scan_fast(FastScanArgs a) {
       const int p = p0 + lane;
       int len = 0;
       if (p < a.nprobe) {
-        const int list = a.probes[row * a.nprobe + p];
+        int list = a.probes[row * a.nprobe + p];
+        if (list >= a.nlist) {
+          atomicExch(a.err, 103);
+          list = -1;
+        }
         int64_t off = 0;
         if (list >= 0) {
           off = a.list_off[list];
@@ -280,24 +344,34 @@ __global__ void __launch_bounds__(FT) k_ivfpq_scan_fast(FastScanArgs a) {
     for (int j0 = 0; j0 < len; j0 += 2 * FT) {
       const int j = j0 + threadIdx.x;
       const bool has0 = j < len;
-      const int c0 = base + (has0 ? j : 0), c1 = c0 + FT;
       const bool has1 = j + FT < len;
-      while (pbeg[p + 1] <= c0) ++p;
-      const int64_t pos0 = poff[p] + (c0 - pbeg[p]);
-      const float t0 = pterm[p];
+      const int c0 = base + j, c1 = c0 + FT;
+      // Lanes without a candidate keep their cursor and use position 0 (a
+      // valid entry: the index is not empty), so no load leaves the lists.
+      if (has0)
+        while (pbeg[p + 1] <= c0) ++p;
+      int64_t pos0c = has0 ? poff[p] + (c0 - pbeg[p]) : 0;
+      const float t0 = has0 ? pterm[p] : 0.0f;
       int p1 = p;
       if (has1)
         while (pbeg[p1 + 1] <= c1) ++p1;
-      const int64_t pos1 = has1 ? poff[p1] + (c1 - pbeg[p1]) : pos0;
-      const float t1 = pterm[p1];
-      const float v0 = a.vterm ? a.vterm[pos0] : 0.0f;
+      int64_t pos1 = has1 ? poff[p1] + (c1 - pbeg[p1]) : 0;
+      const float t1 = has1 ? pterm[p1] : 0.0f;
+      bool keep0 = has0, keep1 = has1;
+      if ((has0 && (pos0c < 0 || pos0c >= a.ntotal)) || (has1 && (pos1 < 0 || pos1 >= a.ntotal))) {
+        atomicExch(a.err, 104);  // never expected: skip both, stay warp-uniform
+        pos0c = 0;
+        pos1 = 0;
+        keep0 = keep1 = false;
+      }
+      const float v0 = a.vterm ? a.vterm[pos0c] : 0.0f;
       const float v1 = a.vterm ? a.vterm[pos1] : 0.0f;
-      const float d0 = adc_fast(lut, a.codes + pos0 * M, M, t0 + v0);
+      const float d0 = adc_fast(lut, a.codes + pos0c * M, M, t0 + v0);
       const float d1 = adc_fast(lut, a.codes + pos1 * M, M, t1 + v1);
-      const unsigned long long k0 = ((unsigned long long)float_to_ordered(d0) << 32) | (uint32_t)pos0;
+      const unsigned long long k0 = ((unsigned long long)float_to_ordered(d0) << 32) | (uint32_t)pos0c;
       const unsigned long long k1 = ((unsigned long long)float_to_ordered(d1) << 32) | (uint32_t)pos1;
-      const bool in0 = has0 && k0 < bound;
-      const bool in1 = has1 && k1 < bound;
+      const bool in0 = keep0 && k0 < bound;
+      const bool in1 = keep1 && k1 < bound;
       const unsigned b0 = __ballot_sync(0xffffffffu, in0);
       const unsigned b1 = __ballot_sync(0xffffffffu, in1);
       int wbase = 0;
@@ -355,6 +429,10 @@ __global__ void __launch_bounds__(FT) k_rerank_fast(RerankArgs a) {
       const int c = c0 + u;
       const uint64_t key = c < a.R ? cand[c] : KEY_NONE;
       pos[u] = key == KEY_NONE ? 0xffffffffu : key_id(key);
+      if (pos[u] != 0xffffffffu && (int64_t)pos[u] >= a.ntotal) {
+        atomicExch(a.err, 105);
+        pos[u] = 0xffffffffu;
+      }
       acc[u] = 0.0f;
     }
     if ((d & 3) == 0) {
@@ -399,7 +477,7 @@ __global__ void __launch_bounds__(FT) k_rerank_fast(RerankArgs a) {
       if (lane == 0 && c < a.R) {
         ck[c] = pos[u] == 0xffffffffu
                     ? KEY_NONE - (uint64_t)c  // distinct keys for empty slots
-                    : make_key(a.metric == MV_METRIC_L2 ? t : -t, a.ids[pos[u]]);
+                    : make_key(a.metric == MV_METRIC_L2 ? t : -t, a.ids ? a.ids[pos[u]] : pos[u]);
       }
     }
   }
@@ -410,7 +488,7 @@ __global__ void __launch_bounds__(FT) k_rerank_fast(RerankArgs a) {
   block_bitonic_sort(outb, a.kp);
   for (int i = threadIdx.x; i < a.k; i += FT) {
     const uint64_t key = outb[i];
-    float dd = 1e38f;
+    float dd = a.fill_d;
     int64_t ll = -1;
     if (key < KEY_NONE - (uint64_t)a.R) {  // padding keys are the top R values
       dd = key_dist(key);
@@ -457,14 +535,28 @@ void launch_vec_terms(const int64_t* off, int nlist, const uint8_t* codes, const
 
 void launch_coarse_fast(const float* approx, int64_t nq, int nlist, const float* q, int d,
                         const float* cent, int metric, int nc, int nprobe, int32_t* probes,
-                        float* term, cudaStream_t s) {
+                        float* term, int* err, cudaStream_t s) {
   if (nq == 0) return;
   const int ncp = next_pow2(nc);
   const size_t smem = (size_t)(CC_CHUNK + nc + ncp) * 8 + (size_t)d * 4;
   MV_REQUIRE(smem <= 200 * 1024, MV_ERR_UNSUPPORTED, "coarse select: nprobe or d too large");
   smem_attr(k_coarse_fast, smem);
   k_coarse_fast<<<(unsigned)nq, FT, smem, s>>>(approx, nlist, q, d, cent, metric, nc, ncp, nprobe,
-                                                probes, term);
+                                                probes, term, err);
+  count_launch();
+  MV_CHECK_CUDA(cudaGetLastError());
+}
+
+void launch_coarse_from_keys(const uint64_t* cand, int64_t nq, int ncand, const float* q, int d,
+                             const float* cent, int nlist, int metric, int nc, int nprobe,
+                             int32_t* probes, float* term, int* err, cudaStream_t s) {
+  if (nq == 0) return;
+  const int ncp = next_pow2(nc);
+  const size_t smem = (size_t)(ncand + ncp) * 8 + (size_t)d * 4;
+  MV_REQUIRE(smem <= 200 * 1024, MV_ERR_UNSUPPORTED, "coarse merge: too many candidates");
+  smem_attr(k_coarse_from_keys, smem);
+  k_coarse_from_keys<<<(unsigned)nq, FT, smem, s>>>(cand, ncand, q, d, cent, nlist, metric, nc, ncp,
+                                                     nprobe, probes, term, err);
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());
 }

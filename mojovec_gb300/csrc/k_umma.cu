@@ -237,6 +237,337 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   if (threadIdx.x == 0 && *verr && g.err) atomicExch(g.err, 1);
 }
 
+// GEMM with a per-row top-K epilogue. CTA (seg, rb) owns the 128-row X
+// block rb (loaded once) and the column tiles [seg * tps, (seg + 1) * tps).
+// Each epilogue thread owns one row and keeps the K smallest (distance,
+// column) keys seen so far in a binary max-heap in shared memory,
+// slot-major (heap[j * 128 + row]) so a warp's 32 rows sit in consecutive
+// words. A distance is tested against the heap top (the current K-th key)
+// with one compare; the few that pass go to a small pending buffer, and the
+// whole warp drains all pending buffers into their heaps together when any
+// of them is nearly full, so the heap updates run in step across the warp.
+// The kept set is the K smallest keys of the segment whatever the order of
+// arrival. The row-constant ||x||^2 is left out of the keys (rows rank the
+// same without it). With gthr, the segments of a row share a threshold: a
+// full heap publishes its K-th key (atomicMin) and every segment filters
+// with the smallest published one, which can only drop keys that are not
+// among the row's K smallest over all segments. At the end each thread writes its heap (unsorted,
+// KEY_NONE padded to ncp) to out[(row * nseg + seg) * ncp + j].
+// Pending slots per row: at least 32, up to 64 when shared memory allows.
+// The warp drains when any row has more than pend - 32 (a 32-column chunk
+// per check), so a larger buffer means fewer, fuller drains.
+constexpr int TOPK_PEND_MIN = 32, TOPK_PEND_MAX = 64;
+
+__device__ __forceinline__ void heap_replace_top(uint64_t* h, int K, uint64_t key) {
+  int i = 0;
+  while (true) {
+    const int l = 2 * i + 1;
+    if (l >= K) break;
+    int c = l;
+    uint64_t hc = h[(size_t)l * BM];
+    if (l + 1 < K) {
+      const uint64_t hr = h[(size_t)(l + 1) * BM];
+      if (hr > hc) {
+        c = l + 1;
+        hc = hr;
+      }
+    }
+    if (hc <= key) break;
+    h[(size_t)i * BM] = hc;
+    i = c;
+  }
+  h[(size_t)i * BM] = key;
+}
+
+template <int BN>
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+    k_umma_topk(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUtensorMap ty,
+                UmmaTopkArgs g) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  const int nkb = g.nkb;
+  const uint32_t a_bytes = (uint32_t)nkb * BM * 128;
+  const uint32_t b_stage = (uint32_t)nkb * BN * 128;
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + a_bytes;
+  uint64_t* heap = reinterpret_cast<uint64_t*>(sB + STAGES * b_stage);  // nc x BM
+  uint64_t* pend = heap + (size_t)g.nc * BM;                             // g.pend x BM
+  float* cnbuf = reinterpret_cast<float*>(pend + (size_t)g.pend * BM);  // 4 x BN
+  uint64_t* bars = reinterpret_cast<uint64_t*>(cnbuf + 4 * BN);
+  uint32_t* holder = reinterpret_cast<uint32_t*>(bars + 12);
+  __shared__ int s_err;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t bar0 = smem_u32(bars);
+  auto b_full = [&](int s) { return bar0 + 8u * s; };
+  auto b_empty = [&](int s) { return bar0 + 8u * (2 + s); };
+  auto b_tfull = [&](int a) { return bar0 + 8u * (4 + a); };
+  auto b_tempty = [&](int a) { return bar0 + 8u * (6 + a); };
+  const uint32_t b_done = bar0 + 8u * 8;
+  const uint32_t b_fulla = bar0 + 8u * 9;
+  if (threadIdx.x == 0) {
+    s_err = 0;
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(b_full(s), 1);
+      mbar_init(b_empty(s), 1);
+    }
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(b_tfull(a), 1);
+      mbar_init(b_tempty(a), 128);
+    }
+    mbar_init(b_done, 1);
+    mbar_init(b_fulla, 1);
+    fence_mbar_init();
+  }
+  if (warp == 0 && lane == 0) {
+    prefetch_tmap(&tx);
+    prefetch_tmap(&ty);
+  }
+  if (warp == 1) tmem_alloc(smem_u32(holder), 2 * BN);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(holder);
+  // Segments vary fastest across the grid, so the segments of a row block
+  // run together and tighten the row's shared threshold from the start.
+  const int seg = blockIdx.x;
+  const int rb = blockIdx.y;
+  const int nct = (int)((g.ncols + BN - 1) / BN);
+  const int ct0 = seg * g.tps;
+  const int ct1 = min(ct0 + g.tps, nct);
+  const int my_count = ct1 > ct0 ? ct1 - ct0 : 0;
+  volatile int* verr = &s_err;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      mbar_arrive_expect_tx(b_fulla, a_bytes);
+      for (int kb = 0; kb < nkb; ++kb)
+        tma_load_2d(smem_u32(sA + kb * (BM * 128)), &tx, kb * 64, rb * BM, b_fulla);
+      int i = 0;
+      for (; i < my_count; ++i) {
+        const int s = i % STAGES;
+        const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
+        if (*verr || !mbar_wait(b_empty(s), ph ^ 1u)) {
+          *verr = 1;
+          break;
+        }
+        uint8_t* st = sB + (size_t)s * b_stage;
+        mbar_arrive_expect_tx(b_full(s), b_stage);
+        for (int kb = 0; kb < nkb; ++kb)
+          tma_load_2d(smem_u32(st + kb * (BN * 128)), &ty, kb * 64, (ct0 + i) * BN, b_full(s));
+      }
+      // Drain: every issued load must land before the CTA exits.
+      if (!mbar_wait(b_fulla, 0)) *verr = 1;
+      for (int j = (i > STAGES ? i - STAGES : 0); j < i; ++j)
+        if (!mbar_wait(b_full(j % STAGES), (uint32_t)(j / STAGES) & 1u)) *verr = 1;
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_f32(BM, BN);
+      bool ok = mbar_wait(b_fulla, 0);
+      if (!ok) *verr = 1;
+      for (int i = 0; ok && i < my_count; ++i) {
+        const int s = i % STAGES;
+        const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
+        const int acc = i & 1;
+        const uint32_t aph = (uint32_t)(i >> 1) & 1u;
+        if (*verr || !mbar_wait(b_tempty(acc), aph ^ 1u) || !mbar_wait(b_full(s), ph)) {
+          *verr = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint8_t* st = sB + (size_t)s * b_stage;
+        const uint32_t d = tmem + (uint32_t)(acc * BN);
+        for (int kb = 0; kb < nkb; ++kb) {
+          const uint64_t ad = desc_k_sw128(smem_u32(sA + kb * (BM * 128)));
+          const uint64_t bd = desc_k_sw128(smem_u32(st + kb * (BN * 128)));
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk)
+            umma_bf16(d, ad + 2u * kk, bd + 2u * kk, idesc, (kb | kk) ? 1u : 0u);
+        }
+        umma_commit(b_empty(s));
+        umma_commit(b_tfull(acc));
+      }
+      umma_commit(b_done);
+    }
+  } else {
+    const int q = warp & 3;
+    const int rloc = q * 32 + lane;
+    const int64_t row = (int64_t)rb * BM + rloc;
+    const bool row_ok = row < g.nrows;
+    const int K = g.nc;
+    const bool l2 = g.metric == MV_METRIC_L2;
+    const float INF = __int_as_float(0x7f800000);
+    uint64_t* H = heap + rloc;  // H[j * BM]
+    uint64_t* P = pend + rloc;  // P[j * BM]
+    float* cs = cnbuf + q * BN;  // this warp's copy of the tile's column norms
+    for (int j = 0; j < K; ++j) H[(size_t)j * BM] = KEY_NONE;
+    int pc = 0;
+    // Work with e = -distance (2 x.y - ||y||^2 for L2, x.y for IP): a column
+    // can enter the heap when e >= thr_e. Rows past the end never enter.
+    float thr_e = row_ok ? -INF : INF;
+    auto drain = [&]() {
+      const int mx = __reduce_max_sync(0xffffffffu, pc);
+      for (int t = 0; t < mx; ++t) {
+        if (t < pc) {
+          const uint64_t pe = P[(size_t)t * BM];
+          const uint64_t key = make_key(-__uint_as_float((uint32_t)(pe >> 32)), (uint32_t)pe);
+          if (key < H[0]) heap_replace_top(H, K, key);
+        }
+      }
+      pc = 0;
+      uint64_t thr = H[0];
+      if (g.gthr && row_ok) {
+        // Publish this segment's K-th key and filter with the row's best.
+        if (thr != KEY_NONE) atomicMin(reinterpret_cast<unsigned long long*>(g.gthr + row), thr);
+        const uint64_t gt = *reinterpret_cast<volatile uint64_t*>(g.gthr + row);
+        thr = gt < thr ? gt : thr;
+      }
+      // e == thr_e may still lose the tie on the column; the drain decides.
+      thr_e = !row_ok ? INF : (thr == KEY_NONE ? -INF : -key_dist(thr));
+    };
+    // Column norms of the next tile, prefetched into registers while the
+    // current tile is processed (lane t holds columns t * CPL ...).
+    constexpr int CPL = BN / 32;
+    float cpre[CPL];
+    auto load_cn = [&](int i) {
+      const int64_t base = (int64_t)(ct0 + i) * BN + lane * CPL;
+#pragma unroll
+      for (int u = 0; u < CPL; ++u)
+        cpre[u] = (l2 && base + u < g.ncols) ? __ldg(g.cnorm + base + u) : 0.0f;
+    };
+    if (my_count > 0) load_cn(0);
+    uint64_t gpre = KEY_NONE;  // the row's shared threshold, read one tile ahead
+    if (g.gthr && row_ok) gpre = *reinterpret_cast<volatile uint64_t*>(g.gthr + row);
+    for (int i = 0; i < my_count; ++i) {
+      const int acc = i & 1;
+      const uint32_t aph = (uint32_t)(i >> 1) & 1u;
+      bool ok = !*verr && mbar_wait(b_tfull(acc), aph);
+      if (!__all_sync(0xffffffffu, ok)) {
+        *verr = 1;
+        break;
+      }
+      tc_fence_after();
+      __syncwarp();
+#pragma unroll
+      for (int u = 0; u < CPL; ++u) cs[lane * CPL + u] = cpre[u];
+      __syncwarp();
+      if (i + 1 < my_count) load_cn(i + 1);
+      if (g.gthr && row_ok) {
+        const float ge = gpre == KEY_NONE ? -INF : -key_dist(gpre);
+        thr_e = ge > thr_e ? ge : thr_e;
+        gpre = *reinterpret_cast<volatile uint64_t*>(g.gthr + row);
+      }
+      const int64_t tile0 = (int64_t)(ct0 + i) * BN;
+      const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN);
+      constexpr int NCH = BN / 32;
+      // e = -distance of the 32 columns of chunk ch (masked past the end).
+      auto chunk_e = [&](const uint32_t* rv, int ch, float* e) {
+        const int c0 = ch * 32;
+        if (l2) {
+#pragma unroll
+          for (int j = 0; j < 32; j += 4) {
+            const float4 c4 = *reinterpret_cast<const float4*>(cs + c0 + j);  // broadcast
+            e[j] = fmaf(2.0f, __uint_as_float(rv[j]), -c4.x);
+            e[j + 1] = fmaf(2.0f, __uint_as_float(rv[j + 1]), -c4.y);
+            e[j + 2] = fmaf(2.0f, __uint_as_float(rv[j + 2]), -c4.z);
+            e[j + 3] = fmaf(2.0f, __uint_as_float(rv[j + 3]), -c4.w);
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) e[j] = __uint_as_float(rv[j]);
+        }
+        const int64_t left = g.ncols - (tile0 + c0);  // the same in every lane
+        if (left < 32) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j)
+            if (j >= left) e[j] = -INF;
+        }
+      };
+      // Phase 1, no branches: the largest e of each chunk.
+      float cmax[NCH];
+      {
+        uint32_t r[2][32];
+        tmem_ld32_issue(tbase, r[0]);
+        tmem_ld32_wait(r[0]);
+#pragma unroll
+        for (int ch = 0; ch < NCH; ++ch) {
+          if (ch + 1 < NCH) tmem_ld32_issue(tbase + (uint32_t)(ch * 32 + 32), r[(ch + 1) & 1]);
+          float e[32];
+          chunk_e(r[ch & 1], ch, e);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) e[j] = fmaxf(e[j], e[j + 16]);
+#pragma unroll
+          for (int w = 8; w > 0; w >>= 1)
+#pragma unroll
+            for (int j = 0; j < w; ++j) e[j] = fmaxf(e[j], e[j + w]);
+          cmax[ch] = e[0];
+          if (ch + 1 < NCH) tmem_ld32_wait(r[(ch + 1) & 1]);
+        }
+      }
+      float tmax = cmax[0];
+#pragma unroll
+      for (int ch = 1; ch < NCH; ++ch) tmax = fmaxf(tmax, cmax[ch]);
+      // Phase 2 (rare once the thresholds settle): the chunks where some
+      // row may gain a key are read again from TMEM and appended per group
+      // of 4 columns (g, g + 8, g + 16, g + 24) with predicated stores.
+      if (__any_sync(0xffffffffu, tmax >= thr_e)) {
+#pragma unroll 1
+        for (int ch = 0; ch < NCH; ++ch) {
+          float cm = cmax[0];
+#pragma unroll
+          for (int c = 1; c < NCH; ++c)
+            if (ch == c) cm = cmax[c];
+          if (!__any_sync(0xffffffffu, cm >= thr_e)) continue;
+          uint32_t rv[32];
+          tmem_ld32_issue(tbase + (uint32_t)(ch * 32), rv);
+          tmem_ld32_wait(rv);
+          float e[32];
+          chunk_e(rv, ch, e);
+          const int64_t col0 = tile0 + ch * 32;
+          const int64_t left = g.ncols - col0;
+          float m[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) m[j] = fmaxf(fmaxf(e[j], e[j + 8]), fmaxf(e[j + 16], e[j + 24]));
+#pragma unroll
+          for (int gi = 0; gi < 8; ++gi) {
+            if (__any_sync(0xffffffffu, m[gi] >= thr_e)) {
+#pragma unroll
+              for (int t = 0; t < 4; ++t) {
+                const int j = gi + 8 * t;
+                const bool pass = e[j] >= thr_e && j < left &&
+                                  !(g.filter && g.filter[col0 + j]);
+                if (pass)
+                  P[(size_t)pc * BM] = ((uint64_t)__float_as_uint(e[j]) << 32) |
+                                       (uint32_t)(col0 + j);
+                pc += pass ? 1 : 0;
+              }
+            }
+          }
+          if (__any_sync(0xffffffffu, pc > g.pend - 32)) drain();
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(b_tempty(acc));
+    }
+    drain();
+    if (row_ok) {
+      uint64_t* o = g.out + ((size_t)row * g.nseg + seg) * g.ncp;
+      for (int j = 0; j < g.ncp; ++j) o[j] = j < K ? H[(size_t)j * BM] : KEY_NONE;
+    }
+  }
+  __syncthreads();
+  if (warp == 1) {
+    bool done = true;
+    if (lane == 0) done = mbar_wait(b_done, 0);
+    done = __shfl_sync(0xffffffffu, done, 0);
+    if (!done && lane == 0) *verr = 1;
+    tc_fence_after();
+    tmem_dealloc(tmem, 2 * BN);
+  }
+  if (threadIdx.x == 0 && *verr && g.err) atomicExch(g.err, 1);
+}
+
 __global__ void k_to_bf16(const float* __restrict__ x, int64_t n, int d, int kp,
                           __nv_bfloat16* __restrict__ out, float* __restrict__ norms) {
   const int lane = threadIdx.x & 31;
@@ -362,6 +693,97 @@ void launch_umma_dist(int epi, const __nv_bfloat16* X, int64_t nx, const __nv_bf
     if (epi == EPI_MATRIX) launch_bn<64, EPI_MATRIX>(g, tx, ty, num_sms, s);
     else launch_bn<64, EPI_ARGMIN>(g, tx, ty, num_sms, s);
   }
+}
+
+namespace {
+// Y tile width of the top-k GEMM: 128 up to d = 128, else 64, so that the
+// X block, two Y stages, the heaps and the pending buffers fit 227 KB.
+int topk_bn(int nkb) { return nkb <= 2 ? 128 : 64; }
+size_t topk_smem_base(int nkb, int bn, int nc) {
+  return 1024 + (size_t)nkb * BM * 128 + (size_t)STAGES * nkb * bn * 128 + (size_t)nc * BM * 8 +
+         (size_t)4 * bn * 4 + 256;
+}
+// Pending slots that fit next to the heaps (multiple of 8).
+int topk_pend(int nkb, int bn, int nc) {
+  const size_t base = topk_smem_base(nkb, bn, nc);
+  const size_t room = base < 227 * 1024 ? (227 * 1024 - base) / ((size_t)BM * 8) : 0;
+  return (int)std::min<size_t>(TOPK_PEND_MAX, room / 8 * 8);
+}
+size_t topk_smem(int nkb, int bn, int nc) {
+  return topk_smem_base(nkb, bn, nc) + (size_t)topk_pend(nkb, bn, nc) * BM * 8;
+}
+}  // namespace
+
+int umma_topk_nseg(int64_t nrows, int64_t ncols, int d, int nc, int num_sms) {
+  const int nkb = umma_kpad(d) / 64;
+  const int bn = topk_bn(nkb);
+  const int64_t nrb = (nrows + BM - 1) / BM;
+  const int64_t nct = (ncols + bn - 1) / bn;
+  // CTAs resident per SM (228 KB of shared memory per SM, 1 KB reserved per
+  // CTA), then the fewest column segments whose CTAs fill the last wave to
+  // 90%; a segment is never shorter than 16 column tiles.
+  const int64_t cps = std::max<int64_t>(1, std::min<int64_t>(4, (228 * 1024) / (topk_smem(nkb, bn, nc) + 1024)));
+  const int64_t slots = (int64_t)std::max(num_sms, 1) * cps;
+  const int64_t maxseg = std::max<int64_t>(1, std::min<int64_t>(nct / 16, 4096));
+  int64_t best = 1;
+  double best_eff = 0.0;
+  for (int64_t ns = 1; ns <= maxseg; ++ns) {
+    const int64_t ctas = nrb * ns;
+    const int64_t waves = (ctas + slots - 1) / slots;
+    const double eff = (double)ctas / (double)(waves * slots);
+    if (eff > best_eff + 1e-9) {
+      best_eff = eff;
+      best = ns;
+    }
+    if (eff >= 0.9) break;
+  }
+  return (int)std::min<int64_t>(best, 65535);
+}
+
+void launch_umma_topk(const __nv_bfloat16* X, int64_t nx, const __nv_bfloat16* Y, int64_t ny,
+                      int d, int metric, const float* xnorm, const float* ynorm, int nc, int nseg,
+                      const uint8_t* filter, uint64_t* gthr, uint64_t* out, int* err,
+                      cudaStream_t s) {
+  if (nx == 0) return;
+  const int kp = umma_kpad(d);
+  MV_REQUIRE(kp <= 256, MV_ERR_UNSUPPORTED, "BF16 GEMM supports d <= 256");
+  MV_REQUIRE(nc >= 1 && nc <= UMMA_TOPK_MAX, MV_ERR_UNSUPPORTED, "fused top-k keeps at most 64 per row");
+  MV_REQUIRE(nx < (1ll << 31) && ny < (1ll << 32) - 1, MV_ERR_UNSUPPORTED, "GEMM too large");
+  MV_REQUIRE(nseg >= 1 && nseg <= 65535, MV_ERR_INTERNAL, "fused top-k: bad segment count");
+  UmmaTopkArgs g;
+  g.nrows = nx;
+  g.ncols = ny;
+  g.nkb = kp / 64;
+  g.metric = metric;
+  g.rnorm = xnorm;
+  g.cnorm = ynorm;
+  g.nc = nc;
+  g.ncp = next_pow2(nc);
+  g.nseg = nseg;
+  g.filter = filter;
+  g.gthr = gthr;
+  if (gthr) MV_CHECK_CUDA(cudaMemsetAsync(gthr, 0xff, sizeof(uint64_t) * nx, s));
+  g.out = out;
+  g.err = err;
+  const int bn = topk_bn(g.nkb);
+  g.pend = topk_pend(g.nkb, bn, nc);
+  MV_REQUIRE(g.pend >= TOPK_PEND_MIN, MV_ERR_UNSUPPORTED, "fused top-k GEMM: nc or d too large");
+  const int64_t nct = (ny + bn - 1) / bn;
+  g.tps = (int)((nct + nseg - 1) / nseg);
+  const CUtensorMap tx = make_tmap(X, nx, kp, BM);
+  const CUtensorMap ty = make_tmap(Y, ny, kp, bn);
+  MV_REQUIRE((nx + BM - 1) / BM <= 65535, MV_ERR_UNSUPPORTED, "fused top-k: too many rows per launch");
+  dim3 grid((unsigned)nseg, (unsigned)((nx + BM - 1) / BM));
+  auto go = [&](auto kernel) {
+    const size_t smem = topk_smem(g.nkb, bn, nc);
+    MV_REQUIRE(smem <= 227 * 1024, MV_ERR_UNSUPPORTED, "fused top-k GEMM: nc or d too large");
+    smem_limit(kernel, smem);
+    kernel<<<grid, NUM_THREADS, smem, s>>>(tx, ty, g);
+  };
+  if (bn == 128) go(k_umma_topk<128>);
+  else go(k_umma_topk<64>);
+  count_launch();
+  MV_CHECK_CUDA(cudaGetLastError());
 }
 
 void launch_keys_argmin(const uint64_t* keys, int64_t n, int32_t* out, float* dist, cudaStream_t s) {

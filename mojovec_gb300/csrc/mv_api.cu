@@ -15,6 +15,7 @@
 #include "mv_fast.h"
 #include "mv_internal.h"
 #include "mv_kernels.h"
+#include "mv_select.cuh"
 #include "mv_umma.h"
 
 namespace mv {
@@ -399,7 +400,9 @@ void check_kernel_errors(mv_ctx* ctx, cudaStream_t s) {
   if (e) {
     MV_CHECK_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, sizeof(int), s));
     sync(s);
-    throw Error(MV_ERR_TIMEOUT, "a tensor-core kernel gave up waiting (bounded wait expired)");
+    if (e == 1)
+      throw Error(MV_ERR_TIMEOUT, "a tensor-core kernel gave up waiting (bounded wait expired)");
+    throw Error(MV_ERR_INTERNAL, "a kernel skipped an out-of-range index (site " + std::to_string(e) + ")");
   }
 }
 
@@ -441,14 +444,22 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
   MV_REQUIRE(nprobe <= 8192, MV_ERR_UNSUPPORTED, "nprobe above 8192 is not supported on the GPU");
   const int nc = fp32_coarse ? nprobe : std::min(ix->nlist, nprobe + std::max(8, nprobe / 4));
   const int kp = umma_kpad(ix->d);
+  // Fused coarse (tensor-core GEMM keeping each query's best nc lists) when
+  // nc fits the epilogue's per-row list; otherwise the distance matrix path.
+  const bool fused = !fp32_coarse && nc <= 64;
   int64_t qb = std::max<int64_t>(128, (int64_t)(1536ll * 1024 * 1024 / ((int64_t)ix->nlist * 4)));
   qb = std::min<int64_t>({qb, nq, 65535ll * 64});
-  ws.ensure(ws_bytes((size_t)qb * kp, 2) + ws_bytes((size_t)qb * ix->nlist, 4) +
-            ws_bytes((size_t)qb * nprobe, 4) * 2 +
-            ws_bytes((size_t)qb * R, 8));
+  const int nseg = fused ? umma_topk_nseg(qb, ix->nlist, ix->d, nc, ix->ctx->num_sms) : 1;
+  const int ncand = nseg * next_pow2(nc);
+  ws.ensure(ws_bytes((size_t)qb * kp, 2) +
+            (fused ? ws_bytes((size_t)qb * ncand, 8) + ws_bytes((size_t)qb, 8)
+                   : ws_bytes((size_t)qb * ix->nlist, 4)) +
+            ws_bytes((size_t)qb * nprobe, 4) * 2 + ws_bytes((size_t)qb * R, 8));
   Arena ar(ws);
   __nv_bfloat16* xq = ar.take<__nv_bfloat16>((size_t)qb * kp);
-  float* dmat = ar.take<float>((size_t)qb * ix->nlist);
+  float* dmat = fused ? nullptr : ar.take<float>((size_t)qb * ix->nlist);
+  uint64_t* ckeys = fused ? ar.take<uint64_t>((size_t)qb * ncand) : nullptr;
+  uint64_t* gthr = fused && nseg > 1 ? ar.take<uint64_t>((size_t)qb) : nullptr;
   int32_t* probes = ar.take<int32_t>((size_t)qb * nprobe);
   float* term = ar.take<float>((size_t)qb * nprobe);
   uint64_t* skeys = ar.take<uint64_t>((size_t)qb * R);
@@ -463,15 +474,24 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
                             ix->nlist, s);
       } else {
         launch_to_bf16(xb, nb, ix->d, xq, nullptr, s);
-        launch_umma_dist(EPI_MATRIX, xq, nb, ix->d_cent_bf16.as<__nv_bfloat16>(), ix->nlist, ix->d,
-                         ix->metric, nullptr, ix->d_cnorm.as<float>(), dmat, ix->nlist, nullptr,
-                         ix->ctx->d_err.as<int>(), ix->ctx->num_sms, s);
+        if (fused)
+          launch_umma_topk(xq, nb, ix->d_cent_bf16.as<__nv_bfloat16>(), ix->nlist, ix->d,
+                           ix->metric, nullptr, ix->d_cnorm.as<float>(), nc, nseg, nullptr, gthr,
+                           ckeys, ix->ctx->d_err.as<int>(), s);
+        else
+          launch_umma_dist(EPI_MATRIX, xq, nb, ix->d_cent_bf16.as<__nv_bfloat16>(), ix->nlist,
+                           ix->d, ix->metric, nullptr, ix->d_cnorm.as<float>(), dmat, ix->nlist,
+                           nullptr, ix->ctx->d_err.as<int>(), ix->ctx->num_sms, s);
       }
     }
     {
       StageTimer t(ix->ctx, MV_STAGE_SELECT, s);
-      launch_coarse_fast(dmat, nb, ix->nlist, xb, ix->d, ix->centroids.as<float>(), ix->metric, nc,
-                         nprobe, probes, term, s);
+      if (fused)
+        launch_coarse_from_keys(ckeys, nb, ncand, xb, ix->d, ix->centroids.as<float>(), ix->nlist,
+                                ix->metric, nc, nprobe, probes, term, ix->ctx->d_err.as<int>(), s);
+      else
+        launch_coarse_fast(dmat, nb, ix->nlist, xb, ix->d, ix->centroids.as<float>(), ix->metric,
+                           nc, nprobe, probes, term, ix->ctx->d_err.as<int>(), s);
     }
     {
       StageTimer t(ix->ctx, MV_STAGE_SCAN, s);
@@ -491,6 +511,9 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
       a.R = R;
       a.sorted = (p && p->rerank > 0) ? 0 : 1;
       a.out_keys = skeys;
+      a.nlist = ix->nlist;
+      a.ntotal = ix->h_off[ix->nlist];
+      a.err = ix->ctx->d_err.as<int>();
       launch_ivfpq_scan_fast(a, s);
     }
     if (p && p->rerank > 0) {
@@ -507,6 +530,8 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
       r.k = k;
       r.out_d = d_out + q0 * k;
       r.out_l = d_lab + q0 * k;
+      r.ntotal = ix->h_off[ix->nlist];
+      r.err = ix->ctx->d_err.as<int>();
       launch_rerank_fast(r, s);
     } else {
       launch_short_to_results(skeys, nb, R, k, ix->d_ids.as<uint32_t>(), ix->metric,
@@ -913,6 +938,135 @@ void flat_search_plain(mv_flat* ix, const float* d_x, int64_t nq, int k, const u
   }
 }
 
+// Fast-form side structures of a flat index: BF16 rows (padded to the
+// GEMM's k-blocks) and the FP32 norms of the rounded rows.
+void ensure_flat_fast(mv_flat* ix, cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(ix->fast_mu);
+  if (ix->fast_ready) return;
+  const int kp = umma_kpad(ix->d);
+  ix->rows_bf16.ensure((size_t)ix->ntotal * kp * 2);
+  ix->norms.ensure((size_t)ix->ntotal * 4);
+  launch_to_bf16(ix->rows.as<float>(), ix->ntotal, ix->d, ix->rows_bf16.as<__nv_bfloat16>(),
+                 ix->norms.as<float>(), s);
+  sync(s);
+  ix->fast_ready = true;
+}
+
+// Flat fast form: BF16 tensor-core distances with the per-row heap epilogue
+// (shortlist of R = max(k, rerank) keys per query, ranked by the BF16
+// distance, ties by the smaller row), then either the exact FP32 rerank of
+// the shortlist or, without rerank, the BF16 distances themselves. A query
+// whose shortlist may be incomplete (a segment overflow, possible only when
+// R > 64) is recomputed with the exact FP32 scan.
+void flat_search_fast(mv_flat* ix, const float* d_x, int64_t nq, int k, const uint8_t* d_filter,
+                      const mv_search_params* p, float* d_out, int64_t* d_lab, DevBuf& ws,
+                      cudaStream_t s) {
+  if (nq == 0) return;
+  const int64_t nb = ix->ntotal;
+  if (nb == 0) {
+    launch_fill(d_out, d_lab, nq * k, 0.0f, s);
+    return;
+  }
+  MV_REQUIRE(umma_kpad(ix->d) <= 256, MV_ERR_UNSUPPORTED, "fast flat form supports d <= 256");
+  ensure_flat_fast(ix, s);
+  const bool rerank = p && p->rerank > 0;
+  const int R = std::max(k, rerank ? (int)p->rerank : k);
+  MV_REQUIRE(R <= 4096, MV_ERR_ARG, "rerank depth must be at most 4096");
+  const int kseg = std::min(R, UMMA_TOPK_MAX);
+  const int ncp = next_pow2(kseg);
+  const int kp = umma_kpad(ix->d);
+  const int64_t qb = std::min<int64_t>(nq, 32768);
+  int nseg = umma_topk_nseg(qb, nb, ix->d, kseg, ix->ctx->num_sms);
+  if (kseg < R) {  // about 16 shortlist keys per segment keeps overflow rare
+    const int64_t nct = (nb + 127) / 128;
+    nseg = (int)std::min<int64_t>(std::max<int64_t>(nseg, (R + 15) / 16), std::max<int64_t>(1, nct));
+  }
+  ws.ensure(ws_bytes((size_t)qb * kp, 2) + ws_bytes((size_t)qb, 4) +
+            ws_bytes((size_t)qb * nseg * ncp, 8) + ws_bytes((size_t)qb * R, 8) +
+            ws_bytes((size_t)qb, 4) + ws_bytes((size_t)qb, 8));
+  Arena ar(ws);
+  __nv_bfloat16* xq = ar.take<__nv_bfloat16>((size_t)qb * kp);
+  float* qnorm = ar.take<float>((size_t)qb);
+  uint64_t* cand = ar.take<uint64_t>((size_t)qb * nseg * ncp);
+  uint64_t* skeys = ar.take<uint64_t>((size_t)qb * R);
+  int* over = ar.take<int>((size_t)qb);
+  // Shared per-row threshold: exact only when a segment keeps all R keys.
+  uint64_t* gthr = (kseg == R && nseg > 1) ? ar.take<uint64_t>((size_t)qb) : nullptr;
+  std::vector<int> h_over;
+  for (int64_t q0 = 0; q0 < nq; q0 += qb) {
+    const int64_t nqb = std::min(qb, nq - q0);
+    const float* xb = d_x + q0 * ix->d;
+    {
+      StageTimer t(ix->ctx, MV_STAGE_FLAT, s);
+      launch_to_bf16(xb, nqb, ix->d, xq, qnorm, s);
+      launch_umma_topk(xq, nqb, ix->rows_bf16.as<__nv_bfloat16>(), nb, ix->d, ix->metric, nullptr,
+                       ix->norms.as<float>(), kseg, nseg, d_filter, gthr, cand,
+                       ix->ctx->d_err.as<int>(), s);
+    }
+    {
+      StageTimer t(ix->ctx, MV_STAGE_SELECT, s);
+      launch_flat_merge(cand, nqb, nseg, ncp, kseg, R, rerank ? skeys : nullptr, k, qnorm,
+                        ix->metric, 0.0f, d_out + q0 * k, d_lab + q0 * k,
+                        kseg < R ? over : nullptr, s);
+    }
+    if (rerank) {
+      StageTimer t(ix->ctx, MV_STAGE_RERANK, s);
+      RerankArgs r;
+      r.q = xb;
+      r.nq = nqb;
+      r.d = ix->d;
+      r.metric = ix->metric;
+      r.raw = ix->rows.as<float>();
+      r.ids = nullptr;
+      r.cand = skeys;
+      r.R = R;
+      r.k = k;
+      r.out_d = d_out + q0 * k;
+      r.out_l = d_lab + q0 * k;
+      r.ntotal = nb;
+      r.err = ix->ctx->d_err.as<int>();
+      r.fill_d = 0.0f;  // index_flat.mojo:232-238
+      launch_rerank_fast(r, s);
+    }
+    if (kseg < R) {
+      h_over.resize((size_t)nqb);
+      d2h(h_over.data(), over, sizeof(int) * nqb, s);
+      sync(s);
+      std::vector<int64_t> rows;
+      for (int64_t i = 0; i < nqb; ++i)
+        if (h_over[(size_t)i]) rows.push_back(q0 + i);
+      if (!rows.empty()) {
+        const int64_t nr = (int64_t)rows.size();
+        DevBuf tmp, tws;
+        tmp.ensure(ws_bytes((size_t)nr * ix->d, 4) + ws_bytes((size_t)nr * k, 4) +
+                   ws_bytes((size_t)nr * k, 8));
+        Arena ta(tmp);
+        float* tx = ta.take<float>((size_t)nr * ix->d);
+        float* td = ta.take<float>((size_t)nr * k);
+        int64_t* tl = ta.take<int64_t>((size_t)nr * k);
+        for (int64_t i = 0; i < nr; ++i)
+          d2d(tx + i * ix->d, d_x + rows[(size_t)i] * ix->d, sizeof(float) * ix->d, s);
+        flat_search_plain(ix, tx, nr, k, d_filter, td, tl, tws, s);
+        for (int64_t i = 0; i < nr; ++i) {
+          d2d(d_out + rows[(size_t)i] * k, td + i * k, sizeof(float) * k, s);
+          d2d(d_lab + rows[(size_t)i] * k, tl + i * k, sizeof(int64_t) * k, s);
+        }
+        sync(s);
+        ix->overflow_rows += nr;
+      }
+    }
+  }
+}
+
+void flat_search_any(mv_flat* ix, const float* d_x, int64_t nq, int k, const uint8_t* d_filter,
+                     const mv_search_params* p, float* d_out, int64_t* d_lab, DevBuf& ws,
+                     cudaStream_t s) {
+  const int form = p ? p->form : MV_FORM_PLAIN;
+  MV_REQUIRE(form == MV_FORM_PLAIN || form == MV_FORM_FAST, MV_ERR_ARG, "unknown search form");
+  if (form == MV_FORM_FAST) flat_search_fast(ix, d_x, nq, k, d_filter, p, d_out, d_lab, ws, s);
+  else flat_search_plain(ix, d_x, nq, k, d_filter, d_out, d_lab, ws, s);
+}
+
 }  // namespace mv
 
 extern "C" {
@@ -973,13 +1127,11 @@ int32_t mv_flat_search_device(mv_flat* ix, const float* d_x, int64_t nq, int32_t
   if (!ix || (nq > 0 && (!d_x || !d_distances || !d_labels))) return MV_ERR_ARG;
   return guard(ix->ctx, [&] {
     check_search_args(nq, k);
-    const int form = params ? params->form : MV_FORM_PLAIN;
-    MV_REQUIRE(form == MV_FORM_PLAIN, MV_ERR_UNSUPPORTED, "fast form not built in this library");
     SlotLease lease(ix->ctx);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : lease.stream();
     lease.use(s);
-    flat_search_plain(ix, d_x, nq, k, d_filter, d_distances, d_labels, lease.slot->ws, s);
-    if (!stream) sync(s);
+    flat_search_any(ix, d_x, nq, k, d_filter, params, d_distances, d_labels, lease.slot->ws, s);
+    if (!stream) check_kernel_errors(ix->ctx, s);
   });
 }
 
@@ -989,8 +1141,6 @@ int32_t mv_flat_search(mv_flat* ix, const float* x, int64_t nq, int32_t k, const
   return guard(ix->ctx, [&] {
     check_search_args(nq, k);
     if (nq == 0) return;
-    const int form = params ? params->form : MV_FORM_PLAIN;
-    MV_REQUIRE(form == MV_FORM_PLAIN, MV_ERR_UNSUPPORTED, "fast form not built in this library");
     SlotLease lease(ix->ctx);
     cudaStream_t s = lease.stream();
     DevBuf& io = lease.slot->io;
@@ -1004,10 +1154,10 @@ int32_t mv_flat_search(mv_flat* ix, const float* x, int64_t nq, int32_t k, const
     uint8_t* df = ar.take<uint8_t>(fl + 1);
     h2d(dx, x, sizeof(float) * nq * ix->d, s);
     if (fl) h2d(df, filter, fl, s);
-    flat_search_plain(ix, dx, nq, k, fl ? df : nullptr, dd, dl, lease.slot->ws, s);
+    flat_search_any(ix, dx, nq, k, fl ? df : nullptr, params, dd, dl, lease.slot->ws, s);
     d2h(distances, dd, sizeof(float) * nq * k, s);
     d2h(labels, dl, sizeof(int64_t) * nq * k, s);
-    sync(s);
+    check_kernel_errors(ix->ctx, s);
   });
 }
 

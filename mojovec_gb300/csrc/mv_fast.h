@@ -21,6 +21,9 @@ struct FastScanArgs {
   int R;                  // shortlist length
   int sorted;             // 1: shortlist sorted ascending (it is the answer)
   uint64_t* out_keys;     // nq x R (distance, CSR position)
+  int nlist;              // bounds of the data-dependent indices
+  int64_t ntotal;
+  int* err;               // set to a site code if an index is out of range
   int cap, Rp;            // set by the launcher
 };
 
@@ -29,11 +32,14 @@ struct RerankArgs {
   int64_t nq;
   int d, metric;
   const float* raw;       // FP32 rows in CSR order
-  const uint32_t* ids;    // id per CSR entry
+  const uint32_t* ids;    // id per CSR entry (null: the position is the id)
   const uint64_t* cand;   // nq x R shortlist keys
   int R, k;
   float* out_d;
   int64_t* out_l;
+  int64_t ntotal;         // CSR entries (bound of the shortlist positions)
+  int* err;
+  float fill_d = 1e38f;   // distance of an unfilled slot (label -1)
   int kp;                 // set by the launcher
 };
 
@@ -42,8 +48,20 @@ void launch_vec_terms(const int64_t* off, int nlist, const uint8_t* codes, const
 // Top-nc of the approximate coarse distances, exact FP32 recheck, top-nprobe.
 void launch_coarse_fast(const float* approx, int64_t nq, int nlist, const float* q, int d,
                         const float* cent, int metric, int nc, int nprobe, int32_t* probes,
-                        float* term, cudaStream_t s);
+                        float* term, int* err, cudaStream_t s);
+// Same from per-row candidate keys (ncand per row, KEY_NONE padded).
+void launch_coarse_from_keys(const uint64_t* cand, int64_t nq, int ncand, const float* q, int d,
+                             const float* cent, int nlist, int metric, int nc, int nprobe,
+                             int32_t* probes, float* term, int* err, cudaStream_t s);
 void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s);
+// Flat fast form: merge nseg x ncp per-segment keys (kseg kept per segment)
+// into the R-key shortlist per query. With out_keys the shortlist is
+// written (unsorted) for the rerank; otherwise the k smallest become the
+// results (L2 adds qnorm back). overflow[q] = 1 when a segment may have
+// dropped a shortlist key (only possible when kseg < R); may be null.
+void launch_flat_merge(const uint64_t* cand, int64_t nq, int nseg, int ncp, int kseg, int R,
+                       uint64_t* out_keys, int k, const float* qnorm, int metric, float fill_d,
+                       float* out_d, int64_t* out_l, int* overflow, cudaStream_t s);
 void launch_rerank_fast(RerankArgs a, cudaStream_t s);
 void launch_short_to_results(const uint64_t* keys, int64_t nq, int R, int k, const uint32_t* ids,
                              int metric, float* out_d, int64_t* out_l, cudaStream_t s);

@@ -198,9 +198,11 @@ struct mv_flat {
   int64_t ntotal = 0, capacity = 0;
   std::mutex mu;
   mv::DevBuf rows;       // capacity x d FP32
-  mv::DevBuf rows_bf16;  // ntotal x d BF16 (fast form, built lazily)
-  mv::DevBuf norms;      // FP32 ||x||^2 per row (fast form)
+  mv::DevBuf rows_bf16;  // ntotal x kpad BF16 (fast form, built lazily)
+  mv::DevBuf norms;      // FP32 ||x||^2 per rounded row (fast form)
+  std::mutex fast_mu;
   bool fast_ready = false;
+  int64_t overflow_rows = 0;  // fast-form queries recomputed exactly (shortlist overflow)
 };
 
 struct mv_sq8 {

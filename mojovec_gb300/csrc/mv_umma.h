@@ -25,6 +25,20 @@ struct UmmaArgs {
   int* err;          // set to 1 when a bounded wait gave up
 };
 
+struct UmmaTopkArgs {
+  int64_t nrows, ncols;
+  int nkb, metric;
+  const float* rnorm;  // may be null
+  const float* cnorm;
+  int nc, ncp;         // keys kept per row, padded output stride (power of two)
+  int nseg, tps;       // column segments (grid.y) and column tiles per segment
+  int pend;            // pending keys per row (multiple of 8, >= 32)
+  const uint8_t* filter;  // filter[col] > 0 excludes the column (may be null)
+  uint64_t* gthr;      // per-row threshold shared by the segments (may be null)
+  uint64_t* out;       // nrows x nseg x ncp keys (distance, column)
+  int* err;
+};
+
 // Rows are padded to this many BF16 elements (a multiple of 64).
 int umma_kpad(int d);
 // FP32 rows -> zero-padded BF16 rows (kpad wide) and FP32 norms of the
@@ -35,6 +49,20 @@ void launch_to_bf16(const float* x, int64_t n, int d, __nv_bfloat16* out, float*
 void launch_umma_dist(int epi, const __nv_bfloat16* X, int64_t nx, const __nv_bfloat16* Y,
                       int64_t ny, int d, int metric, const float* xnorm, const float* ynorm,
                       float* out, int64_t ldo, uint64_t* keys, int* err, int num_sms,
+                      cudaStream_t s);
+// Most keys the fused top-k GEMM keeps per row and column segment.
+constexpr int UMMA_TOPK_MAX = 64;
+// Column segments for the fused top-k GEMM: enough CTAs to fill the SMs
+// in whole waves.
+int umma_topk_nseg(int64_t nrows, int64_t ncols, int d, int nc, int num_sms);
+// Per-row nc smallest (distance, column) keys of the BF16 distances, per
+// column segment: out[(row * nseg + seg) * next_pow2(nc) + j], unsorted,
+// KEY_NONE padded. The key distance leaves out the row's own ||x||^2.
+// gthr (nx keys, may be null) lets the segments share the row threshold;
+// only valid when the caller needs no more than nc keys per row.
+void launch_umma_topk(const __nv_bfloat16* X, int64_t nx, const __nv_bfloat16* Y, int64_t ny,
+                      int d, int metric, const float* xnorm, const float* ynorm, int nc, int nseg,
+                      const uint8_t* filter, uint64_t* gthr, uint64_t* out, int* err,
                       cudaStream_t s);
 // keys -> argmin columns (and distances).
 void launch_keys_argmin(const uint64_t* keys, int64_t n, int32_t* out, float* dist, cudaStream_t s);

@@ -135,3 +135,20 @@ def test_fast_search_in_fresh_process():
     r = subprocess.run([sys.executable, "-c", script], cwd=root, capture_output=True, text=True,
                        timeout=600)
     assert r.returncode == 0 and "ok" in r.stdout, r.stderr[-2000:]
+
+
+def test_fast_fused_coarse_matches_matrix_coarse(mv):
+    """The fused GEMM + per-row top-k coarse step (used while nprobe plus its
+    margin fits 64 lists per query) and the distance-matrix path must pick
+    the same probes as the exact FP32 coarse step up to BF16 near-ties."""
+    from mojovec_gb300 import synth
+
+    base, q = synth.sift_like(40000, d=96, n_centers=64, nq=400, seed=33)
+    g = _index(mv, base, 96, 512, 24)
+    # nprobe 4, 16, 48 keep at most 64 lists per query (fused GEMM + heap);
+    # nprobe 80 keeps 100 (distance matrix + radix select)
+    for nprobe in (4, 16, 48, 80):
+        _, lf = g.search(q, 10, form=mv.FORM_FAST, nprobe=nprobe, rerank=100)
+        _, lc = g.search(q, 10, form=mv.FORM_FAST, nprobe=nprobe, rerank=100, coarse_fp32=True)
+        agree = np.mean([len(set(a) & set(b)) / 10 for a, b in zip(lf, lc)])
+        assert agree > 0.97, (nprobe, agree)
