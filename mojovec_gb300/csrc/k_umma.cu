@@ -279,8 +279,8 @@ __device__ __forceinline__ void heap_replace_top(uint64_t* h, int K, uint64_t ke
   h[(size_t)i * BM] = key;
 }
 
-template <int BN>
-__global__ void __launch_bounds__(NUM_THREADS, 1)
+template <int BN, bool L2, int EG>
+__global__ void __launch_bounds__(64 + 128 * EG, 1)
     k_umma_topk(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUtensorMap ty,
                 UmmaTopkArgs g) {
   extern __shared__ uint8_t smem_raw[];
@@ -291,10 +291,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   const uint32_t b_stage = (uint32_t)nkb * BN * 128;
   uint8_t* sA = smem;
   uint8_t* sB = smem + a_bytes;
-  uint64_t* heap = reinterpret_cast<uint64_t*>(sB + STAGES * b_stage);  // nc x BM
-  uint64_t* pend = heap + (size_t)g.nc * BM;                             // g.pend x BM
-  float* cnbuf = reinterpret_cast<float*>(pend + (size_t)g.pend * BM);  // 4 x BN
-  uint64_t* bars = reinterpret_cast<uint64_t*>(cnbuf + 4 * BN);
+  // Per epilogue group: heaps (nc x BM), pending (g.pend x BM); per
+  // epilogue warp: the tile's column biases (BN floats).
+  uint64_t* heap = reinterpret_cast<uint64_t*>(sB + STAGES * b_stage);
+  uint64_t* pend = heap + (size_t)EG * g.nc * BM;
+  float* cnbuf = reinterpret_cast<float*>(pend + (size_t)EG * g.pend * BM);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(cnbuf + 4 * EG * BN);
   uint32_t* holder = reinterpret_cast<uint32_t*>(bars + 12);
   __shared__ int s_err;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -313,7 +315,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     }
     for (int a = 0; a < 2; ++a) {
       mbar_init(b_tfull(a), 1);
-      mbar_init(b_tempty(a), 128);
+      mbar_init(b_tempty(a), 128 * EG);
     }
     mbar_init(b_done, 1);
     mbar_init(b_fulla, 1);
@@ -391,16 +393,20 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       umma_commit(b_done);
     }
   } else {
+    // Epilogue warp (q, h): TMEM lane quarter q (= warp % 4, as tcgen05.ld
+    // requires) and group h, which owns chunks [h * NCHG, (h + 1) * NCHG) of
+    // every tile and keeps its own heaps (an output segment of its own).
     const int q = warp & 3;
+    const int h = (warp - 2) >> 2;
     const int rloc = q * 32 + lane;
     const int64_t row = (int64_t)rb * BM + rloc;
     const bool row_ok = row < g.nrows;
     const int K = g.nc;
-    const bool l2 = g.metric == MV_METRIC_L2;
     const float INF = __int_as_float(0x7f800000);
-    uint64_t* H = heap + rloc;  // H[j * BM]
-    uint64_t* P = pend + rloc;  // P[j * BM]
-    float* cs = cnbuf + q * BN;  // this warp's copy of the tile's column norms
+    constexpr float SCALE = L2 ? 2.0f : 1.0f;
+    uint64_t* H = heap + (size_t)h * K * BM + rloc;      // H[j * BM]
+    uint64_t* P = pend + (size_t)h * g.pend * BM + rloc;  // P[j * BM]
+    float* cs = cnbuf + (h * 4 + q) * BN;  // this warp's copy of the tile's column biases
     for (int j = 0; j < K; ++j) H[(size_t)j * BM] = KEY_NONE;
     int pc = 0;
     // Work with e = -distance (2 x.y - ||y||^2 for L2, x.y for IP): a column
@@ -426,15 +432,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       // e == thr_e may still lose the tie on the column; the drain decides.
       thr_e = !row_ok ? INF : (thr == KEY_NONE ? -INF : -key_dist(thr));
     };
-    // Column norms of the next tile, prefetched into registers while the
-    // current tile is processed (lane t holds columns t * CPL ...).
+    // e = SCALE * acc + bias: bias = -||y||^2 (L2) or 0 (IP), and -inf for
+    // columns past the end, so the hot loop needs no masking. The next
+    // tile's biases are prefetched into registers (lane t holds columns
+    // t * CPL ...) while the current tile is processed.
     constexpr int CPL = BN / 32;
     float cpre[CPL];
     auto load_cn = [&](int i) {
       const int64_t base = (int64_t)(ct0 + i) * BN + lane * CPL;
 #pragma unroll
       for (int u = 0; u < CPL; ++u)
-        cpre[u] = (l2 && base + u < g.ncols) ? __ldg(g.cnorm + base + u) : 0.0f;
+        cpre[u] = base + u >= g.ncols ? -INF : (L2 ? -__ldg(g.cnorm + base + u) : 0.0f);
     };
     if (my_count > 0) load_cn(0);
     uint64_t gpre = KEY_NONE;  // the row's shared threshold, read one tile ahead
@@ -460,41 +468,32 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       }
       const int64_t tile0 = (int64_t)(ct0 + i) * BN;
       const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN);
-      constexpr int NCH = BN / 32;
-      // e = -distance of the 32 columns of chunk ch (masked past the end).
+      constexpr int NCH = BN / 32 / EG;  // chunks of this group
+      const int chb = h * NCH;           // its first chunk
+      // e = -distance of the 32 columns of chunk ch (-inf past the end).
       auto chunk_e = [&](const uint32_t* rv, int ch, float* e) {
-        const int c0 = ch * 32;
-        if (l2) {
 #pragma unroll
-          for (int j = 0; j < 32; j += 4) {
-            const float4 c4 = *reinterpret_cast<const float4*>(cs + c0 + j);  // broadcast
-            e[j] = fmaf(2.0f, __uint_as_float(rv[j]), -c4.x);
-            e[j + 1] = fmaf(2.0f, __uint_as_float(rv[j + 1]), -c4.y);
-            e[j + 2] = fmaf(2.0f, __uint_as_float(rv[j + 2]), -c4.z);
-            e[j + 3] = fmaf(2.0f, __uint_as_float(rv[j + 3]), -c4.w);
-          }
-        } else {
-#pragma unroll
-          for (int j = 0; j < 32; ++j) e[j] = __uint_as_float(rv[j]);
-        }
-        const int64_t left = g.ncols - (tile0 + c0);  // the same in every lane
-        if (left < 32) {
-#pragma unroll
-          for (int j = 0; j < 32; ++j)
-            if (j >= left) e[j] = -INF;
+        for (int j = 0; j < 32; j += 4) {
+          const float4 b4 = *reinterpret_cast<const float4*>(cs + ch * 32 + j);  // broadcast
+          e[j] = fmaf(SCALE, __uint_as_float(rv[j]), b4.x);
+          e[j + 1] = fmaf(SCALE, __uint_as_float(rv[j + 1]), b4.y);
+          e[j + 2] = fmaf(SCALE, __uint_as_float(rv[j + 2]), b4.z);
+          e[j + 3] = fmaf(SCALE, __uint_as_float(rv[j + 3]), b4.w);
         }
       };
-      // Phase 1, no branches: the largest e of each chunk.
+      // Phase 1, no branches: the largest e of each chunk. All of the
+      // tile's TMEM loads are issued before the first wait.
       float cmax[NCH];
       {
-        uint32_t r[2][32];
-        tmem_ld32_issue(tbase, r[0]);
-        tmem_ld32_wait(r[0]);
+        uint32_t r[NCH][32];
+#pragma unroll
+        for (int ch = 0; ch < NCH; ++ch) tmem_ld32_issue(tbase + (uint32_t)((chb + ch) * 32), r[ch]);
+#pragma unroll
+        for (int ch = 0; ch < NCH; ++ch) tmem_ld32_wait(r[ch]);
 #pragma unroll
         for (int ch = 0; ch < NCH; ++ch) {
-          if (ch + 1 < NCH) tmem_ld32_issue(tbase + (uint32_t)(ch * 32 + 32), r[(ch + 1) & 1]);
           float e[32];
-          chunk_e(r[ch & 1], ch, e);
+          chunk_e(r[ch], chb + ch, e);
 #pragma unroll
           for (int j = 0; j < 16; ++j) e[j] = fmaxf(e[j], e[j + 16]);
 #pragma unroll
@@ -502,7 +501,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
             for (int j = 0; j < w; ++j) e[j] = fmaxf(e[j], e[j + w]);
           cmax[ch] = e[0];
-          if (ch + 1 < NCH) tmem_ld32_wait(r[(ch + 1) & 1]);
         }
       }
       float tmax = cmax[0];
@@ -520,11 +518,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             if (ch == c) cm = cmax[c];
           if (!__any_sync(0xffffffffu, cm >= thr_e)) continue;
           uint32_t rv[32];
-          tmem_ld32_issue(tbase + (uint32_t)(ch * 32), rv);
+          tmem_ld32_issue(tbase + (uint32_t)((chb + ch) * 32), rv);
           tmem_ld32_wait(rv);
           float e[32];
-          chunk_e(rv, ch, e);
-          const int64_t col0 = tile0 + ch * 32;
+          chunk_e(rv, chb + ch, e);
+          const int64_t col0 = tile0 + (chb + ch) * 32;
           const int64_t left = g.ncols - col0;
           float m[8];
 #pragma unroll
@@ -552,7 +550,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     }
     drain();
     if (row_ok) {
-      uint64_t* o = g.out + ((size_t)row * g.nseg + seg) * g.ncp;
+      uint64_t* o = g.out + ((size_t)row * g.nseg * EG + (size_t)seg * EG + h) * g.ncp;
       for (int j = 0; j < g.ncp; ++j) o[j] = j < K ? H[(size_t)j * BM] : KEY_NONE;
     }
   }
@@ -696,33 +694,45 @@ void launch_umma_dist(int epi, const __nv_bfloat16* X, int64_t nx, const __nv_bf
 }
 
 namespace {
-// Y tile width of the top-k GEMM: 128 up to d = 128, else 64, so that the
-// X block, two Y stages, the heaps and the pending buffers fit 227 KB.
-int topk_bn(int nkb) { return nkb <= 2 ? 128 : 64; }
-size_t topk_smem_base(int nkb, int bn, int nc) {
-  return 1024 + (size_t)nkb * BM * 128 + (size_t)STAGES * nkb * bn * 128 + (size_t)nc * BM * 8 +
-         (size_t)4 * bn * 4 + 256;
+// Shape of the top-k GEMM: Y tile width, epilogue groups and pending slots.
+// One epilogue group (4 warps) with the widest Y tile that fits: 128 up to
+// d = 128, else 64. The kernel template also takes two groups (8 warps, two
+// per TMEM lane quarter, each with its own heaps), which hides more of the
+// epilogue's latency but needs 64-wide tiles to fit 227 KB; measured on
+// 10k x 1M x 128 that halves the TMA/MMA pipeline's rate and leaves too few
+// pending slots, so it is slower (14.7 ms against 10.9 ms) and not chosen.
+struct TopkCfg {
+  int bn, eg, pend;
+};
+size_t topk_smem_base(int nkb, int bn, int nc, int eg) {
+  return 1024 + (size_t)nkb * BM * 128 + (size_t)STAGES * nkb * bn * 128 +
+         (size_t)eg * nc * BM * 8 + (size_t)4 * eg * bn * 4 + 256;
 }
-// Pending slots that fit next to the heaps (multiple of 8).
-int topk_pend(int nkb, int bn, int nc) {
-  const size_t base = topk_smem_base(nkb, bn, nc);
-  const size_t room = base < 227 * 1024 ? (227 * 1024 - base) / ((size_t)BM * 8) : 0;
+int topk_pend_fit(int nkb, int bn, int nc, int eg) {
+  const size_t base = topk_smem_base(nkb, bn, nc, eg);
+  const size_t room = base < 227 * 1024 ? (227 * 1024 - base) / ((size_t)eg * BM * 8) : 0;
   return (int)std::min<size_t>(TOPK_PEND_MAX, room / 8 * 8);
 }
-size_t topk_smem(int nkb, int bn, int nc) {
-  return topk_smem_base(nkb, bn, nc) + (size_t)topk_pend(nkb, bn, nc) * BM * 8;
+TopkCfg topk_cfg(int nkb, int nc) {
+  const int bn = nkb <= 2 ? 128 : 64;
+  return {bn, 1, topk_pend_fit(nkb, bn, nc, 1)};
+}
+size_t topk_smem(int nkb, const TopkCfg& c, int nc) {
+  return topk_smem_base(nkb, c.bn, nc, c.eg) + (size_t)c.eg * c.pend * BM * 8;
 }
 }  // namespace
 
+int umma_topk_groups(int d, int nc) { return topk_cfg(umma_kpad(d) / 64, nc).eg; }
+
 int umma_topk_nseg(int64_t nrows, int64_t ncols, int d, int nc, int num_sms) {
   const int nkb = umma_kpad(d) / 64;
-  const int bn = topk_bn(nkb);
+  const TopkCfg c = topk_cfg(nkb, nc);
   const int64_t nrb = (nrows + BM - 1) / BM;
-  const int64_t nct = (ncols + bn - 1) / bn;
+  const int64_t nct = (ncols + c.bn - 1) / c.bn;
   // CTAs resident per SM (228 KB of shared memory per SM, 1 KB reserved per
   // CTA), then the fewest column segments whose CTAs fill the last wave to
   // 90%; a segment is never shorter than 16 column tiles.
-  const int64_t cps = std::max<int64_t>(1, std::min<int64_t>(4, (228 * 1024) / (topk_smem(nkb, bn, nc) + 1024)));
+  const int64_t cps = std::max<int64_t>(1, std::min<int64_t>(4, (228 * 1024) / (topk_smem(nkb, c, nc) + 1024)));
   const int64_t slots = (int64_t)std::max(num_sms, 1) * cps;
   const int64_t maxseg = std::max<int64_t>(1, std::min<int64_t>(nct / 16, 4096));
   int64_t best = 1;
@@ -765,23 +775,27 @@ void launch_umma_topk(const __nv_bfloat16* X, int64_t nx, const __nv_bfloat16* Y
   if (gthr) MV_CHECK_CUDA(cudaMemsetAsync(gthr, 0xff, sizeof(uint64_t) * nx, s));
   g.out = out;
   g.err = err;
-  const int bn = topk_bn(g.nkb);
-  g.pend = topk_pend(g.nkb, bn, nc);
+  const TopkCfg c = topk_cfg(g.nkb, nc);
+  g.pend = c.pend;
   MV_REQUIRE(g.pend >= TOPK_PEND_MIN, MV_ERR_UNSUPPORTED, "fused top-k GEMM: nc or d too large");
-  const int64_t nct = (ny + bn - 1) / bn;
+  const int64_t nct = (ny + c.bn - 1) / c.bn;
   g.tps = (int)((nct + nseg - 1) / nseg);
   const CUtensorMap tx = make_tmap(X, nx, kp, BM);
-  const CUtensorMap ty = make_tmap(Y, ny, kp, bn);
+  const CUtensorMap ty = make_tmap(Y, ny, kp, c.bn);
   MV_REQUIRE((nx + BM - 1) / BM <= 65535, MV_ERR_UNSUPPORTED, "fused top-k: too many rows per launch");
   dim3 grid((unsigned)nseg, (unsigned)((nx + BM - 1) / BM));
-  auto go = [&](auto kernel) {
-    const size_t smem = topk_smem(g.nkb, bn, nc);
-    MV_REQUIRE(smem <= 227 * 1024, MV_ERR_UNSUPPORTED, "fused top-k GEMM: nc or d too large");
+  const size_t smem = topk_smem(g.nkb, c, nc);
+  MV_REQUIRE(smem <= 227 * 1024, MV_ERR_UNSUPPORTED, "fused top-k GEMM: nc or d too large");
+  auto go = [&](auto kernel, int threads) {
     smem_limit(kernel, smem);
-    kernel<<<grid, NUM_THREADS, smem, s>>>(tx, ty, g);
+    kernel<<<grid, threads, smem, s>>>(tx, ty, g);
   };
-  if (bn == 128) go(k_umma_topk<128>);
-  else go(k_umma_topk<64>);
+  const bool l2m = metric == MV_METRIC_L2;
+  if (c.bn == 128) {
+    l2m ? go(k_umma_topk<128, true, 1>, 192) : go(k_umma_topk<128, false, 1>, 192);
+  } else {
+    l2m ? go(k_umma_topk<64, true, 1>, 192) : go(k_umma_topk<64, false, 1>, 192);
+  }
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());
 }

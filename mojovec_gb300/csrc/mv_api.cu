@@ -450,7 +450,7 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
   int64_t qb = std::max<int64_t>(128, (int64_t)(1536ll * 1024 * 1024 / ((int64_t)ix->nlist * 4)));
   qb = std::min<int64_t>({qb, nq, 65535ll * 64});
   const int nseg = fused ? umma_topk_nseg(qb, ix->nlist, ix->d, nc, ix->ctx->num_sms) : 1;
-  const int ncand = nseg * next_pow2(nc);
+  const int ncand = nseg * (fused ? umma_topk_groups(ix->d, nc) : 1) * next_pow2(nc);
   ws.ensure(ws_bytes((size_t)qb * kp, 2) +
             (fused ? ws_bytes((size_t)qb * ncand, 8) + ws_bytes((size_t)qb, 8)
                    : ws_bytes((size_t)qb * ix->nlist, 4)) +
@@ -459,7 +459,7 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
   __nv_bfloat16* xq = ar.take<__nv_bfloat16>((size_t)qb * kp);
   float* dmat = fused ? nullptr : ar.take<float>((size_t)qb * ix->nlist);
   uint64_t* ckeys = fused ? ar.take<uint64_t>((size_t)qb * ncand) : nullptr;
-  uint64_t* gthr = fused && nseg > 1 ? ar.take<uint64_t>((size_t)qb) : nullptr;
+  uint64_t* gthr = fused && ncand > next_pow2(nc) ? ar.take<uint64_t>((size_t)qb) : nullptr;
   int32_t* probes = ar.take<int32_t>((size_t)qb * nprobe);
   float* term = ar.take<float>((size_t)qb * nprobe);
   uint64_t* skeys = ar.take<uint64_t>((size_t)qb * R);
@@ -977,21 +977,24 @@ void flat_search_fast(mv_flat* ix, const float* d_x, int64_t nq, int k, const ui
   const int kp = umma_kpad(ix->d);
   const int64_t qb = std::min<int64_t>(nq, 32768);
   int nseg = umma_topk_nseg(qb, nb, ix->d, kseg, ix->ctx->num_sms);
+  const int groups = umma_topk_groups(ix->d, kseg);
   if (kseg < R) {  // about 16 shortlist keys per segment keeps overflow rare
     const int64_t nct = (nb + 127) / 128;
-    nseg = (int)std::min<int64_t>(std::max<int64_t>(nseg, (R + 15) / 16), std::max<int64_t>(1, nct));
+    nseg = (int)std::min<int64_t>(std::max<int64_t>(nseg, (R + 15) / 16 / groups + 1),
+                                  std::max<int64_t>(1, nct));
   }
+  const int osegs = nseg * groups;  // output segments per query
   ws.ensure(ws_bytes((size_t)qb * kp, 2) + ws_bytes((size_t)qb, 4) +
-            ws_bytes((size_t)qb * nseg * ncp, 8) + ws_bytes((size_t)qb * R, 8) +
+            ws_bytes((size_t)qb * osegs * ncp, 8) + ws_bytes((size_t)qb * R, 8) +
             ws_bytes((size_t)qb, 4) + ws_bytes((size_t)qb, 8));
   Arena ar(ws);
   __nv_bfloat16* xq = ar.take<__nv_bfloat16>((size_t)qb * kp);
   float* qnorm = ar.take<float>((size_t)qb);
-  uint64_t* cand = ar.take<uint64_t>((size_t)qb * nseg * ncp);
+  uint64_t* cand = ar.take<uint64_t>((size_t)qb * osegs * ncp);
   uint64_t* skeys = ar.take<uint64_t>((size_t)qb * R);
   int* over = ar.take<int>((size_t)qb);
   // Shared per-row threshold: exact only when a segment keeps all R keys.
-  uint64_t* gthr = (kseg == R && nseg > 1) ? ar.take<uint64_t>((size_t)qb) : nullptr;
+  uint64_t* gthr = (kseg == R && osegs > 1) ? ar.take<uint64_t>((size_t)qb) : nullptr;
   std::vector<int> h_over;
   for (int64_t q0 = 0; q0 < nq; q0 += qb) {
     const int64_t nqb = std::min(qb, nq - q0);
@@ -1005,7 +1008,7 @@ void flat_search_fast(mv_flat* ix, const float* d_x, int64_t nq, int k, const ui
     }
     {
       StageTimer t(ix->ctx, MV_STAGE_SELECT, s);
-      launch_flat_merge(cand, nqb, nseg, ncp, kseg, R, rerank ? skeys : nullptr, k, qnorm,
+      launch_flat_merge(cand, nqb, osegs, ncp, kseg, R, rerank ? skeys : nullptr, k, qnorm,
                         ix->metric, 0.0f, d_out + q0 * k, d_lab + q0 * k,
                         kseg < R ? over : nullptr, s);
     }

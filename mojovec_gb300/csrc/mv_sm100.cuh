@@ -43,13 +43,30 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
+// try_wait that may suspend the thread in hardware for up to kSuspendNs
+// while the phase is incomplete (it resumes when the phase completes), so a
+// waiting warp does not spin and take issue slots from the warps that share
+// its scheduler.
+constexpr uint32_t kSuspendNs = 100000;  // 0.1 ms per attempt
+__device__ __forceinline__ bool mbar_try_wait_suspend(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity), "r"(kSuspendNs)
+      : "memory");
+  return ok != 0;
+}
+
 // Waits until the phase with the given parity completed. Returns false on
 // timeout.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
   if (mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   while (true) {
-    if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_try_wait_suspend(bar, parity)) return true;
     if (clock64() - t0 > kWaitLimitCycles) return false;
   }
 }

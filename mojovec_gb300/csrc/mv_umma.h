@@ -31,7 +31,7 @@ struct UmmaTopkArgs {
   const float* rnorm;  // may be null
   const float* cnorm;
   int nc, ncp;         // keys kept per row, padded output stride (power of two)
-  int nseg, tps;       // column segments (grid.y) and column tiles per segment
+  int nseg, tps;       // column segments (grid.x) and column tiles per segment
   int pend;            // pending keys per row (multiple of 8, >= 32)
   const uint8_t* filter;  // filter[col] > 0 excludes the column (may be null)
   uint64_t* gthr;      // per-row threshold shared by the segments (may be null)
@@ -52,12 +52,17 @@ void launch_umma_dist(int epi, const __nv_bfloat16* X, int64_t nx, const __nv_bf
                       cudaStream_t s);
 // Most keys the fused top-k GEMM keeps per row and column segment.
 constexpr int UMMA_TOPK_MAX = 64;
+// Epilogue groups of the fused top-k GEMM for (d, nc): each CTA writes one
+// output segment per group, so a launch with nseg column segments leaves
+// nseg * groups segments per row.
+int umma_topk_groups(int d, int nc);
 // Column segments for the fused top-k GEMM: enough CTAs to fill the SMs
 // in whole waves.
 int umma_topk_nseg(int64_t nrows, int64_t ncols, int d, int nc, int num_sms);
 // Per-row nc smallest (distance, column) keys of the BF16 distances, per
-// column segment: out[(row * nseg + seg) * next_pow2(nc) + j], unsorted,
-// KEY_NONE padded. The key distance leaves out the row's own ||x||^2.
+// output segment: out[(row * S + s) * next_pow2(nc) + j] with
+// S = nseg * umma_topk_groups(d, nc), unsorted, KEY_NONE padded. The key
+// distance leaves out the row's own ||x||^2.
 // gthr (nx keys, may be null) lets the segments share the row threshold;
 // only valid when the caller needs no more than nc keys per row.
 void launch_umma_topk(const __nv_bfloat16* X, int64_t nx, const __nv_bfloat16* Y, int64_t ny,
