@@ -367,29 +367,46 @@ def run_gpu(args, rank, world):
 
 
 FLAT_METRIC = "Flat QPS (1Mx128 SIFT-like, 10k queries), BF16 tcgen05 + FP32 rerank of k*4 vs plain FP32"
+SQ8_METRIC = ("SQ8 QPS (1Mx128 SIFT-like, 10k queries, FP32 rerank of k*2), tensor-core shortlist "
+              "vs integer scan (identical results)")
 
 
 def run_flat(args, rank, world):
-    """Flat scan: plain FP32 (the reference's IndexFlat arithmetic) and the
-    fast form on the same rows; recall against the plain form, which equals
-    FP64 on these integer-valued rows."""
+    """Flat or SQ8 scan. Flat: plain FP32 (the reference's IndexFlat
+    arithmetic) against the fast form (BF16 shortlist + exact FP32 rerank).
+    SQ8: the integer (dp4a) scan against the tensor-core scan over the same
+    codes, both with the exact FP32 rerank of k * rerank_factor; the two
+    must return identical results. Recall is against the exact FP32 flat
+    search, which equals FP64 on these integer-valued rows."""
     import torch
 
     import mojovec_gb300 as mv
 
     nb, nq, k = args.nb, args.nq, args.k
+    sq8 = args.workload == "sq8"
     metric = mv.METRIC_L2 if args.metric == "l2" else mv.METRIC_IP
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
     ctx = mv.Context(dev)
     t_setup = time.perf_counter()
     base, queries = build_workload(nb, nq)
-    flat = mv.IndexFlat(D, metric, ctx=ctx)
-    flat.add(base)
+    exact = mv.IndexFlat(D, metric, ctx=ctx)
+    exact.add(base)
+    if sq8:
+        flat = mv.IndexFlatSQ8(D, metric, ctx=ctx)
+        flat.add(base)
+        _, gt_exact = exact.search(queries, k)
+        del exact
+        factor = args.rerank_factor
+        fast = dict(form=mv.FORM_FAST, rerank_factor=factor)
+        plain = dict(form=mv.FORM_PLAIN, rerank_factor=factor)
+        rerank = k * factor
+    else:
+        flat = exact
+        rerank = args.rerank
+        fast = dict(form=mv.FORM_FAST, rerank=rerank)
+        plain = dict(form=mv.FORM_PLAIN)
     setup_s = time.perf_counter() - t_setup
-    rerank = args.rerank
-    fast = dict(form=mv.FORM_FAST, rerank=rerank)
-    plain = dict(form=mv.FORM_PLAIN)
     d_q = torch.from_numpy(queries).cuda()
     d_dist = torch.empty((nq, k), dtype=torch.float32, device="cuda")
     d_lab = torch.empty((nq, k), dtype=torch.int64, device="cuda")
@@ -403,7 +420,7 @@ def run_flat(args, rank, world):
         return step
 
     results = {}
-    plain_steps = max(1, min(args.steps, 3))  # the FP32 scan is ~50x slower
+    plain_steps = max(1, min(args.steps, 3))  # the plain scans are 10-50x slower
     for name, opts, steps in (("plain", plain, plain_steps), ("fast", fast, args.steps)):
         step = make_step(opts)
         for _ in range(args.warmup if name == "fast" else 1):
@@ -426,6 +443,10 @@ def run_flat(args, rank, world):
         results[name]["ms"] = _max_over_ranks(torch, world, ms) / steps
     gt = results["plain"]["labels"]
     rec = recall_at(gt, results["fast"]["labels"], k)
+    if sq8:
+        identical = bool(np.array_equal(results["fast"]["labels"], gt) and
+                         np.array_equal(results["fast"]["dist"], results["plain"]["dist"]))
+        rec_exact = recall_at(gt_exact, results["fast"]["labels"], k)
     value = world * nq / (results["fast"]["ms"] / 1e3)
     plain_qps = world * nq / (results["plain"]["ms"] / 1e3)
 
@@ -453,7 +474,7 @@ def run_flat(args, rank, world):
     flops = 2.0 * nq * nb * D
     achieved = flops / (per_launch_ms / 1e3) / 1e12 if per_launch_ms > 0 else 0.0
     out = {
-        "metric": FLAT_METRIC,
+        "metric": SQ8_METRIC if sq8 else FLAT_METRIC,
         "value": round(value, 1),
         "unit": "queries/s",
         "n_gpus": world,
@@ -466,13 +487,17 @@ def run_flat(args, rank, world):
         "dtype": "bf16+f32",
         "data": "synthetic SIFT-like (seeded Gaussian mixture, integer-valued), not SIFT1M",
         "config": {
-            "workload": f"flat_{nb}x128_{args.metric}_nq{nq}_k{k}",
-            "form": f"fast: BF16 tcgen05 GEMM + per-row heap top-{min(max(rerank, k), 64)} per "
-                    f"segment, exact FP32 rerank of {rerank}" if rerank else
-                    "fast: BF16 tcgen05 GEMM + per-row heap, BF16 distances (no rerank)",
-            "recall_at_k_vs_plain_fp32": round(rec, 5),
-            "plain_fp32_qps": round(plain_qps, 1),
-            "speedup_vs_plain_fp32": round(value / plain_qps, 2),
+            "workload": f"{'sq8' if sq8 else 'flat'}_{nb}x128_{args.metric}_nq{nq}_k{k}",
+            "form": (f"fast: SQ8 codes as BF16 on tcgen05 (exact integer dots) + per-row heap, "
+                     f"exact FP32 rerank of {rerank}") if sq8 else
+                    (f"fast: BF16 tcgen05 GEMM + per-row heap top-{min(max(rerank, k), 64)} per "
+                     f"segment, exact FP32 rerank of {rerank}" if rerank else
+                     "fast: BF16 tcgen05 GEMM + per-row heap, BF16 distances (no rerank)"),
+            ("identical_to_integer_scan" if sq8 else "recall_at_k_vs_plain_fp32"):
+                identical if sq8 else round(rec, 5),
+            **({"recall_at_k_vs_exact_fp32": round(rec_exact, 5)} if sq8 else {}),
+            ("plain_integer_scan_qps" if sq8 else "plain_fp32_qps"): round(plain_qps, 1),
+            "speedup_vs_plain": round(value / plain_qps, 2),
             "l2_policy": "inputs larger than L2 (256 MB BF16 rows) and a 256 MiB flush per step",
             "parallelism": f"replicas x{world}",
             "setup_s": round(setup_s, 1),
@@ -495,7 +520,23 @@ def run_flat(args, rank, world):
         "stages_ms_per_step": {kk: round(v[0] / args.steps, 4) for kk, v in stage.items()},
         "clocks": clk,
     }
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and not args.no_cpu and sq8:
+        from oracle import oracle as orc
+
+        sample = min(args.cpu_sample // 10, nq)
+        threads = os.cpu_count() or 1
+        ref = orc.SQ8(D, metric)
+        ref.add(base)
+        ref.search(queries[:2], k, nthreads=threads)
+        t0 = time.perf_counter()
+        _, clab = ref.search(queries[:sample], k, nthreads=threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {
+            "value": round(sample / dt, 1), "unit": "queries/s", "cores": threads, "kind": "port",
+            "sample": f"{sample} of the {nq} queries over all {nb} codes, reference IndexFlatSQ8 "
+                      f"integer scan (no rerank), query-parallel on {threads} threads",
+        }
+    elif rank == 0 and not args.no_cpu:
         from oracle import oracle as orc
 
         sample = min(args.cpu_sample // 10, nq)
@@ -580,20 +621,27 @@ def run_reference_flat(args):
     metric = 0 if args.metric == "l2" else 1
     sample = min(max(args.cpu_sample // 10, 1), args.nq)
     q = queries[:sample]
+    if args.workload == "sq8":
+        ref = orc.SQ8(D, metric)
+        ref.add(base)
+        run = lambda qq: ref.search(qq, args.k, nthreads=threads)  # noqa: E731
+    else:
+        run = lambda qq: orc.flat_search(base, qq, args.k, metric=metric, nthreads=threads)  # noqa: E731
     for _ in range(max(args.warmup, 0)):
-        orc.flat_search(base, q[:2], args.k, metric=metric, nthreads=threads)
+        run(q[:2])
     t = time.perf_counter()
     for _ in range(args.steps):
-        orc.flat_search(base, q, args.k, metric=metric, nthreads=threads)
+        run(q)
     total = time.perf_counter() - t
     qps = sample * args.steps / total
     return {
-        "metric": FLAT_METRIC, "impl": "reference", "value": round(qps, 1), "unit": "queries/s",
+        "metric": SQ8_METRIC if args.workload == "sq8" else FLAT_METRIC, "impl": "reference",
+        "value": round(qps, 1), "unit": "queries/s",
         "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1e3 * total / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic SIFT-like (seeded Gaussian mixture, integer-valued), not SIFT1M",
-        "config": {"workload": f"flat_{args.nb}x128_{args.metric}_nq{args.nq}_k{args.k}",
+        "config": {"workload": f"{args.workload}_{args.nb}x128_{args.metric}_nq{args.nq}_k{args.k}",
                    "form": "reference CPU path (oracle port)"},
         "cpu_baseline": {"value": round(qps, 1), "unit": "queries/s", "cores": threads,
                          "kind": "port",
@@ -618,7 +666,8 @@ def main():
     ap.add_argument("--nq", type=int, default=NQ, help="queries per step")
     ap.add_argument("--cpu-sample", type=int, default=500)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="ivfpq", choices=["ivfpq", "flat"])
+    ap.add_argument("--workload", default="ivfpq", choices=["ivfpq", "flat", "sq8"])
+    ap.add_argument("--rerank-factor", type=int, default=2, help="sq8 workload: shortlist k * factor")
     ap.add_argument("--k", type=int, default=K, help="flat workload: results per query")
     ap.add_argument("--metric", default="l2", choices=["l2", "ip"], help="flat workload metric")
     args = ap.parse_args()
@@ -630,7 +679,7 @@ def main():
 
     if args.impl == "reference":
         if rank == 0:
-            ref = run_reference_flat(args) if args.workload == "flat" else run_reference(args)
+            ref = run_reference_flat(args) if args.workload in ("flat", "sq8") else run_reference(args)
             print(json.dumps(ref), flush=True)
         return
 
@@ -638,7 +687,7 @@ def main():
         import torch
 
         torch.distributed.init_process_group("nccl")
-    out = run_flat(args, rank, world) if args.workload == "flat" else run_gpu(args, rank, world)
+    out = run_flat(args, rank, world) if args.workload in ("flat", "sq8") else run_gpu(args, rank, world)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

@@ -192,6 +192,22 @@ int32_t mv_sq8_search(mv_sq8* index, const float* x, int64_t nq, int32_t k,
  * distances on the retained rows (index/index_hnsw.mojo:433-497 semantics). */
 int32_t mv_sq8_search_rerank(mv_sq8* index, const float* x, int64_t nq, int32_t k,
                              int32_t rerank_factor, float* distances, int64_t* labels);
+/* SQ8 search with a form: MV_FORM_PLAIN is mv_sq8_search (rerank_factor 0)
+ * or mv_sq8_search_rerank; MV_FORM_FAST takes the shortlist from the BF16
+ * tensor cores over the codes (exact integer dot products) and returns the
+ * same ids and distances as the plain form: used where exact (L2 for
+ * d <= 129, IP for d <= 256), a query whose shortlist could differ through
+ * a distance tie is rescanned with the integer kernel. */
+int32_t mv_sq8_search_ex(mv_sq8* index, const float* x, int64_t nq, int32_t k,
+                         const uint8_t* filter, int32_t rerank_factor,
+                         const mv_search_params* params, float* distances, int64_t* labels);
+/* Same on device buffers, enqueued on `stream` (NULL: a pool stream, and the
+ * call returns when done). The SQ8 path synchronizes the stream before it
+ * returns (it reads back the per-query tie flags). */
+int32_t mv_sq8_search_device(mv_sq8* index, const float* d_x, int64_t nq, int32_t k,
+                             const uint8_t* d_filter, int32_t rerank_factor,
+                             const mv_search_params* params, float* d_distances,
+                             int64_t* d_labels, void* stream);
 
 /* ---- Training and encoding primitives --------------------------------- */
 

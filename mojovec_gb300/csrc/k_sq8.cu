@@ -10,6 +10,8 @@
 // order gives the reference's value. Rows are stored dpad (multiple of 16)
 // bytes wide with zero padding, which leaves dots and norms unchanged.
 #include "mv_exact.cuh"
+#include <cuda_bf16.h>
+
 #include "mv_internal.h"
 #include "mv_kernels.h"
 #include "mv_select.cuh"
@@ -321,6 +323,36 @@ void launch_minmax(const float* x, int64_t n, float* out2, cudaStream_t s) {
     count_launch();
   }
   k_ord_to_float<<<1, 1, 0, s>>>(reinterpret_cast<unsigned int*>(out2));
+  count_launch();
+  MV_CHECK_CUDA(cudaGetLastError());
+}
+
+// SQ8 codes -> zero-padded BF16 rows (kp wide) for the tensor-core scan:
+// u8 codes (L2) as 0..255, s8 codes (IP) as -127..127, both exact in BF16;
+// norms (integer sums of squares) as FP32, exact below 2^24.
+__global__ void k_sq8_codes_to_bf16(const uint8_t* __restrict__ codes, int64_t n, int d, int dpad,
+                                    int kp, int symmetric, const uint32_t* __restrict__ norms,
+                                    __nv_bfloat16* __restrict__ out, float* __restrict__ fnorms) {
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  for (int j = lane; j < kp; j += 32) {
+    float v = 0.0f;
+    if (j < d) {
+      const uint8_t c = codes[row * dpad + j];
+      v = symmetric ? (float)(int8_t)c : (float)c;
+    }
+    out[row * kp + j] = __float2bfloat16_rn(v);
+  }
+  if (lane == 0 && fnorms) fnorms[row] = (float)norms[row];
+}
+
+void launch_sq8_codes_to_bf16(const uint8_t* codes, int64_t n, int d, int dpad, int kp,
+                              bool symmetric, const uint32_t* norms, __nv_bfloat16* out,
+                              float* fnorms, cudaStream_t s) {
+  if (n == 0) return;
+  k_sq8_codes_to_bf16<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(codes, n, d, dpad, kp,
+                                                              symmetric ? 1 : 0, norms, out, fnorms);
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());
 }

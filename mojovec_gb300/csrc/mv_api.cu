@@ -1212,10 +1212,103 @@ __global__ void k_keys_to_cand(const uint64_t* __restrict__ keys, int64_t n, int
   if (i < n) out[i] = keys[i] == ~0ull ? -1 : (int64_t)(uint32_t)keys[i];
 }
 
+// The tensor-core SQ8 scan is exact when every BF16 product and FP32
+// partial sum is an integer below 2^24: L2 (u8 codes) needs
+// 2 * d * 255^2 < 2^24 (d <= 129), IP (s8 codes) d * 127^2 < 2^24; the
+// GEMM takes d <= 256.
+bool sq8_tensor_exact(const mv_sq8* ix) {
+  if (umma_kpad(ix->d) > 256) return false;
+  if (ix->metric == MV_METRIC_L2) return 2ll * ix->d * 255 * 255 < (1ll << 24);
+  return (int64_t)ix->d * 127 * 127 < (1ll << 24);
+}
+
+void ensure_sq8_fast(mv_sq8* ix, cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(ix->fast_mu);
+  if (ix->fast_ready) return;
+  const int kp = umma_kpad(ix->d);
+  ix->codes_bf16.ensure((size_t)ix->ntotal * kp * 2);
+  ix->fnorms.ensure((size_t)ix->ntotal * 4);
+  launch_sq8_codes_to_bf16(ix->codes.as<uint8_t>(), ix->ntotal, ix->d, ix->dpad, kp,
+                           ix->metric != MV_METRIC_L2, ix->norms.as<uint32_t>(),
+                           ix->codes_bf16.as<__nv_bfloat16>(), ix->fnorms.as<float>(), s);
+  sync(s);
+  ix->fast_ready = true;
+}
+
+// Shortlist keys of the SQ8 scan (nq x R canonical (distance, row) keys,
+// the same set and order as sq8_scan_keys) from the tensor-core GEMM over
+// BF16 codes; queries flagged by the merge are rescanned with the exact
+// integer kernel.
+void sq8_tensor_keys(mv_sq8* ix, const float* d_x, int64_t nq, int R, const uint8_t* d_filter,
+                     uint64_t* out_keys, DevBuf& ws, cudaStream_t s) {
+  ensure_sq8_fast(ix, s);
+  const bool ip = ix->metric != MV_METRIC_L2;
+  const int64_t nb = ix->ntotal;
+  const int kp = umma_kpad(ix->d);
+  const int kseg = std::min(R + 8, UMMA_TOPK_MAX);  // a margin for distance ties
+  const int ncp = next_pow2(kseg);
+  int nseg = umma_topk_nseg(nq, nb, ix->d, kseg, ix->ctx->num_sms);
+  const int groups = umma_topk_groups(ix->d, kseg);
+  if (kseg < R + 8) {  // about 16 shortlist keys per segment keeps flags rare
+    const int64_t nct = (nb + 127) / 128;
+    nseg = (int)std::min<int64_t>(std::max<int64_t>(nseg, (R + 15) / 16 / groups + 1),
+                                  std::max<int64_t>(1, nct));
+  }
+  const int osegs = nseg * groups;
+  ws.ensure(ws_bytes((size_t)nq * ix->dpad, 1) + ws_bytes((size_t)nq, 4) +
+            ws_bytes((size_t)nq * kp, 2) + ws_bytes((size_t)nq * osegs * ncp, 8) +
+            ws_bytes((size_t)nq, 4));
+  Arena ar(ws);
+  uint8_t* qc = ar.take<uint8_t>((size_t)nq * ix->dpad);
+  uint32_t* qn = ar.take<uint32_t>((size_t)nq);
+  __nv_bfloat16* xq = ar.take<__nv_bfloat16>((size_t)nq * kp);
+  uint64_t* cand = ar.take<uint64_t>((size_t)nq * osegs * ncp);
+  int* flag = ar.take<int>((size_t)nq);
+  launch_sq8_encode(d_x, nq, ix->d, ix->dpad, ip ? 0.0f : ix->gmin, 1.0f / ix->scale, ip, qc, qn, s);
+  launch_sq8_codes_to_bf16(qc, nq, ix->d, ix->dpad, kp, ip, qn, xq, nullptr, s);
+  {
+    StageTimer t(ix->ctx, MV_STAGE_FLAT, s);
+    launch_umma_topk(xq, nq, ix->codes_bf16.as<__nv_bfloat16>(), nb, ix->d, ix->metric, nullptr,
+                     ix->fnorms.as<float>(), kseg, nseg, d_filter, nullptr, cand,
+                     ix->ctx->d_err.as<int>(), s);
+  }
+  {
+    StageTimer t(ix->ctx, MV_STAGE_SELECT, s);
+    launch_sq8_merge(cand, nq, osegs, ncp, kseg, R, qn, ip, ix->scale * ix->scale, out_keys, flag,
+                     s);
+  }
+  std::vector<int> h_flag((size_t)nq);
+  d2h(h_flag.data(), flag, sizeof(int) * nq, s);
+  sync(s);
+  std::vector<int64_t> rows;
+  for (int64_t i = 0; i < nq; ++i)
+    if (h_flag[(size_t)i]) rows.push_back(i);
+  if (rows.empty()) return;
+  const int64_t nr = (int64_t)rows.size();
+  DevBuf tmp, tws;
+  tmp.ensure(ws_bytes((size_t)nr * ix->d, 4) + ws_bytes((size_t)nr * R, 8));
+  Arena ta(tmp);
+  float* tx = ta.take<float>((size_t)nr * ix->d);
+  uint64_t* tk = ta.take<uint64_t>((size_t)nr * R);
+  for (int64_t i = 0; i < nr; ++i)
+    d2d(tx + i * ix->d, d_x + rows[(size_t)i] * ix->d, sizeof(float) * ix->d, s);
+  sq8_scan_keys(ix, tx, nr, R, d_filter, tk, tws, s);
+  for (int64_t i = 0; i < nr; ++i)
+    d2d(out_keys + rows[(size_t)i] * R, tk + i * R, sizeof(uint64_t) * R, s);
+  sync(s);
+  ix->fallback_rows += nr;
+}
+
 void sq8_search_impl(mv_sq8* ix, const float* d_x, int64_t nq, int k, int rerank_factor,
                      const uint8_t* d_filter, float* d_out, int64_t* d_lab, DevBuf& ws,
-                     cudaStream_t s) {
+                     cudaStream_t s, bool tensor = false) {
   if (nq == 0) return;
+  // The tensor-core scan returns the same keys as the integer scan; it is
+  // used when asked for and exact for this dimension and metric.
+  auto keys_of = [&](int R, uint64_t* out) {
+    if (tensor && sq8_tensor_exact(ix)) sq8_tensor_keys(ix, d_x, nq, R, d_filter, out, ws, s);
+    else sq8_scan_keys(ix, d_x, nq, R, d_filter, out, ws, s);
+  };
   const bool ip = ix->metric != MV_METRIC_L2;
   if (ix->ntotal == 0) {
     launch_fill(d_out, d_lab, nq * k, 0.0f, s);
@@ -1224,7 +1317,7 @@ void sq8_search_impl(mv_sq8* ix, const float* d_x, int64_t nq, int k, int rerank
   if (rerank_factor <= 0) {
     DevBuf keys;
     keys.ensure(sizeof(uint64_t) * nq * k);
-    sq8_scan_keys(ix, d_x, nq, k, d_filter, keys.as<uint64_t>(), ws, s);
+    keys_of(k, keys.as<uint64_t>());
     launch_keys_to_results(keys.as<uint64_t>(), nq, k, 0.0f, ip, d_out, d_lab, s);  // :595-602
     sync(s);
     return;
@@ -1234,7 +1327,7 @@ void sq8_search_impl(mv_sq8* ix, const float* d_x, int64_t nq, int k, int rerank
   keys.ensure(sizeof(uint64_t) * nq * kk);
   cand.ensure(sizeof(int64_t) * nq * kk);
   fk.ensure(sizeof(uint64_t) * nq * k);
-  sq8_scan_keys(ix, d_x, nq, kk, d_filter, keys.as<uint64_t>(), ws, s);
+  keys_of(kk, keys.as<uint64_t>());
   k_keys_to_cand<<<(unsigned)((nq * kk + 255) / 256), 256, 0, s>>>(keys.as<uint64_t>(), nq * kk,
                                                                   cand.as<int64_t>());
   count_launch();
@@ -1335,6 +1428,7 @@ int32_t mv_sq8_add(mv_sq8* ix, const float* x, int64_t n) {
                       ix->norms.as<uint32_t>() + ix->ntotal, s);
     sync(s);
     ix->ntotal = need;
+    ix->fast_ready = false;
   });
 }
 
@@ -1363,7 +1457,7 @@ int32_t mv_sq8_get_codes(mv_sq8* ix, uint8_t* codes, uint32_t* norms) {
 
 static int32_t sq8_search_host(mv_sq8* ix, const float* x, int64_t nq, int32_t k,
                                const uint8_t* filter, int rerank_factor, float* distances,
-                               int64_t* labels) {
+                               int64_t* labels, bool tensor = false) {
   if (!ix || (nq > 0 && (!x || !distances || !labels))) return MV_ERR_ARG;
   return guard(ix->ctx, [&] {
     check_search_args(nq, k);
@@ -1381,10 +1475,11 @@ static int32_t sq8_search_host(mv_sq8* ix, const float* x, int64_t nq, int32_t k
     uint8_t* df = ar.take<uint8_t>(fl + 1);
     h2d(dx, x, sizeof(float) * nq * ix->d, s);
     if (fl) h2d(df, filter, fl, s);
-    sq8_search_impl(ix, dx, nq, k, rerank_factor, fl ? df : nullptr, dd, dl, lease.slot->ws, s);
+    sq8_search_impl(ix, dx, nq, k, rerank_factor, fl ? df : nullptr, dd, dl, lease.slot->ws, s,
+                    tensor);
     d2h(distances, dd, sizeof(float) * nq * k, s);
     d2h(labels, dl, sizeof(int64_t) * nq * k, s);
-    sync(s);
+    check_kernel_errors(ix->ctx, s);
   });
 }
 
@@ -1397,6 +1492,35 @@ int32_t mv_sq8_search_rerank(mv_sq8* ix, const float* x, int64_t nq, int32_t k,
                              int32_t rerank_factor, float* distances, int64_t* labels) {
   if (rerank_factor < 1) return MV_ERR_ARG;
   return sq8_search_host(ix, x, nq, k, nullptr, rerank_factor, distances, labels);
+}
+
+int32_t mv_sq8_search_device(mv_sq8* ix, const float* d_x, int64_t nq, int32_t k,
+                             const uint8_t* d_filter, int32_t rerank_factor,
+                             const mv_search_params* params, float* d_distances,
+                             int64_t* d_labels, void* stream) {
+  if (!ix || rerank_factor < 0 || (nq > 0 && (!d_x || !d_distances || !d_labels)))
+    return MV_ERR_ARG;
+  const int form = params ? params->form : MV_FORM_PLAIN;
+  if (form != MV_FORM_PLAIN && form != MV_FORM_FAST) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    check_search_args(nq, k);
+    SlotLease lease(ix->ctx);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : lease.stream();
+    lease.use(s);
+    sq8_search_impl(ix, d_x, nq, k, rerank_factor, d_filter, d_distances, d_labels,
+                    lease.slot->ws, s, form == MV_FORM_FAST);
+    if (!stream) check_kernel_errors(ix->ctx, s);
+  });
+}
+
+int32_t mv_sq8_search_ex(mv_sq8* ix, const float* x, int64_t nq, int32_t k,
+                         const uint8_t* filter, int32_t rerank_factor,
+                         const mv_search_params* params, float* distances, int64_t* labels) {
+  if (rerank_factor < 0) return MV_ERR_ARG;
+  const int form = params ? params->form : MV_FORM_PLAIN;
+  if (form != MV_FORM_PLAIN && form != MV_FORM_FAST) return MV_ERR_ARG;
+  return sq8_search_host(ix, x, nq, k, filter, rerank_factor, distances, labels,
+                         form == MV_FORM_FAST);
 }
 
 // ---------------------------------------------------------------------------

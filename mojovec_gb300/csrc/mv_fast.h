@@ -59,6 +59,12 @@ void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s);
 // written (unsorted) for the rerank; otherwise the k smallest become the
 // results (L2 adds qnorm back). overflow[q] = 1 when a segment may have
 // dropped a shortlist key (only possible when kseg < R); may be null.
+// SQ8 tensor-core scan: per-segment (-e, row) keys -> the R smallest
+// canonical (SQ8 distance, row) keys per query (unsorted, KEY_NONE padded);
+// flag[q] = 1 when a dropped row could tie into the shortlist.
+void launch_sq8_merge(const uint64_t* cand, int64_t nq, int nseg, int ncp, int kseg, int R,
+                      const uint32_t* qnorm, bool ip, float scale_sq, uint64_t* out_keys, int* flag,
+                      cudaStream_t s);
 void launch_flat_merge(const uint64_t* cand, int64_t nq, int nseg, int ncp, int kseg, int R,
                        uint64_t* out_keys, int k, const float* qnorm, int metric, float fill_d,
                        float* out_d, int64_t* out_l, int* overflow, cudaStream_t s);

@@ -214,4 +214,10 @@ struct mv_sq8 {
   mv::DevBuf f32;    // capacity x d
   mv::DevBuf codes;  // capacity x dpad (zero padded)
   mv::DevBuf norms;  // capacity uint32
+  // Tensor-core scan state (built lazily): codes as BF16 rows, norms as FP32.
+  std::mutex fast_mu;
+  bool fast_ready = false;
+  mv::DevBuf codes_bf16;
+  mv::DevBuf fnorms;
+  int64_t fallback_rows = 0;  // queries rescanned because of a possible tie
 };

@@ -2,6 +2,7 @@
 // given stream and throws mv::Error on a launch failure.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -98,6 +99,10 @@ void launch_minmax(const float* x, int64_t n, float* out2, cudaStream_t s);
 void launch_sq8_encode(const float* x, int64_t n, int d, int dpad, float minimum, float inv_scale,
                        bool symmetric, uint8_t* codes, uint32_t* norms, cudaStream_t s);
 // Distances between query codes and base codes (sq8.mojo:62-79).
+// SQ8 codes as BF16 rows (kp wide) and FP32 norms, for the tensor-core scan.
+void launch_sq8_codes_to_bf16(const uint8_t* codes, int64_t n, int d, int dpad, int kp,
+                              bool symmetric, const uint32_t* norms, __nv_bfloat16* out,
+                              float* fnorms, cudaStream_t s);
 void launch_sq8_matrix(const uint8_t* qc, const uint32_t* qn, int64_t nq, const uint8_t* bc,
                        const uint32_t* bn, int64_t nb, int dpad, bool ip, float scale_sq,
                        float* D, int64_t ldd, cudaStream_t s);

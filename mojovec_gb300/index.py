@@ -282,14 +282,29 @@ class IndexFlatSQ8:
         check(_lib.load().mv_sq8_get_codes(self._h, _p(c), _p(nm)))
         return c[:n], nm[:n]
 
-    def search(self, x, k: int, filter=None):
+    def search(self, x, k: int, filter=None, form=None, rerank_factor: int = 0):
+        """IndexFlatSQ8.search; with rerank_factor > 0 the shortlist of
+        k * rerank_factor is reranked with exact FP32 distances. form=FORM_FAST
+        takes the shortlist from the tensor cores (same results)."""
         x = _f32(x, self.d)
         n = x.shape[0]
         dist = np.empty((n, k), np.float32)
         lab = np.empty((n, k), np.int64)
         flt = None if filter is None else np.ascontiguousarray(filter, dtype=np.uint8)
-        check(_lib.load().mv_sq8_search(self._h, _p(x), n, k, _p(flt), _p(dist), _p(lab)))
+        if form is None and rerank_factor == 0:
+            check(_lib.load().mv_sq8_search(self._h, _p(x), n, k, _p(flt), _p(dist), _p(lab)))
+        else:
+            p = _params(form)
+            check(_lib.load().mv_sq8_search_ex(self._h, _p(x), n, k, _p(flt), rerank_factor,
+                                               C.byref(p), _p(dist), _p(lab)))
         return dist, lab
+
+    def search_device(self, x_ptr: int, n: int, k: int, dist_ptr: int, lab_ptr: int,
+                      stream: int = 0, form=None, rerank_factor: int = 0, filter_ptr: int = 0):
+        p = _params(form)
+        check(_lib.load().mv_sq8_search_device(self._h, x_ptr, n, k, filter_ptr or None,
+                                               rerank_factor, C.byref(p), dist_ptr, lab_ptr,
+                                               stream or None))
 
     def search_rerank(self, x, k: int, rerank_factor: int = 2):
         x = _f32(x, self.d)
