@@ -623,6 +623,84 @@ def run_reference(args):
     }
 
 
+KM_METRIC = "k-means training throughput (1M x 96 cosine mixture, k 16384, 25 iterations)"
+
+
+def run_kmeans(args, rank, world):
+    """k-means training as the IVF coarse quantizer of the batched workload:
+    1,000,000 x 96 rows of a 4,096-component unit-normalised mixture (per-dim
+    std 0.05, rows L2-normalised), 16,384 centroids, 25 iterations. Both
+    forms run through the public C ABI (mv_kmeans_train_ex); the device time
+    of the training is taken from the context's stage events (inputs already
+    copied), e2e includes the host->device copy of the rows and the copy back
+    of centroids and assignments. The objective (sum of squared distances of
+    the final centroids) of the fast form is compared with the plain,
+    reference-exact form's."""
+    import torch
+
+    import mojovec_gb300 as mv
+    from mojovec_gb300 import synth
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    ctx = mv.Context(dev)
+    n, d, k, niter = args.km_n, 96, args.km_k, args.km_iter
+    x, _ = synth.cos_mixture(n, d=d, n_centers=4096, std=0.05)
+    out = {}
+    for name, form in (("plain", mv.FORM_PLAIN), ("fast", mv.FORM_FAST)):
+        km = mv.KMeans(d, k, niter=niter, ctx=ctx, form=form)
+        if name == "fast":  # warm-up of the fast path (kernels, smem limits)
+            mv.KMeans(d, k, niter=1, ctx=ctx, form=form).train(x[:200000])
+        clocks = ClockSampler(dev)
+        clocks.start()
+        ctx.profile(True)
+        l0 = ctx.kernel_launches()
+        t0 = time.perf_counter()
+        km.train(x)
+        e2e_s = time.perf_counter() - t0
+        st = ctx.stage_times()
+        ctx.profile(False)
+        out[name] = {"km": km, "dev_ms": st.get("coarse", (0.0, 0))[0], "e2e_s": e2e_s,
+                     "launches": ctx.kernel_launches() - l0, "clocks": clocks.stop()}
+    f, p = out["fast"], out["plain"]
+    rel = abs(f["km"].objective[-1] - p["km"].objective[-1]) / p["km"].objective[-1]
+    value = niter / (f["dev_ms"] / 1e3)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    tc_peak = float(peaks.get("bf16_tflops", 1900.0))
+    flops = 2.0 * n * k * d * (niter + 1)  # assignment GEMMs (niter steps + final objective)
+    achieved = flops / (f["dev_ms"] / 1e3) / 1e12
+    return {
+        "metric": KM_METRIC,
+        "value": round(value, 3),
+        "unit": "iterations/s",
+        "n_gpus": 1, "steps": niter, "warmup": 1,
+        "ms_per_step": round(f["dev_ms"] / niter, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16+f32+f64",
+        "data": "synthetic unit-normalised Gaussian mixture (seeded), not a public dataset",
+        "config": {
+            "workload": f"kmeans_{n}x{d}_k{k}_iter{niter}",
+            "form": "fast: tcgen05 BF16 candidates (4 per row) + FP32 recheck, FP64 ordered sums",
+            "objective_fast": f["km"].objective[-1],
+            "objective_plain": p["km"].objective[-1],
+            "objective_rel_diff": rel,
+            "plain_iterations_per_s": round(niter / (p["dev_ms"] / 1e3), 3),
+            "speedup_vs_plain": round(p["dev_ms"] / f["dev_ms"], 2),
+        },
+        "e2e": {"value": round(niter / f["e2e_s"], 3), "unit": "iterations/s",
+                "h2d_bytes_per_step": n * d * 4 // niter, "d2h_bytes_per_step": (k * d * 4 + n * 8) // niter},
+        "gpu_launches": int(f["launches"]),
+        "roofline": {"bound": "tensor", "kernel": "whole training (assignment GEMMs counted)",
+                     "achieved": round(achieved, 1), "peak": tc_peak, "unit": "TFLOP/s",
+                     "frac": round(achieved / tc_peak, 4), "traffic": None},
+        "clocks": f["clocks"],
+    }
+
+
 def run_reference_flat(args):
     """The oracle's IndexFlat search over all rows for a bounded query sample."""
     from oracle import oracle as orc
@@ -677,7 +755,10 @@ def main():
     ap.add_argument("--nq", type=int, default=NQ, help="queries per step")
     ap.add_argument("--cpu-sample", type=int, default=500)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="ivfpq", choices=["ivfpq", "flat", "sq8"])
+    ap.add_argument("--workload", default="ivfpq", choices=["ivfpq", "flat", "sq8", "kmeans"])
+    ap.add_argument("--km-n", type=int, default=1_000_000)
+    ap.add_argument("--km-k", type=int, default=16384)
+    ap.add_argument("--km-iter", type=int, default=25)
     ap.add_argument("--rerank-factor", type=int, default=2, help="sq8 workload: shortlist k * factor")
     ap.add_argument("--k", type=int, default=K, help="flat workload: results per query")
     ap.add_argument("--metric", default="l2", choices=["l2", "ip"], help="flat workload metric")
@@ -698,7 +779,12 @@ def main():
         import torch
 
         torch.distributed.init_process_group("nccl")
-    out = run_flat(args, rank, world) if args.workload in ("flat", "sq8") else run_gpu(args, rank, world)
+    if args.workload == "kmeans":
+        out = run_kmeans(args, rank, world)
+    elif args.workload in ("flat", "sq8"):
+        out = run_flat(args, rank, world)
+    else:
+        out = run_gpu(args, rank, world)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

@@ -217,6 +217,15 @@ int32_t mv_sq8_search_device(mv_sq8* index, const float* d_x, int64_t nq, int32_
  * assignments (may be NULL) receive the last iteration's clusters. */
 int32_t mv_kmeans_train(mv_ctx* ctx, const float* x, int64_t n, int32_t d, int32_t k,
                         int32_t niter, float* centroids, int64_t* assignments);
+/* k-means with a form. MV_FORM_PLAIN is mv_kmeans_train. MV_FORM_FAST assigns
+ * on the tensor cores (BF16 distances pick 4 candidate centroids per row, the
+ * reference's FP32 distance picks among them) and accumulates the centroid
+ * sums in FP64 in a fixed order (deterministic); same initial rows and empty-
+ * cluster rule; d <= 256. objective (niter + 1 doubles, may be NULL): the sum
+ * of squared distances at each assignment step and for the final centroids. */
+int32_t mv_kmeans_train_ex(mv_ctx* ctx, const float* x, int64_t n, int32_t d, int32_t k,
+                           int32_t niter, const mv_search_params* params, float* centroids,
+                           int64_t* assignments, double* objective);
 /* ProductQuantizer.train (quantization/pq.mojo:125-176): M subspace
  * k-means of 256 centroids each. out: M x 256 x (d/M). */
 int32_t mv_pq_train(mv_ctx* ctx, const float* x, int64_t n, int32_t d, int32_t M,

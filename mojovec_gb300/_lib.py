@@ -107,6 +107,7 @@ SIGNATURES = {
     "mv_sq8_search_ex": (_i32, [_vp, _vp, _i64, _i32, _vp, _i32, _vp, _vp, _vp]),
     "mv_sq8_search_device": (_i32, [_vp, _vp, _i64, _i32, _vp, _i32, _vp, _vp, _vp, _vp]),
     "mv_kmeans_train": (_i32, [_vp, _vp, _i64, _i32, _i32, _i32, _vp, _vp]),
+    "mv_kmeans_train_ex": (_i32, [_vp, _vp, _i64, _i32, _i32, _i32, _vp, _vp, _vp, _vp]),
     "mv_pq_train": (_i32, [_vp, _vp, _i64, _i32, _i32, _i32, _vp]),
     "mv_pq_encode": (_i32, [_vp, _vp, _i32, _i32, _vp, _i64, _vp]),
     "mv_pq_distance_tables": (_i32, [_vp, _vp, _i32, _i32, _vp, _i64, _i32, _vp]),

@@ -116,7 +116,8 @@ constexpr uint64_t KMEANS_SEED = 0x4D4F4A4F564543ull;
 // and k: x[b] at x + b*n*d, centroids[b] at cent + b*k*d, assign[b] at
 // assign + b*n.
 void kmeans_train_device(const float* x, int64_t n, int d, int k, int niter, int batch,
-                         float* cent, int32_t* assign, DevBuf& scratch, cudaStream_t s) {
+                         float* cent, int32_t* assign, DevBuf& scratch, cudaStream_t s,
+                         double* d_obj = nullptr) {
   if (n == 0 || k <= 0) return;
   MV_REQUIRE(n <= 0xffffffffll, MV_ERR_UNSUPPORTED, "k-means: too many rows");
   // :70-82 initial rows
@@ -131,22 +132,91 @@ void kmeans_train_device(const float* x, int64_t n, int d, int k, int niter, int
   }
   const size_t sums = (size_t)32 * k * d * batch;
   const size_t counts = (size_t)32 * k * batch;
-  scratch.ensure(ws_bytes(sums, 4) + ws_bytes(counts, 4) + ws_bytes(k, 8));
+  const bool obj = d_obj && batch == 1;
+  scratch.ensure(ws_bytes(sums, 4) + ws_bytes(counts, 4) + ws_bytes(k, 8) +
+                 (obj ? 2 * ws_bytes(n, 4) + ws_bytes(256, 8) : 0));
   Arena ar(scratch);
   float* local_sums = ar.take<float>(sums);
   int32_t* local_counts = ar.take<int32_t>(counts);
   int64_t* d_idx = ar.take<int64_t>(k);
+  float* mind = obj ? ar.take<float>(n) : nullptr;
+  int32_t* final_assign = obj ? ar.take<int32_t>(n) : nullptr;  // keeps `assign` of the last step
+  double* part = obj ? ar.take<double>(256) : nullptr;
   h2d(d_idx, idx.data(), sizeof(int64_t) * k, s);
   launch_gather_rows(x, d, d_idx, k, cent, batch, n * d, (int64_t)k * d, s);
   const int kind = d <= 4 ? KIND_L2_SHORT4 : KIND_L2_SIMD8;  // kmeans.mojo:131-139
   for (int it = 0; it < niter; ++it) {
-    launch_exact_argmin(kind, 1, x, n, d, cent, k, d, d, assign, nullptr, batch, n * d,
+    launch_exact_argmin(kind, 1, x, n, d, cent, k, d, d, assign, mind, batch, n * d,
                         (int64_t)k * d, n, s);
+    if (obj) launch_sum_fp64(mind, n, part, d_obj + it, s);
     launch_kmeans_accumulate(x, n, d, k, assign, local_sums, local_counts, batch, n * d, n,
                              (int64_t)32 * k * d, (int64_t)32 * k, s);
     launch_kmeans_update(x, n, d, k, local_sums, local_counts, sample_offset, it, cent, batch,
                          n * d, (int64_t)32 * k * d, (int64_t)32 * k, (int64_t)k * d, s);
   }
+  if (obj) {  // inertia of the final centroids
+    launch_exact_argmin(kind, 1, x, n, d, cent, k, d, d, final_assign, mind, 1, n * d,
+                        (int64_t)k * d, n, s);
+    launch_sum_fp64(mind, n, part, d_obj + niter, s);
+  }
+  sync(s);  // the host-side idx vector and scratch must outlive the kernels
+}
+
+// Fast k-means: BF16 tensor-core candidates (4 per row) with an exact FP32
+// recheck for the assignment, deterministic FP64 sums for the update. Same
+// initial rows and empty-cluster rule as the plain form. d_obj (niter + 1
+// doubles, may be null): the inertia at each assignment step and of the
+// final centroids.
+void kmeans_train_fast(const float* x, int64_t n, int d, int k, int niter, float* cent,
+                       int32_t* assign, DevBuf& scratch, mv_ctx* ctx, cudaStream_t s,
+                       double* d_obj) {
+  if (n == 0 || k <= 0) return;
+  MV_REQUIRE(n <= 0x7fffffffll, MV_ERR_UNSUPPORTED, "fast k-means: too many rows");
+  MV_REQUIRE(umma_kpad(d) <= 256, MV_ERR_UNSUPPORTED, "fast k-means supports d <= 256");
+  Philox gen(KMEANS_SEED);  // kmeans.mojo:70-82, as in the plain form
+  uint32_t words[4];
+  gen.step(words);
+  const int64_t sample_offset = (int64_t)(words[0] % (uint32_t)n);
+  std::vector<int64_t> idx(k);
+  for (int i = 0; i < k; ++i) {
+    if (i != 0 && i % 4 == 0) gen.step(words);
+    idx[i] = (int64_t)(words[i % 4] % (uint32_t)n);
+  }
+  const int kp = umma_kpad(d);
+  const int kc = std::min(4, k);  // BF16 candidates per row
+  const int ncp = next_pow2(kc);
+  const int nseg = umma_topk_nseg(n, k, d, kc, ctx->num_sms);
+  const int osegs = nseg * umma_topk_groups(d, kc);
+  scratch.ensure(ws_bytes((size_t)n * kp, 2) + ws_bytes((size_t)k * kp, 2) + ws_bytes(k, 4) +
+                 ws_bytes((size_t)n * osegs * ncp, 8) + ws_bytes(n, 8) + ws_bytes(n, 4) +
+                 ws_bytes(k, 8) + ws_bytes(256, 8) + ws_bytes(km_sort_scratch_bytes(n, k), 1) +
+                 ws_bytes(n, 4));
+  Arena ar(scratch);
+  __nv_bfloat16* xb = ar.take<__nv_bfloat16>((size_t)n * kp);
+  __nv_bfloat16* cb = ar.take<__nv_bfloat16>((size_t)k * kp);
+  float* cn = ar.take<float>(k);
+  uint64_t* cand = ar.take<uint64_t>((size_t)n * osegs * ncp);
+  uint64_t* gthr = osegs > 1 ? ar.take<uint64_t>(n) : nullptr;
+  float* mind = ar.take<float>(n);
+  int64_t* d_idx = ar.take<int64_t>(k);
+  double* part = ar.take<double>(256);
+  void* sort_ws = ar.take<uint8_t>(km_sort_scratch_bytes(n, k));
+  int32_t* final_assign = ar.take<int32_t>(n);  // keeps `assign` of the last step
+  h2d(d_idx, idx.data(), sizeof(int64_t) * k, s);
+  launch_gather_rows(x, d, d_idx, k, cent, 1, n * d, (int64_t)k * d, s);
+  launch_to_bf16(x, n, d, xb, nullptr, s);
+  auto assign_step = [&](int32_t* out, double* obj_slot) {
+    launch_to_bf16(cent, k, d, cb, cn, s);
+    launch_umma_topk(xb, n, cb, k, d, MV_METRIC_L2, nullptr, cn, kc, nseg, nullptr, gthr, cand,
+                     ctx->d_err.as<int>(), s);
+    launch_km_recheck(x, n, d, cent, k, cand, osegs * ncp, out, mind, s);
+    if (obj_slot) launch_sum_fp64(mind, n, part, obj_slot, s);
+  };
+  for (int it = 0; it < niter; ++it) {
+    assign_step(assign, d_obj ? d_obj + it : nullptr);
+    launch_km_update_fp64(x, n, d, k, assign, sample_offset, it, cent, sort_ws, s);
+  }
+  if (d_obj) assign_step(final_assign, d_obj + niter);
   sync(s);  // the host-side idx vector and scratch must outlive the kernels
 }
 
@@ -1549,6 +1619,46 @@ int32_t mv_kmeans_train(mv_ctx* ctx, const float* x, int64_t n, int32_t d, int32
       sync(s);
     }
     sync(s);
+  });
+}
+
+int32_t mv_kmeans_train_ex(mv_ctx* ctx, const float* x, int64_t n, int32_t d, int32_t k,
+                           int32_t niter, const mv_search_params* params, float* centroids,
+                           int64_t* assignments, double* objective) {
+  if (!ctx || n < 0 || (n > 0 && (!x || !centroids)) || d <= 0 || k <= 0 || niter < 0)
+    return MV_ERR_ARG;
+  const int form = params ? params->form : MV_FORM_PLAIN;
+  if (form != MV_FORM_PLAIN && form != MV_FORM_FAST) return MV_ERR_ARG;
+  return guard(ctx, [&] {
+    if (n == 0) return;  // kmeans.mojo:62
+    SlotLease lease(ctx);
+    cudaStream_t s = lease.stream();
+    DevBuf dx, dc, da, scratch, dobj;
+    dx.ensure(sizeof(float) * n * d);
+    dc.ensure(sizeof(float) * k * d);
+    da.ensure(sizeof(int32_t) * n);
+    if (objective) dobj.ensure(sizeof(double) * (niter + 1));
+    h2d(dx.p, x, sizeof(float) * n * d, s);
+    double* d_obj = objective ? dobj.as<double>() : nullptr;
+    {
+      StageTimer t(ctx, MV_STAGE_COARSE, s);
+      if (form == MV_FORM_FAST)
+        kmeans_train_fast(dx.as<float>(), n, d, k, niter, dc.as<float>(), da.as<int32_t>(),
+                          scratch, ctx, s, d_obj);
+      else
+        kmeans_train_device(dx.as<float>(), n, d, k, niter, 1, dc.as<float>(), da.as<int32_t>(),
+                            scratch, s, d_obj);
+    }
+    d2h(centroids, dc.p, sizeof(float) * k * d, s);
+    if (objective) d2h(objective, d_obj, sizeof(double) * (niter + 1), s);
+    if (assignments) {
+      DevBuf a64;
+      a64.ensure(sizeof(int64_t) * n);
+      launch_i32_to_i64(da.as<int32_t>(), n, a64.as<int64_t>(), s);
+      d2h(assignments, a64.p, sizeof(int64_t) * n, s);
+      sync(s);
+    }
+    check_kernel_errors(ctx, s);
   });
 }
 

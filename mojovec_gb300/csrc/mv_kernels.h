@@ -99,6 +99,20 @@ void launch_minmax(const float* x, int64_t n, float* out2, cudaStream_t s);
 void launch_sq8_encode(const float* x, int64_t n, int d, int dpad, float minimum, float inv_scale,
                        bool symmetric, uint8_t* codes, uint32_t* norms, cudaStream_t s);
 // Distances between query codes and base codes (sq8.mojo:62-79).
+// ---- fast k-means (k_kmeans_fast.cu) ---------------------------------------
+// Exact FP32 pick among ncand candidate keys per row (reference distance and
+// tie rule): assign[r], mind[r].
+void launch_km_recheck(const float* x, int64_t n, int d, const float* cent, int k,
+                       const uint64_t* cand, int ncand, int32_t* assign, float* mind,
+                       cudaStream_t s);
+size_t km_sort_scratch_bytes(int64_t n, int k);
+// Deterministic FP64 centroid update (stable counting sort + ordered sums).
+void launch_km_update_fp64(const float* x, int64_t n, int d, int k, const int32_t* assign,
+                           int64_t sample_offset, int it, float* cent, void* scratch,
+                           cudaStream_t s);
+// out = sum of v in FP64 in a fixed order (part256: 256 doubles of scratch).
+void launch_sum_fp64(const float* v, int64_t n, double* part256, double* out, cudaStream_t s);
+
 // SQ8 codes as BF16 rows (kp wide) and FP32 norms, for the tensor-core scan.
 void launch_sq8_codes_to_bf16(const uint8_t* codes, int64_t n, int d, int dpad, int kp,
                               bool symmetric, const uint32_t* norms, __nv_bfloat16* out,

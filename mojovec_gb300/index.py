@@ -317,20 +317,28 @@ class IndexFlatSQ8:
 
 
 class KMeans:
-    """KMeans(d, k, niter) (clustering/kmeans.mojo:8), plain exact form."""
+    """KMeans(d, k, niter) (clustering/kmeans.mojo:8). form=None/FORM_PLAIN is
+    the reference-exact form; FORM_FAST assigns on the tensor cores with an
+    exact FP32 recheck and sums in FP64. After train, `objective` holds the
+    sum of squared distances at each assignment step and for the final
+    centroids (niter + 1 values)."""
 
-    def __init__(self, d: int, k: int, niter: int = 15, ctx: Context | None = None):
+    def __init__(self, d: int, k: int, niter: int = 15, ctx: Context | None = None, form=None):
         self.ctx = ctx or Context.default()
-        self.d, self.k, self.niter = d, k, niter
+        self.d, self.k, self.niter, self.form = d, k, niter, form
         self.centroids = np.zeros((k, d), np.float32)
         self.assignments = np.zeros(0, np.int64)
+        self.objective = np.zeros(0, np.float64)
 
     def train(self, x):
         x = _f32(x, self.d)
         n = x.shape[0]
         self.assignments = np.zeros(n, np.int64)
-        check(_lib.load().mv_kmeans_train(self.ctx.handle, _p(x), n, self.d, self.k, self.niter,
-                                          _p(self.centroids), _p(self.assignments)))
+        self.objective = np.zeros(self.niter + 1, np.float64)
+        p = _params(self.form)
+        check(_lib.load().mv_kmeans_train_ex(self.ctx.handle, _p(x), n, self.d, self.k,
+                                             self.niter, C.byref(p), _p(self.centroids),
+                                             _p(self.assignments), _p(self.objective)))
         return self.centroids
 
 
