@@ -54,6 +54,7 @@ typedef struct mv_ctx mv_ctx;
 typedef struct mv_ivfpq mv_ivfpq;
 typedef struct mv_flat mv_flat;
 typedef struct mv_sq8 mv_sq8;
+typedef struct mv_ivfpq_plan mv_ivfpq_plan;
 
 /* Search options for the IVF-PQ and Flat searches. Zero-initialised means
  * the plain form with the index's own nprobe. */
@@ -117,6 +118,10 @@ int32_t mv_ivfpq_get_codebooks(mv_ivfpq* index, float* centroids, float* pq);
  * (niter_pq, reference 15) on the GPU in the plain exact form. */
 int32_t mv_ivfpq_train(mv_ivfpq* index, const float* x, int64_t n, int32_t niter_coarse,
                        int32_t niter_pq);
+/* Train with a form: MV_FORM_FAST runs the coarse k-means in its fast form
+ * (tensor-core assignment with FP32 recheck, FP64 sums; d <= 256). */
+int32_t mv_ivfpq_train_ex(mv_ivfpq* index, const float* x, int64_t n, int32_t niter_coarse,
+                          int32_t niter_pq, const mv_search_params* params);
 /* IndexIVFPQ.add (index_ivf_pq.mojo:138-148): sequential ids from ntotal. */
 int32_t mv_ivfpq_add(mv_ivfpq* index, const float* x, int64_t n);
 /* IndexIVFPQ.add_with_ids (index_ivf_pq.mojo:150-213). */
@@ -157,6 +162,40 @@ int32_t mv_ivfpq_search_device(mv_ivfpq* index, const float* d_x, int64_t nq, in
 int32_t mv_ivfpq_search_noalloc(mv_ivfpq* index, const float* d_x, int64_t nq, int32_t k,
                                 int32_t nprobe, float* d_distances, int64_t* d_labels,
                                 void* stream);
+
+/* ---- Batched IVF-PQ (fast form): per-query nprobe and k ---------------- */
+/* One call over queries with their own nprobe (<= nprobe_max) and k
+ * (<= kmax). Results: nq rows of kmax slots; slots past a query's k read
+ * 1e38 / -1 (index_ivf_pq.mojo:284-286). */
+int32_t mv_ivfpq_search_batch(mv_ivfpq* index, const float* x, int64_t nq, const int32_t* nprobe,
+                              const int32_t* k, int32_t kmax, const mv_search_params* params,
+                              float* distances, int64_t* labels);
+/* A plan owns device buffers for up to max_nq queries of a batched search
+ * and replays it as a CUDA graph (captured once per batch size). The scan
+ * runs as a persistent grid that takes queries from a counter in order of
+ * decreasing nprobe. */
+int32_t mv_ivfpq_plan_create(mv_ivfpq* index, int64_t max_nq, int32_t nprobe_max, int32_t kmax,
+                             const mv_search_params* params, mv_ivfpq_plan** out);
+int32_t mv_ivfpq_plan_destroy(mv_ivfpq_plan* plan);
+/* Device pointers of the plan's buffers (any may be NULL): queries
+ * (max_nq x d), per-query nprobe, k and scan order, results (max_nq x kmax). */
+int32_t mv_ivfpq_plan_buffers(mv_ivfpq_plan* plan, float** d_x, int32_t** d_nprobe, int32_t** d_k,
+                              int32_t** d_order, float** d_distances, int64_t** d_labels);
+/* Copies host per-query nprobe / k (and x when not NULL) into the plan and
+ * sets the scan order. */
+int32_t mv_ivfpq_plan_set_queries(mv_ivfpq_plan* plan, const float* x, int64_t nq,
+                                  const int32_t* nprobe, const int32_t* k);
+/* Tuner: times the plan's launch choices on its current batch and keeps the
+ * fastest. config (may be NULL): [coarse by distance matrix (1) or fused
+ * top-k GEMM (0), scan threads per CTA, scan CTAs per SM (0 = one per
+ * query)]; best_ms: the chosen configuration's time. */
+int32_t mv_ivfpq_plan_tune(mv_ivfpq_plan* plan, int64_t nq, int32_t* config, float* best_ms);
+/* Runs the plan on its first nq queries; use_graph != 0 replays a CUDA graph.
+ * stream NULL: the plan's own stream, and the call returns when done. */
+int32_t mv_ivfpq_plan_run(mv_ivfpq_plan* plan, int64_t nq, int32_t use_graph, void* stream);
+/* Copies the first nq result rows (nq x kmax) to host memory after all
+ * pending work on the device. */
+int32_t mv_ivfpq_plan_results(mv_ivfpq_plan* plan, int64_t nq, float* distances, int64_t* labels);
 
 /* ---- Flat index: replaces IndexFlat (index/index_flat.mojo:117-330) ---- */
 int32_t mv_flat_create(mv_ctx* ctx, int32_t d, int32_t metric, mv_flat** out);

@@ -20,6 +20,7 @@ from .index import (  # noqa: F401
     IndexFlat,
     IndexFlatSQ8,
     IndexIVFPQ,
+    IVFPQBatchPlan,
     KMeans,
     distance_matrix,
     ProductQuantizer,

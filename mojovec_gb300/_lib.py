@@ -84,6 +84,7 @@ SIGNATURES = {
     "mv_ivfpq_set_codebooks": (_i32, [_vp, _vp, _vp]),
     "mv_ivfpq_get_codebooks": (_i32, [_vp, _vp, _vp]),
     "mv_ivfpq_train": (_i32, [_vp, _vp, _i64, _i32, _i32]),
+    "mv_ivfpq_train_ex": (_i32, [_vp, _vp, _i64, _i32, _i32, _vp]),
     "mv_ivfpq_add": (_i32, [_vp, _vp, _i64]),
     "mv_ivfpq_add_with_ids": (_i32, [_vp, _vp, _vp, _i64]),
     "mv_ivfpq_get_lists": (_i32, [_vp, _vp, _vp, _vp]),
@@ -107,6 +108,14 @@ SIGNATURES = {
     "mv_sq8_search_ex": (_i32, [_vp, _vp, _i64, _i32, _vp, _i32, _vp, _vp, _vp]),
     "mv_sq8_search_device": (_i32, [_vp, _vp, _i64, _i32, _vp, _i32, _vp, _vp, _vp, _vp]),
     "mv_kmeans_train": (_i32, [_vp, _vp, _i64, _i32, _i32, _i32, _vp, _vp]),
+    "mv_ivfpq_search_batch": (_i32, [_vp, _vp, _i64, _vp, _vp, _i32, _vp, _vp, _vp]),
+    "mv_ivfpq_plan_create": (_i32, [_vp, _i64, _i32, _i32, _vp, _vp]),
+    "mv_ivfpq_plan_destroy": (_i32, [_vp]),
+    "mv_ivfpq_plan_buffers": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "mv_ivfpq_plan_set_queries": (_i32, [_vp, _vp, _i64, _vp, _vp]),
+    "mv_ivfpq_plan_tune": (_i32, [_vp, _i64, _vp, _vp]),
+    "mv_ivfpq_plan_run": (_i32, [_vp, _i64, _i32, _vp]),
+    "mv_ivfpq_plan_results": (_i32, [_vp, _i64, _vp, _vp]),
     "mv_kmeans_train_ex": (_i32, [_vp, _vp, _i64, _i32, _i32, _i32, _vp, _vp, _vp, _vp]),
     "mv_pq_train": (_i32, [_vp, _vp, _i64, _i32, _i32, _i32, _vp]),
     "mv_pq_encode": (_i32, [_vp, _vp, _i32, _i32, _vp, _i64, _vp]),

@@ -197,10 +197,11 @@ __global__ void __launch_bounds__(FT)
 // Per-query table lut[m][k] = scale * <q_m, C[m][k]>: warp w builds
 // subspaces w, w + 8, ...; each lane owns 8 codewords and keeps q_m in
 // registers, with the codeword rows read as float4 when dsub is 4 or 8.
+template <int NT>
 __device__ __forceinline__ void build_lut(float* lut, const float* qv, const float* pq, int M,
                                           int dsub, float scale) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int mm = warp; mm < M; mm += FT / 32) {
+  for (int mm = warp; mm < M; mm += NT / 32) {
     const float* cm = pq + (int64_t)mm * 256 * dsub;
     const float* xm = qv + mm * dsub;
     if (dsub == 8) {
@@ -256,7 +257,9 @@ __device__ __forceinline__ void build_lut(float* lut, const float* qv, const flo
 // would overflow the staging area, and once at the end, a radix select keeps
 // the R smallest. The shortlist is written unsorted (the rerank orders it),
 // or sorted when it is the final answer.
-__global__ void __launch_bounds__(FT) k_ivfpq_scan_fast(FastScanArgs a) {
+template <int NT>
+__global__ void __launch_bounds__(NT) k_ivfpq_scan_fast(FastScanArgs a) {
+  constexpr int FT = NT;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int M = a.M, d = a.d, dsub = d / M;
   float* lut = reinterpret_cast<float*>(smraw);
@@ -270,17 +273,33 @@ __global__ void __launch_bounds__(FT) k_ivfpq_scan_fast(FastScanArgs a) {
   float* pterm = reinterpret_cast<float*>(pbeg + a.nprobe + 1);
   __shared__ RadixScratch rs;
   __shared__ int s_fill;
-  const int64_t row = blockIdx.x;
+  __shared__ int s_q;
   const int lane = threadIdx.x & 31;
+  // One query per CTA, or (with a.counter) a persistent CTA that takes
+  // queries from a global counter in a.order until none are left.
+  for (int iter = 0;; ++iter) {
+  int qi;
+  if (a.counter) {
+    __syncthreads();  // the previous query is done with shared memory
+    if (threadIdx.x == 0) s_q = atomicAdd(a.counter, 1);
+    __syncthreads();
+    qi = s_q;
+    if (qi >= a.nq) break;
+  } else {
+    if (iter > 0) break;
+    qi = blockIdx.x;
+  }
+  const int64_t row = a.order ? a.order[qi] : qi;
+  const int nprobe = a.nprobe_q ? min(max(a.nprobe_q[row], 1), a.nprobe) : a.nprobe;
   if (threadIdx.x == 0) s_fill = 0;
   for (int j = threadIdx.x; j < d; j += FT) qv[j] = a.q[row * d + j];
   // probe table: offsets, lengths -> prefix sums (warp 0)
   if (threadIdx.x < 32) {
     int carry = 0;
-    for (int p0 = 0; p0 < a.nprobe; p0 += 32) {
+    for (int p0 = 0; p0 < nprobe; p0 += 32) {
       const int p = p0 + lane;
       int len = 0;
-      if (p < a.nprobe) {
+      if (p < nprobe) {
         int list = a.probes[row * a.nprobe + p];
         if (list >= a.nlist) {
           atomicExch(a.err, 103);
@@ -299,16 +318,16 @@ __global__ void __launch_bounds__(FT) k_ivfpq_scan_fast(FastScanArgs a) {
         const int t = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += t;
       }
-      if (p < a.nprobe) pbeg[p] = carry + incl - len;
+      if (p < nprobe) pbeg[p] = carry + incl - len;
       carry += __shfl_sync(0xffffffffu, incl, 31);
     }
-    if (lane == 0) pbeg[a.nprobe] = carry;
+    if (lane == 0) pbeg[nprobe] = carry;
   }
   __syncthreads();
   const float scale = a.metric == MV_METRIC_L2 ? -2.0f : -1.0f;
-  build_lut(lut, qv, a.pq, M, dsub, scale);
+  build_lut<NT>(lut, qv, a.pq, M, dsub, scale);
   __syncthreads();
-  const int total = pbeg[a.nprobe];
+  const int total = pbeg[nprobe];
   const int chunk = a.cap - a.R;
   int m = 0;
   int p = 0;  // per-thread probe cursor (candidate indices only grow)
@@ -401,6 +420,7 @@ __global__ void __launch_bounds__(FT) k_ivfpq_scan_fast(FastScanArgs a) {
     block_bitonic_sort(outb, a.Rp);
   }
   for (int i = threadIdx.x; i < a.R; i += FT) a.out_keys[row * a.R + i] = i < r ? outb[i] : KEY_NONE;
+  }  // queries
 }
 
 // Exact FP32 rerank of the shortlist against the raw rows (CSR order), one
@@ -486,11 +506,12 @@ __global__ void __launch_bounds__(FT) k_rerank_fast(RerankArgs a) {
   for (int j = r + threadIdx.x; j < a.kp; j += FT) outb[j] = KEY_NONE;
   __syncthreads();
   block_bitonic_sort(outb, a.kp);
+  const int kq = a.k_q ? min(max(a.k_q[row], 0), a.k) : a.k;
   for (int i = threadIdx.x; i < a.k; i += FT) {
     const uint64_t key = outb[i];
     float dd = a.fill_d;
     int64_t ll = -1;
-    if (key < KEY_NONE - (uint64_t)a.R) {  // padding keys are the top R values
+    if (i < kq && key < KEY_NONE - (uint64_t)a.R) {  // padding keys are the top R values
       dd = key_dist(key);
       if (a.metric != MV_METRIC_L2) dd = -dd;
       ll = (int64_t)key_id(key);
@@ -503,13 +524,14 @@ __global__ void __launch_bounds__(FT) k_rerank_fast(RerankArgs a) {
 // Shortlist without rerank: the first k keys (already sorted) -> results.
 __global__ void k_short_to_results(const uint64_t* __restrict__ keys, int64_t nq, int R, int k,
                                    const uint32_t* __restrict__ ids, int metric,
-                                   float* __restrict__ out_d, int64_t* __restrict__ out_l) {
+                                   const int32_t* __restrict__ k_q, float* __restrict__ out_d,
+                                   int64_t* __restrict__ out_l) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nq * k) return;
   const int64_t r = i / k;
   const int j = (int)(i - r * k);
   const uint64_t key = keys[r * R + j];
-  if (key == KEY_NONE) {
+  if (key == KEY_NONE || (k_q && j >= k_q[r])) {
     out_d[i] = 1e38f;
     out_l[i] = -1;
   } else {
@@ -563,16 +585,29 @@ void launch_coarse_from_keys(const uint64_t* cand, int64_t nq, int ncand, const 
 
 int fast_scan_cap(int R) { return std::max(2048, 2 * R + 1024); }
 
-void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s) {
+size_t fast_scan_smem(const FastScanArgs& a) {
+  return (((size_t)(a.M * 256 + a.d) * 4 + 15) & ~size_t(15)) + (size_t)next_pow2(a.R) * 8 +
+         (size_t)fast_scan_cap(a.R) * 8 + (size_t)a.nprobe * 8 + (size_t)(a.nprobe + 1) * 4 +
+         (size_t)a.nprobe * 4;
+}
+
+// Threads per CTA nt (128, 256 or 512); grid: one CTA per query, or with
+// a.counter a persistent grid of `persistent_ctas` CTAs.
+void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s, int nt, int persistent_ctas) {
   if (a.nq == 0) return;
   a.cap = fast_scan_cap(a.R);
   a.Rp = next_pow2(a.R);
-  const size_t smem = (((size_t)(a.M * 256 + a.d) * 4 + 15) & ~size_t(15)) +
-                      (size_t)a.Rp * 8 + (size_t)a.cap * 8 + (size_t)a.nprobe * 8 +
-                      (size_t)(a.nprobe + 1) * 4 + (size_t)a.nprobe * 4;
+  const size_t smem = fast_scan_smem(a);
   MV_REQUIRE(smem <= 220 * 1024, MV_ERR_UNSUPPORTED, "fast IVF-PQ scan: M, d or shortlist too large");
-  smem_attr(k_ivfpq_scan_fast, smem);
-  k_ivfpq_scan_fast<<<(unsigned)a.nq, FT, smem, s>>>(a);
+  MV_REQUIRE(!a.counter || persistent_ctas > 0, MV_ERR_INTERNAL, "persistent scan without a grid");
+  const unsigned grid = a.counter ? (unsigned)std::min<int64_t>(persistent_ctas, a.nq) : (unsigned)a.nq;
+  auto go = [&](auto kernel, int threads) {
+    smem_attr(kernel, smem);
+    kernel<<<grid, threads, smem, s>>>(a);
+  };
+  if (nt == 128) go(k_ivfpq_scan_fast<128>, 128);
+  else if (nt == 512) go(k_ivfpq_scan_fast<512>, 512);
+  else go(k_ivfpq_scan_fast<256>, 256);
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());
 }
@@ -589,11 +624,12 @@ void launch_rerank_fast(RerankArgs a, cudaStream_t s) {
 }
 
 void launch_short_to_results(const uint64_t* keys, int64_t nq, int R, int k, const uint32_t* ids,
-                             int metric, float* out_d, int64_t* out_l, cudaStream_t s) {
+                             int metric, float* out_d, int64_t* out_l, cudaStream_t s,
+                             const int32_t* k_q) {
   const int64_t total = nq * k;
   if (total == 0) return;
   k_short_to_results<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(keys, nq, R, k, ids, metric,
-                                                                     out_d, out_l);
+                                                                     k_q, out_d, out_l);
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());
 }

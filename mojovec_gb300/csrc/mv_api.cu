@@ -10,6 +10,7 @@
 #include <limits>
 #include <memory>
 #include <new>
+#include <map>
 #include <unordered_map>
 
 #include "mv_fast.h"
@@ -498,16 +499,22 @@ void ensure_fast(mv_ivfpq* ix, cudaStream_t s) {
 }
 
 // Fast-form IVF-PQ search (BF16 coarse GEMM + exact FP32 recheck, one LUT
-// per query with precomputed per-vector terms, exact FP32 rerank).
+// per query with precomputed per-vector terms, exact FP32 rerank). With
+// `batch`, queries carry their own nprobe (<= nprobe) and k (<= k; each
+// result row keeps k slots), the scan runs as a persistent grid that takes
+// queries in batch->order from a counter, and the launch shapes come from
+// batch (the tuner's choice). The whole batch is one chunk then, and the
+// call makes no allocation, host read or synchronisation once the
+// workspace is sized, so it can be captured in a CUDA graph.
 void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int nprobe,
                        const mv_search_params* p, float* d_out, int64_t* d_lab, DevBuf& ws,
-                       cudaStream_t s) {
+                       cudaStream_t s, const FastBatch* batch = nullptr) {
   if (nq == 0) return;
   if (!ix->trained || ix->ntotal == 0) {
     launch_fill(d_out, d_lab, nq * k, 1e38f, s);
     return;
   }
-  ensure_fast(ix, s);
+  if (!batch) ensure_fast(ix, s);
   const bool fp32_coarse = p && p->coarse_fp32;
   const int R = std::max(k, (p && p->rerank > 0) ? (int)p->rerank : k);
   MV_REQUIRE(R <= 4096, MV_ERR_ARG, "rerank depth must be at most 4096");
@@ -516,9 +523,13 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
   const int kp = umma_kpad(ix->d);
   // Fused coarse (tensor-core GEMM keeping each query's best nc lists) when
   // nc fits the epilogue's per-row list; otherwise the distance matrix path.
-  const bool fused = !fp32_coarse && nc <= 64;
+  const bool fused = !fp32_coarse && nc <= 64 && !(batch && batch->coarse_matrix);
   int64_t qb = std::max<int64_t>(128, (int64_t)(1536ll * 1024 * 1024 / ((int64_t)ix->nlist * 4)));
   qb = std::min<int64_t>({qb, nq, 65535ll * 64});
+  if (batch) {
+    MV_REQUIRE(nq <= 65535ll * 64, MV_ERR_UNSUPPORTED, "batch too large for one launch");
+    qb = nq;
+  }
   const int nseg = fused ? umma_topk_nseg(qb, ix->nlist, ix->d, nc, ix->ctx->num_sms) : 1;
   const int ncand = nseg * (fused ? umma_topk_groups(ix->d, nc) : 1) * next_pow2(nc);
   ws.ensure(ws_bytes((size_t)qb * kp, 2) +
@@ -584,7 +595,16 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
       a.nlist = ix->nlist;
       a.ntotal = ix->h_off[ix->nlist];
       a.err = ix->ctx->d_err.as<int>();
-      launch_ivfpq_scan_fast(a, s);
+      if (batch) {
+        a.nprobe_q = batch->nprobe_q;
+        a.order = batch->order;
+        a.counter = batch->scan_ctas_per_sm > 0 ? batch->counter : nullptr;
+        if (a.counter) MV_CHECK_CUDA(cudaMemsetAsync(a.counter, 0, sizeof(int), s));
+        launch_ivfpq_scan_fast(a, s, batch->scan_threads,
+                               batch->scan_ctas_per_sm * ix->ctx->num_sms);
+      } else {
+        launch_ivfpq_scan_fast(a, s);
+      }
     }
     if (p && p->rerank > 0) {
       StageTimer t(ix->ctx, MV_STAGE_RERANK, s);
@@ -602,10 +622,11 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
       r.out_l = d_lab + q0 * k;
       r.ntotal = ix->h_off[ix->nlist];
       r.err = ix->ctx->d_err.as<int>();
+      r.k_q = batch ? batch->k_q : nullptr;
       launch_rerank_fast(r, s);
     } else {
       launch_short_to_results(skeys, nb, R, k, ix->d_ids.as<uint32_t>(), ix->metric,
-                              d_out + q0 * k, d_lab + q0 * k, s);
+                              d_out + q0 * k, d_lab + q0 * k, s, batch ? batch->k_q : nullptr);
     }
   }
 }
@@ -848,9 +869,11 @@ int32_t mv_ivfpq_get_codebooks(mv_ivfpq* ix, float* centroids, float* pq) {
   });
 }
 
-int32_t mv_ivfpq_train(mv_ivfpq* ix, const float* x, int64_t n, int32_t niter_coarse,
-                       int32_t niter_pq) {
+int32_t mv_ivfpq_train_ex(mv_ivfpq* ix, const float* x, int64_t n, int32_t niter_coarse,
+                          int32_t niter_pq, const mv_search_params* params) {
   if (!ix || (!x && n > 0)) return MV_ERR_ARG;
+  const int form = params ? params->form : MV_FORM_PLAIN;
+  if (form != MV_FORM_PLAIN && form != MV_FORM_FAST) return MV_ERR_ARG;
   return guard(ix->ctx, [&] {
     std::lock_guard<std::mutex> lk(ix->mu);
     if (ix->trained) return;  // :93
@@ -864,8 +887,12 @@ int32_t mv_ivfpq_train(mv_ivfpq* ix, const float* x, int64_t n, int32_t niter_co
     h2d(dx.p, x, sizeof(float) * n * d, s);
     // 1. coarse k-means (:98-103)
     assign.ensure(sizeof(int32_t) * n);
-    kmeans_train_device(dx.as<float>(), n, d, ix->nlist, niter_coarse, 1, ix->centroids.as<float>(),
-                        assign.as<int32_t>(), scratch, s);
+    if (form == MV_FORM_FAST && umma_kpad(d) <= 256)
+      kmeans_train_fast(dx.as<float>(), n, d, ix->nlist, niter_coarse, ix->centroids.as<float>(),
+                        assign.as<int32_t>(), scratch, ix->ctx, s, nullptr);
+    else
+      kmeans_train_device(dx.as<float>(), n, d, ix->nlist, niter_coarse, 1,
+                          ix->centroids.as<float>(), assign.as<int32_t>(), scratch, s);
     // 2. index-metric assignment and residuals (:113-128)
     const int kind = ix->metric == MV_METRIC_L2 ? KIND_L2_SIMD8 : KIND_IP_SIMD8;
     launch_exact_argmin(kind, 2, dx.as<float>(), n, d, ix->centroids.as<float>(), ix->nlist, d, d,
@@ -880,6 +907,11 @@ int32_t mv_ivfpq_train(mv_ivfpq* ix, const float* x, int64_t n, int32_t niter_co
     ix->trained = true;
     ix->fast_ready = false;
   });
+}
+
+int32_t mv_ivfpq_train(mv_ivfpq* ix, const float* x, int64_t n, int32_t niter_coarse,
+                       int32_t niter_pq) {
+  return mv_ivfpq_train_ex(ix, x, n, niter_coarse, niter_pq, nullptr);
 }
 
 int32_t mv_ivfpq_add_with_ids(mv_ivfpq* ix, const float* x, const int64_t* ids, int64_t n) {
@@ -1796,6 +1828,296 @@ int32_t mv_normalize(mv_ctx* ctx, const float* x, int64_t n, int32_t d, float* o
     d2h(out, dy.p, sizeof(float) * n * d, s);
     sync(s);
   });
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched fast IVF-PQ: plan with per-query nprobe / k, a persistent scan,
+// CUDA graphs per batch size and a tuner for the launch shapes.
+// ---------------------------------------------------------------------------
+struct mv_ivfpq_plan {
+  mv_ivfpq* ix = nullptr;
+  int64_t max_nq = 0;
+  int nprobe_max = 1, kmax = 1;
+  mv_search_params params{};
+  cudaStream_t stream = nullptr;
+  mv::DevBuf x, nprobe_q, k_q, order, out_d, out_l, counter, ws;
+  mv::FastBatch cfg;
+  std::map<int64_t, cudaGraphExec_t> graphs;   // one per batch size
+  std::map<int64_t, int64_t> graph_kernels;    // kernels per replay
+  std::mutex mu;
+  ~mv_ivfpq_plan() {
+    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace mv {
+
+FastBatch plan_batch(mv_ivfpq_plan* pl) {
+  FastBatch b = pl->cfg;
+  b.nprobe_q = pl->nprobe_q.as<int32_t>();
+  b.k_q = pl->k_q.as<int32_t>();
+  b.order = pl->order.as<int32_t>();
+  b.counter = pl->counter.as<int>();
+  return b;
+}
+
+void plan_enqueue(mv_ivfpq_plan* pl, int64_t nq, cudaStream_t s) {
+  const FastBatch b = plan_batch(pl);
+  ivfpq_search_fast(pl->ix, pl->x.as<float>(), nq, pl->kmax, pl->nprobe_max, &pl->params,
+                    pl->out_d.as<float>(), pl->out_l.as<int64_t>(), pl->ws, s, &b);
+}
+
+void plan_drop_graphs(mv_ivfpq_plan* pl) {
+  for (auto& g : pl->graphs) cudaGraphExecDestroy(g.second);
+  pl->graphs.clear();
+  pl->graph_kernels.clear();
+}
+
+// Runs the batch; with use_graph the enqueue is captured once per batch size
+// (after a direct run that sizes the workspace and raises the kernels'
+// shared-memory limits) and replayed.
+void plan_run(mv_ivfpq_plan* pl, int64_t nq, cudaStream_t s, bool use_graph) {
+  mv_ivfpq* ix = pl->ix;
+  ensure_fast(ix, s);
+  if (!use_graph) {
+    plan_enqueue(pl, nq, s);
+    return;
+  }
+  auto it = pl->graphs.find(nq);
+  if (it == pl->graphs.end()) {
+    plan_enqueue(pl, nq, s);
+    sync(s);
+    const bool prof = ix->ctx->profile.exchange(false);  // no event nodes in the graph
+    const int64_t l0 = ix->ctx->launches.load();
+    cudaGraph_t g = nullptr;
+    MV_CHECK_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      plan_enqueue(pl, nq, s);
+    } catch (...) {
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+      ix->ctx->profile.store(prof);
+      throw;
+    }
+    MV_CHECK_CUDA(cudaStreamEndCapture(s, &g));
+    ix->ctx->profile.store(prof);
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    MV_CHECK_CUDA(e);
+    it = pl->graphs.emplace(nq, exec).first;
+    pl->graph_kernels[nq] = ix->ctx->launches.load() - l0;
+    ix->ctx->launches.fetch_sub(pl->graph_kernels[nq]);  // counted again per replay
+  }
+  MV_CHECK_CUDA(cudaGraphLaunch(it->second, s));
+  ix->ctx->launches.fetch_add(pl->graph_kernels[nq]);
+}
+
+// Tuner: coordinate descent over the coarse method (fused top-k GEMM or
+// distance matrix, where both apply), the scan's threads per CTA and its
+// persistent grid, each candidate timed with CUDA events on the plan's own
+// batch (median of 3 after a warm-up). Returns the best time in ms.
+float plan_tune(mv_ivfpq_plan* pl, int64_t nq, cudaStream_t s) {
+  mv_ivfpq* ix = pl->ix;
+  ensure_fast(ix, s);
+  cudaEvent_t a, b;
+  MV_CHECK_CUDA(cudaEventCreate(&a));
+  MV_CHECK_CUDA(cudaEventCreate(&b));
+  auto time_cfg = [&](const FastBatch& c) -> float {
+    pl->cfg = c;
+    plan_enqueue(pl, nq, s);
+    float t[3];
+    for (int r = 0; r < 3; ++r) {
+      cudaEventRecord(a, s);
+      plan_enqueue(pl, nq, s);
+      cudaEventRecord(b, s);
+      MV_CHECK_CUDA(cudaEventSynchronize(b));
+      cudaEventElapsedTime(&t[r], a, b);
+    }
+    std::sort(t, t + 3);
+    return t[1];
+  };
+  FastBatch best = pl->cfg;
+  float best_ms = time_cfg(best);
+  auto consider = [&](FastBatch c) {
+    const float ms = time_cfg(c);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = c;
+    }
+  };
+  const int nc = std::min(ix->nlist, pl->nprobe_max + std::max(8, pl->nprobe_max / 4));
+  if (nc <= 64 && !pl->params.coarse_fp32) {
+    FastBatch c = best;
+    c.coarse_matrix = !c.coarse_matrix;
+    consider(c);
+  }
+  for (int nt : {128, 256, 512}) {
+    if (nt == best.scan_threads) continue;
+    FastBatch c = best;
+    c.scan_threads = nt;
+    consider(c);
+  }
+  for (int cps : {0, 2, 4, 8}) {
+    if (cps == best.scan_ctas_per_sm) continue;
+    FastBatch c = best;
+    c.scan_ctas_per_sm = cps;
+    consider(c);
+  }
+  pl->cfg = best;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  plan_drop_graphs(pl);
+  return best_ms;
+}
+
+// Host-side per-query parameters -> plan buffers, and the scan order:
+// queries by decreasing nprobe (ties by index), so the persistent grid
+// starts the longest scans first.
+void plan_set_queries(mv_ivfpq_plan* pl, const float* x, int64_t nq, const int32_t* nprobe,
+                      const int32_t* k, cudaStream_t s) {
+  MV_REQUIRE(nq >= 0 && nq <= pl->max_nq, MV_ERR_ARG, "batch larger than the plan");
+  std::vector<int32_t> np(nq), kk(nq), ord(nq);
+  for (int64_t i = 0; i < nq; ++i) {
+    np[i] = nprobe ? std::min(nprobe[i], pl->ix->nlist) : pl->nprobe_max;  // at most nlist lists
+    kk[i] = k ? k[i] : pl->kmax;
+    MV_REQUIRE(np[i] >= 1 && np[i] <= pl->nprobe_max, MV_ERR_ARG,
+               "per-query nprobe must be between 1 and the plan's nprobe");
+    MV_REQUIRE(kk[i] >= 1 && kk[i] <= pl->kmax, MV_ERR_ARG,
+               "per-query k must be between 1 and the plan's k");
+    ord[i] = (int32_t)i;
+  }
+  std::stable_sort(ord.begin(), ord.end(), [&](int32_t p, int32_t q) { return np[p] > np[q]; });
+  if (x) h2d(pl->x.p, x, sizeof(float) * nq * pl->ix->d, s);
+  h2d(pl->nprobe_q.p, np.data(), sizeof(int32_t) * nq, s);
+  h2d(pl->k_q.p, kk.data(), sizeof(int32_t) * nq, s);
+  h2d(pl->order.p, ord.data(), sizeof(int32_t) * nq, s);
+  sync(s);  // the host vectors go out of scope
+}
+
+}  // namespace mv
+
+extern "C" {
+
+int32_t mv_ivfpq_plan_create(mv_ivfpq* ix, int64_t max_nq, int32_t nprobe_max, int32_t kmax,
+                             const mv_search_params* params, mv_ivfpq_plan** out) {
+  if (!ix || !out || max_nq <= 0 || nprobe_max <= 0 || kmax <= 0) return MV_ERR_ARG;
+  *out = nullptr;
+  return guard(ix->ctx, [&] {
+    MV_REQUIRE(ix->trained, MV_ERR_STATE, "index is not trained");
+    MV_REQUIRE(kmax <= 4096, MV_ERR_ARG, "k must be at most 4096");
+    nprobe_max = std::min(nprobe_max, ix->nlist);
+    auto pl = std::make_unique<mv_ivfpq_plan>();
+    pl->ix = ix;
+    pl->max_nq = max_nq;
+    pl->nprobe_max = nprobe_max;
+    pl->kmax = kmax;
+    if (params) pl->params = *params;
+    pl->params.form = MV_FORM_FAST;
+    MV_CHECK_CUDA(cudaStreamCreateWithFlags(&pl->stream, cudaStreamNonBlocking));
+    pl->x.ensure(sizeof(float) * max_nq * ix->d);
+    pl->nprobe_q.ensure(sizeof(int32_t) * max_nq);
+    pl->k_q.ensure(sizeof(int32_t) * max_nq);
+    pl->order.ensure(sizeof(int32_t) * max_nq);
+    pl->out_d.ensure(sizeof(float) * max_nq * kmax);
+    pl->out_l.ensure(sizeof(int64_t) * max_nq * kmax);
+    pl->counter.ensure(sizeof(int));
+    *out = pl.release();
+  });
+}
+
+int32_t mv_ivfpq_plan_destroy(mv_ivfpq_plan* pl) {
+  if (!pl) return MV_ERR_ARG;
+  return guard(pl->ix->ctx, [&] {
+    cudaStreamSynchronize(pl->stream);
+    delete pl;
+  });
+}
+
+int32_t mv_ivfpq_plan_buffers(mv_ivfpq_plan* pl, float** d_x, int32_t** d_nprobe, int32_t** d_k,
+                              int32_t** d_order, float** d_distances, int64_t** d_labels) {
+  if (!pl) return MV_ERR_ARG;
+  if (d_x) *d_x = pl->x.as<float>();
+  if (d_nprobe) *d_nprobe = pl->nprobe_q.as<int32_t>();
+  if (d_k) *d_k = pl->k_q.as<int32_t>();
+  if (d_order) *d_order = pl->order.as<int32_t>();
+  if (d_distances) *d_distances = pl->out_d.as<float>();
+  if (d_labels) *d_labels = pl->out_l.as<int64_t>();
+  return MV_OK;
+}
+
+int32_t mv_ivfpq_plan_set_queries(mv_ivfpq_plan* pl, const float* x, int64_t nq,
+                                  const int32_t* nprobe, const int32_t* k) {
+  if (!pl || nq < 0) return MV_ERR_ARG;
+  return guard(pl->ix->ctx, [&] {
+    std::lock_guard<std::mutex> lk(pl->mu);
+    plan_set_queries(pl, x, nq, nprobe, k, pl->stream);
+  });
+}
+
+int32_t mv_ivfpq_plan_tune(mv_ivfpq_plan* pl, int64_t nq, int32_t* config, float* best_ms) {
+  if (!pl || nq <= 0) return MV_ERR_ARG;
+  return guard(pl->ix->ctx, [&] {
+    std::lock_guard<std::mutex> lk(pl->mu);
+    MV_REQUIRE(nq <= pl->max_nq, MV_ERR_ARG, "batch larger than the plan");
+    const float ms = plan_tune(pl, nq, pl->stream);
+    if (best_ms) *best_ms = ms;
+    if (config) {
+      config[0] = pl->cfg.coarse_matrix ? 1 : 0;
+      config[1] = pl->cfg.scan_threads;
+      config[2] = pl->cfg.scan_ctas_per_sm;
+    }
+    check_kernel_errors(pl->ix->ctx, pl->stream);
+  });
+}
+
+int32_t mv_ivfpq_plan_run(mv_ivfpq_plan* pl, int64_t nq, int32_t use_graph, void* stream) {
+  if (!pl || nq < 0) return MV_ERR_ARG;
+  return guard(pl->ix->ctx, [&] {
+    std::lock_guard<std::mutex> lk(pl->mu);
+    MV_REQUIRE(nq <= pl->max_nq, MV_ERR_ARG, "batch larger than the plan");
+    if (nq == 0) return;
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : pl->stream;
+    plan_run(pl, nq, s, use_graph != 0);
+    if (!stream) check_kernel_errors(pl->ix->ctx, s);
+  });
+}
+
+int32_t mv_ivfpq_plan_results(mv_ivfpq_plan* pl, int64_t nq, float* distances, int64_t* labels) {
+  if (!pl || nq < 0 || (nq > 0 && (!distances || !labels))) return MV_ERR_ARG;
+  return guard(pl->ix->ctx, [&] {
+    std::lock_guard<std::mutex> lk(pl->mu);
+    MV_REQUIRE(nq <= pl->max_nq, MV_ERR_ARG, "batch larger than the plan");
+    MV_CHECK_CUDA(cudaDeviceSynchronize());  // results of runs on any stream
+    d2h(distances, pl->out_d.p, sizeof(float) * nq * pl->kmax, pl->stream);
+    d2h(labels, pl->out_l.p, sizeof(int64_t) * nq * pl->kmax, pl->stream);
+    sync(pl->stream);
+  });
+}
+
+int32_t mv_ivfpq_search_batch(mv_ivfpq* ix, const float* x, int64_t nq, const int32_t* nprobe,
+                              const int32_t* k, int32_t kmax, const mv_search_params* params,
+                              float* distances, int64_t* labels) {
+  if (!ix || nq < 0 || kmax <= 0 || (nq > 0 && (!x || !nprobe || !k || !distances || !labels)))
+    return MV_ERR_ARG;
+  if (nq == 0) return MV_OK;
+  int32_t npmax = 1;
+  for (int64_t i = 0; i < nq; ++i) npmax = std::max(npmax, nprobe[i]);
+  mv_ivfpq_plan* pl = nullptr;
+  int32_t st = mv_ivfpq_plan_create(ix, nq, npmax, kmax, params, &pl);
+  if (st != MV_OK) return st;
+  st = guard(ix->ctx, [&] {
+    plan_set_queries(pl, x, nq, nprobe, k, pl->stream);
+    plan_run(pl, nq, pl->stream, false);
+    d2h(distances, pl->out_d.p, sizeof(float) * nq * kmax, pl->stream);
+    d2h(labels, pl->out_l.p, sizeof(int64_t) * nq * kmax, pl->stream);
+    check_kernel_errors(ix->ctx, pl->stream);
+  });
+  mv_ivfpq_plan_destroy(pl);
+  return st;
 }
 
 }  // extern "C"

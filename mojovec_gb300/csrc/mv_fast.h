@@ -24,6 +24,9 @@ struct FastScanArgs {
   int nlist;              // bounds of the data-dependent indices
   int64_t ntotal;
   int* err;               // set to a site code if an index is out of range
+  const int32_t* nprobe_q = nullptr;  // per-query nprobe (<= nprobe), may be null
+  const int32_t* order = nullptr;     // scan order of the queries, may be null
+  int* counter = nullptr;             // persistent grid: next position in `order`
   int cap, Rp;            // set by the launcher
 };
 
@@ -40,6 +43,7 @@ struct RerankArgs {
   int64_t ntotal;         // CSR entries (bound of the shortlist positions)
   int* err;
   float fill_d = 1e38f;   // distance of an unfilled slot (label -1)
+  const int32_t* k_q = nullptr;  // per-query k (<= k; the row keeps k slots), may be null
   int kp;                 // set by the launcher
 };
 
@@ -53,7 +57,8 @@ void launch_coarse_fast(const float* approx, int64_t nq, int nlist, const float*
 void launch_coarse_from_keys(const uint64_t* cand, int64_t nq, int ncand, const float* q, int d,
                              const float* cent, int nlist, int metric, int nc, int nprobe,
                              int32_t* probes, float* term, int* err, cudaStream_t s);
-void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s);
+size_t fast_scan_smem(const FastScanArgs& a);
+void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s, int nt = 256, int persistent_ctas = 0);
 // Flat fast form: merge nseg x ncp per-segment keys (kseg kept per segment)
 // into the R-key shortlist per query. With out_keys the shortlist is
 // written (unsorted) for the rerank; otherwise the k smallest become the
@@ -70,6 +75,7 @@ void launch_flat_merge(const uint64_t* cand, int64_t nq, int nseg, int ncp, int 
                        float* out_d, int64_t* out_l, int* overflow, cudaStream_t s);
 void launch_rerank_fast(RerankArgs a, cudaStream_t s);
 void launch_short_to_results(const uint64_t* keys, int64_t nq, int R, int k, const uint32_t* ids,
-                             int metric, float* out_d, int64_t* out_l, cudaStream_t s);
+                             int metric, float* out_d, int64_t* out_l, cudaStream_t s,
+                             const int32_t* k_q = nullptr);
 
 }  // namespace mv

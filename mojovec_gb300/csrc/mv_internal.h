@@ -167,6 +167,17 @@ struct SlotLease {
   void use(cudaStream_t s) { used = s; }
 };
 
+// Per-query parameters and launch shapes of a batched fast IVF-PQ search.
+struct FastBatch {
+  const int32_t* nprobe_q = nullptr;  // device, per query
+  const int32_t* k_q = nullptr;       // device, per query
+  const int32_t* order = nullptr;     // device, scan order (a permutation)
+  int* counter = nullptr;             // device, persistent scan work counter
+  int scan_threads = 256;             // 128, 256 or 512
+  int scan_ctas_per_sm = 4;           // persistent grid size; 0 = one CTA per query
+  bool coarse_matrix = false;         // distance matrix + select even where the fused GEMM fits
+};
+
 }  // namespace mv
 
 struct mv_ivfpq {

@@ -25,7 +25,7 @@ import threading
 import numpy as np
 
 from . import _lib
-from ._lib import METRIC_IP, METRIC_L2, SearchParams, check
+from ._lib import FORM_FAST, METRIC_IP, METRIC_L2, SearchParams, check
 
 
 def _f32(a, d=None):
@@ -144,11 +144,17 @@ class IndexIVFPQ:
         check(_lib.load().mv_ivfpq_get_codebooks(self._h, _p(c), _p(p)))
         return c, p
 
-    def train(self, x, niter_coarse: int = 15, niter_pq: int = 15):
+    def train(self, x, niter_coarse: int = 15, niter_pq: int = 15, form=None):
         """IndexIVFPQ.train; the reference hard-codes 15 iterations for both
-        k-means runs (index_ivf_pq.mojo:98, pq.mojo:64)."""
+        k-means runs (index_ivf_pq.mojo:98, pq.mojo:64). form=FORM_FAST runs
+        the coarse k-means in its fast form."""
         x = _f32(x, self.d)
-        check(_lib.load().mv_ivfpq_train(self._h, _p(x), x.shape[0], niter_coarse, niter_pq))
+        if form is None:
+            check(_lib.load().mv_ivfpq_train(self._h, _p(x), x.shape[0], niter_coarse, niter_pq))
+        else:
+            p = _params(form)
+            check(_lib.load().mv_ivfpq_train_ex(self._h, _p(x), x.shape[0], niter_coarse,
+                                                niter_pq, C.byref(p)))
 
     def add(self, x):
         x = _f32(x, self.d)
@@ -181,6 +187,22 @@ class IndexIVFPQ:
         check(_lib.load().mv_ivfpq_search(self._h, _p(x), n, k, _p(flt),
                                           0 if flt is None else flt.size, C.byref(p), _p(dist),
                                           _p(lab)))
+        return dist, lab
+
+    def search_batch(self, x, nprobe, k, rerank: int = 0, coarse_fp32: bool = False):
+        """Fast-form search with per-query nprobe and k (mv_ivfpq_search_batch).
+        Returns (distances, labels) of shape (n, max(k)); slots past a
+        query's k read 1e38 / -1."""
+        x = _f32(x, self.d)
+        n = x.shape[0]
+        nprobe = np.ascontiguousarray(nprobe, dtype=np.int32)
+        k = np.ascontiguousarray(k, dtype=np.int32)
+        kmax = int(k.max()) if n else 1
+        dist = np.empty((n, kmax), np.float32)
+        lab = np.empty((n, kmax), np.int64)
+        p = _params(FORM_FAST, 0, rerank, coarse_fp32)
+        check(_lib.load().mv_ivfpq_search_batch(self._h, _p(x), n, _p(nprobe), _p(k), kmax,
+                                                C.byref(p), _p(dist), _p(lab)))
         return dist, lab
 
     def search_device(self, x_ptr: int, n: int, k: int, dist_ptr: int, lab_ptr: int,
@@ -420,3 +442,57 @@ def normalize(x, ctx: Context | None = None):
     if st != 0:
         raise ValueError(_lib.last_error())
     return out
+
+
+class IVFPQBatchPlan:
+    """A batched fast IVF-PQ search replayed as a CUDA graph
+    (mv_ivfpq_plan_*): per-query nprobe and k, persistent scan, tuner."""
+
+    def __init__(self, index: IndexIVFPQ, max_nq: int, nprobe_max: int, kmax: int,
+                 rerank: int = 0, coarse_fp32: bool = False):
+        self.index = index
+        self.max_nq, self.kmax, self.d = max_nq, kmax, index.d
+        h = C.c_void_p()
+        p = _params(FORM_FAST, 0, rerank, coarse_fp32)
+        check(_lib.load().mv_ivfpq_plan_create(index._h, max_nq, nprobe_max, kmax, C.byref(p),
+                                               C.byref(h)))
+        self._h = h
+        ptrs = [C.c_void_p() for _ in range(6)]
+        check(_lib.load().mv_ivfpq_plan_buffers(h, *[C.byref(q) for q in ptrs]))
+        (self.d_x, self.d_nprobe, self.d_k, self.d_order, self.d_dist,
+         self.d_labels) = [q.value for q in ptrs]
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib._lib is not None:
+            _lib._lib.mv_ivfpq_plan_destroy(h)
+            self._h = None
+
+    def set_queries(self, x, nprobe, k):
+        """Host queries (or None when d_x was filled on the device), per-query
+        nprobe and k."""
+        n = len(nprobe)
+        xp = None
+        if x is not None:
+            x = _f32(x, self.d)
+            xp = _p(x)
+        nprobe = np.ascontiguousarray(nprobe, dtype=np.int32)
+        k = np.ascontiguousarray(k, dtype=np.int32)
+        check(_lib.load().mv_ivfpq_plan_set_queries(self._h, xp, n, _p(nprobe), _p(k)))
+
+    def tune(self, n: int):
+        cfg = np.zeros(3, np.int32)
+        ms = C.c_float(0.0)
+        check(_lib.load().mv_ivfpq_plan_tune(self._h, n, _p(cfg), C.byref(ms)))
+        return {"coarse_matrix": bool(cfg[0]), "scan_threads": int(cfg[1]),
+                "scan_ctas_per_sm": int(cfg[2]), "best_ms": float(ms.value)}
+
+    def run(self, n: int, use_graph: bool = True, stream: int = 0):
+        check(_lib.load().mv_ivfpq_plan_run(self._h, n, 1 if use_graph else 0, stream or None))
+
+    def results(self, n: int):
+        """Copies the first n result rows to the host (synchronous)."""
+        dist = np.empty((n, self.kmax), np.float32)
+        lab = np.empty((n, self.kmax), np.int64)
+        check(_lib.load().mv_ivfpq_plan_results(self._h, n, _p(dist), _p(lab)))
+        return dist, lab
