@@ -55,6 +55,7 @@ typedef struct mv_ivfpq mv_ivfpq;
 typedef struct mv_flat mv_flat;
 typedef struct mv_sq8 mv_sq8;
 typedef struct mv_ivfpq_plan mv_ivfpq_plan;
+typedef struct mv_server mv_server;
 
 /* Search options for the IVF-PQ and Flat searches. Zero-initialised means
  * the plain form with the index's own nprobe. */
@@ -196,6 +197,36 @@ int32_t mv_ivfpq_plan_run(mv_ivfpq_plan* plan, int64_t nq, int32_t use_graph, vo
 /* Copies the first nq result rows (nq x kmax) to host memory after all
  * pending work on the device. */
 int32_t mv_ivfpq_plan_results(mv_ivfpq_plan* plan, int64_t nq, float* distances, int64_t* labels);
+
+/* ---- Serving loop: continuous batching over resident collections ------- */
+/* A server batches submitted requests per (collection, k) in arrival order
+ * (up to max_batch_queries rows per batch) and runs them on `lanes` worker
+ * streams; a batch is admitted when a lane is idle and its device-memory
+ * estimate fits hbm_budget_bytes beside the batches in flight. Requests that
+ * arrive while others run are admitted as lanes and memory free up. Each
+ * request gets the same results alone and in any mix. */
+int32_t mv_server_create(mv_ctx* ctx, int64_t hbm_budget_bytes, int32_t lanes,
+                         int64_t max_batch_queries, mv_server** out);
+/* Finishes queued and running requests, then stops the server. */
+int32_t mv_server_destroy(mv_server* server);
+/* Registers a collection searched with `params` (form, nprobe, rerank);
+ * returns its id. The index must outlive the server. */
+int32_t mv_server_add_ivfpq(mv_server* server, mv_ivfpq* index, const mv_search_params* params,
+                            int32_t* id);
+int32_t mv_server_add_flat(mv_server* server, mv_flat* index, const mv_search_params* params,
+                           int32_t* id);
+int32_t mv_server_add_sq8(mv_server* server, mv_sq8* index, int32_t rerank_factor,
+                          const mv_search_params* params, int32_t* id);
+/* Queues nq query rows (copied; x is free on return) for collection `id`;
+ * distances / labels (nq x k) are written before mv_server_wait returns. */
+int32_t mv_server_submit(mv_server* server, int32_t id, const float* x, int64_t nq, int32_t k,
+                         float* distances, int64_t* labels, int64_t* request_id);
+/* Blocks until the request is done; returns its status and the latency from
+ * submit to completion in seconds (may be NULL). */
+int32_t mv_server_wait(mv_server* server, int64_t request_id, double* latency_s);
+/* [completed requests, batches, queries in batches, peak in-flight device
+ * bytes (estimate)]. */
+int32_t mv_server_stats(mv_server* server, int64_t* out4);
 
 /* ---- Flat index: replaces IndexFlat (index/index_flat.mojo:117-330) ---- */
 int32_t mv_flat_create(mv_ctx* ctx, int32_t d, int32_t metric, mv_flat** out);

@@ -22,6 +22,7 @@ from .index import (  # noqa: F401
     IndexIVFPQ,
     IVFPQBatchPlan,
     KMeans,
+    Server,
     distance_matrix,
     ProductQuantizer,
     normalize,

@@ -116,6 +116,14 @@ SIGNATURES = {
     "mv_ivfpq_plan_tune": (_i32, [_vp, _i64, _vp, _vp]),
     "mv_ivfpq_plan_run": (_i32, [_vp, _i64, _i32, _vp]),
     "mv_ivfpq_plan_results": (_i32, [_vp, _i64, _vp, _vp]),
+    "mv_server_create": (_i32, [_vp, _i64, _i32, _i64, _vp]),
+    "mv_server_destroy": (_i32, [_vp]),
+    "mv_server_add_ivfpq": (_i32, [_vp, _vp, _vp, _vp]),
+    "mv_server_add_flat": (_i32, [_vp, _vp, _vp, _vp]),
+    "mv_server_add_sq8": (_i32, [_vp, _vp, _i32, _vp, _vp]),
+    "mv_server_submit": (_i32, [_vp, _i32, _vp, _i64, _i32, _vp, _vp, _vp]),
+    "mv_server_wait": (_i32, [_vp, _i64, _vp]),
+    "mv_server_stats": (_i32, [_vp, _vp]),
     "mv_kmeans_train_ex": (_i32, [_vp, _vp, _i64, _i32, _i32, _i32, _vp, _vp, _vp, _vp]),
     "mv_pq_train": (_i32, [_vp, _vp, _i64, _i32, _i32, _i32, _vp]),
     "mv_pq_encode": (_i32, [_vp, _vp, _i32, _i32, _vp, _i64, _vp]),

@@ -320,6 +320,33 @@ __global__ void __launch_bounds__(NT) k_exact_argmin(const float* __restrict__ X
 
 size_t tile_smem(int d) { return (size_t)2 * TB * d * sizeof(float); }
 
+// Pairwise form for dimensions whose 64-row tiles do not fit shared memory:
+// warp w of a CTA stages one X row, lane t computes its distance to Y row
+// (blockIdx.x * 32 + t) with the same per-thread exact-order function, so
+// the bits equal the tile kernel's.
+template <int KIND>
+__global__ void __launch_bounds__(256)
+    k_exact_pairs(const float* __restrict__ X, int64_t nx, int64_t ldx, const float* __restrict__ Y,
+                  int64_t ny, int64_t ldy, int d, float* __restrict__ D, int64_t ldd) {
+  extern __shared__ float xs[];  // 8 rows x d
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t r = (int64_t)blockIdx.y * 8 + warp;
+  const int64_t c = (int64_t)blockIdx.x * 32 + lane;
+  float* xr = xs + (size_t)warp * d;
+  if (r < nx)
+    for (int j = lane; j < d; j += 32) xr[j] = X[r * ldx + j];
+  __syncwarp();
+  if (r >= nx || c >= ny) return;
+  const float* yr = Y + c * ldy;
+  float v;
+  if (KIND == KIND_IP_SIMD8) v = -ip_simd<8>(xr, yr, d);
+  else if (KIND == KIND_L2_SHORT4) v = l2_short4(xr, yr, d);
+  else v = l2_simd<8>(xr, yr, d);
+  D[r * ldd + c] = v;
+}
+
+
+
 template <typename K>
 void set_smem(K kernel, size_t bytes) {
   smem_limit(kernel, bytes);
@@ -331,7 +358,22 @@ void launch_exact_matrix(int kind, const float* X, int64_t nx, int64_t ldx, cons
                          int64_t ny, int64_t ldy, int d, float* D, int64_t ldd, cudaStream_t s) {
   if (nx == 0 || ny == 0) return;
   size_t smem = tile_smem(d);
-  MV_REQUIRE(smem <= 200 * 1024, MV_ERR_UNSUPPORTED, "exact distance tile: dimension too large");
+  if (smem > 200 * 1024) {  // large d: the pairwise form
+    const size_t ps = (size_t)8 * d * sizeof(float);
+    MV_REQUIRE(ps <= 200 * 1024, MV_ERR_UNSUPPORTED, "exact distances: dimension too large");
+    MV_REQUIRE((nx + 7) / 8 <= 65535, MV_ERR_UNSUPPORTED, "too many query rows in one call");
+    dim3 pg((unsigned)((ny + 31) / 32), (unsigned)((nx + 7) / 8));
+    auto go = [&](auto kernel) {
+      set_smem(kernel, ps);
+      kernel<<<pg, 256, ps, s>>>(X, nx, ldx, Y, ny, ldy, d, D, ldd);
+    };
+    if (kind == KIND_IP_SIMD8) go(k_exact_pairs<KIND_IP_SIMD8>);
+    else if (kind == KIND_L2_SHORT4) go(k_exact_pairs<KIND_L2_SHORT4>);
+    else go(k_exact_pairs<KIND_L2_SIMD8>);
+    count_launch();
+    MV_CHECK_CUDA(cudaGetLastError());
+    return;
+  }
   MV_REQUIRE((nx + TB - 1) / TB <= 65535, MV_ERR_UNSUPPORTED, "too many query rows in one call");
   dim3 grid((unsigned)((ny + TB - 1) / TB), (unsigned)((nx + TB - 1) / TB));
   switch (kind) {

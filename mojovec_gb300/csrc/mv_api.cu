@@ -1080,10 +1080,13 @@ void flat_search_fast(mv_flat* ix, const float* d_x, int64_t nq, int k, const ui
   const int64_t qb = std::min<int64_t>(nq, 32768);
   int nseg = umma_topk_nseg(qb, nb, ix->d, kseg, ix->ctx->num_sms);
   const int groups = umma_topk_groups(ix->d, kseg);
-  if (kseg < R) {  // about 16 shortlist keys per segment keeps overflow rare
+  if (kseg < R) {
+    // About 16 shortlist keys per segment keeps overflow rare. The count
+    // depends on the index and R only, never on the batch, so whether a
+    // query overflows (and is recomputed exactly) does not depend on the
+    // other queries it was batched with.
     const int64_t nct = (nb + 127) / 128;
-    nseg = (int)std::min<int64_t>(std::max<int64_t>(nseg, (R + 15) / 16 / groups + 1),
-                                  std::max<int64_t>(1, nct));
+    nseg = (int)std::min<int64_t>((R + 15) / 16 / groups + 1, std::max<int64_t>(1, nct));
   }
   const int osegs = nseg * groups;  // output segments per query
   ws.ensure(ws_bytes((size_t)qb * kp, 2) + ws_bytes((size_t)qb, 4) +
@@ -1351,10 +1354,9 @@ void sq8_tensor_keys(mv_sq8* ix, const float* d_x, int64_t nq, int R, const uint
   const int ncp = next_pow2(kseg);
   int nseg = umma_topk_nseg(nq, nb, ix->d, kseg, ix->ctx->num_sms);
   const int groups = umma_topk_groups(ix->d, kseg);
-  if (kseg < R + 8) {  // about 16 shortlist keys per segment keeps flags rare
+  if (kseg < R + 8) {  // as for the flat scan: independent of the batch
     const int64_t nct = (nb + 127) / 128;
-    nseg = (int)std::min<int64_t>(std::max<int64_t>(nseg, (R + 15) / 16 / groups + 1),
-                                  std::max<int64_t>(1, nct));
+    nseg = (int)std::min<int64_t>((R + 15) / 16 / groups + 1, std::max<int64_t>(1, nct));
   }
   const int osegs = nseg * groups;
   ws.ensure(ws_bytes((size_t)nq * ix->dpad, 1) + ws_bytes((size_t)nq, 4) +

@@ -496,3 +496,68 @@ class IVFPQBatchPlan:
         lab = np.empty((n, self.kmax), np.int64)
         check(_lib.load().mv_ivfpq_plan_results(self._h, n, _p(dist), _p(lab)))
         return dist, lab
+
+
+class Server:
+    """Continuous-batching serving loop over resident collections
+    (mv_server_*). submit() returns a request id at once; wait() blocks and
+    returns (distances, labels, latency_s)."""
+
+    def __init__(self, ctx: Context | None = None, hbm_budget: int = 8 << 30, lanes: int = 4,
+                 max_batch_queries: int = 4096):
+        self.ctx = ctx or Context.default()
+        h = C.c_void_p()
+        check(_lib.load().mv_server_create(self.ctx.handle, int(hbm_budget), lanes,
+                                           max_batch_queries, C.byref(h)))
+        self._h = h
+        self._dims = {}
+        self._pending = {}
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h and _lib._lib is not None:
+            _lib._lib.mv_server_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def add(self, index, form=None, nprobe: int = 0, rerank: int = 0, rerank_factor: int = 0):
+        cid = C.c_int32(0)
+        p = _params(form, nprobe, rerank)
+        lib = _lib.load()
+        if isinstance(index, IndexIVFPQ):
+            check(lib.mv_server_add_ivfpq(self._h, index._h, C.byref(p), C.byref(cid)))
+        elif isinstance(index, IndexFlat):
+            check(lib.mv_server_add_flat(self._h, index._h, C.byref(p), C.byref(cid)))
+        elif isinstance(index, IndexFlatSQ8):
+            check(lib.mv_server_add_sq8(self._h, index._h, rerank_factor, C.byref(p),
+                                        C.byref(cid)))
+        else:
+            raise TypeError("unsupported index type")
+        self._dims[cid.value] = index.d
+        return cid.value
+
+    def submit(self, coll: int, x, k: int) -> int:
+        x = _f32(x, self._dims[coll])
+        n = x.shape[0]
+        dist = np.empty((n, k), np.float32)
+        lab = np.empty((n, k), np.int64)
+        rid = C.c_int64(0)
+        check(_lib.load().mv_server_submit(self._h, coll, _p(x), n, k, _p(dist), _p(lab),
+                                           C.byref(rid)))
+        self._pending[rid.value] = (dist, lab)
+        return rid.value
+
+    def wait(self, rid: int):
+        lat = C.c_double(0.0)
+        st = _lib.load().mv_server_wait(self._h, rid, C.byref(lat))
+        dist, lab = self._pending.pop(rid)
+        check(st)
+        return dist, lab, lat.value
+
+    def stats(self):
+        out = np.zeros(4, np.int64)
+        check(_lib.load().mv_server_stats(self._h, _p(out)))
+        return {"completed": int(out[0]), "batches": int(out[1]), "batched_queries": int(out[2]),
+                "peak_inflight_bytes": int(out[3])}

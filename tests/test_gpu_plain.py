@@ -28,7 +28,7 @@ def _same(a, b):
     return a.shape == b.shape and bool(np.all((a == b) | (np.isnan(a) & np.isnan(b))))
 
 
-@pytest.mark.parametrize("d", [1, 3, 4, 7, 8, 12, 16, 31, 32, 33, 96, 128, 130, 256])
+@pytest.mark.parametrize("d", [1, 3, 4, 7, 8, 12, 16, 31, 32, 33, 96, 128, 130, 256, 401, 768, 1000])
 @pytest.mark.parametrize("metric", [0, 1])
 def test_flat_exact_matches_oracle(mv, orc, d, metric):
     base = _rand(1500, d, 3.0)
