@@ -955,6 +955,72 @@ def run_serve(args, rank, world):
     }
 
 
+CURVE_METRIC = "IVF-PQ QPS-recall curve (1M x 128 SIFT-like, nlist 4096, M 16/32, 10k queries, k 10)"
+
+
+def run_curve(args, rank, world):
+    """QPS against recall@10 for nprobe 8..128 and M 16 / 32: the plain form
+    and fast variants (BF16 or FP32 coarse, FP32 or FP16 tables, with and
+    without the exact rerank of 40). Device-resident queries, CUDA events,
+    L2 flushed per step; recall against the exact FP32 flat search (equal to
+    FP64 on these integer-valued rows)."""
+    import torch
+
+    import mojovec_gb300 as mv
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    ctx = mv.Context(dev)
+    base, queries = build_workload(args.nb, args.nq)
+    nq = queries.shape[0]
+    flat = mv.IndexFlat(D, mv.METRIC_L2, ctx=ctx)
+    flat.add(base)
+    _, gt = flat.search(queries, K)
+    del flat
+    d_q = torch.from_numpy(queries).cuda()
+    d_dist = torch.empty((nq, K), dtype=torch.float32, device="cuda")
+    d_lab = torch.empty((nq, K), dtype=torch.int64, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    variants = {
+        "plain": dict(form=mv.FORM_PLAIN),
+        "fast_bf16coarse_fp32lut_rerank40": dict(form=mv.FORM_FAST, rerank=40),
+        "fast_fp32coarse_fp32lut_rerank40": dict(form=mv.FORM_FAST, rerank=40, coarse_fp32=True),
+        "fast_bf16coarse_fp16lut_rerank40": dict(form=mv.FORM_FAST, rerank=40, lut_fp16=True),
+        "fast_bf16coarse_fp32lut_norerank": dict(form=mv.FORM_FAST),
+    }
+    curve = []
+    for m in (16, 32):
+        index = mv.IndexIVFPQ(D, NLIST, m, mv.METRIC_L2, ctx=ctx)
+        index.train(base[:TRAIN_N], niter_coarse=NITER, niter_pq=NITER)
+        index.add(base)
+        for nprobe in (8, 16, 32, 64, 128):
+            for name, opts in variants.items():
+                def step():
+                    index.search_device(d_q.data_ptr(), nq, K, d_dist.data_ptr(), d_lab.data_ptr(),
+                                        stream=stream.cuda_stream, nprobe=nprobe, **opts)
+                step()
+                torch.cuda.synchronize()
+                rec = recall_at(gt, d_lab.cpu().numpy(), K)
+                steps = 3 if name == "plain" else 5
+                ms = _timed_steps(torch, step, steps, stream, flush) / steps
+                curve.append({"M": m, "nprobe": nprobe, "variant": name,
+                              "qps": round(nq / (ms / 1e3), 1), "recall_at_10": round(rec, 4)})
+        del index
+    head = [c for c in curve if c["M"] == 16 and c["nprobe"] == 16 and
+            c["variant"] == "fast_bf16coarse_fp32lut_rerank40"][0]
+    return {
+        "metric": CURVE_METRIC, "value": head["qps"], "unit": "queries/s", "n_gpus": 1,
+        "steps": 5, "warmup": 1, "ms_per_step": round(nq / head["qps"] * 1e3, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f32",
+        "data": "synthetic SIFT-like (seeded Gaussian mixture, integer-valued), not SIFT1M",
+        "config": {"workload": f"ivfpq_curve_{args.nb}x128_nlist4096_nq{nq}_k10",
+                   "value_is": "M 16, nprobe 16, BF16 coarse, FP32 tables, rerank 40",
+                   "curve": curve},
+        "e2e": None, "gpu_launches": None,
+    }
+
+
 def run_reference_flat(args):
     """The oracle's IndexFlat search over all rows for a bounded query sample."""
     from oracle import oracle as orc
@@ -1010,7 +1076,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=500)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="ivfpq",
-                    choices=["ivfpq", "flat", "sq8", "kmeans", "batch", "serve"])
+                    choices=["ivfpq", "flat", "sq8", "kmeans", "batch", "serve", "curve"])
     ap.add_argument("--batch-nb", type=int, default=10_000_000)
     ap.add_argument("--serve-scale", type=float, default=1.0)
     ap.add_argument("--serve-requests", type=int, default=300)
@@ -1046,6 +1112,8 @@ def main():
         out = run_batch(args, rank, world)
     elif args.workload == "serve":
         out = run_serve(args, rank, world)
+    elif args.workload == "curve":
+        out = run_curve(args, rank, world)
     elif args.workload in ("flat", "sq8"):
         out = run_flat(args, rank, world)
     else:

@@ -17,6 +17,10 @@
 // The ADC scan keeps a shortlist of R candidates per query (BlockTopK over
 // (distance, CSR position) keys); k_rerank_fast then computes exact FP32
 // distances to the raw rows of the shortlist and selects the final k.
+#include <cuda_fp16.h>
+
+#include <type_traits>
+
 #include "mv_internal.h"
 #include "mv_kernels.h"
 #include "mv_fast.h"
@@ -110,7 +114,14 @@ __global__ void __launch_bounds__(FT)
 
 // Sum of the M table entries of one code; four partial sums break the
 // dependency chain (the fast form does not reproduce the reference's order).
-__device__ __forceinline__ float adc_fast(const float* lut, const uint8_t* code, int M, float acc) {
+template <typename T>
+__device__ __forceinline__ float lut_val(const T* lut, int i) {
+  if constexpr (sizeof(T) == 2) return __half2float(lut[i]);
+  else return lut[i];
+}
+
+template <typename T>
+__device__ __forceinline__ float adc_fast(const T* lut, const uint8_t* code, int M, float acc) {
   float p[4] = {acc, 0.0f, 0.0f, 0.0f};
   if ((M & 15) == 0) {
     for (int m0 = 0; m0 < M; m0 += 16) {
@@ -119,7 +130,7 @@ __device__ __forceinline__ float adc_fast(const float* lut, const uint8_t* code,
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int b = 0; b < 4; ++b) p[b] += lut[((m0 + 4 * i + b) << 8) + ((w[i] >> (8 * b)) & 255u)];
+        for (int b = 0; b < 4; ++b) p[b] += lut_val(lut, ((m0 + 4 * i + b) << 8) + ((w[i] >> (8 * b)) & 255u));
     }
   } else if ((M & 7) == 0) {
     for (int m0 = 0; m0 < M; m0 += 8) {
@@ -128,10 +139,10 @@ __device__ __forceinline__ float adc_fast(const float* lut, const uint8_t* code,
 #pragma unroll
       for (int i = 0; i < 2; ++i)
 #pragma unroll
-        for (int b = 0; b < 4; ++b) p[b] += lut[((m0 + 4 * i + b) << 8) + ((w[i] >> (8 * b)) & 255u)];
+        for (int b = 0; b < 4; ++b) p[b] += lut_val(lut, ((m0 + 4 * i + b) << 8) + ((w[i] >> (8 * b)) & 255u));
     }
   } else {
-    for (int m = 0; m < M; ++m) p[m & 3] += lut[(m << 8) + code[m]];
+    for (int m = 0; m < M; ++m) p[m & 3] += lut_val(lut, (m << 8) + code[m]);
   }
   return (p[0] + p[1]) + (p[2] + p[3]);
 }
@@ -197,8 +208,9 @@ __global__ void __launch_bounds__(FT)
 // Per-query table lut[m][k] = scale * <q_m, C[m][k]>: warp w builds
 // subspaces w, w + 8, ...; each lane owns 8 codewords and keeps q_m in
 // registers, with the codeword rows read as float4 when dsub is 4 or 8.
-template <int NT>
-__device__ __forceinline__ void build_lut(float* lut, const float* qv, const float* pq, int M,
+// Emits value v of entry (mm, k) through put(index, v).
+template <int NT, typename Put>
+__device__ __forceinline__ void build_lut(Put put, const float* qv, const float* pq, int M,
                                           int dsub, float scale) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int mm = warp; mm < M; mm += NT / 32) {
@@ -224,7 +236,7 @@ __device__ __forceinline__ void build_lut(float* lut, const float* qv, const flo
         dot = fmaf(qb.y, cb[u].y, dot);
         dot = fmaf(qb.z, cb[u].z, dot);
         dot = fmaf(qb.w, cb[u].w, dot);
-        lut[(mm << 8) + lane + 32 * u] = scale * dot;
+        put((mm << 8) + lane + 32 * u, scale * dot);
       }
     } else if (dsub == 4) {
       const float4 qa = *reinterpret_cast<const float4*>(xm);
@@ -237,14 +249,14 @@ __device__ __forceinline__ void build_lut(float* lut, const float* qv, const flo
         dot = fmaf(qa.y, ca[u].y, dot);
         dot = fmaf(qa.z, ca[u].z, dot);
         dot = fmaf(qa.w, ca[u].w, dot);
-        lut[(mm << 8) + lane + 32 * u] = scale * dot;
+        put((mm << 8) + lane + 32 * u, scale * dot);
       }
     } else {
       for (int u = 0; u < 8; ++u) {
         const float* c = cm + (lane + 32 * u) * dsub;
         float dot = 0.0f;
         for (int t = 0; t < dsub; ++t) dot = fmaf(xm[t], c[t], dot);
-        lut[(mm << 8) + lane + 32 * u] = scale * dot;
+        put((mm << 8) + lane + 32 * u, scale * dot);
       }
     }
   }
@@ -257,13 +269,15 @@ __device__ __forceinline__ void build_lut(float* lut, const float* qv, const flo
 // would overflow the staging area, and once at the end, a radix select keeps
 // the R smallest. The shortlist is written unsorted (the rerank orders it),
 // or sorted when it is the final answer.
-template <int NT>
+template <int NT, bool HALF>
 __global__ void __launch_bounds__(NT) k_ivfpq_scan_fast(FastScanArgs a) {
   constexpr int FT = NT;
+  using LutT = typename std::conditional<HALF, __half, float>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int M = a.M, d = a.d, dsub = d / M;
-  float* lut = reinterpret_cast<float*>(smraw);
-  float* qv = lut + M * 256;
+  // The table region is sized for FP32 entries either way.
+  LutT* lut = reinterpret_cast<LutT*>(smraw);
+  float* qv = reinterpret_cast<float*>(smraw) + M * 256;
   uint64_t* outb =
       reinterpret_cast<uint64_t*>(smraw + (((size_t)(M * 256 + d) * 4 + 15) & ~size_t(15)));
   uint32_t* khi = reinterpret_cast<uint32_t*>(outb + a.Rp);
@@ -274,6 +288,7 @@ __global__ void __launch_bounds__(NT) k_ivfpq_scan_fast(FastScanArgs a) {
   __shared__ RadixScratch rs;
   __shared__ int s_fill;
   __shared__ int s_q;
+  __shared__ unsigned s_amax;  // FP16 tables: largest |entry| (float bits)
   const int lane = threadIdx.x & 31;
   // One query per CTA, or (with a.counter) a persistent CTA that takes
   // queries from a global counter in a.order until none are left.
@@ -325,7 +340,25 @@ __global__ void __launch_bounds__(NT) k_ivfpq_scan_fast(FastScanArgs a) {
   }
   __syncthreads();
   const float scale = a.metric == MV_METRIC_L2 ? -2.0f : -1.0f;
-  build_lut<NT>(lut, qv, a.pq, M, dsub, scale);
+  // FP16 tables carry a per-query power-of-two scale so no entry overflows
+  // (a first pass finds the largest magnitude); sums stay in FP32.
+  float lscale = 1.0f;
+  if constexpr (HALF) {
+    if (threadIdx.x == 0) s_amax = 0u;
+    __syncthreads();
+    float mx = 0.0f;
+    build_lut<NT>([&](int, float v) { mx = fmaxf(mx, fabsf(v)); }, qv, a.pq, M, dsub, scale);
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) atomicMax(&s_amax, __float_as_uint(mx));
+    __syncthreads();
+    const float amax = __uint_as_float(s_amax);
+    if (amax > 0.0f) lscale = exp2f((float)(ilogbf(amax) - 14));  // amax / lscale < 2^15
+    const float inv = 1.0f / lscale;  // a power of two: exact
+    build_lut<NT>([&](int i, float v) { lut[i] = __float2half_rn(v * inv); }, qv, a.pq, M, dsub,
+                  scale);
+  } else {
+    build_lut<NT>([&](int i, float v) { lut[i] = v; }, qv, a.pq, M, dsub, scale);
+  }
   __syncthreads();
   const int total = pbeg[nprobe];
   const int chunk = a.cap - a.R;
@@ -385,8 +418,14 @@ __global__ void __launch_bounds__(NT) k_ivfpq_scan_fast(FastScanArgs a) {
       }
       const float v0 = a.vterm ? a.vterm[pos0c] : 0.0f;
       const float v1 = a.vterm ? a.vterm[pos1] : 0.0f;
-      const float d0 = adc_fast(lut, a.codes + pos0c * M, M, t0 + v0);
-      const float d1 = adc_fast(lut, a.codes + pos1 * M, M, t1 + v1);
+      float d0, d1;
+      if constexpr (HALF) {
+        d0 = fmaf(lscale, adc_fast(lut, a.codes + pos0c * M, M, 0.0f), t0 + v0);
+        d1 = fmaf(lscale, adc_fast(lut, a.codes + pos1 * M, M, 0.0f), t1 + v1);
+      } else {
+        d0 = adc_fast(lut, a.codes + pos0c * M, M, t0 + v0);
+        d1 = adc_fast(lut, a.codes + pos1 * M, M, t1 + v1);
+      }
       const unsigned long long k0 = ((unsigned long long)float_to_ordered(d0) << 32) | (uint32_t)pos0c;
       const unsigned long long k1 = ((unsigned long long)float_to_ordered(d1) << 32) | (uint32_t)pos1;
       const bool in0 = keep0 && k0 < bound;
@@ -593,7 +632,8 @@ size_t fast_scan_smem(const FastScanArgs& a) {
 
 // Threads per CTA nt (128, 256 or 512); grid: one CTA per query, or with
 // a.counter a persistent grid of `persistent_ctas` CTAs.
-void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s, int nt, int persistent_ctas) {
+void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s, int nt, int persistent_ctas,
+                            bool lut_fp16) {
   if (a.nq == 0) return;
   a.cap = fast_scan_cap(a.R);
   a.Rp = next_pow2(a.R);
@@ -605,9 +645,15 @@ void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s, int nt, int persiste
     smem_attr(kernel, smem);
     kernel<<<grid, threads, smem, s>>>(a);
   };
-  if (nt == 128) go(k_ivfpq_scan_fast<128>, 128);
-  else if (nt == 512) go(k_ivfpq_scan_fast<512>, 512);
-  else go(k_ivfpq_scan_fast<256>, 256);
+  if (lut_fp16) {
+    if (nt == 128) go(k_ivfpq_scan_fast<128, true>, 128);
+    else if (nt == 512) go(k_ivfpq_scan_fast<512, true>, 512);
+    else go(k_ivfpq_scan_fast<256, true>, 256);
+  } else {
+    if (nt == 128) go(k_ivfpq_scan_fast<128, false>, 128);
+    else if (nt == 512) go(k_ivfpq_scan_fast<512, false>, 512);
+    else go(k_ivfpq_scan_fast<256, false>, 256);
+  }
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());
 }

@@ -601,9 +601,9 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
         a.counter = batch->scan_ctas_per_sm > 0 ? batch->counter : nullptr;
         if (a.counter) MV_CHECK_CUDA(cudaMemsetAsync(a.counter, 0, sizeof(int), s));
         launch_ivfpq_scan_fast(a, s, batch->scan_threads,
-                               batch->scan_ctas_per_sm * ix->ctx->num_sms);
+                               batch->scan_ctas_per_sm * ix->ctx->num_sms, p && p->lut_fp16);
       } else {
-        launch_ivfpq_scan_fast(a, s);
+        launch_ivfpq_scan_fast(a, s, 256, 0, p && p->lut_fp16);
       }
     }
     if (p && p->rerank > 0) {

@@ -58,7 +58,9 @@ void launch_coarse_from_keys(const uint64_t* cand, int64_t nq, int ncand, const 
                              const float* cent, int nlist, int metric, int nc, int nprobe,
                              int32_t* probes, float* term, int* err, cudaStream_t s);
 size_t fast_scan_smem(const FastScanArgs& a);
-void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s, int nt = 256, int persistent_ctas = 0);
+// lut_fp16: FP16 tables with a per-query power-of-two scale (FP32 sums).
+void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s, int nt = 256, int persistent_ctas = 0,
+                            bool lut_fp16 = false);
 // Flat fast form: merge nseg x ncp per-segment keys (kseg kept per segment)
 // into the R-key shortlist per query. With out_keys the shortlist is
 // written (unsorted) for the rerank; otherwise the k smallest become the

@@ -68,6 +68,8 @@ def test_fast_exhaustive_equals_flat(mv, metric):
     q = RNG.standard_normal((40, 64)).astype(np.float32)
     g = _index(mv, base, 64, 16, 8, metric)
     d, l = g.search(q, 10, form=mv.FORM_FAST, nprobe=16, rerank=3000)
+    dh, lh = g.search(q, 10, form=mv.FORM_FAST, nprobe=16, rerank=3000, lut_fp16=True)
+    assert np.array_equal(l, lh) and np.array_equal(d, dh)  # every candidate reranked
     flat = mv.IndexFlat(64, metric)
     flat.add(base)
     fd, fl = flat.search(q, 10)
@@ -98,6 +100,10 @@ def test_fast_recall_and_determinism(mv):
         assert np.array_equal(l, runs[0][1]) and np.array_equal(d, runs[0][0])
     r_rerank = recall(runs[0][1])
     assert r_rerank > r_plain + 0.2
+    # FP16 tables (per-query power-of-two scale): same recall within 0.01
+    h = [g.search(q, 10, form=mv.FORM_FAST, nprobe=32, rerank=400, lut_fp16=True) for _ in range(2)]
+    assert np.array_equal(h[0][1], h[1][1])
+    assert abs(recall(h[0][1]) - r_rerank) < 0.01
     _, lc = g.search(q, 10, form=mv.FORM_FAST, nprobe=32, rerank=400, coarse_fp32=True)
     assert abs(recall(lc) - r_rerank) < 0.02
 
