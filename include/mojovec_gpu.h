@@ -56,6 +56,7 @@ typedef struct mv_flat mv_flat;
 typedef struct mv_sq8 mv_sq8;
 typedef struct mv_ivfpq_plan mv_ivfpq_plan;
 typedef struct mv_server mv_server;
+typedef struct mv_ivfflat mv_ivfflat;
 
 /* Search options for the IVF-PQ and Flat searches. Zero-initialised means
  * the plain form with the index's own nprobe. */
@@ -228,6 +229,25 @@ int32_t mv_server_wait(mv_server* server, int64_t request_id, double* latency_s)
  * bytes (estimate)]. */
 int32_t mv_server_stats(mv_server* server, int64_t* out4);
 
+/* ---- IVF-Flat (index/index_ivf_flat.mojo:10-243) ----------------------- */
+int32_t mv_ivfflat_create(mv_ctx* ctx, int32_t d, int32_t nlist, int32_t metric, mv_ivfflat** out);
+int32_t mv_ivfflat_destroy(mv_ivfflat* index);
+int32_t mv_ivfflat_set_nprobe(mv_ivfflat* index, int32_t nprobe);
+int64_t mv_ivfflat_ntotal(mv_ivfflat* index);
+/* train (:65-77): k-means of nlist centroids, niter iterations (the
+ * reference uses 15); params->form FAST runs the fast k-means. */
+int32_t mv_ivfflat_train(mv_ivfflat* index, const float* x, int64_t n, int32_t niter,
+                         const mv_search_params* params);
+int32_t mv_ivfflat_get_centroids(mv_ivfflat* index, float* centroids);
+/* add / add_with_ids (:79-135): rows kept exactly, in list order. */
+int32_t mv_ivfflat_add(mv_ivfflat* index, const float* x, int64_t n);
+int32_t mv_ivfflat_add_with_ids(mv_ivfflat* index, const float* x, const int64_t* ids, int64_t n);
+/* search (:137-243): exact l2_distance_simd[8] / -inner_product_simd[4]
+ * over the nprobe nearest lists, tail 1e38 / -1, IP un-negated. PLAIN is
+ * bit-exact; FAST takes the probes from the BF16 coarse step. */
+int32_t mv_ivfflat_search(mv_ivfflat* index, const float* x, int64_t nq, int32_t k,
+                          const mv_search_params* params, float* distances, int64_t* labels);
+
 /* ---- Flat index: replaces IndexFlat (index/index_flat.mojo:117-330) ---- */
 int32_t mv_flat_create(mv_ctx* ctx, int32_t d, int32_t metric, mv_flat** out);
 int32_t mv_flat_destroy(mv_flat* index);
@@ -239,6 +259,13 @@ int64_t mv_flat_ntotal(mv_flat* index);
 int32_t mv_flat_search(mv_flat* index, const float* x, int64_t nq, int32_t k,
                        const uint8_t* filter, const mv_search_params* params,
                        float* distances, int64_t* labels);
+/* Exact FP32 rerank of candidate lists against the index's rows, the HNSW
+ * SQ8 shortlist rerank (index/index_hnsw.mojo:433-497): per query the k
+ * smallest l2_distance_simd[64] / -inner_product_simd[64] over its ncand
+ * candidate ids (-1 = empty slot), ascending, ties by the smaller id, tail
+ * 0.0 / -1, IP un-negated. */
+int32_t mv_flat_rerank(mv_flat* index, const float* x, int64_t nq, const int64_t* cand,
+                       int32_t ncand, int32_t k, float* distances, int64_t* labels);
 int32_t mv_flat_search_device(mv_flat* index, const float* d_x, int64_t nq, int32_t k,
                               const uint8_t* d_filter, const mv_search_params* params,
                               float* d_distances, int64_t* d_labels, void* stream);

@@ -19,6 +19,7 @@ from .index import (  # noqa: F401
     Context,
     IndexFlat,
     IndexFlatSQ8,
+    IndexIVFFlat,
     IndexIVFPQ,
     IVFPQBatchPlan,
     KMeans,

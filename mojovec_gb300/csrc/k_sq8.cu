@@ -258,8 +258,8 @@ __device__ float warp_simd64(const float* x, const float* y, int d) {
 constexpr int RR_THREADS = 256;
 
 __global__ void __launch_bounds__(RR_THREADS)
-    k_rerank_simd64(const float* __restrict__ q, int d, const float* __restrict__ base, int metric,
-                    const int64_t* __restrict__ cand, int ncand, int k, int bufcap,
+    k_rerank_simd64(const float* __restrict__ q, int d, const float* __restrict__ base, int64_t nb,
+                    int metric, const int64_t* __restrict__ cand, int ncand, int k, int bufcap,
                     uint64_t* __restrict__ out_keys) {
   extern __shared__ uint64_t skeys[];
   __shared__ int cnt;
@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(RR_THREADS)
     int c = c0 + warp;
     if (c < ncand) {
       int64_t id = cand[row * ncand + c];
-      if (id >= 0) {
+      if (id >= 0 && id < nb) {  // -1 marks an empty slot
         const float* bp = base + id * d;
         float dist = metric == MV_METRIC_L2 ? warp_simd64<false>(qp, bp, d)
                                            : -warp_simd64<true>(qp, bp, d);
@@ -385,7 +385,7 @@ void launch_sq8_matrix(const uint8_t* qc, const uint32_t* qn, int64_t nq, const 
   MV_CHECK_CUDA(cudaGetLastError());
 }
 
-void launch_rerank_simd64(const float* q, int64_t nq, int d, const float* base, int metric,
+void launch_rerank_simd64(const float* q, int64_t nq, int d, const float* base, int64_t nb, int metric,
                           const int64_t* cand, int ncand, int k, uint64_t* out_keys,
                           cudaStream_t s) {
   if (nq == 0) return;
@@ -393,8 +393,8 @@ void launch_rerank_simd64(const float* q, int64_t nq, int d, const float* base, 
   size_t smem = (size_t)BlockTopK::smem_keys(k, bufcap) * 8;
   MV_REQUIRE(smem <= 200 * 1024, MV_ERR_UNSUPPORTED, "rerank: k too large");
   smem_limit(k_rerank_simd64, smem);
-  k_rerank_simd64<<<(unsigned)nq, RR_THREADS, smem, s>>>(q, d, base, metric, cand, ncand, k, bufcap,
-                                                          out_keys);
+  k_rerank_simd64<<<(unsigned)nq, RR_THREADS, smem, s>>>(q, d, base, nb, metric, cand, ncand, k,
+                                                          bufcap, out_keys);
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());
 }

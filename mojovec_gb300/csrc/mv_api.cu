@@ -1243,6 +1243,41 @@ int32_t mv_flat_search_device(mv_flat* ix, const float* d_x, int64_t nq, int32_t
   });
 }
 
+int32_t mv_flat_rerank(mv_flat* ix, const float* x, int64_t nq, const int64_t* cand,
+                       int32_t ncand, int32_t k, float* distances, int64_t* labels) {
+  if (!ix || nq < 0 || ncand < 0 || (nq > 0 && (!x || !distances || !labels)) ||
+      (nq > 0 && ncand > 0 && !cand))
+    return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    check_search_args(nq, k);
+    if (nq == 0) return;
+    for (int64_t i = 0; i < nq * (int64_t)ncand; ++i)
+      MV_REQUIRE(cand[i] >= -1 && cand[i] < ix->ntotal, MV_ERR_ARG,
+                 "candidate ids must be -1 or rows of the index");
+    SlotLease lease(ix->ctx);
+    cudaStream_t s = lease.stream();
+    DevBuf& io = lease.slot->io;
+    io.ensure(ws_bytes((size_t)nq * ix->d, 4) + ws_bytes((size_t)nq * ncand + 1, 8) +
+              ws_bytes((size_t)nq * k, 8) + ws_bytes((size_t)nq * k, 4) +
+              ws_bytes((size_t)nq * k, 8));
+    Arena ar(io);
+    float* dx = ar.take<float>((size_t)nq * ix->d);
+    int64_t* dc = ar.take<int64_t>((size_t)nq * ncand + 1);
+    uint64_t* keys = ar.take<uint64_t>((size_t)nq * k);
+    float* dd = ar.take<float>((size_t)nq * k);
+    int64_t* dl = ar.take<int64_t>((size_t)nq * k);
+    h2d(dx, x, sizeof(float) * nq * ix->d, s);
+    if (ncand > 0) h2d(dc, cand, sizeof(int64_t) * nq * ncand, s);
+    launch_rerank_simd64(dx, nq, ix->d, ix->rows.as<float>(), ix->ntotal, ix->metric, dc, ncand, k,
+                         keys, s);
+    // index_hnsw.mojo:486-497: ascending, tail 0.0 / -1, IP un-negated
+    launch_keys_to_results(keys, nq, k, 0.0f, ix->metric == MV_METRIC_IP, dd, dl, s);
+    d2h(distances, dd, sizeof(float) * nq * k, s);
+    d2h(labels, dl, sizeof(int64_t) * nq * k, s);
+    check_kernel_errors(ix->ctx, s);
+  });
+}
+
 int32_t mv_flat_search(mv_flat* ix, const float* x, int64_t nq, int32_t k, const uint8_t* filter,
                        const mv_search_params* params, float* distances, int64_t* labels) {
   if (!ix || (nq > 0 && (!x || !distances || !labels))) return MV_ERR_ARG;
@@ -1435,8 +1470,8 @@ void sq8_search_impl(mv_sq8* ix, const float* d_x, int64_t nq, int k, int rerank
   k_keys_to_cand<<<(unsigned)((nq * kk + 255) / 256), 256, 0, s>>>(keys.as<uint64_t>(), nq * kk,
                                                                   cand.as<int64_t>());
   count_launch();
-  launch_rerank_simd64(d_x, nq, ix->d, ix->f32.as<float>(), ix->metric, cand.as<int64_t>(), kk, k,
-                       fk.as<uint64_t>(), s);
+  launch_rerank_simd64(d_x, nq, ix->d, ix->f32.as<float>(), ix->ntotal, ix->metric,
+                       cand.as<int64_t>(), kk, k, fk.as<uint64_t>(), s);
   launch_keys_to_results(fk.as<uint64_t>(), nq, k, 0.0f, ip, d_out, d_lab, s);
   sync(s);
 }
@@ -2120,6 +2155,291 @@ int32_t mv_ivfpq_search_batch(mv_ivfpq* ix, const float* x, int64_t nq, const in
   });
   mv_ivfpq_plan_destroy(pl);
   return st;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// IVF-Flat (index/index_ivf_flat.mojo)
+// ---------------------------------------------------------------------------
+namespace mv {
+
+// index_ivf_flat.mojo:91-135: nearest centroid (quantizer search k = 1),
+// rows appended to their list in input order.
+void ivfflat_add(mv_ivfflat* ix, const float* x, const int64_t* ids, int64_t n) {
+  if (!ix->trained || n == 0) return;  // :103-105
+  for (int64_t i = 0; i < n; ++i)
+    MV_REQUIRE(ids[i] >= 0 && ids[i] <= 0xfffffffell, MV_ERR_ARG,
+               "ids must be in [0, 2^32 - 2] for the GPU index");
+  SlotLease lease(ix->ctx);
+  cudaStream_t s = lease.stream();
+  const int d = ix->d, nlist = ix->nlist;
+  std::vector<int32_t> h_assign(n);
+  DevBuf new_rows;
+  new_rows.ensure((size_t)n * d * 4 + 16);
+  h2d(new_rows.p, x, sizeof(float) * n * d, s);
+  {
+    DevBuf& ws = lease.slot->ws;
+    ws.ensure(ws_bytes(n, 4));
+    int32_t* assign = ws.as<int32_t>();
+    const int kind = ix->metric == MV_METRIC_L2 ? KIND_L2_SIMD8 : KIND_IP_SIMD8;
+    launch_exact_argmin(kind, 2, new_rows.as<float>(), n, d, ix->centroids.as<float>(), nlist, d,
+                        d, assign, nullptr, 1, 0, 0, 0, s);
+    d2h(h_assign.data(), assign, sizeof(int32_t) * n, s);
+    sync(s);
+  }
+  const std::vector<int64_t> old_off = ix->h_off;
+  std::vector<int64_t> add_cnt(nlist, 0);
+  int64_t kept = 0;
+  for (int64_t i = 0; i < n; ++i)
+    if (h_assign[i] >= 0 && h_assign[i] < nlist) {
+      add_cnt[h_assign[i]]++;
+      kept++;
+    }
+  std::vector<int64_t> new_off(nlist + 1, 0);
+  for (int l = 0; l < nlist; ++l)
+    new_off[l + 1] = new_off[l] + (old_off[l + 1] - old_off[l]) + add_cnt[l];
+  const int64_t old_total = old_off[nlist], new_total = old_total + kept;
+  std::vector<int64_t> pos_old(old_total), pos_new(n), fill(nlist);
+  for (int l = 0; l < nlist; ++l) {
+    for (int64_t p = old_off[l]; p < old_off[l + 1]; ++p) pos_old[p] = p - old_off[l] + new_off[l];
+    fill[l] = new_off[l] + (old_off[l + 1] - old_off[l]);
+  }
+  std::vector<uint32_t> ids32(n);
+  int64_t dropped = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    ids32[i] = (uint32_t)ids[i];
+    const int l = h_assign[i];
+    pos_new[i] = (l < 0 || l >= nlist) ? new_total + dropped++ : fill[l]++;  // :126
+  }
+  const int64_t cap = new_total + dropped;
+  DevBuf off_d, ids_d, rows_d, pos_d, ids_new;
+  off_d.ensure(sizeof(int64_t) * (nlist + 1));
+  ids_d.ensure(sizeof(uint32_t) * cap + 16);
+  rows_d.ensure(sizeof(float) * cap * d + 16);
+  pos_d.ensure(sizeof(int64_t) * (old_total + n) + 16);
+  ids_new.ensure(sizeof(uint32_t) * n + 16);
+  h2d(off_d.p, new_off.data(), sizeof(int64_t) * (nlist + 1), s);
+  h2d(pos_d.p, pos_old.data(), sizeof(int64_t) * old_total, s);
+  h2d(pos_d.as<int64_t>() + old_total, pos_new.data(), sizeof(int64_t) * n, s);
+  h2d(ids_new.p, ids32.data(), sizeof(uint32_t) * n, s);
+  if (old_total) {
+    scatter_rows(ix->d_ids.p, old_total, 4, pos_d.as<int64_t>(), ids_d.p, s);
+    scatter_rows(ix->d_rows.p, old_total, 4 * d, pos_d.as<int64_t>(), rows_d.p, s);
+  }
+  scatter_rows(ids_new.p, n, 4, pos_d.as<int64_t>() + old_total, ids_d.p, s);
+  scatter_rows(new_rows.p, n, 4 * d, pos_d.as<int64_t>() + old_total, rows_d.p, s);
+  sync(s);
+  std::swap(ix->d_off.p, off_d.p);
+  std::swap(ix->d_off.bytes, off_d.bytes);
+  std::swap(ix->d_ids.p, ids_d.p);
+  std::swap(ix->d_ids.bytes, ids_d.bytes);
+  std::swap(ix->d_rows.p, rows_d.p);
+  std::swap(ix->d_rows.bytes, rows_d.bytes);
+  ix->h_off = new_off;
+  ix->ntotal += n;  // :135
+}
+
+// Search: plain = the reference's coarse step (exact FP32, canonical
+// top-nprobe) then the exact scan; fast = BF16 coarse (fused top-k GEMM or
+// distance matrix) with an exact FP32 recheck, then the same exact scan.
+void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int nprobe,
+                    const mv_search_params* p, float* d_out, int64_t* d_lab, DevBuf& ws,
+                    cudaStream_t s) {
+  if (nq == 0) return;
+  if (!ix->trained || ix->ntotal == 0) {  // :176-180
+    launch_fill(d_out, d_lab, nq * k, 1e38f, s);
+    return;
+  }
+  MV_REQUIRE(nprobe <= 8192, MV_ERR_UNSUPPORTED, "nprobe above 8192 is not supported on the GPU");
+  const bool fast = p && p->form == MV_FORM_FAST && umma_kpad(ix->d) <= 256;
+  const int kp = umma_kpad(ix->d);
+  const int nc = std::min(ix->nlist, nprobe + std::max(8, nprobe / 4));
+  const bool fused = fast && nc <= 64;
+  if (fast) {
+    std::lock_guard<std::mutex> lk(ix->fast_mu);
+    if (!ix->fast_ready) {
+      ix->d_cent_bf16.ensure((size_t)ix->nlist * kp * 2);
+      ix->d_cnorm.ensure((size_t)ix->nlist * 4);
+      launch_to_bf16(ix->centroids.as<float>(), ix->nlist, ix->d,
+                     ix->d_cent_bf16.as<__nv_bfloat16>(), ix->d_cnorm.as<float>(), s);
+      sync(s);
+      ix->fast_ready = true;
+    }
+  }
+  int64_t qb = std::max<int64_t>(64, (int64_t)(1536ll * 1024 * 1024 / ((int64_t)ix->nlist * 4)));
+  qb = std::min<int64_t>({qb, nq, 65535ll * 64});
+  const int nseg = fused ? umma_topk_nseg(qb, ix->nlist, ix->d, nc, ix->ctx->num_sms) : 1;
+  const int ncand = nseg * (fused ? umma_topk_groups(ix->d, nc) : 1) * next_pow2(nc);
+  ws.ensure(ws_bytes((size_t)qb * ix->nlist, 4) + ws_bytes((size_t)qb * nprobe, 8) +
+            ws_bytes((size_t)qb * nprobe, 4) * 2 + ws_bytes((size_t)qb * kp, 2) +
+            ws_bytes((size_t)qb * ncand, 8) + ws_bytes((size_t)qb, 8));
+  Arena ar(ws);
+  float* dmat = ar.take<float>((size_t)qb * ix->nlist);
+  uint64_t* ckeys = ar.take<uint64_t>((size_t)qb * nprobe);
+  int32_t* probes = ar.take<int32_t>((size_t)qb * nprobe);
+  float* term = ar.take<float>((size_t)qb * nprobe);
+  __nv_bfloat16* xq = ar.take<__nv_bfloat16>((size_t)qb * kp);
+  uint64_t* fkeys = ar.take<uint64_t>((size_t)qb * ncand);
+  uint64_t* gthr = ar.take<uint64_t>((size_t)qb);
+  const int kind = ix->metric == MV_METRIC_L2 ? KIND_L2_SIMD8 : KIND_IP_SIMD8;
+  for (int64_t q0 = 0; q0 < nq; q0 += qb) {
+    const int64_t nb = std::min(qb, nq - q0);
+    const float* xb = d_x + q0 * ix->d;
+    {
+      StageTimer t(ix->ctx, MV_STAGE_COARSE, s);
+      if (!fast) {
+        launch_exact_matrix(kind, xb, nb, ix->d, ix->centroids.as<float>(), ix->nlist, ix->d,
+                            ix->d, dmat, ix->nlist, s);
+      } else {
+        launch_to_bf16(xb, nb, ix->d, xq, nullptr, s);
+        if (fused)
+          launch_umma_topk(xq, nb, ix->d_cent_bf16.as<__nv_bfloat16>(), ix->nlist, ix->d,
+                           ix->metric, nullptr, ix->d_cnorm.as<float>(), nc, nseg, nullptr,
+                           ncand > next_pow2(nc) ? gthr : nullptr, fkeys, ix->ctx->d_err.as<int>(),
+                           s);
+        else
+          launch_umma_dist(EPI_MATRIX, xq, nb, ix->d_cent_bf16.as<__nv_bfloat16>(), ix->nlist,
+                           ix->d, ix->metric, nullptr, ix->d_cnorm.as<float>(), dmat, ix->nlist,
+                           nullptr, ix->ctx->d_err.as<int>(), ix->ctx->num_sms, s);
+      }
+    }
+    {
+      StageTimer t(ix->ctx, MV_STAGE_SELECT, s);
+      if (!fast) {  // :185-194 coarse quantizer search with k = nprobe
+        launch_select_rows(dmat, nb, ix->nlist, ix->nlist, 0, nprobe, nullptr, ckeys, nullptr, s);
+        launch_keys_to_ids(ckeys, nb * nprobe, probes, s);
+      } else if (fused) {
+        launch_coarse_from_keys(fkeys, nb, ncand, xb, ix->d, ix->centroids.as<float>(), ix->nlist,
+                                ix->metric, nc, nprobe, probes, term, ix->ctx->d_err.as<int>(), s);
+      } else {
+        launch_coarse_fast(dmat, nb, ix->nlist, xb, ix->d, ix->centroids.as<float>(), ix->metric,
+                           nc, nprobe, probes, term, ix->ctx->d_err.as<int>(), s);
+      }
+    }
+    StageTimer t(ix->ctx, MV_STAGE_SCAN, s);
+    launch_ivfflat_scan(xb, nb, ix->d, ix->metric, probes, nprobe, ix->nlist,
+                        ix->d_off.as<int64_t>(), ix->d_rows.as<float>(), ix->d_ids.as<uint32_t>(),
+                        k, d_out + q0 * k, d_lab + q0 * k, s);
+  }
+}
+
+}  // namespace mv
+
+extern "C" {
+
+int32_t mv_ivfflat_create(mv_ctx* ctx, int32_t d, int32_t nlist, int32_t metric, mv_ivfflat** out) {
+  if (!ctx || !out) return MV_ERR_ARG;
+  *out = nullptr;
+  return guard(ctx, [&] {
+    MV_REQUIRE(d > 0 && d <= 65536, MV_ERR_ARG, "dimension must be between 1 and 65536.");
+    MV_REQUIRE(nlist > 0 && nlist <= 1000000, MV_ERR_ARG, "IVF nlist must be between 1 and 1000000.");
+    MV_REQUIRE(metric == MV_METRIC_L2 || metric == MV_METRIC_IP, MV_ERR_ARG, "unknown metric");
+    auto ix = std::make_unique<mv_ivfflat>();
+    ix->ctx = ctx;
+    ix->d = d;
+    ix->nlist = nlist;
+    ix->metric = metric;
+    ix->centroids.ensure(sizeof(float) * nlist * d);
+    ix->h_off.assign(nlist + 1, 0);
+    ix->d_off.ensure(sizeof(int64_t) * (nlist + 1));
+    MV_CHECK_CUDA(cudaMemset(ix->d_off.p, 0, sizeof(int64_t) * (nlist + 1)));
+    *out = ix.release();
+  });
+}
+
+int32_t mv_ivfflat_destroy(mv_ivfflat* ix) {
+  if (!ix) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    cudaDeviceSynchronize();
+    delete ix;
+  });
+}
+
+int32_t mv_ivfflat_set_nprobe(mv_ivfflat* ix, int32_t nprobe) {
+  if (!ix || nprobe < 1) return MV_ERR_ARG;
+  ix->nprobe = nprobe;
+  return MV_OK;
+}
+
+int64_t mv_ivfflat_ntotal(mv_ivfflat* ix) { return ix ? ix->ntotal : -1; }
+
+int32_t mv_ivfflat_train(mv_ivfflat* ix, const float* x, int64_t n, int32_t niter,
+                         const mv_search_params* params) {
+  if (!ix || (!x && n > 0) || niter < 0) return MV_ERR_ARG;
+  const int form = params ? params->form : MV_FORM_PLAIN;
+  return guard(ix->ctx, [&] {
+    std::lock_guard<std::mutex> lk(ix->mu);
+    if (ix->trained) return;  // :71
+    MV_REQUIRE(n > 0, MV_ERR_ARG, "training needs at least one vector");
+    SlotLease lease(ix->ctx);
+    cudaStream_t s = lease.stream();
+    DevBuf dx, assign, scratch;
+    dx.ensure(sizeof(float) * n * ix->d);
+    assign.ensure(sizeof(int32_t) * n);
+    h2d(dx.p, x, sizeof(float) * n * ix->d, s);
+    // :73-77 KMeans(d, nlist, 15)
+    if (form == MV_FORM_FAST && umma_kpad(ix->d) <= 256)
+      kmeans_train_fast(dx.as<float>(), n, ix->d, ix->nlist, niter, ix->centroids.as<float>(),
+                        assign.as<int32_t>(), scratch, ix->ctx, s, nullptr);
+    else
+      kmeans_train_device(dx.as<float>(), n, ix->d, ix->nlist, niter, 1, ix->centroids.as<float>(),
+                          assign.as<int32_t>(), scratch, s);
+    sync(s);
+    ix->trained = true;
+    ix->fast_ready = false;
+  });
+}
+
+int32_t mv_ivfflat_get_centroids(mv_ivfflat* ix, float* out) {
+  if (!ix || !out) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    MV_CHECK_CUDA(cudaMemcpy(out, ix->centroids.p, sizeof(float) * ix->nlist * ix->d,
+                             cudaMemcpyDeviceToHost));
+  });
+}
+
+int32_t mv_ivfflat_add_with_ids(mv_ivfflat* ix, const float* x, const int64_t* ids, int64_t n) {
+  if (!ix || n < 0 || (n > 0 && (!x || !ids))) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    std::lock_guard<std::mutex> lk(ix->mu);
+    ivfflat_add(ix, x, ids, n);
+  });
+}
+
+int32_t mv_ivfflat_add(mv_ivfflat* ix, const float* x, int64_t n) {
+  if (!ix || n < 0 || (n > 0 && !x)) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    std::lock_guard<std::mutex> lk(ix->mu);
+    std::vector<int64_t> ids(n);
+    for (int64_t i = 0; i < n; ++i) ids[i] = ix->ntotal + i;  // :86-89
+    ivfflat_add(ix, x, ids.data(), n);
+  });
+}
+
+int32_t mv_ivfflat_search(mv_ivfflat* ix, const float* x, int64_t nq, int32_t k,
+                          const mv_search_params* params, float* distances, int64_t* labels) {
+  if (!ix || (nq > 0 && (!x || !distances || !labels))) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    check_search_args(nq, k);
+    if (nq == 0) return;
+    int nprobe = params && params->nprobe > 0 ? params->nprobe : ix->nprobe;
+    nprobe = std::min(nprobe, ix->nlist);  // :182-183
+    SlotLease lease(ix->ctx);
+    cudaStream_t s = lease.stream();
+    DevBuf& io = lease.slot->io;
+    io.ensure(ws_bytes((size_t)nq * ix->d, 4) + ws_bytes((size_t)nq * k, 4) +
+              ws_bytes((size_t)nq * k, 8));
+    Arena ar(io);
+    float* dx = ar.take<float>((size_t)nq * ix->d);
+    float* dd = ar.take<float>((size_t)nq * k);
+    int64_t* dl = ar.take<int64_t>((size_t)nq * k);
+    h2d(dx, x, sizeof(float) * nq * ix->d, s);
+    ivfflat_search(ix, dx, nq, k, nprobe, params, dd, dl, lease.slot->ws, s);
+    d2h(distances, dd, sizeof(float) * nq * k, s);
+    d2h(labels, dl, sizeof(int64_t) * nq * k, s);
+    check_kernel_errors(ix->ctx, s);
+  });
 }
 
 }  // extern "C"

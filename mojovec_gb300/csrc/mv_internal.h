@@ -203,6 +203,22 @@ struct mv_ivfpq {
   mv::DevBuf d_cent_bf16;   // nlist x d BF16
 };
 
+struct mv_ivfflat {
+  mv_ctx* ctx;
+  int d, nlist, metric, nprobe = 1;
+  bool trained = false;
+  int64_t ntotal = 0;
+  std::mutex mu;
+  mv::DevBuf centroids;           // nlist x d FP32 (quantizer rows)
+  std::vector<int64_t> h_off;     // nlist + 1
+  mv::DevBuf d_off;               // int64 nlist + 1
+  mv::DevBuf d_ids;               // uint32 per entry
+  mv::DevBuf d_rows;              // FP32 rows per entry, in list order
+  std::mutex fast_mu;
+  bool fast_ready = false;
+  mv::DevBuf d_cent_bf16, d_cnorm;  // fast coarse step
+};
+
 struct mv_flat {
   mv_ctx* ctx;
   int d, metric;

@@ -113,6 +113,11 @@ void launch_km_update_fp64(const float* x, int64_t n, int d, int k, const int32_
 // out = sum of v in FP64 in a fixed order (part256: 256 doubles of scratch).
 void launch_sum_fp64(const float* v, int64_t n, double* part256, double* out, cudaStream_t s);
 
+// IVF-Flat scan of the probed lists (k_ivfflat.cu).
+void launch_ivfflat_scan(const float* q, int64_t nq, int d, int metric, const int32_t* probes,
+                         int nprobe, int nlist, const int64_t* list_off, const float* rows,
+                         const uint32_t* ids, int k, float* out_d, int64_t* out_l, cudaStream_t s);
+
 // SQ8 codes as BF16 rows (kp wide) and FP32 norms, for the tensor-core scan.
 void launch_sq8_codes_to_bf16(const uint8_t* codes, int64_t n, int d, int dpad, int kp,
                               bool symmetric, const uint32_t* norms, __nv_bfloat16* out,
@@ -122,7 +127,7 @@ void launch_sq8_matrix(const uint8_t* qc, const uint32_t* qn, int64_t nq, const 
                        float* D, int64_t ldd, cudaStream_t s);
 // Exact FP32 rerank of candidate ids (cand rows x ncand, -1 = none) with
 // l2_distance_simd[64] / -inner_product_simd[64]; keys out rows x k.
-void launch_rerank_simd64(const float* q, int64_t nq, int d, const float* base, int metric,
+void launch_rerank_simd64(const float* q, int64_t nq, int d, const float* base, int64_t nb, int metric,
                           const int64_t* cand, int ncand, int k, uint64_t* out_keys,
                           cudaStream_t s);
 

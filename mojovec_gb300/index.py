@@ -214,6 +214,63 @@ class IndexIVFPQ:
                                                  dist_ptr, lab_ptr, stream or None))
 
 
+class IndexIVFFlat:
+    """IVF-Flat index on the GPU (index/index_ivf_flat.mojo:10)."""
+
+    def __init__(self, d: int, nlist: int, metric: int = METRIC_L2, ctx: Context | None = None):
+        self.ctx = ctx or Context.default()
+        h = C.c_void_p()
+        check(_lib.load().mv_ivfflat_create(self.ctx.handle, d, nlist, metric, C.byref(h)))
+        self._h = h
+        self.d, self.nlist, self.metric_type = d, nlist, metric
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib._lib is not None:
+            _lib._lib.mv_ivfflat_destroy(h)
+            self._h = None
+
+    @property
+    def ntotal(self) -> int:
+        return int(_lib.load().mv_ivfflat_ntotal(self._h))
+
+    @property
+    def nprobe(self) -> int:
+        return getattr(self, "_nprobe", 1)
+
+    @nprobe.setter
+    def nprobe(self, v: int):
+        check(_lib.load().mv_ivfflat_set_nprobe(self._h, int(v)))
+        self._nprobe = int(v)
+
+    def train(self, x, niter: int = 15, form=None):
+        x = _f32(x, self.d)
+        p = _params(form)
+        check(_lib.load().mv_ivfflat_train(self._h, _p(x), x.shape[0], niter, C.byref(p)))
+
+    def centroids(self):
+        out = np.zeros((self.nlist, self.d), np.float32)
+        check(_lib.load().mv_ivfflat_get_centroids(self._h, _p(out)))
+        return out
+
+    def add(self, x, ids=None):
+        x = _f32(x, self.d)
+        if ids is None:
+            check(_lib.load().mv_ivfflat_add(self._h, _p(x), x.shape[0]))
+        else:
+            ids = np.ascontiguousarray(ids, dtype=np.int64)
+            check(_lib.load().mv_ivfflat_add_with_ids(self._h, _p(x), _p(ids), x.shape[0]))
+
+    def search(self, x, k: int, nprobe: int = 0, form=None):
+        x = _f32(x, self.d)
+        n = x.shape[0]
+        dist = np.empty((n, k), np.float32)
+        lab = np.empty((n, k), np.int64)
+        p = _params(form, nprobe)
+        check(_lib.load().mv_ivfflat_search(self._h, _p(x), n, k, C.byref(p), _p(dist), _p(lab)))
+        return dist, lab
+
+
 class IndexFlat:
     """Exact index over raw FP32 rows (index/index_flat.mojo:117)."""
 
@@ -246,6 +303,18 @@ class IndexFlat:
         flt = None if filter is None else np.ascontiguousarray(filter, dtype=np.uint8)
         p = _params(form, 0, rerank)
         check(_lib.load().mv_flat_search(self._h, _p(x), n, k, _p(flt), C.byref(p), _p(dist),
+                                         _p(lab)))
+        return dist, lab
+
+    def rerank(self, x, cand, k: int):
+        """Exact FP32 rerank of candidate ids (n, ncand; -1 = empty) against
+        this index's rows (the HNSW SQ8 shortlist rerank)."""
+        x = _f32(x, self.d)
+        n = x.shape[0]
+        cand = np.ascontiguousarray(cand, dtype=np.int64).reshape(n, -1)
+        dist = np.empty((n, k), np.float32)
+        lab = np.empty((n, k), np.int64)
+        check(_lib.load().mv_flat_rerank(self._h, _p(x), n, _p(cand), cand.shape[1], k, _p(dist),
                                          _p(lab)))
         return dist, lab
 

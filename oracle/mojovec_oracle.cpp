@@ -761,6 +761,85 @@ void ivfpq_search(const IVFPQ& ix, const float* x, int64_t n, int64_t k, int64_t
 }
 
 // ---------------------------------------------------------------------------
+// IndexIVFFlat (index/index_ivf_flat.mojo:10-243): coarse k-means of 15
+// iterations (:65-77), rows appended to the list of their nearest centroid
+// in input order (:91-135), search over the nprobe nearest lists with
+// l2_distance_simd[8] or -inner_product_simd[4] (:176-243; the filter
+// argument is not applied there), tail 1e38 / -1, IP un-negated.
+// ---------------------------------------------------------------------------
+struct IVFFlat {
+  int d, nlist, metric;
+  bool trained = false;
+  int64_t ntotal = 0;
+  std::vector<float> centroids;
+  std::vector<std::vector<int64_t>> list_ids;
+  std::vector<std::vector<float>> list_rows;
+};
+
+void ivfflat_train(IVFFlat& ix, const float* x, int64_t n, int niter, int nthreads) {
+  if (ix.trained) return;  // :71
+  ix.centroids.assign((size_t)ix.nlist * ix.d, 0.0f);
+  kmeans_train(x, n, ix.d, ix.nlist, niter, nthreads, ix.centroids.data(), nullptr);
+  ix.trained = true;
+}
+
+void ivfflat_add_with_ids(IVFFlat& ix, const float* x, int64_t n, const int64_t* ids, int nthreads) {
+  if (!ix.trained) return;  // :103-105
+  std::vector<float> dd(n);
+  std::vector<int64_t> lab(n);
+  flat_search(ix.centroids.data(), ix.nlist, ix.d, ix.metric, x, n, 1, nullptr, 0, dd.data(),
+              lab.data(), nthreads);  // :117, quantizer.search(x, 1)
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t l = lab[i];
+    if (l < 0 || l >= ix.nlist) continue;  // :126
+    ix.list_ids[l].push_back(ids[i]);
+    ix.list_rows[l].insert(ix.list_rows[l].end(), x + i * ix.d, x + (i + 1) * ix.d);
+  }
+  ix.ntotal += n;
+}
+
+void ivfflat_search(const IVFFlat& ix, const float* x, int64_t n, int64_t k, int64_t nprobe,
+                    int mode, float* distances, int64_t* labels, int nthreads) {
+  if (!ix.trained || ix.ntotal == 0) {  // :176-180
+    for (int64_t i = 0; i < n * k; ++i) {
+      distances[i] = 1e38f;
+      labels[i] = -1;
+    }
+    return;
+  }
+  if (nprobe > ix.nlist) nprobe = ix.nlist;  // :182-183
+  std::vector<float> qd((size_t)n * nprobe);
+  std::vector<int64_t> ql((size_t)n * nprobe);
+  flat_search(ix.centroids.data(), ix.nlist, ix.d, ix.metric, x, n, nprobe, nullptr, mode,
+              qd.data(), ql.data(), nthreads);
+  parallel_for(n, nthreads, [&](int64_t i) {
+    const float* qp = x + i * ix.d;
+    float* rd = distances + i * k;
+    int64_t* rl = labels + i * k;
+    for (int64_t j = 0; j < k; ++j) {  // :201-203
+      rd[j] = 1e38f;
+      rl[j] = -1;
+    }
+    TopK top(mode, k, rd, rl);
+    for (int64_t p = 0; p < nprobe; ++p) {
+      const int64_t list_no = ql[i * nprobe + p];
+      if (list_no < 0 || list_no >= ix.nlist) continue;
+      const auto& ids = ix.list_ids[list_no];
+      const float* rows = ix.list_rows[list_no].data();
+      for (size_t j = 0; j < ids.size(); ++j) {
+        const float* bp = rows + j * ix.d;
+        const float dist = ix.metric == METRIC_L2 ? l2_simd<8>(qp, bp, ix.d)
+                                                  : -ip_simd<4>(qp, bp, ix.d);  // :222-226
+        top.push(dist, ids[j]);
+      }
+    }
+    const int64_t cnt = top.finish();
+    if (ix.metric == METRIC_IP)
+      for (int64_t j = 0; j < cnt; ++j) rd[j] = -rd[j];  // :241-243
+  });
+}
+
+// ---------------------------------------------------------------------------
 // SQ8 codec (quantization/sq8.mojo) and IndexFlatSQ8
 // (index/index_flat_sq8.mojo:286-526)
 // ---------------------------------------------------------------------------
@@ -1017,6 +1096,34 @@ void orc_ivfpq_search(void* h, const float* x, int64_t n, int64_t k, int64_t npr
 }
 
 // --- SQ8 handle ---
+void* orc_ivfflat_create(int d, int nlist, int metric) {
+  auto* ix = new IVFFlat();
+  ix->d = d;
+  ix->nlist = nlist;
+  ix->metric = metric;
+  ix->list_ids.resize(nlist);
+  ix->list_rows.resize(nlist);
+  return ix;
+}
+void orc_ivfflat_destroy(void* h) { delete static_cast<IVFFlat*>(h); }
+void orc_ivfflat_train(void* h, const float* x, int64_t n, int niter, int nthreads) {
+  ivfflat_train(*static_cast<IVFFlat*>(h), x, n, niter, nthreads);
+}
+void orc_ivfflat_add(void* h, const float* x, int64_t n, int nthreads) {
+  auto* ix = static_cast<IVFFlat*>(h);
+  std::vector<int64_t> ids(n);
+  for (int64_t i = 0; i < n; ++i) ids[i] = ix->ntotal + i;  // :86-89
+  ivfflat_add_with_ids(*ix, x, n, ids.data(), nthreads);
+}
+void orc_ivfflat_centroids(void* h, float* out) {
+  auto* ix = static_cast<IVFFlat*>(h);
+  std::copy(ix->centroids.begin(), ix->centroids.end(), out);
+}
+void orc_ivfflat_search(void* h, const float* x, int64_t n, int64_t k, int64_t nprobe, int mode,
+                        float* distances, int64_t* labels, int nthreads) {
+  ivfflat_search(*static_cast<IVFFlat*>(h), x, n, k, nprobe, mode, distances, labels, nthreads);
+}
+
 void* orc_sq8_create(int d, int metric) {
   auto* s = new SQ8();
   s->d = d;

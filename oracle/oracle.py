@@ -76,6 +76,12 @@ def lib():
     _sig(L, "orc_ivfpq_set_lists", None, [_vp, _i64p, _i64p, _u8p])
     _sig(L, "orc_ivfpq_search", None,
          [_vp, _f32p, _i64, _i64, _i64, _vp, _i64, _int, _f32p, _i64p, _int, _int])
+    _sig(L, "orc_ivfflat_create", _vp, [_int, _int, _int])
+    _sig(L, "orc_ivfflat_destroy", None, [_vp])
+    _sig(L, "orc_ivfflat_train", None, [_vp, _f32p, _i64, _int, _int])
+    _sig(L, "orc_ivfflat_add", None, [_vp, _f32p, _i64, _int])
+    _sig(L, "orc_ivfflat_centroids", None, [_vp, _f32p])
+    _sig(L, "orc_ivfflat_search", None, [_vp, _f32p, _i64, _i64, _i64, _int, _f32p, _i64p, _int])
     _sig(L, "orc_sq8_create", _vp, [_int, _int])
     _sig(L, "orc_sq8_destroy", None, [_vp])
     _sig(L, "orc_sq8_add", None, [_vp, _f32p, _i64])
@@ -290,6 +296,41 @@ class IVFPQ:
 
 
 # --- index/index_flat_sq8.mojo ----------------------------------------------
+class IVFFlat:
+    """IndexIVFFlat restated (index/index_ivf_flat.mojo)."""
+
+    def __init__(self, d, nlist, metric=METRIC_L2):
+        self.d, self.nlist, self.metric = d, nlist, metric
+        self._h = lib().orc_ivfflat_create(d, nlist, metric)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().orc_ivfflat_destroy(h)
+            self._h = None
+
+    def train(self, x, niter=15, nthreads=0):
+        x = _f32(x)
+        lib().orc_ivfflat_train(self._h, x, x.shape[0], niter, _threads(nthreads))
+
+    def add(self, x, nthreads=0):
+        x = _f32(x)
+        lib().orc_ivfflat_add(self._h, x, x.shape[0], _threads(nthreads))
+
+    def centroids(self):
+        out = np.zeros((self.nlist, self.d), np.float32)
+        lib().orc_ivfflat_centroids(self._h, out)
+        return out
+
+    def search(self, q, k, nprobe, mode=MODE_CANONICAL, nthreads=0):
+        q = _f32(q)
+        n = q.shape[0]
+        dist = np.zeros((n, k), np.float32)
+        lab = np.zeros((n, k), np.int64)
+        lib().orc_ivfflat_search(self._h, q, n, k, nprobe, mode, dist, lab, _threads(nthreads))
+        return dist, lab
+
+
 class SQ8:
     """Restatement of IndexFlatSQ8 (index/index_flat_sq8.mojo:271)."""
 

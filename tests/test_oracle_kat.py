@@ -262,3 +262,19 @@ def test_golden_fixtures(orc):
         assert np.array_equal(norms, g[f"sq8_m{metric}_norms"])
         dd, ll = s.search(g["sq8_a"][:8], 5)
         assert np.array_equal(dd, g[f"sq8_m{metric}_dist"]) and np.array_equal(ll, g[f"sq8_m{metric}_labels"])
+
+
+def test_oracle_ivfflat_known_answers(orc):
+    # tests/test_ivf_flat.mojo exact match and sparse tail, on the restatement
+    row = np.arange(4, dtype=np.float32)[None, :]
+    o = orc.IVFFlat(4, 1, 0)
+    o.train(row)
+    o.add(row)
+    d, l = o.search(row, 1, 1)
+    assert l[0, 0] == 0 and abs(d[0, 0]) < 1e-6
+    z = np.zeros((1, 4), np.float32)
+    t = orc.IVFFlat(4, 1, 0)
+    t.train(z)
+    t.add(z)
+    d, l = t.search(z, 5, 1)
+    assert l[0].tolist() == [0, -1, -1, -1, -1] and (d[0, 1:] == 1e38).all()
