@@ -131,6 +131,30 @@ int32_t mv_ivfpq_add_with_ids(mv_ivfpq* index, const float* x, const int64_t* id
 /* Exports the inverted lists as CSR: offsets[nlist+1], ids[ntotal],
  * codes[ntotal*M] (storage/inverted_lists.mojo:93-117 per list). */
 int32_t mv_ivfpq_get_lists(mv_ivfpq* index, int64_t* offsets, int64_t* ids, uint8_t* codes);
+/* Replaces the inverted lists with CSR data (offsets nlist + 1, ids and
+ * M-byte codes per entry), e.g. lists built by the reference. Such an index
+ * has no rows: the plain search and the fast form without rerank work. */
+int32_t mv_ivfpq_set_lists(mv_ivfpq* index, const int64_t* offsets, const int64_t* ids,
+                           const uint8_t* codes);
+/* CollectionIVFPQ snapshots (api/collection_ivfpq.mojo:335-476): the
+ * collection header (name, metric "l2" / "cosine" / "ip", user ids), the
+ * IndexIVFPQ body (io/serialization.mojo:1024-1090) and the checksum trailer
+ * (io/snapshot_file.mojo:64-108). load applies the reference's validation and
+ * builds the device CSR directly; the loaded index carries no FP32 rows (the
+ * snapshot has none), so the fast form runs without rerank. save writes the
+ * same bytes the reference would for these lists (capacity written as size),
+ * through a temporary file and a rename. */
+int32_t mv_ivfpq_load_snapshot(mv_ctx* ctx, const char* path, mv_ivfpq** out);
+int32_t mv_ivfpq_save_snapshot(mv_ivfpq* index, const char* path, const char* name,
+                               const char* metric, const int64_t* user_ids, int64_t num_ids);
+/* Collection metadata of a loaded snapshot: name and metric as
+ * NUL-terminated strings (truncated to the buffer), user ids (num_ids of
+ * them, indexed by internal id). Any output may be NULL. */
+int32_t mv_ivfpq_snapshot_info(mv_ivfpq* index, char* name, size_t name_len, char* metric,
+                               size_t metric_len, int64_t* user_ids, int64_t* num_ids);
+/* The snapshot checksum of a payload (io/snapshot_file.mojo:19-61): seed
+ * 0xD6E8FEB86659FD93, 8 MiB chunks. */
+uint64_t mv_snapshot_checksum(const void* payload, size_t bytes);
 /* IndexIVFPQ.search (index_ivf_pq.mojo:215-360), host buffers. filter may be
  * NULL; filter[id] != 0 excludes id (:328-334). Results distances[nq*k],
  * labels[nq*k]; unfilled slots are 1e38 / -1 (:284-286). params may be NULL

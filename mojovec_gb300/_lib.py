@@ -88,6 +88,11 @@ SIGNATURES = {
     "mv_ivfpq_add": (_i32, [_vp, _vp, _i64]),
     "mv_ivfpq_add_with_ids": (_i32, [_vp, _vp, _vp, _i64]),
     "mv_ivfpq_get_lists": (_i32, [_vp, _vp, _vp, _vp]),
+    "mv_ivfpq_set_lists": (_i32, [_vp, _vp, _vp, _vp]),
+    "mv_ivfpq_load_snapshot": (_i32, [_vp, C.c_char_p, C.POINTER(_vp)]),
+    "mv_ivfpq_save_snapshot": (_i32, [_vp, C.c_char_p, C.c_char_p, C.c_char_p, _vp, _i64]),
+    "mv_ivfpq_snapshot_info": (_i32, [_vp, C.c_char_p, C.c_size_t, C.c_char_p, C.c_size_t, _vp, _vp]),
+    "mv_snapshot_checksum": (C.c_uint64, [_vp, C.c_size_t]),
     "mv_ivfpq_search": (_i32, [_vp, _vp, _i64, _i32, _vp, _i64, _vp, _vp, _vp]),
     "mv_ivfpq_search_device": (_i32, [_vp, _vp, _i64, _i32, _vp, _i64, _vp, _vp, _vp, _vp]),
     "mv_ivfpq_search_noalloc": (_i32, [_vp, _vp, _i64, _i32, _i32, _vp, _vp, _vp]),

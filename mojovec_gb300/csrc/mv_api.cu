@@ -515,6 +515,9 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
     return;
   }
   if (!batch) ensure_fast(ix, s);
+  MV_REQUIRE(ix->has_raw || !(p && p->rerank > 0), MV_ERR_STATE,
+             "the exact rerank needs the index's rows, which a snapshot does not carry; "
+             "search with rerank 0");
   const bool fp32_coarse = p && p->coarse_fp32;
   const int R = std::max(k, (p && p->rerank > 0) ? (int)p->rerank : k);
   MV_REQUIRE(R <= 4096, MV_ERR_ARG, "rerank depth must be at most 4096");
@@ -766,7 +769,10 @@ void ivfpq_add(mv_ivfpq* ix, const float* x, const int64_t* ids, int64_t n) {
   if (old_total) {
     scatter_rows(ix->d_ids.p, old_total, 4, pos_d.as<int64_t>(), ids_d.p, s);
     scatter_rows(ix->d_codes.p, old_total, M, pos_d.as<int64_t>(), codes_d.p, s);
-    scatter_rows(ix->d_raw.p, old_total, 4 * d, pos_d.as<int64_t>(), raw_d.p, s);
+    if (ix->has_raw)  // lists set without rows keep no rows for their old entries
+      scatter_rows(ix->d_raw.p, old_total, 4 * d, pos_d.as<int64_t>(), raw_d.p, s);
+    else
+      MV_CHECK_CUDA(cudaMemsetAsync(raw_d.p, 0, sizeof(float) * cap * d, s));
   }
   scatter_rows(ids_new.p, n, 4, pos_d.as<int64_t>() + old_total, ids_d.p, s);
   scatter_rows(new_codes.p, n, M, pos_d.as<int64_t>() + old_total, codes_d.p, s);
@@ -782,6 +788,7 @@ void ivfpq_add(mv_ivfpq* ix, const float* x, const int64_t* ids, int64_t n) {
   std::swap(ix->d_raw.bytes, raw_d.bytes);
   ix->h_off = new_off;
   ix->ntotal += n;  // :213 counts every input row
+  if (old_total == 0) ix->has_raw = true;  // every entry now has its row
   ix->fast_ready = false;
 }
 
@@ -866,6 +873,38 @@ int32_t mv_ivfpq_get_codebooks(mv_ivfpq* ix, float* centroids, float* pq) {
                                cudaMemcpyDeviceToHost));
     if (pq)
       MV_CHECK_CUDA(cudaMemcpy(pq, ix->pq.p, sizeof(float) * 256 * ix->d, cudaMemcpyDeviceToHost));
+  });
+}
+
+int32_t mv_ivfpq_set_lists(mv_ivfpq* ix, const int64_t* offsets, const int64_t* ids,
+                           const uint8_t* codes) {
+  if (!ix || !offsets) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    std::lock_guard<std::mutex> lk(ix->mu);
+    const int nlist = ix->nlist;
+    MV_REQUIRE(offsets[0] == 0, MV_ERR_ARG, "list offsets must start at 0");
+    for (int l = 0; l < nlist; ++l)
+      MV_REQUIRE(offsets[l + 1] >= offsets[l], MV_ERR_ARG, "list offsets must not decrease");
+    const int64_t total = offsets[nlist];
+    MV_REQUIRE(total == 0 || (ids && codes), MV_ERR_ARG, "ids and codes are required");
+    std::vector<uint32_t> ids32((size_t)total);
+    for (int64_t i = 0; i < total; ++i) {
+      MV_REQUIRE(ids[i] >= 0 && ids[i] <= 0xfffffffell, MV_ERR_ARG,
+                 "ids must be in [0, 2^32 - 2] for the GPU index");
+      ids32[(size_t)i] = (uint32_t)ids[i];
+    }
+    ix->d_off.ensure(sizeof(int64_t) * (nlist + 1));
+    ix->d_ids.ensure(sizeof(uint32_t) * total + 16);
+    ix->d_codes.ensure((size_t)total * ix->M + 16);
+    MV_CHECK_CUDA(cudaMemcpy(ix->d_off.p, offsets, sizeof(int64_t) * (nlist + 1), cudaMemcpyHostToDevice));
+    if (total) {
+      MV_CHECK_CUDA(cudaMemcpy(ix->d_ids.p, ids32.data(), sizeof(uint32_t) * total, cudaMemcpyHostToDevice));
+      MV_CHECK_CUDA(cudaMemcpy(ix->d_codes.p, codes, (size_t)total * ix->M, cudaMemcpyHostToDevice));
+    }
+    ix->h_off.assign(offsets, offsets + nlist + 1);
+    ix->ntotal = total;
+    ix->has_raw = false;  // no rows: plain search and the fast form without rerank
+    ix->fast_ready = false;
   });
 }
 

@@ -195,6 +195,10 @@ struct mv_ivfpq {
   mv::DevBuf d_ids;     // uint32 per entry
   mv::DevBuf d_codes;   // M bytes per entry
   mv::DevBuf d_raw;     // FP32 rows per entry (exact rerank in the fast form)
+  bool has_raw = true;  // false when the lists came without rows (snapshot, set_lists)
+  // Collection metadata carried through snapshots (api/collection_ivfpq.mojo).
+  std::vector<int64_t> user_ids;
+  std::string coll_name, coll_metric;
   // Fast-form state (built lazily from the above).
   std::mutex fast_mu;
   bool fast_ready = false;

@@ -20,6 +20,7 @@ int64 (n, k)) instead of filling caller Spans.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import threading
 
 import numpy as np
@@ -175,6 +176,47 @@ class IndexIVFPQ:
         codes = np.zeros((max(n, 1), self.M), np.uint8)
         check(_lib.load().mv_ivfpq_get_lists(self._h, None, _p(ids), _p(codes)))
         return off, ids[:n], codes[:n]
+
+    def set_lists(self, offsets, ids, codes):
+        """Replaces the lists with CSR data (e.g. the reference's own). The
+        index then has no rows: the fast form runs without rerank."""
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        ids = np.ascontiguousarray(ids, dtype=np.int64)
+        codes = np.ascontiguousarray(codes, dtype=np.uint8)
+        assert off.shape == (self.nlist + 1,) and ids.shape[0] == off[-1]
+        assert codes.size == ids.shape[0] * self.M
+        check(_lib.load().mv_ivfpq_set_lists(self._h, _p(off), _p(ids), _p(codes)))
+
+    def save_snapshot(self, path: str, name: str, metric: str, user_ids):
+        """CollectionIVFPQ.save (api/collection_ivfpq.mojo:335-370): user_ids
+        holds the collection's record id of each internal id."""
+        u = np.ascontiguousarray(user_ids, dtype=np.int64)
+        check(_lib.load().mv_ivfpq_save_snapshot(self._h, os.fsencode(path), name.encode(),
+                                                 metric.encode(), _p(u), u.shape[0]))
+
+    @classmethod
+    def load_snapshot(cls, path: str, ctx: Context | None = None) -> "IndexIVFPQ":
+        """CollectionIVFPQ.load (api/collection_ivfpq.mojo:372-476) onto the
+        GPU: the checksum and the reference's validation, then the lists go
+        straight to device CSR. .collection holds (name, metric, user_ids)."""
+        ctx = ctx or Context.default()
+        lib = _lib.load()
+        h = C.c_void_p()
+        check(lib.mv_ivfpq_load_snapshot(ctx.handle, os.fsencode(path), C.byref(h)))
+        self = cls.__new__(cls)
+        self.ctx, self._h, self.ksub = ctx, h, 256
+        info = np.zeros(7, np.int64)
+        check(lib.mv_ivfpq_info(h, _p(info)))
+        self.d, self.nlist, self.M = int(info[0]), int(info[1]), int(info[2])
+        n = C.c_int64()
+        name, metric = C.create_string_buffer(1 << 20), C.create_string_buffer(16)
+        check(lib.mv_ivfpq_snapshot_info(h, name, len(name), metric, len(metric), None, C.byref(n)))
+        u = np.zeros(max(n.value, 1), np.int64)
+        check(lib.mv_ivfpq_snapshot_info(h, None, 0, None, 0, _p(u), None))
+        m = metric.value.decode()
+        self.metric_type = METRIC_L2 if m == "l2" else METRIC_IP
+        self.collection = (name.value.decode("utf-8"), m, u[: n.value])
+        return self
 
     def search(self, x, k: int, filter=None, form=None, nprobe: int = 0, rerank: int = 0,
                coarse_fp32: bool = False, lut_fp16: bool = False):
