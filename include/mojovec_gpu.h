@@ -94,8 +94,15 @@ int64_t mv_ctx_kernel_launches(mv_ctx* ctx);
 #define MV_STAGE_LUT 3      /* per-query lookup tables (fast form) */
 #define MV_STAGE_RERANK 4   /* exact FP32 rerank */
 #define MV_STAGE_FLAT 5     /* Flat / SQ8 distance tiles */
+#define MV_STAGE_ENCODE 6   /* residuals + PQ codes of added rows */
+#define MV_STAGE_APPEND 7   /* list append: CSR layout + scatter */
 #define MV_STAGE_COUNT 8
 int32_t mv_ctx_profile(mv_ctx* ctx, int32_t enable);
+/* Nearest-centroid assignments (index add, training, plain k-means) run on
+ * the tensor cores with an exact FP32 recheck and an error bound; rows the
+ * bound cannot settle take the exact FP32 scan. Reports the rows assigned
+ * that way and how many of them took the exact scan, since context creation. */
+int32_t mv_ctx_assign_stats(mv_ctx* ctx, int64_t* rows, int64_t* fallback_rows);
 int32_t mv_ctx_stage_times(mv_ctx* ctx, double* ms, int64_t* counts, int32_t nstages);
 
 /* ---- IVF-PQ index: replaces IndexIVFPQ[IndexFlat]

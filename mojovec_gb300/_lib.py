@@ -28,7 +28,7 @@ METRIC_IP = 1
 FORM_PLAIN = 0
 FORM_FAST = 1
 
-STAGES = ("coarse", "select", "scan", "lut", "rerank", "flat", "stage6", "stage7")
+STAGES = ("coarse", "select", "scan", "lut", "rerank", "flat", "encode", "append")
 
 _ERR_NAMES = {
     MV_ERR_ARG: "MV_ERR_ARG",
@@ -72,6 +72,7 @@ SIGNATURES = {
     "mv_last_error": (_i32, [C.c_char_p, C.c_size_t]),
     "mv_version": (C.c_char_p, []),
     "mv_ctx_create": (_i32, [_i32, C.POINTER(_vp)]),
+    "mv_ctx_assign_stats": (_i32, [_vp, _vp, _vp]),
     "mv_ctx_destroy": (_i32, [_vp]),
     "mv_ctx_synchronize": (_i32, [_vp]),
     "mv_ctx_kernel_launches": (_i64, [_vp]),

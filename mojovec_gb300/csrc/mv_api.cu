@@ -113,6 +113,76 @@ struct Philox {
 };
 constexpr uint64_t KMEANS_SEED = 0x4D4F4A4F564543ull;
 
+// Exact nearest-centroid assignment with launch_exact_argmin's result (mode
+// 2: the coarse quantizer's k = 1 search; mode 1: the k-means rule, with the
+// best distance in mind[] when mind is not null), computed through the
+// certified tensor-core path of k_assign.cu where it applies: BF16 top-16
+// candidates, their reference FP32 distances, and the exact SIMT argmin for
+// the rows the error bound leaves open.
+constexpr int ASSIGN_KC = 16;
+void check_kernel_errors(mv_ctx* ctx, cudaStream_t s);
+void assign_nearest(const float* x, int64_t n, int d, const float* cent, int k, int metric,
+                    int mode, int32_t* assign, float* mind, cudaStream_t s) {
+  if (n == 0) return;
+  const int kind = metric == MV_METRIC_IP ? KIND_IP_SIMD8
+                                          : (mode == 1 && d <= 4 ? KIND_L2_SHORT4 : KIND_L2_SIMD8);
+  mv_ctx* ctx = g_cur_ctx;
+  const bool cert = ctx && kind != KIND_L2_SHORT4 && umma_kpad(d) <= 256 && k > 2 * ASSIGN_KC &&
+                    n >= 4096 && n <= 0x7fffffffll;
+  if (!cert) {
+    launch_exact_argmin(kind, mode, x, n, d, cent, k, d, d, assign, mind, 1, 0, 0, 0, s);
+    return;
+  }
+  const int kp = umma_kpad(d), kc = ASSIGN_KC, ncp = next_pow2(kc);
+  const int64_t chunk = std::min<int64_t>(n, 1 << 19);
+  const int nseg = umma_topk_nseg(chunk, k, d, kc, ctx->num_sms);
+  const int osegs = nseg * umma_topk_groups(d, kc);
+  DevBuf buf;
+  buf.ensure(ws_bytes((size_t)k * kp, 2) + ws_bytes(k, 4) + ws_bytes(1, 8) +
+             ws_bytes((size_t)chunk * kp, 2) + ws_bytes((size_t)chunk * osegs * ncp, 8) +
+             2 * ws_bytes(chunk, 8) + ws_bytes(1, 4) + ws_bytes((size_t)chunk * d, 4) +
+             2 * ws_bytes(chunk, 4));
+  Arena ar(buf);
+  __nv_bfloat16* cb = ar.take<__nv_bfloat16>((size_t)k * kp);
+  float* cn = ar.take<float>(k);
+  double* bmax2 = ar.take<double>(1);
+  __nv_bfloat16* xb = ar.take<__nv_bfloat16>((size_t)chunk * kp);
+  uint64_t* cand = ar.take<uint64_t>((size_t)chunk * osegs * ncp);
+  uint64_t* gthr = ar.take<uint64_t>(chunk);
+  int64_t* flagged = ar.take<int64_t>(chunk);
+  int* nflag = ar.take<int>(1);
+  float* sub_x = ar.take<float>((size_t)chunk * d);
+  int32_t* sub_a = ar.take<int32_t>(chunk);
+  float* sub_d = ar.take<float>(chunk);
+  launch_to_bf16(cent, k, d, cb, cn, s);
+  launch_max_norm(cn, k, d, bmax2, s);
+  int64_t fallback = 0;
+  for (int64_t r0 = 0; r0 < n; r0 += chunk) {
+    const int64_t nb = std::min(chunk, n - r0);
+    const float* xr = x + r0 * d;
+    launch_to_bf16(xr, nb, d, xb, nullptr, s);
+    launch_umma_topk(xb, nb, cb, k, d, metric, nullptr, cn, kc, nseg, nullptr,
+                     osegs > 1 ? gthr : nullptr, cand, ctx->d_err.as<int>(), s);
+    MV_CHECK_CUDA(cudaMemsetAsync(nflag, 0, sizeof(int), s));
+    launch_assign_certify(xr, nb, d, cent, k, metric, cand, osegs * ncp, kc, bmax2, assign + r0,
+                          mind ? mind + r0 : nullptr, flagged, nflag, s);
+    int h_nflag = 0;
+    d2h(&h_nflag, nflag, sizeof(int), s);
+    check_kernel_errors(ctx, s);  // syncs; a bounded wait that gave up raises
+    if (h_nflag > 0) {
+      launch_gather_rows(xr, d, flagged, h_nflag, sub_x, 1, 0, 0, s);
+      launch_exact_argmin(kind, mode, sub_x, h_nflag, d, cent, k, d, d, sub_a,
+                          mind ? sub_d : nullptr, 1, 0, 0, 0, s);
+      launch_scatter_assign(sub_a, mind ? sub_d : nullptr, flagged, h_nflag, assign + r0,
+                            mind ? mind + r0 : nullptr, s);
+    }
+    fallback += h_nflag;
+  }
+  sync(s);  // the scratch is freed on return
+  ctx->assign_rows += n;
+  ctx->assign_fallback += fallback;
+}
+
 // Batched plain k-means over `batch` independent problems that share n, d
 // and k: x[b] at x + b*n*d, centroids[b] at cent + b*k*d, assign[b] at
 // assign + b*n.
@@ -147,8 +217,11 @@ void kmeans_train_device(const float* x, int64_t n, int d, int k, int niter, int
   launch_gather_rows(x, d, d_idx, k, cent, batch, n * d, (int64_t)k * d, s);
   const int kind = d <= 4 ? KIND_L2_SHORT4 : KIND_L2_SIMD8;  // kmeans.mojo:131-139
   for (int it = 0; it < niter; ++it) {
-    launch_exact_argmin(kind, 1, x, n, d, cent, k, d, d, assign, mind, batch, n * d,
-                        (int64_t)k * d, n, s);
+    if (batch == 1)
+      assign_nearest(x, n, d, cent, k, MV_METRIC_L2, 1, assign, mind, s);
+    else
+      launch_exact_argmin(kind, 1, x, n, d, cent, k, d, d, assign, mind, batch, n * d,
+                          (int64_t)k * d, n, s);
     if (obj) launch_sum_fp64(mind, n, part, d_obj + it, s);
     launch_kmeans_accumulate(x, n, d, k, assign, local_sums, local_counts, batch, n * d, n,
                              (int64_t)32 * k * d, (int64_t)32 * k, s);
@@ -156,8 +229,7 @@ void kmeans_train_device(const float* x, int64_t n, int d, int k, int niter, int
                          n * d, (int64_t)32 * k * d, (int64_t)32 * k, (int64_t)k * d, s);
   }
   if (obj) {  // inertia of the final centroids
-    launch_exact_argmin(kind, 1, x, n, d, cent, k, d, d, final_assign, mind, 1, n * d,
-                        (int64_t)k * d, n, s);
+    assign_nearest(x, n, d, cent, k, MV_METRIC_L2, 1, final_assign, mind, s);
     launch_sum_fp64(mind, n, part, d_obj + niter, s);
   }
   sync(s);  // the host-side idx vector and scratch must outlive the kernels
@@ -333,6 +405,13 @@ int32_t mv_ctx_synchronize(mv_ctx* ctx) {
 }
 
 int64_t mv_ctx_kernel_launches(mv_ctx* ctx) { return ctx ? ctx->launches.load() : -1; }
+
+int32_t mv_ctx_assign_stats(mv_ctx* ctx, int64_t* rows, int64_t* fallback_rows) {
+  if (!ctx) return MV_ERR_ARG;
+  if (rows) *rows = ctx->assign_rows.load();
+  if (fallback_rows) *fallback_rows = ctx->assign_fallback.load();
+  return MV_OK;
+}
 
 int32_t mv_ctx_profile(mv_ctx* ctx, int32_t enable) {
   if (!ctx) return MV_ERR_ARG;
@@ -683,101 +762,97 @@ void scatter_rows(const void* src, int64_t n, int width_bytes, const int64_t* po
   MV_CHECK_CUDA(cudaGetLastError());
 }
 
+// Device list-append layout (k_lists.cu): the rebuilt CSR positions of the
+// old entries, then of the n new ones, and the new offsets (device and host).
+struct AppendLayout {
+  DevBuf off_d, pos_d;
+  std::vector<int64_t> new_off;
+  int64_t cap = 0;  // entries the rebuilt arrays hold (skipped rows parked at the end)
+};
+void append_layout(mv_ctx* ctx, const int32_t* d_assign, int64_t n, int nlist,
+                   const int64_t* d_old_off, int64_t old_total, AppendLayout& L, cudaStream_t s) {
+  StageTimer t(ctx, MV_STAGE_APPEND, s);
+  L.off_d.ensure(sizeof(int64_t) * (nlist + 1));
+  L.pos_d.ensure(sizeof(int64_t) * (old_total + n) + 16);
+  DevBuf scratch;
+  scratch.ensure(list_append_scratch_bytes(n, nlist));
+  launch_list_append_layout(d_assign, n, nlist, d_old_off, old_total, L.off_d.as<int64_t>(),
+                            L.pos_d.as<int64_t>(), scratch.p, s);
+  L.new_off.resize(nlist + 1);
+  d2h(L.new_off.data(), L.off_d.p, sizeof(int64_t) * (nlist + 1), s);
+  sync(s);
+  L.cap = old_total + n;
+}
+
 // IndexIVFPQ.add_with_ids (index_ivf_pq.mojo:150-213): assign with the
 // index-metric quantizer, residual PQ codes, append to the lists in input
 // order (storage/inverted_lists.mojo:162-186). Lists are kept as CSR on the
-// device; an append rebuilds it with one scatter per array.
+// device; an append rebuilds it on the device (layout, then one scatter per
+// array).
 void ivfpq_add(mv_ivfpq* ix, const float* x, const int64_t* ids, int64_t n) {
   if (!ix->trained || n == 0) return;  // :161
-  for (int64_t i = 0; i < n; ++i)
+  std::vector<uint32_t> ids32(n);
+  for (int64_t i = 0; i < n; ++i) {
     MV_REQUIRE(ids[i] >= 0 && ids[i] <= 0xfffffffell, MV_ERR_ARG,
                "ids must be in [0, 2^32 - 2] for the GPU index");
+    ids32[i] = (uint32_t)ids[i];
+  }
   SlotLease lease(ix->ctx);
   cudaStream_t s = lease.stream();
-  const int d = ix->d, M = ix->M;
-  std::vector<int32_t> h_assign(n);
-  DevBuf new_codes, new_raw;
+  const int d = ix->d, M = ix->M, nlist = ix->nlist;
+  DevBuf new_codes, new_raw, assign_d;
   new_codes.ensure((size_t)n * M + 16);
   new_raw.ensure((size_t)n * d * 4 + 16);
+  assign_d.ensure((size_t)n * 4 + 16);
   const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(n, (1ll << 28) / d));
   {
     DevBuf& ws = lease.slot->ws;
-    ws.ensure(ws_bytes((size_t)chunk * d, 4) * 2 + ws_bytes(chunk, 4));
+    ws.ensure(ws_bytes((size_t)chunk * d, 4));
     Arena ar(ws);
-    float* dx = ar.take<float>((size_t)chunk * d);
     float* res = ar.take<float>((size_t)chunk * d);
-    int32_t* assign = ar.take<int32_t>(chunk);
-    const int kind = ix->metric == MV_METRIC_L2 ? KIND_L2_SIMD8 : KIND_IP_SIMD8;
     for (int64_t r0 = 0; r0 < n; r0 += chunk) {
       const int64_t nb = std::min(chunk, n - r0);
+      float* dx = new_raw.as<float>() + r0 * d;
+      int32_t* assign = assign_d.as<int32_t>() + r0;
       h2d(dx, x + r0 * d, sizeof(float) * nb * d, s);
-      // :172 quantizer.search(x, 1)
-      launch_exact_argmin(kind, 2, dx, nb, d, ix->centroids.as<float>(), ix->nlist, d, d, assign,
-                          nullptr, 1, 0, 0, 0, s);
-      launch_residuals(dx, nb, d, ix->centroids.as<float>(), ix->nlist, assign, res, s);
+      {
+        StageTimer t(ix->ctx, MV_STAGE_COARSE, s);  // :172 quantizer.search(x, 1)
+        assign_nearest(dx, nb, d, ix->centroids.as<float>(), nlist, ix->metric, 2, assign, nullptr,
+                       s);
+      }
+      StageTimer t(ix->ctx, MV_STAGE_ENCODE, s);
+      launch_residuals(dx, nb, d, ix->centroids.as<float>(), nlist, assign, res, s);
       launch_pq_encode(res, nb, d, M, ix->pq.as<float>(), new_codes.as<uint8_t>() + r0 * M, s);
-      d2d(new_raw.as<float>() + r0 * d, dx, sizeof(float) * nb * d, s);
-      d2h(h_assign.data() + r0, assign, sizeof(int32_t) * nb, s);
-      sync(s);
     }
   }
   // New CSR layout: old entries of list l keep their order, new ones follow
   // in input order (:199-211 appends one at a time).
-  const int nlist = ix->nlist;
-  std::vector<int64_t> old_off = ix->h_off;
-  std::vector<int64_t> add_cnt(nlist, 0);
-  int64_t kept = 0;
-  for (int64_t i = 0; i < n; ++i) {
-    int l = h_assign[i];
-    if (l < 0 || l >= nlist) continue;  // :201
-    add_cnt[l]++;
-    kept++;
-  }
-  std::vector<int64_t> new_off(nlist + 1, 0);
-  for (int l = 0; l < nlist; ++l)
-    new_off[l + 1] = new_off[l] + (old_off[l + 1] - old_off[l]) + add_cnt[l];
-  const int64_t old_total = old_off[nlist];
-  const int64_t new_total = old_total + kept;
-  std::vector<int64_t> pos_old(old_total), pos_new(n);
-  for (int l = 0; l < nlist; ++l)
-    for (int64_t p = old_off[l]; p < old_off[l + 1]; ++p) pos_old[p] = p - old_off[l] + new_off[l];
-  std::vector<int64_t> fill(nlist);
-  for (int l = 0; l < nlist; ++l) fill[l] = new_off[l] + (old_off[l + 1] - old_off[l]);
-  std::vector<uint32_t> ids32(n);
-  int64_t dropped = 0;
-  for (int64_t i = 0; i < n; ++i) {
-    int l = h_assign[i];
-    ids32[i] = (uint32_t)ids[i];
-    if (l < 0 || l >= nlist) {
-      pos_new[i] = new_total + dropped++;  // parked past the end, never read
-      continue;
-    }
-    pos_new[i] = fill[l]++;
-  }
-  const int64_t cap = new_total + dropped;
-  DevBuf off_d, ids_d, codes_d, raw_d, pos_d, ids_new;
-  off_d.ensure(sizeof(int64_t) * (nlist + 1));
+  const int64_t old_total = ix->h_off[nlist];
+  AppendLayout L;
+  append_layout(ix->ctx, assign_d.as<int32_t>(), n, nlist, ix->d_off.as<int64_t>(), old_total, L, s);
+  const int64_t cap = L.cap;
+  const int64_t* pos = L.pos_d.as<int64_t>();
+  DevBuf ids_d, codes_d, raw_d, ids_new;
   ids_d.ensure(sizeof(uint32_t) * cap + 16);
   codes_d.ensure((size_t)cap * M + 16);
   raw_d.ensure(sizeof(float) * cap * d + 16);
-  pos_d.ensure(sizeof(int64_t) * (old_total + n) + 16);
   ids_new.ensure(sizeof(uint32_t) * n + 16);
-  h2d(off_d.p, new_off.data(), sizeof(int64_t) * (nlist + 1), s);
-  h2d(pos_d.p, pos_old.data(), sizeof(int64_t) * old_total, s);
-  h2d(pos_d.as<int64_t>() + old_total, pos_new.data(), sizeof(int64_t) * n, s);
   h2d(ids_new.p, ids32.data(), sizeof(uint32_t) * n, s);
+  StageTimer t(ix->ctx, MV_STAGE_APPEND, s);
   if (old_total) {
-    scatter_rows(ix->d_ids.p, old_total, 4, pos_d.as<int64_t>(), ids_d.p, s);
-    scatter_rows(ix->d_codes.p, old_total, M, pos_d.as<int64_t>(), codes_d.p, s);
+    scatter_rows(ix->d_ids.p, old_total, 4, pos, ids_d.p, s);
+    scatter_rows(ix->d_codes.p, old_total, M, pos, codes_d.p, s);
     if (ix->has_raw)  // lists set without rows keep no rows for their old entries
-      scatter_rows(ix->d_raw.p, old_total, 4 * d, pos_d.as<int64_t>(), raw_d.p, s);
+      scatter_rows(ix->d_raw.p, old_total, 4 * d, pos, raw_d.p, s);
     else
       MV_CHECK_CUDA(cudaMemsetAsync(raw_d.p, 0, sizeof(float) * cap * d, s));
   }
-  scatter_rows(ids_new.p, n, 4, pos_d.as<int64_t>() + old_total, ids_d.p, s);
-  scatter_rows(new_codes.p, n, M, pos_d.as<int64_t>() + old_total, codes_d.p, s);
-  scatter_rows(new_raw.p, n, 4 * d, pos_d.as<int64_t>() + old_total, raw_d.p, s);
+  scatter_rows(ids_new.p, n, 4, pos + old_total, ids_d.p, s);
+  scatter_rows(new_codes.p, n, M, pos + old_total, codes_d.p, s);
+  scatter_rows(new_raw.p, n, 4 * d, pos + old_total, raw_d.p, s);
   sync(s);
+  DevBuf& off_d = L.off_d;
+  std::vector<int64_t>& new_off = L.new_off;
   std::swap(ix->d_off.p, off_d.p);
   std::swap(ix->d_off.bytes, off_d.bytes);
   std::swap(ix->d_ids.p, ids_d.p);
@@ -933,9 +1008,8 @@ int32_t mv_ivfpq_train_ex(mv_ivfpq* ix, const float* x, int64_t n, int32_t niter
       kmeans_train_device(dx.as<float>(), n, d, ix->nlist, niter_coarse, 1,
                           ix->centroids.as<float>(), assign.as<int32_t>(), scratch, s);
     // 2. index-metric assignment and residuals (:113-128)
-    const int kind = ix->metric == MV_METRIC_L2 ? KIND_L2_SIMD8 : KIND_IP_SIMD8;
-    launch_exact_argmin(kind, 2, dx.as<float>(), n, d, ix->centroids.as<float>(), ix->nlist, d, d,
-                        assign.as<int32_t>(), nullptr, 1, 0, 0, 0, s);
+    assign_nearest(dx.as<float>(), n, d, ix->centroids.as<float>(), ix->nlist, ix->metric, 2,
+                   assign.as<int32_t>(), nullptr, s);
     res.ensure(sizeof(float) * n * d);
     launch_residuals(dx.as<float>(), n, d, ix->centroids.as<float>(), ix->nlist,
                      assign.as<int32_t>(), res.as<float>(), s);
@@ -2207,68 +2281,44 @@ namespace mv {
 // rows appended to their list in input order.
 void ivfflat_add(mv_ivfflat* ix, const float* x, const int64_t* ids, int64_t n) {
   if (!ix->trained || n == 0) return;  // :103-105
-  for (int64_t i = 0; i < n; ++i)
+  std::vector<uint32_t> ids32(n);
+  for (int64_t i = 0; i < n; ++i) {
     MV_REQUIRE(ids[i] >= 0 && ids[i] <= 0xfffffffell, MV_ERR_ARG,
                "ids must be in [0, 2^32 - 2] for the GPU index");
+    ids32[i] = (uint32_t)ids[i];
+  }
   SlotLease lease(ix->ctx);
   cudaStream_t s = lease.stream();
   const int d = ix->d, nlist = ix->nlist;
-  std::vector<int32_t> h_assign(n);
-  DevBuf new_rows;
+  DevBuf new_rows, assign_d;
   new_rows.ensure((size_t)n * d * 4 + 16);
+  assign_d.ensure((size_t)n * 4 + 16);
   h2d(new_rows.p, x, sizeof(float) * n * d, s);
   {
-    DevBuf& ws = lease.slot->ws;
-    ws.ensure(ws_bytes(n, 4));
-    int32_t* assign = ws.as<int32_t>();
-    const int kind = ix->metric == MV_METRIC_L2 ? KIND_L2_SIMD8 : KIND_IP_SIMD8;
-    launch_exact_argmin(kind, 2, new_rows.as<float>(), n, d, ix->centroids.as<float>(), nlist, d,
-                        d, assign, nullptr, 1, 0, 0, 0, s);
-    d2h(h_assign.data(), assign, sizeof(int32_t) * n, s);
-    sync(s);
+    StageTimer t(ix->ctx, MV_STAGE_COARSE, s);  // :115-118 quantizer.search(x, 1)
+    assign_nearest(new_rows.as<float>(), n, d, ix->centroids.as<float>(), nlist, ix->metric, 2,
+                   assign_d.as<int32_t>(), nullptr, s);
   }
-  const std::vector<int64_t> old_off = ix->h_off;
-  std::vector<int64_t> add_cnt(nlist, 0);
-  int64_t kept = 0;
-  for (int64_t i = 0; i < n; ++i)
-    if (h_assign[i] >= 0 && h_assign[i] < nlist) {
-      add_cnt[h_assign[i]]++;
-      kept++;
-    }
-  std::vector<int64_t> new_off(nlist + 1, 0);
-  for (int l = 0; l < nlist; ++l)
-    new_off[l + 1] = new_off[l] + (old_off[l + 1] - old_off[l]) + add_cnt[l];
-  const int64_t old_total = old_off[nlist], new_total = old_total + kept;
-  std::vector<int64_t> pos_old(old_total), pos_new(n), fill(nlist);
-  for (int l = 0; l < nlist; ++l) {
-    for (int64_t p = old_off[l]; p < old_off[l + 1]; ++p) pos_old[p] = p - old_off[l] + new_off[l];
-    fill[l] = new_off[l] + (old_off[l + 1] - old_off[l]);
-  }
-  std::vector<uint32_t> ids32(n);
-  int64_t dropped = 0;
-  for (int64_t i = 0; i < n; ++i) {
-    ids32[i] = (uint32_t)ids[i];
-    const int l = h_assign[i];
-    pos_new[i] = (l < 0 || l >= nlist) ? new_total + dropped++ : fill[l]++;  // :126
-  }
-  const int64_t cap = new_total + dropped;
-  DevBuf off_d, ids_d, rows_d, pos_d, ids_new;
-  off_d.ensure(sizeof(int64_t) * (nlist + 1));
+  const int64_t old_total = ix->h_off[nlist];
+  AppendLayout L;  // skipped rows (:126) are parked past the end
+  append_layout(ix->ctx, assign_d.as<int32_t>(), n, nlist, ix->d_off.as<int64_t>(), old_total, L, s);
+  const int64_t cap = L.cap;
+  const int64_t* pos = L.pos_d.as<int64_t>();
+  DevBuf ids_d, rows_d, ids_new;
   ids_d.ensure(sizeof(uint32_t) * cap + 16);
   rows_d.ensure(sizeof(float) * cap * d + 16);
-  pos_d.ensure(sizeof(int64_t) * (old_total + n) + 16);
   ids_new.ensure(sizeof(uint32_t) * n + 16);
-  h2d(off_d.p, new_off.data(), sizeof(int64_t) * (nlist + 1), s);
-  h2d(pos_d.p, pos_old.data(), sizeof(int64_t) * old_total, s);
-  h2d(pos_d.as<int64_t>() + old_total, pos_new.data(), sizeof(int64_t) * n, s);
   h2d(ids_new.p, ids32.data(), sizeof(uint32_t) * n, s);
+  StageTimer t(ix->ctx, MV_STAGE_APPEND, s);
   if (old_total) {
-    scatter_rows(ix->d_ids.p, old_total, 4, pos_d.as<int64_t>(), ids_d.p, s);
-    scatter_rows(ix->d_rows.p, old_total, 4 * d, pos_d.as<int64_t>(), rows_d.p, s);
+    scatter_rows(ix->d_ids.p, old_total, 4, pos, ids_d.p, s);
+    scatter_rows(ix->d_rows.p, old_total, 4 * d, pos, rows_d.p, s);
   }
-  scatter_rows(ids_new.p, n, 4, pos_d.as<int64_t>() + old_total, ids_d.p, s);
-  scatter_rows(new_rows.p, n, 4 * d, pos_d.as<int64_t>() + old_total, rows_d.p, s);
+  scatter_rows(ids_new.p, n, 4, pos + old_total, ids_d.p, s);
+  scatter_rows(new_rows.p, n, 4 * d, pos + old_total, rows_d.p, s);
   sync(s);
+  DevBuf& off_d = L.off_d;
+  std::vector<int64_t>& new_off = L.new_off;
   std::swap(ix->d_off.p, off_d.p);
   std::swap(ix->d_off.bytes, off_d.bytes);
   std::swap(ix->d_ids.p, ids_d.p);

@@ -113,6 +113,9 @@ struct mv_ctx {
   std::atomic<int64_t> launches{0};
   cudaStream_t main_stream = nullptr;
   mv::DevBuf d_err;  // int: set by kernels whose bounded waits gave up
+  // certified nearest-centroid assignment: rows assigned, rows the bound left
+  // to the exact SIMT argmin (mv_ctx_assign_stats)
+  std::atomic<int64_t> assign_rows{0}, assign_fallback{0};
   // stage profiling (mv_ctx_profile)
   std::atomic<bool> profile{false};
   std::mutex prof_mu;

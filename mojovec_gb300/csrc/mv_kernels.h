@@ -76,6 +76,32 @@ void launch_pq_tables(const float* x, int64_t nq, int d, int M, const float* pq,
 // [n x d] -> [M x n x dsub] (subspace extraction, pq.mojo:58-62).
 void launch_split_subspaces(const float* x, int64_t n, int d, int M, float* out, cudaStream_t s);
 
+// ---- list append (k_lists.cu) -------------------------------------------
+// Rebuilt-CSR positions for an append of n entries with list numbers
+// assign[i] (outside [0, nlist): skipped, parked past the end): pos[0,
+// old_total) for the old entries, pos[old_total, old_total + n) for the new
+// ones in input order; new_off[nlist + 1]. scratch: list_append_scratch_bytes.
+size_t list_append_scratch_bytes(int64_t n, int nlist);
+void launch_list_append_layout(const int32_t* assign, int64_t n, int nlist, const int64_t* old_off,
+                               int64_t old_total, int64_t* new_off, int64_t* pos, void* scratch,
+                               cudaStream_t s);
+
+// ---- certified nearest-centroid assignment (k_assign.cu) ------------------
+// out = B^2 bound: max of n FP32 norms (of BF16 rows) with summation slack,
+// or -1 when a norm is NaN or infinite.
+void launch_max_norm(const float* norms, int n, int d, double* out, cudaStream_t s);
+// Exact recheck of the top-k GEMM candidates (cand: n x ncand keys) with the
+// reference distance (l2_simd<8> / -ip_simd<8>), best candidate to assign[],
+// and rows the BF16 error bound does not settle appended to flagged[]
+// (count in *nflag).
+void launch_assign_certify(const float* x, int64_t n, int d, const float* cent, int nlist, int metric,
+                           const uint64_t* cand, int ncand, int kc, const double* bmax2,
+                           int32_t* assign, float* mind, int64_t* flagged, int* nflag,
+                           cudaStream_t s);
+// assign[idx[i]] = sub[i] (and mind[idx[i]] = sub_d[i] when mind is not null).
+void launch_scatter_assign(const int32_t* sub, const float* sub_d, const int64_t* idx, int64_t count,
+                           int32_t* assign, float* mind, cudaStream_t s);
+
 // ---- k-means (k_kmeans.cu) -----------------------------------------------
 // Gathers rows: out[i] = x[idx[i]].
 void launch_gather_rows(const float* x, int d, const int64_t* idx, int64_t count, float* out,

@@ -70,6 +70,13 @@ class Context:
     def kernel_launches(self) -> int:
         return int(_lib.load().mv_ctx_kernel_launches(self._h))
 
+    def assign_stats(self) -> tuple:
+        """(rows assigned on the tensor cores with the certified recheck, rows
+        of those that took the exact FP32 scan)."""
+        rows, fb = C.c_int64(), C.c_int64()
+        check(_lib.load().mv_ctx_assign_stats(self._h, C.byref(rows), C.byref(fb)))
+        return rows.value, fb.value
+
     def profile(self, enable: bool = True):
         """Enables (and resets) per-stage CUDA-event timing."""
         check(_lib.load().mv_ctx_profile(self._h, 1 if enable else 0))
