@@ -62,25 +62,39 @@ def _env_int(name, default):
 
 
 class ClockSampler:
-    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+    """Samples nvidia-smi clocks and throttle reasons during the timed region.
+
+    start() returns once nvidia-smi is producing samples, so sampling is
+    live when the region begins; stop() waits for one more sample, so a
+    region shorter than the sampling period still has the sample taken as it
+    ends. The record covers the samples from start() to that one."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    PERIOD_MS = 50
 
     def __init__(self, device=0):
         self.device = device
         self.proc = None
         self.lines = []
+        self.first = 0
+
+    def _wait_lines(self, count, timeout_s):
+        t0 = time.perf_counter()
+        while len(self.lines) < count and time.perf_counter() - t0 < timeout_s:
+            time.sleep(0.005)
 
     def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
+            self._wait_lines(1, 5.0)
+            self.first = len(self.lines)  # samples from here on
         except OSError:
             self.proc = None
 
@@ -91,6 +105,7 @@ class ClockSampler:
     def stop(self):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self._wait_lines(len(self.lines) + 1, 1.0)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -98,7 +113,7 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        for line in self.lines[self.first:]:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 8:
                 continue
@@ -848,9 +863,9 @@ def run_serve(args, rank, world):
     colls = [("ivfpq_1Mx128_l2", ivf, a_q), ("sq8_2Mx768_cos", sq8, b_q),
              ("flat_500kx256_ip", flat, c_q)]
     forms = {
-        "plain": [dict(form=mv.FORM_PLAIN, nprobe=16), dict(form=mv.FORM_PLAIN, rerank_factor=2),
+        "plain": [dict(form=mv.FORM_PLAIN, nprobe=8), dict(form=mv.FORM_PLAIN, rerank_factor=2),
                   dict(form=mv.FORM_PLAIN)],
-        "fast": [dict(form=mv.FORM_FAST, nprobe=16, rerank=256),
+        "fast": [dict(form=mv.FORM_FAST, nprobe=8, rerank=256),
                  dict(form=mv.FORM_FAST, rerank_factor=2), dict(form=mv.FORM_FAST, rerank=40)],
     }
     rng = np.random.default_rng(np.random.SeedSequence(20261203).spawn(8)[6])
@@ -941,9 +956,9 @@ def run_serve(args, rank, world):
             "workload": f"serve_ivfpq1M_sq8_2Mx768_flat500kx256_req{nreq}_scale{s}",
             "arrivals": "Poisson; batch size log-uniform on [1, 1024]; collection uniform; k in {10, 100}",
             "server": f"4 lanes, HBM budget {args.serve_budget_gb} GB, batches up to 4096 queries",
-            "forms": {"plain": "IVF-PQ plain nprobe 16; SQ8 integer scan + FP32 rerank of 2k; "
+            "forms": {"plain": "IVF-PQ plain nprobe 8; SQ8 integer scan + FP32 rerank of 2k; "
                                "Flat exact FP32",
-                      "fast": "IVF-PQ fast nprobe 16 rerank 256; SQ8 integer scan + FP32 rerank of "
+                      "fast": "IVF-PQ fast nprobe 8 rerank 256; SQ8 integer scan + FP32 rerank of "
                               "2k (d = 768 is above the tensor path's 256); Flat BF16 + FP32 "
                               "rerank of max(k, 40)"},
             "results": results,
@@ -1068,7 +1083,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--form", default="fast", choices=["plain", "fast"])
-    ap.add_argument("--nprobe", type=int, default=16)
+    ap.add_argument("--nprobe", type=int, default=8)
     ap.add_argument("--rerank", type=int, default=None,
                     help="shortlist depth (IVF-PQ default 256, flat default k * 4)")
     ap.add_argument("--nb", type=int, default=NB, help="base rows (profiling runs use fewer)")

@@ -67,7 +67,10 @@ typedef struct mv_search_params {
                           (0 = no rerank) */
   int32_t coarse_fp32; /* fast form: 1 = FP32 SIMT coarse instead of BF16 */
   int32_t lut_fp16;    /* fast form: 1 = FP16 lookup tables */
-  int32_t reserved[3];
+  int32_t coarse_path; /* fast form, BF16 coarse step: 0 = automatic, 1 = GEMM with a
+                          per-row top-k epilogue, 2 = distance matrix then one warp
+                          per query selecting its lists */
+  int32_t reserved[2];
 } mv_search_params;
 
 /* ---- library / context ---------------------------------------------- */

@@ -58,7 +58,8 @@ class SearchParams(C.Structure):
         ("rerank", C.c_int32),
         ("coarse_fp32", C.c_int32),
         ("lut_fp16", C.c_int32),
-        ("reserved", C.c_int32 * 3),
+        ("coarse_path", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 

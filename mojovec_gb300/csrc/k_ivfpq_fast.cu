@@ -205,6 +205,137 @@ __global__ void __launch_bounds__(FT)
   }
 }
 
+// Coarse step from the approximate distance matrix, one warp per query
+// (nc <= 64). Each lane keeps its two smallest (distance, list) keys; the
+// nc-th smallest of those 64 keys is a threshold T with at least nc keys of
+// the row at or below it, usually a few dozen. Those are gathered, the nc
+// smallest kept (the same set a top-nc heap keeps), their exact FP32
+// distances computed as in k_coarse_from_keys, and the nprobe smallest
+// written sorted by (distance, list). When more than CR_CAP keys sit at or
+// below T, the exact nc-th smallest key is found by bisection over the key
+// values first.
+constexpr int CR_WARPS = 8, CR_CAP = 256;
+
+__device__ __forceinline__ void warp_bitonic_sort(uint64_t* a, int n) {
+  const int lane = threadIdx.x & 31;
+  for (int k = 2; k <= n; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = lane; i < n; i += 32) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const uint64_t x = a[i], y = a[ixj];
+          const bool up = (i & k) == 0;
+          if ((x > y) == up) {
+            a[i] = y;
+            a[ixj] = x;
+          }
+        }
+      }
+      __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(CR_WARPS * 32)
+    k_coarse_rows(const float* __restrict__ approx, int64_t nq, int nlist, const float* __restrict__ q,
+                  int d, const float* __restrict__ cent, int metric, int nc, int nprobe,
+                  int32_t* __restrict__ probes, float* __restrict__ term, int* __restrict__ err) {
+  __shared__ uint64_t bufs[CR_WARPS][CR_CAP];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * CR_WARPS + warp;
+  if (row >= nq) return;  // warps are independent: no block-wide barrier below
+  uint64_t* B = bufs[warp];
+  const float* arow = approx + row * (int64_t)nlist;
+  // 1. the two smallest keys of each lane
+  uint64_t m0 = KEY_NONE, m1 = KEY_NONE;
+  for (int i = lane; i < nlist; i += 32) {
+    const uint64_t k = make_key(arow[i], (uint32_t)i);
+    if (k < m1) {
+      if (k < m0) {
+        m1 = m0;
+        m0 = k;
+      } else {
+        m1 = k;
+      }
+    }
+  }
+  B[lane] = m0;
+  B[32 + lane] = m1;
+  __syncwarp();
+  warp_bitonic_sort(B, 64);
+  const uint64_t T = B[nc - 1];  // nc <= min(nlist, 64) keys are valid
+  __syncwarp();
+  // 2. gather the keys <= T
+  auto gather = [&](uint64_t thr) -> int {
+    int cnt = 0;
+    for (int i0 = 0; i0 < nlist; i0 += 32) {
+      const int i = i0 + lane;
+      const uint64_t k = i < nlist ? make_key(arow[i], (uint32_t)i) : KEY_NONE;
+      const bool pass = i < nlist && k <= thr;
+      const unsigned bal = __ballot_sync(0xffffffffu, pass);
+      const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
+      if (pass && pos < CR_CAP) B[pos] = k;
+      cnt += __popc(bal);
+    }
+    return cnt;
+  };
+  int cnt = gather(T);
+  if (cnt > CR_CAP) {
+    // bisection: the smallest key value with at least nc keys at or below it
+    uint64_t lo = 0, hi = T;
+    while (lo < hi) {
+      const uint64_t mid = lo + ((hi - lo) >> 1);
+      int c = 0;
+      for (int i = lane; i < nlist; i += 32) c += make_key(arow[i], (uint32_t)i) <= mid ? 1 : 0;
+      for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+      if (c >= nc) hi = mid;
+      else lo = mid + 1;
+    }
+    __syncwarp();
+    cnt = gather(lo);  // exactly nc keys (keys are distinct)
+  }
+  __syncwarp();
+  int np2 = 32;
+  while (np2 < cnt) np2 <<= 1;
+  for (int i = cnt + lane; i < np2; i += 32) B[i] = KEY_NONE;
+  __syncwarp();
+  warp_bitonic_sort(B, np2);
+  // 3. exact FP32 distances of the nc smallest (as k_coarse_from_keys)
+  const float* qr = q + row * d;
+  const int ncp = next_pow2(nc);
+  for (int c = 0; c < ncp; ++c) {
+    uint64_t out = KEY_NONE - (uint64_t)c;
+    if (c < nc) {
+      const uint32_t list = key_id(B[c]);
+      if (list < (uint32_t)nlist) {
+        const float* cp = cent + (int64_t)list * d;
+        float acc = 0.0f;
+        for (int j = lane; j < d; j += 32) {
+          if (metric == MV_METRIC_L2) {
+            const float df = qr[j] - cp[j];
+            acc = fmaf(df, df, acc);
+          } else {
+            acc = fmaf(qr[j], cp[j], acc);
+          }
+        }
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        out = make_key(metric == MV_METRIC_L2 ? acc : -acc, list);
+      } else if (lane == 0) {
+        atomicExch(err, 106);
+      }
+    }
+    __syncwarp();
+    if (lane == 0) B[c] = out;
+    __syncwarp();
+  }
+  warp_bitonic_sort(B, ncp);
+  for (int p = lane; p < nprobe; p += 32) {
+    const uint64_t key = B[p];
+    const bool ok = key < KEY_NONE - (uint64_t)ncp;
+    probes[row * nprobe + p] = ok ? (int32_t)key_id(key) : -1;
+    term[row * nprobe + p] = ok ? key_dist(key) : 0.0f;
+  }
+}
+
 // Per-query table lut[m][k] = scale * <q_m, C[m][k]>: warp w builds
 // subspaces w, w + 8, ...; each lane owns 8 codewords and keeps q_m in
 // registers, with the codeword rows read as float4 when dsub is 4 or 8.
@@ -604,6 +735,18 @@ void launch_coarse_fast(const float* approx, int64_t nq, int nlist, const float*
   smem_attr(k_coarse_fast, smem);
   k_coarse_fast<<<(unsigned)nq, FT, smem, s>>>(approx, nlist, q, d, cent, metric, nc, ncp, nprobe,
                                                 probes, term, err);
+  count_launch();
+  MV_CHECK_CUDA(cudaGetLastError());
+}
+
+void launch_coarse_rows(const float* approx, int64_t nq, int nlist, const float* q, int d,
+                        const float* cent, int metric, int nc, int nprobe, int32_t* probes,
+                        float* term, int* err, cudaStream_t s) {
+  if (nq == 0) return;
+  MV_REQUIRE(nc >= 1 && nc <= 64 && nc <= nlist && nprobe <= nc, MV_ERR_UNSUPPORTED,
+             "coarse rows: nc must be in [nprobe, min(64, nlist)]");
+  k_coarse_rows<<<(unsigned)((nq + CR_WARPS - 1) / CR_WARPS), CR_WARPS * 32, 0, s>>>(
+      approx, nq, nlist, q, d, cent, metric, nc, nprobe, probes, term, err);
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());
 }

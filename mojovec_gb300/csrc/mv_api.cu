@@ -605,7 +605,12 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
   const int kp = umma_kpad(ix->d);
   // Fused coarse (tensor-core GEMM keeping each query's best nc lists) when
   // nc fits the epilogue's per-row list; otherwise the distance matrix path.
-  const bool fused = !fp32_coarse && nc <= 64 && !(batch && batch->coarse_matrix);
+  const int cpath = p ? p->coarse_path : 0;
+  MV_REQUIRE(cpath >= 0 && cpath <= 2, MV_ERR_ARG, "coarse_path must be 0, 1 or 2");
+  // Automatic: the fused epilogue up to 16 candidates per row; above that
+  // the distance matrix with one warp per query selecting is faster.
+  const bool fused = !fp32_coarse && nc <= 64 &&
+                     (batch ? !batch->coarse_matrix : (cpath == 1 || (cpath == 0 && nc <= 16)));
   int64_t qb = std::max<int64_t>(128, (int64_t)(1536ll * 1024 * 1024 / ((int64_t)ix->nlist * 4)));
   qb = std::min<int64_t>({qb, nq, 65535ll * 64});
   if (batch) {
@@ -652,6 +657,9 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
       if (fused)
         launch_coarse_from_keys(ckeys, nb, ncand, xb, ix->d, ix->centroids.as<float>(), ix->nlist,
                                 ix->metric, nc, nprobe, probes, term, ix->ctx->d_err.as<int>(), s);
+      else if (nc <= 64)
+        launch_coarse_rows(dmat, nb, ix->nlist, xb, ix->d, ix->centroids.as<float>(), ix->metric,
+                           nc, nprobe, probes, term, ix->ctx->d_err.as<int>(), s);
       else
         launch_coarse_fast(dmat, nb, ix->nlist, xb, ix->d, ix->centroids.as<float>(), ix->metric,
                            nc, nprobe, probes, term, ix->ctx->d_err.as<int>(), s);
@@ -2167,6 +2175,10 @@ int32_t mv_ivfpq_plan_create(mv_ivfpq* ix, int64_t max_nq, int32_t nprobe_max, i
     pl->kmax = kmax;
     if (params) pl->params = *params;
     pl->params.form = MV_FORM_FAST;
+    // the tuner may change it
+    const int nc = std::min(ix->nlist, nprobe_max + std::max(8, nprobe_max / 4));
+    pl->cfg.coarse_matrix =
+        pl->params.coarse_path == 2 || (pl->params.coarse_path == 0 && nc > 16);
     MV_CHECK_CUDA(cudaStreamCreateWithFlags(&pl->stream, cudaStreamNonBlocking));
     pl->x.ensure(sizeof(float) * max_nq * ix->d);
     pl->nprobe_q.ensure(sizeof(int32_t) * max_nq);
@@ -2344,7 +2356,9 @@ void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int npr
   const bool fast = p && p->form == MV_FORM_FAST && umma_kpad(ix->d) <= 256;
   const int kp = umma_kpad(ix->d);
   const int nc = std::min(ix->nlist, nprobe + std::max(8, nprobe / 4));
-  const bool fused = fast && nc <= 64;
+  const int cpath = p ? p->coarse_path : 0;
+  MV_REQUIRE(cpath >= 0 && cpath <= 2, MV_ERR_ARG, "coarse_path must be 0, 1 or 2");
+  const bool fused = fast && nc <= 64 && (cpath == 1 || (cpath == 0 && nc <= 16));
   if (fast) {
     std::lock_guard<std::mutex> lk(ix->fast_mu);
     if (!ix->fast_ready) {
@@ -2401,6 +2415,9 @@ void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int npr
       } else if (fused) {
         launch_coarse_from_keys(fkeys, nb, ncand, xb, ix->d, ix->centroids.as<float>(), ix->nlist,
                                 ix->metric, nc, nprobe, probes, term, ix->ctx->d_err.as<int>(), s);
+      } else if (nc <= 64) {
+        launch_coarse_rows(dmat, nb, ix->nlist, xb, ix->d, ix->centroids.as<float>(), ix->metric,
+                           nc, nprobe, probes, term, ix->ctx->d_err.as<int>(), s);
       } else {
         launch_coarse_fast(dmat, nb, ix->nlist, xb, ix->d, ix->centroids.as<float>(), ix->metric,
                            nc, nprobe, probes, term, ix->ctx->d_err.as<int>(), s);

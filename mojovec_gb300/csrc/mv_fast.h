@@ -53,6 +53,10 @@ void launch_vec_terms(const int64_t* off, int nlist, const uint8_t* codes, const
 void launch_coarse_fast(const float* approx, int64_t nq, int nlist, const float* q, int d,
                         const float* cent, int metric, int nc, int nprobe, int32_t* probes,
                         float* term, int* err, cudaStream_t s);
+// Same with one warp per query and a lane-minimum threshold (nc <= 64).
+void launch_coarse_rows(const float* approx, int64_t nq, int nlist, const float* q, int d,
+                        const float* cent, int metric, int nc, int nprobe, int32_t* probes,
+                        float* term, int* err, cudaStream_t s);
 // Same from per-row candidate keys (ncand per row, KEY_NONE padded).
 void launch_coarse_from_keys(const uint64_t* cand, int64_t nq, int ncand, const float* q, int d,
                              const float* cent, int nlist, int metric, int nc, int nprobe,

@@ -19,14 +19,36 @@ int64 (n, k)) instead of filling caller Spans.
 
 from __future__ import annotations
 
+import atexit
 import ctypes as C
 import os
 import threading
+import weakref
 
 import numpy as np
 
 from . import _lib
 from ._lib import FORM_FAST, METRIC_IP, METRIC_L2, SearchParams, check
+
+
+# Native objects still alive at interpreter exit are destroyed by an atexit
+# hook, servers first, then plans, then indexes (servers and plans use their
+# indexes), before the interpreter's teardown would run their finalizers in
+# an arbitrary order (a plan's CUDA graphs outliving its index).
+_LIVE = (weakref.WeakSet(), weakref.WeakSet(), weakref.WeakSet())
+_TIER_SERVER, _TIER_PLAN, _TIER_INDEX = 0, 1, 2
+
+
+def _release_all():
+    for tier in _LIVE:
+        for obj in list(tier):
+            try:
+                obj._release()
+            except Exception:  # noqa: BLE001 - best effort at exit
+                pass
+
+
+atexit.register(_release_all)
 
 
 def _f32(a, d=None):
@@ -90,8 +112,9 @@ class Context:
         return {name: (float(ms[i]), int(cnt[i])) for i, name in enumerate(_lib.STAGES) if cnt[i]}
 
 
-def _params(form=None, nprobe=0, rerank=0, coarse_fp32=False, lut_fp16=False):
+def _params(form=None, nprobe=0, rerank=0, coarse_fp32=False, lut_fp16=False, coarse_path=0):
     p = SearchParams()
+    p.coarse_path = int(coarse_path)
     p.form = _lib.FORM_PLAIN if form is None else int(form)
     p.nprobe = int(nprobe)
     p.rerank = int(rerank)
@@ -108,14 +131,18 @@ class IndexIVFPQ:
         h = C.c_void_p()
         check(_lib.load().mv_ivfpq_create(self.ctx.handle, d, nlist, M, metric, C.byref(h)))
         self._h = h
+        _LIVE[_TIER_INDEX].add(self)
         self.d, self.nlist, self.M, self.metric_type = d, nlist, M, metric
         self.ksub = 256
 
-    def __del__(self):
+    def _release(self):
         h = getattr(self, "_h", None)
         if h and _lib._lib is not None:
             _lib._lib.mv_ivfpq_destroy(h)
-            self._h = None
+        self._h = None
+
+    def __del__(self):
+        self._release()
 
     def _info(self):
         out = np.zeros(7, np.int64)
@@ -212,6 +239,7 @@ class IndexIVFPQ:
         check(lib.mv_ivfpq_load_snapshot(ctx.handle, os.fsencode(path), C.byref(h)))
         self = cls.__new__(cls)
         self.ctx, self._h, self.ksub = ctx, h, 256
+        _LIVE[_TIER_INDEX].add(self)
         info = np.zeros(7, np.int64)
         check(lib.mv_ivfpq_info(h, _p(info)))
         self.d, self.nlist, self.M = int(info[0]), int(info[1]), int(info[2])
@@ -226,13 +254,13 @@ class IndexIVFPQ:
         return self
 
     def search(self, x, k: int, filter=None, form=None, nprobe: int = 0, rerank: int = 0,
-               coarse_fp32: bool = False, lut_fp16: bool = False):
+               coarse_fp32: bool = False, lut_fp16: bool = False, coarse_path: int = 0):
         x = _f32(x, self.d)
         n = x.shape[0]
         dist = np.empty((n, k), np.float32)
         lab = np.empty((n, k), np.int64)
         flt = None if filter is None else np.ascontiguousarray(filter, dtype=np.uint8)
-        p = _params(form, nprobe, rerank, coarse_fp32, lut_fp16)
+        p = _params(form, nprobe, rerank, coarse_fp32, lut_fp16, coarse_path)
         check(_lib.load().mv_ivfpq_search(self._h, _p(x), n, k, _p(flt),
                                           0 if flt is None else flt.size, C.byref(p), _p(dist),
                                           _p(lab)))
@@ -256,9 +284,9 @@ class IndexIVFPQ:
 
     def search_device(self, x_ptr: int, n: int, k: int, dist_ptr: int, lab_ptr: int,
                       stream: int = 0, form=None, nprobe: int = 0, rerank: int = 0,
-                      coarse_fp32: bool = False, lut_fp16: bool = False):
+                      coarse_fp32: bool = False, lut_fp16: bool = False, coarse_path: int = 0):
         """Device-pointer search (e.g. torch tensors' data_ptr())."""
-        p = _params(form, nprobe, rerank, coarse_fp32, lut_fp16)
+        p = _params(form, nprobe, rerank, coarse_fp32, lut_fp16, coarse_path)
         check(_lib.load().mv_ivfpq_search_device(self._h, x_ptr, n, k, None, 0, C.byref(p),
                                                  dist_ptr, lab_ptr, stream or None))
 
@@ -271,13 +299,17 @@ class IndexIVFFlat:
         h = C.c_void_p()
         check(_lib.load().mv_ivfflat_create(self.ctx.handle, d, nlist, metric, C.byref(h)))
         self._h = h
+        _LIVE[_TIER_INDEX].add(self)
         self.d, self.nlist, self.metric_type = d, nlist, metric
 
-    def __del__(self):
+    def _release(self):
         h = getattr(self, "_h", None)
         if h and _lib._lib is not None:
             _lib._lib.mv_ivfflat_destroy(h)
-            self._h = None
+        self._h = None
+
+    def __del__(self):
+        self._release()
 
     @property
     def ntotal(self) -> int:
@@ -328,13 +360,17 @@ class IndexFlat:
         h = C.c_void_p()
         check(_lib.load().mv_flat_create(self.ctx.handle, d, metric, C.byref(h)))
         self._h = h
+        _LIVE[_TIER_INDEX].add(self)
         self.d, self.metric_type = d, metric
 
-    def __del__(self):
+    def _release(self):
         h = getattr(self, "_h", None)
         if h and _lib._lib is not None:
             _lib._lib.mv_flat_destroy(h)
-            self._h = None
+        self._h = None
+
+    def __del__(self):
+        self._release()
 
     @property
     def ntotal(self) -> int:
@@ -382,13 +418,17 @@ class IndexFlatSQ8:
         h = C.c_void_p()
         check(_lib.load().mv_sq8_create(self.ctx.handle, d, metric, C.byref(h)))
         self._h = h
+        _LIVE[_TIER_INDEX].add(self)
         self.d, self.metric_type = d, metric
 
-    def __del__(self):
+    def _release(self):
         h = getattr(self, "_h", None)
         if h and _lib._lib is not None:
             _lib._lib.mv_sq8_destroy(h)
-            self._h = None
+        self._h = None
+
+    def __del__(self):
+        self._release()
 
     def _params(self):
         out = np.zeros(3, np.float32)
@@ -575,16 +615,20 @@ class IVFPQBatchPlan:
         check(_lib.load().mv_ivfpq_plan_create(index._h, max_nq, nprobe_max, kmax, C.byref(p),
                                                C.byref(h)))
         self._h = h
+        _LIVE[_TIER_PLAN].add(self)
         ptrs = [C.c_void_p() for _ in range(6)]
         check(_lib.load().mv_ivfpq_plan_buffers(h, *[C.byref(q) for q in ptrs]))
         (self.d_x, self.d_nprobe, self.d_k, self.d_order, self.d_dist,
          self.d_labels) = [q.value for q in ptrs]
 
-    def __del__(self):
+    def _release(self):
         h = getattr(self, "_h", None)
         if h and _lib._lib is not None:
             _lib._lib.mv_ivfpq_plan_destroy(h)
-            self._h = None
+        self._h = None
+
+    def __del__(self):
+        self._release()
 
     def set_queries(self, x, nprobe, k):
         """Host queries (or None when d_x was filled on the device), per-query
@@ -628,6 +672,7 @@ class Server:
         check(_lib.load().mv_server_create(self.ctx.handle, int(hbm_budget), lanes,
                                            max_batch_queries, C.byref(h)))
         self._h = h
+        _LIVE[_TIER_SERVER].add(self)
         self._dims = {}
         self._pending = {}
 
@@ -635,7 +680,9 @@ class Server:
         h = getattr(self, "_h", None)
         if h and _lib._lib is not None:
             _lib._lib.mv_server_destroy(h)
-            self._h = None
+        self._h = None
+
+    _release = close
 
     def __del__(self):
         self.close()
