@@ -547,6 +547,11 @@ __global__ void __launch_bounds__(NT) k_ivfpq_scan_fast(FastScanArgs a) {
         pos1 = 0;
         keep0 = keep1 = false;
       }
+      if (a.filter) {  // filtered ids never enter the shortlist
+        const uint32_t id0 = a.ids[pos0c], id1 = a.ids[pos1];
+        if ((int64_t)id0 < a.filter_len && a.filter[id0] != 0) keep0 = false;
+        if ((int64_t)id1 < a.filter_len && a.filter[id1] != 0) keep1 = false;
+      }
       const float v0 = a.vterm ? a.vterm[pos0c] : 0.0f;
       const float v1 = a.vterm ? a.vterm[pos1] : 0.0f;
       float d0, d1;

@@ -587,7 +587,8 @@ void ensure_fast(mv_ivfpq* ix, cudaStream_t s) {
 // workspace is sized, so it can be captured in a CUDA graph.
 void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int nprobe,
                        const mv_search_params* p, float* d_out, int64_t* d_lab, DevBuf& ws,
-                       cudaStream_t s, const FastBatch* batch = nullptr) {
+                       cudaStream_t s, const FastBatch* batch = nullptr,
+                       const uint8_t* d_filter = nullptr, int64_t filter_len = 0) {
   if (nq == 0) return;
   if (!ix->trained || ix->ntotal == 0) {
     launch_fill(d_out, d_lab, nq * k, 1e38f, s);
@@ -685,6 +686,11 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
       a.nlist = ix->nlist;
       a.ntotal = ix->h_off[ix->nlist];
       a.err = ix->ctx->d_err.as<int>();
+      if (d_filter && filter_len > 0) {
+        a.filter = d_filter;
+        a.filter_len = filter_len;
+        a.ids = ix->d_ids.as<uint32_t>();
+      }
       if (batch) {
         a.nprobe_q = batch->nprobe_q;
         a.order = batch->order;
@@ -727,8 +733,8 @@ void ivfpq_search_any(mv_ivfpq* ix, const float* d_x, int64_t nq, int k,
   const int form = p ? p->form : MV_FORM_PLAIN;
   const int nprobe = effective_nprobe(ix, p);
   if (form == MV_FORM_FAST) {
-    MV_REQUIRE(d_filter == nullptr, MV_ERR_UNSUPPORTED, "the fast form takes no filter");
-    ivfpq_search_fast(ix, d_x, nq, k, nprobe, p, d_out, d_lab, ws, s);
+    ivfpq_search_fast(ix, d_x, nq, k, nprobe, p, d_out, d_lab, ws, s, nullptr, d_filter,
+                      filter_len);
   } else {
     MV_REQUIRE(form == MV_FORM_PLAIN, MV_ERR_ARG, "unknown search form");
     ivfpq_search_plain(ix, d_x, nq, k, nprobe, d_filter, filter_len, d_out, d_lab, ws, s);

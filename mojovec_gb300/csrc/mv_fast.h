@@ -27,6 +27,11 @@ struct FastScanArgs {
   const int32_t* nprobe_q = nullptr;  // per-query nprobe (<= nprobe), may be null
   const int32_t* order = nullptr;     // scan order of the queries, may be null
   int* counter = nullptr;             // persistent grid: next position in `order`
+  // index_ivf_pq.mojo:328-334: an entry whose id is below filter_len and has
+  // filter[id] != 0 is skipped (ids: the id of each CSR entry)
+  const uint8_t* filter = nullptr;
+  int64_t filter_len = 0;
+  const uint32_t* ids = nullptr;
   int cap, Rp;            // set by the launcher
 };
 

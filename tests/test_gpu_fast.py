@@ -158,3 +158,43 @@ def test_fast_fused_coarse_matches_matrix_coarse(mv):
         _, lc = g.search(q, 10, form=mv.FORM_FAST, nprobe=nprobe, rerank=100, coarse_fp32=True)
         agree = np.mean([len(set(a) & set(b)) / 10 for a, b in zip(lf, lc)])
         assert agree > 0.97, (nprobe, agree)
+
+
+def test_fast_paths_pick_the_same_lists(mv):
+    """coarse_path 1 (fused GEMM + per-row heap) and 2 (distance matrix + one
+    warp per query) keep the same approximate top-nc lists, so the searches
+    agree exactly."""
+    from mojovec_gb300 import synth
+
+    base, q = synth.sift_like(40000, d=96, n_centers=64, nq=300, seed=34)
+    g = _index(mv, base, 96, 512, 24)
+    for nprobe in (4, 16, 48):
+        a = g.search(q, 10, form=mv.FORM_FAST, nprobe=nprobe, rerank=64, coarse_path=1)
+        b = g.search(q, 10, form=mv.FORM_FAST, nprobe=nprobe, rerank=64, coarse_path=2)
+        assert np.array_equal(a[1], b[1]) and np.array_equal(a[0], b[0]), nprobe
+
+
+@pytest.mark.parametrize("rerank", [0, 128])
+def test_fast_filter_equals_index_without_filtered_rows(mv, rerank):
+    """index_ivf_pq.mojo:328-334 in the fast form: a filtered id never enters
+    the shortlist, so the search equals the same search over an index that
+    never held those rows (same codebooks, same ids). A filter shorter than
+    the ids leaves the ids past its end unfiltered."""
+    rng = np.random.default_rng(31)
+    d, nlist, M, n = 64, 64, 8, 20000
+    x = rng.standard_normal((n, d)).astype(np.float32)
+    q = rng.standard_normal((200, d)).astype(np.float32)
+    g = mv.IndexIVFPQ(d, nlist, M)
+    g.train(x[:8000], niter_coarse=4, niter_pq=4)
+    cent, pq = g.codebooks()
+    g.add(x)
+    filt = (rng.random(n - 3000) < 0.3).astype(np.uint8)  # ids >= n - 3000 stay in
+    keep = np.flatnonzero(np.concatenate([filt, np.zeros(3000, np.uint8)]) == 0)
+    h = mv.IndexIVFPQ(d, nlist, M)
+    h.set_codebooks(cent, pq)
+    h.add_with_ids(x[keep], keep)
+    a_d, a_l = g.search(q, 10, filter=filt, form=mv.FORM_FAST, nprobe=8, rerank=rerank)
+    b_d, b_l = h.search(q, 10, form=mv.FORM_FAST, nprobe=8, rerank=rerank)
+    hit = a_l[(a_l >= 0) & (a_l < len(filt))]
+    assert not filt[hit].any()
+    assert np.array_equal(a_l, b_l) and np.array_equal(a_d, b_d)
