@@ -460,7 +460,9 @@ def run_flat(args, rank, world):
             clocks.start()
             ctx.profile(True)
             launches0 = ctx.kernel_launches()
+        torch.cuda.nvtx.range_push(f"timed_{args.workload}_{name}")
         ms = _timed_steps(torch, step, steps, stream, flush)
+        torch.cuda.nvtx.range_pop()
         if name == "fast":
             launches = ctx.kernel_launches() - launches0
             stage = ctx.stage_times()
@@ -690,7 +692,9 @@ def run_batch(args, rank, world):
     clocks = ClockSampler(dev)
     clocks.start()
     l0 = ctx.kernel_launches()
+    torch.cuda.nvtx.range_push("timed_batch")
     ms = timed(lambda: plan.run(nq, use_graph=True, stream=stream.cuda_stream), args.steps)
+    torch.cuda.nvtx.range_pop()
     launches = ctx.kernel_launches() - l0
     clk = clocks.stop()
     dist, lab = plan.results(nq)
@@ -777,7 +781,9 @@ def run_kmeans(args, rank, world):
         ctx.profile(True)
         l0 = ctx.kernel_launches()
         t0 = time.perf_counter()
+        torch.cuda.nvtx.range_push(f"timed_kmeans_{name}")
         km.train(x)
+        torch.cuda.nvtx.range_pop()
         e2e_s = time.perf_counter() - t0
         st = ctx.stage_times()
         ctx.profile(False)
