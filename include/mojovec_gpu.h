@@ -70,7 +70,10 @@ typedef struct mv_search_params {
   int32_t coarse_path; /* fast form, BF16 coarse step: 0 = automatic, 1 = GEMM with a
                           per-row top-k epilogue, 2 = distance matrix then one warp
                           per query selecting its lists */
-  int32_t reserved[2];
+  int32_t plain_scan;  /* plain form, Flat and SQ8: 1 = the exact SIMT scan alone, without
+                          the tensor-core shortlist that is proven (Flat) or exact by
+                          construction (SQ8) to give the same results */
+  int32_t reserved[1];
 } mv_search_params;
 
 /* ---- library / context ---------------------------------------------- */
@@ -101,11 +104,14 @@ int64_t mv_ctx_kernel_launches(mv_ctx* ctx);
 #define MV_STAGE_APPEND 7   /* list append: CSR layout + scatter */
 #define MV_STAGE_COUNT 8
 int32_t mv_ctx_profile(mv_ctx* ctx, int32_t enable);
-/* Nearest-centroid assignments (index add, training, plain k-means) run on
- * the tensor cores with an exact FP32 recheck and an error bound; rows the
- * bound cannot settle take the exact FP32 scan. Reports the rows assigned
- * that way and how many of them took the exact scan, since context creation. */
-int32_t mv_ctx_assign_stats(mv_ctx* ctx, int64_t* rows, int64_t* fallback_rows);
+/* Plain-form selections run on the tensor cores with an exact FP32 recheck
+ * and an error bound that proves the result equals the exact scan's;
+ * selections the bound cannot settle take the exact FP32 scan. out4: rows
+ * assigned to their nearest centroid that way (index add, training, plain
+ * k-means), how many of them took the exact scan, plain Flat queries
+ * answered that way, how many of them took the exact scan (since context
+ * creation). */
+int32_t mv_ctx_certify_stats(mv_ctx* ctx, int64_t* out4);
 int32_t mv_ctx_stage_times(mv_ctx* ctx, double* ms, int64_t* counts, int32_t nstages);
 
 /* ---- IVF-PQ index: replaces IndexIVFPQ[IndexFlat]

@@ -59,7 +59,8 @@ class SearchParams(C.Structure):
         ("coarse_fp32", C.c_int32),
         ("lut_fp16", C.c_int32),
         ("coarse_path", C.c_int32),
-        ("reserved", C.c_int32 * 2),
+        ("plain_scan", C.c_int32),
+        ("reserved", C.c_int32 * 1),
     ]
 
 
@@ -73,7 +74,7 @@ SIGNATURES = {
     "mv_last_error": (_i32, [C.c_char_p, C.c_size_t]),
     "mv_version": (C.c_char_p, []),
     "mv_ctx_create": (_i32, [_i32, C.POINTER(_vp)]),
-    "mv_ctx_assign_stats": (_i32, [_vp, _vp, _vp]),
+    "mv_ctx_certify_stats": (_i32, [_vp, _vp]),
     "mv_ctx_destroy": (_i32, [_vp]),
     "mv_ctx_synchronize": (_i32, [_vp]),
     "mv_ctx_kernel_launches": (_i64, [_vp]),

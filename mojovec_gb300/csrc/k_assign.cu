@@ -1,37 +1,19 @@
-// Certified exact nearest-centroid assignment.
+// Certified exact selections on the tensor cores.
 //
-// The reference assigns a row to its nearest centroid with FP32 distances in
-// a fixed operation order (index/index_flat.mojo:292-310 with k = 1 for the
-// coarse quantizer; clustering/kmeans.mojo:123-141 in k-means): the smallest
-// distance, the smaller index on equal distances. Here the BF16 tensor-core
-// top-k GEMM (k_umma_topk) proposes kc candidates per row, k_assign_certify
-// recomputes the candidates with the reference's FP32 distance and keeps the
-// best, and a rigorous bound on the BF16 ranking error decides whether any
-// centroid outside the candidates could still be nearer. Rows the bound does
-// not settle (and rows with NaN or huge distances) are listed for the exact
-// SIMT argmin, so the result always equals the exact one.
-//
-// Bound (bx, by: the rows rounded to BF16, round to nearest, unit roundoff
-// u = 2^-8; X = ||bx||, B = max over centroids of ||by||). The candidate key
-// of centroid c is kd(c) = fl(||by||^2 - 2 acc), acc the tensor-core FP32 sum
-// of the exact products bx_i * by_i, ||by||^2 summed in FP32:
-//   | kd(c) - (||by||^2 - 2 bx.by) | <= (d + 1) 2^-23 B^2 + (d + 1) 2^-21 X B
-// (each FP32 addition of the tensor core's sum taken as losing up to 2^-22
-// of the sum of |products|; the code doubles that term). Rows or centroids
-// with norms outside [1e-15, 1e150] are not certified.
-// Every centroid outside the candidates has kd(c) >= K, the kc-th smallest
-// candidate key (a per-segment heap or the shared threshold dropped it only
-// below kc better keys that the candidates still hold, or beat). Then
-//   L2: ||bx - by|| >= sqrt(X^2 + K - eps) and, as ||x - bx|| <= u ||x||,
-//       ||x - y|| >= sqrt(X^2 + K - eps) - u (X + B) / (1 - u) = s,
-//       and the reference distance is at least s^2 (1 - g), g = (d + 16) 2^-23
-//       (FP32 sum of non-negative squares);
-//   IP: x.y <= -K + (2u (1 + 2u) + (d + 1) 2^-21) X B, and the reference
-//       distance -fl(x.y) >= K - (2u (1 + 2u) + (d + 1) 2^-21 + g (1 + 3u)) X B.
-// A row is settled when that lower bound exceeds the best candidate's
-// reference distance (strictly, so ties cannot hide outside).
+// The plain form must return the reference's own FP32 results: the nearest
+// centroid of a row (index/index_flat.mojo:292-310 with k = 1 for the coarse
+// quantizer; clustering/kmeans.mojo:123-141 in k-means) and the Flat top-k
+// (index/index_flat.mojo:260-325), with the smaller index on equal
+// distances. Here the BF16 tensor-core top-k GEMM (k_umma_topk) proposes
+// candidates, their distances are recomputed with the reference's FP32
+// operation order (l2_simd<8> / -ip_simd<8>), and the bound of mv_cert.cuh
+// decides whether any row outside the candidates could still rank ahead.
+// Selections the bound does not settle (and those with NaN or huge
+// distances) are listed for the exact SIMT scan, so the result always equals
+// the exact one.
 #include <cuda_bf16.h>
 
+#include "mv_cert.cuh"
 #include "mv_exact.cuh"
 #include "mv_internal.h"
 #include "mv_kernels.h"
@@ -40,13 +22,14 @@
 namespace mv {
 namespace {
 
-// B^2 upper bound: max of the FP32 norms of the BF16 rows, with the FP32
-// summation error added.
-__global__ void k_max_norm(const float* __restrict__ norms, int n, int d, double* __restrict__ out) {
+// cert[0] = B^2 bound: max of the FP32 norms of the BF16 rows with the
+// summation slack, or -1 when a norm is NaN or infinite.
+__global__ void k_max_norm(const float* __restrict__ norms, int64_t n, int d,
+                           double* __restrict__ out) {
   __shared__ double part[32];
   double m = 0.0;
   bool bad = false;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
     const float v = norms[i];
     if (!(v <= 3.0e38f)) bad = true;  // NaN or inf
     m = fmax(m, (double)v);
@@ -66,6 +49,26 @@ __global__ void k_max_norm(const float* __restrict__ norms, int n, int d, double
   }
 }
 
+// out = max over rows of ||y - bf16(y)|| (bits of a non-negative double,
+// zeroed by the caller), one warp per row.
+__global__ void k_resid_max(const float* __restrict__ rows, int64_t n, int d,
+                            unsigned long long* __restrict__ out) {
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  double s = 0.0;
+  for (int j = lane; j < d; j += 32) {
+    const float v = rows[row * d + j];
+    const double r = (double)v - (double)__bfloat162float(__float2bfloat16_rn(v));
+    s = fma(r, r, s);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    const double v = s != s ? 1e300 : sqrt(s) * (1.0 + 1e-12);
+    atomicMax(out, (unsigned long long)__double_as_longlong(v));
+  }
+}
+
 __device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
   for (int o = 16; o > 0; o >>= 1) {
     const uint64_t w = __shfl_xor_sync(0xffffffffu, v, o);
@@ -74,12 +77,34 @@ __device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
   return v;
 }
 
-// One warp per row.
+// X^2 = ||bx||^2 and rq^2 = ||x - bx||^2 of one row, in double (one warp).
+__device__ __forceinline__ void bf16_norms(const float* x, int d, double& xs, double& rs) {
+  const int lane = threadIdx.x & 31;
+  xs = 0.0;
+  rs = 0.0;
+  for (int j = lane; j < d; j += 32) {
+    const float v = x[j];
+    const double b = (double)__bfloat162float(__float2bfloat16_rn(v));
+    const double r = (double)v - b;
+    xs = fma(b, b, xs);
+    rs = fma(r, r, rs);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    xs += __shfl_xor_sync(0xffffffffu, xs, o);
+    rs += __shfl_xor_sync(0xffffffffu, rs, o);
+  }
+}
+
+__device__ __forceinline__ bool cert_inputs_ok(double xs, double B2, double rmax) {
+  return B2 >= 1e-30 && B2 <= 1e300 && xs >= 1e-30 && xs <= 1e300 && rmax <= 1e150;
+}
+
+// Nearest centroid, one warp per row.
 template <bool IP>
 __global__ void k_assign_certify(const float* __restrict__ x, int64_t n, int d,
                                  const float* __restrict__ cent, int nlist,
                                  const uint64_t* __restrict__ cand, int ncand, int kc,
-                                 const double* __restrict__ bmax2, int32_t* __restrict__ assign,
+                                 const double* __restrict__ cert, int32_t* __restrict__ assign,
                                  float* __restrict__ mind, int64_t* __restrict__ flagged,
                                  int* __restrict__ nflag) {
   const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -117,7 +142,7 @@ __global__ void k_assign_certify(const float* __restrict__ x, int64_t n, int d,
   bad = __any_sync(0xffffffffu, bad);
   bool ok = !bad && bi != 0x7fffffff && best < 1e38f;
   if (ok && valid < nlist) {
-    // K: the kc-th smallest candidate key
+    // K: the kc-th smallest candidate key (the largest a full heap keeps)
     uint64_t prev = 0;
     for (int t = 0; t < kc; ++t) {
       uint64_t m = KEY_NONE;
@@ -128,32 +153,15 @@ __global__ void k_assign_certify(const float* __restrict__ x, int64_t n, int d,
       }
       prev = warp_min_u64(m);
     }
-    // X^2 = ||bx||^2 (exact in double)
-    double xs = 0.0;
-    for (int j = lane; j < d; j += 32) {
-      const double b = (double)__bfloat162float(__float2bfloat16_rn(xr[j]));
-      xs = fma(b, b, xs);
-    }
-    for (int o = 16; o > 0; o >>= 1) xs += __shfl_xor_sync(0xffffffffu, xs, o);
-    const double B2 = *bmax2;
-    if (valid < kc || prev == KEY_NONE || !(B2 >= 1e-30) || !(xs >= 1e-30 && xs <= 1e300)) {
+    double xs, rs;
+    bf16_norms(xr, d, xs, rs);
+    const double B2 = cert[0], rmax = cert[1];
+    if (valid < kc || prev == KEY_NONE || !cert_inputs_ok(xs, B2, rmax)) {
       ok = false;
     } else {
       const double K = (double)key_dist(prev);
-      const double X = sqrt(xs), B = sqrt(B2);
-      const double u = 0x1p-8;
-      const double g = (d + 16) * 0x1p-23;
-      const double ea = (d + 1) * 0x1p-20;  // twice the tensor-core accumulation bound
-      const double eabs = d * 1e-36;         // products below FP32's normal range
-      double lower;
-      if (IP) {
-        lower = K - (2.0 * u * (1.0 + 2.0 * u) + ea + g * (1.0 + 3.0 * u)) * X * B * 1.01 - eabs;
-      } else {
-        const double eps = ((d + 1) * 0x1p-23 * B2 + ea * X * B) * 1.01 + eabs;
-        const double sb = X * X + K - eps;
-        const double s = (sb > 0.0 ? sqrt(sb) : 0.0) - u * (X + B) / (1.0 - u) * 1.01;
-        lower = s > 0.0 ? s * s * (1.0 - g) : -1.0;
-      }
+      const double lower = IP ? cert_lower_ip(sqrt(xs), sqrt(rs), B2, rmax, K, d)
+                              : cert_lower_l2(sqrt(xs), sqrt(rs), B2, rmax, K, d);
       ok = lower > (double)best;
     }
   }
@@ -161,6 +169,114 @@ __global__ void k_assign_certify(const float* __restrict__ x, int64_t n, int d,
     assign[row] = bi == 0x7fffffff ? 0 : bi;
     if (mind) mind[row] = best;
     if (!ok) flagged[atomicAdd(nflag, 1)] = row;
+  }
+}
+
+// Flat top-k, one CTA per query over its shortlist of R approximate keys
+// (the R smallest of the GEMM's candidates, KEY_NONE padded): the rows are
+// staged in shared memory (stride d + 1, so thread t reading row t touches
+// its own bank) in chunks of FC_CHUNK rows, each thread computes one row's
+// reference distance, the k smallest (distance, row) keys are selected and
+// written, and the certificate compares the k-th with the bound for the
+// rows outside the shortlist. flag[q] = 1 when it does not settle the query
+// (the host recomputes those with the exact scan).
+constexpr int FC_THREADS = 128, FC_CHUNK = 64;
+
+template <bool IP>
+__global__ void __launch_bounds__(FC_THREADS)
+    k_flat_certify(const float* __restrict__ q, int d, const float* __restrict__ rows, int64_t nb,
+                   const uint64_t* __restrict__ skeys, int R, int k,
+                   const double* __restrict__ cert, const int* __restrict__ over,
+                   float* __restrict__ out_d, int64_t* __restrict__ out_l,
+                   int* __restrict__ flag) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int stride = d + 1;
+  float* qv = reinterpret_cast<float*>(smraw);
+  float* tile = qv + d;  // FC_CHUNK x (d + 1)
+  uint64_t* ek = reinterpret_cast<uint64_t*>(
+      smraw + (((size_t)d + (size_t)FC_CHUNK * stride) * 4 + 15) / 16 * 16);  // R
+  uint64_t* outb = ek + R;                                                  // next_pow2(k)
+  __shared__ RadixScratch rs;
+  __shared__ unsigned long long s_kmax;
+  __shared__ int s_valid, s_bad;
+  __shared__ double s_xs, s_rs;
+  const int64_t row = blockIdx.x;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint64_t* sk = skeys + row * R;
+  for (int j = tid; j < d; j += FC_THREADS) qv[j] = q[row * d + j];
+  if (tid == 0) {
+    s_kmax = 0ull;
+    s_valid = 0;
+    s_bad = 0;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    double xs, rsq;
+    bf16_norms(qv, d, xs, rsq);
+    if (lane == 0) {
+      s_xs = xs;
+      s_rs = rsq;
+    }
+  }
+  for (int c0 = 0; c0 < R; c0 += FC_CHUNK) {
+    const int n = min(FC_CHUNK, R - c0);
+    // stage the chunk's rows, one warp per row, coalesced
+    for (int i = warp; i < n; i += FC_THREADS / 32) {
+      const uint64_t key = sk[c0 + i];
+      const int64_t pos = key == KEY_NONE ? -1 : (int64_t)key_id(key);
+      if (pos >= 0 && pos < nb)
+        for (int j = lane; j < d; j += 32) tile[i * stride + j] = rows[pos * d + j];
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += FC_THREADS) {
+      const uint64_t key = sk[c0 + i];
+      const int64_t pos = key == KEY_NONE ? -1 : (int64_t)key_id(key);
+      uint64_t e = KEY_NONE - (uint64_t)(c0 + i);  // distinct padding keys
+      if (pos >= 0 && pos < nb) {
+        const float* yr = tile + i * stride;
+        const float r = IP ? -ip_simd<8>(qv, yr, d) : l2_simd<8>(qv, yr, d);
+        if (!(r < 1e38f && r > -1e38f)) atomicExch(&s_bad, 1);  // NaN, inf or huge
+        e = make_key(r, (uint32_t)pos);
+        atomicMax(&s_kmax, (unsigned long long)key);
+        atomicAdd(&s_valid, 1);
+      }
+      ek[c0 + i] = e;
+    }
+    __syncthreads();  // the tile is reused by the next chunk
+  }
+  const int kp = next_pow2(k);
+  const int r = block_radix_select<FC_THREADS>(ek, R, k, outb, rs);
+  for (int j = r + tid; j < kp; j += FC_THREADS) outb[j] = KEY_NONE;
+  __syncthreads();
+  block_bitonic_sort(outb, kp);
+  const int valid = s_valid;
+  for (int i = tid; i < k; i += FC_THREADS) {
+    const uint64_t key = outb[i];
+    float dd = 0.0f;  // index_flat.mojo:232-238: unfilled slots 0.0 / -1
+    int64_t ll = -1;
+    if (i < valid && key < KEY_NONE - (uint64_t)R) {
+      dd = key_dist(key);
+      if (IP) dd = -dd;
+      ll = (int64_t)key_id(key);
+    }
+    out_d[row * k + i] = dd;
+    out_l[row * k + i] = ll;
+  }
+  if (tid == 0) {
+    bool ok = !s_bad && !(over && over[row]);
+    if (ok && valid >= R) {  // rows outside the shortlist exist: bound them
+      const double B2 = cert[0], rmax = cert[1];
+      if (!cert_inputs_ok(s_xs, B2, rmax) || valid < k) {
+        ok = false;
+      } else {
+        const double K = (double)key_dist((uint64_t)s_kmax);
+        const double X = sqrt(s_xs), rq = sqrt(s_rs);
+        const double lower = IP ? cert_lower_ip(X, rq, B2, rmax, K, d)
+                                : cert_lower_l2(X, rq, B2, rmax, K, d);
+        ok = lower > (double)key_dist(outb[k - 1]);
+      }
+    }
+    flag[row] = ok ? 0 : 1;
   }
 }
 
@@ -175,24 +291,54 @@ __global__ void k_scatter_assign(const int32_t* __restrict__ sub, const float* _
 
 }  // namespace
 
-void launch_max_norm(const float* norms, int n, int d, double* out, cudaStream_t s) {
-  k_max_norm<<<1, 1024, 0, s>>>(norms, n, d, out);
+void launch_cert_bounds(const float* norms, const float* rows, int64_t n, int d, double* cert,
+                        cudaStream_t s) {
+  k_max_norm<<<1, 1024, 0, s>>>(norms, n, d, cert);
+  MV_CHECK_CUDA(cudaMemsetAsync(cert + 1, 0, sizeof(double), s));
+  if (n > 0)
+    k_resid_max<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(
+        rows, n, d, reinterpret_cast<unsigned long long*>(cert + 1));
+  count_launch();
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());
 }
 
 void launch_assign_certify(const float* x, int64_t n, int d, const float* cent, int nlist, int metric,
-                           const uint64_t* cand, int ncand, int kc, const double* bmax2,
+                           const uint64_t* cand, int ncand, int kc, const double* cert,
                            int32_t* assign, float* mind, int64_t* flagged, int* nflag,
                            cudaStream_t s) {
   if (n == 0) return;
   const unsigned grid = (unsigned)((n + 7) / 8);
   if (metric == MV_METRIC_IP)
-    k_assign_certify<true><<<grid, 256, 0, s>>>(x, n, d, cent, nlist, cand, ncand, kc, bmax2,
-                                                       assign, mind, flagged, nflag);
+    k_assign_certify<true><<<grid, 256, 0, s>>>(x, n, d, cent, nlist, cand, ncand, kc, cert,
+                                                assign, mind, flagged, nflag);
   else
-    k_assign_certify<false><<<grid, 256, 0, s>>>(x, n, d, cent, nlist, cand, ncand, kc, bmax2,
-                                                        assign, mind, flagged, nflag);
+    k_assign_certify<false><<<grid, 256, 0, s>>>(x, n, d, cent, nlist, cand, ncand, kc, cert,
+                                                 assign, mind, flagged, nflag);
+  count_launch();
+  MV_CHECK_CUDA(cudaGetLastError());
+}
+
+size_t flat_certify_smem(int d, int R, int k) {
+  return ((size_t)d + (size_t)FC_CHUNK * (d + 1)) * 4 + 16 + (size_t)(R + next_pow2(k)) * 8;
+}
+
+void launch_flat_certify(const float* q, int64_t nq, int d, int metric, const float* rows,
+                         int64_t nb, const uint64_t* skeys, int R, int k, const double* cert,
+                         const int* over, float* out_d, int64_t* out_l, int* flag,
+                         cudaStream_t s) {
+  if (nq == 0) return;
+  const size_t smem = flat_certify_smem(d, R, k);
+  MV_REQUIRE(smem <= 200 * 1024, MV_ERR_UNSUPPORTED, "flat certify: d or shortlist too large");
+  if (metric == MV_METRIC_IP) {
+    smem_limit(k_flat_certify<true>, smem);
+    k_flat_certify<true><<<(unsigned)nq, FC_THREADS, smem, s>>>(q, d, rows, nb, skeys, R, k, cert,
+                                                               over, out_d, out_l, flag);
+  } else {
+    smem_limit(k_flat_certify<false>, smem);
+    k_flat_certify<false><<<(unsigned)nq, FC_THREADS, smem, s>>>(q, d, rows, nb, skeys, R, k,
+                                                                cert, over, out_d, out_l, flag);
+  }
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());
 }

@@ -138,14 +138,14 @@ void assign_nearest(const float* x, int64_t n, int d, const float* cent, int k, 
   const int nseg = umma_topk_nseg(chunk, k, d, kc, ctx->num_sms);
   const int osegs = nseg * umma_topk_groups(d, kc);
   DevBuf buf;
-  buf.ensure(ws_bytes((size_t)k * kp, 2) + ws_bytes(k, 4) + ws_bytes(1, 8) +
+  buf.ensure(ws_bytes((size_t)k * kp, 2) + ws_bytes(k, 4) + ws_bytes(2, 8) +
              ws_bytes((size_t)chunk * kp, 2) + ws_bytes((size_t)chunk * osegs * ncp, 8) +
              2 * ws_bytes(chunk, 8) + ws_bytes(1, 4) + ws_bytes((size_t)chunk * d, 4) +
              2 * ws_bytes(chunk, 4));
   Arena ar(buf);
   __nv_bfloat16* cb = ar.take<__nv_bfloat16>((size_t)k * kp);
   float* cn = ar.take<float>(k);
-  double* bmax2 = ar.take<double>(1);
+  double* bounds = ar.take<double>(2);
   __nv_bfloat16* xb = ar.take<__nv_bfloat16>((size_t)chunk * kp);
   uint64_t* cand = ar.take<uint64_t>((size_t)chunk * osegs * ncp);
   uint64_t* gthr = ar.take<uint64_t>(chunk);
@@ -155,7 +155,7 @@ void assign_nearest(const float* x, int64_t n, int d, const float* cent, int k, 
   int32_t* sub_a = ar.take<int32_t>(chunk);
   float* sub_d = ar.take<float>(chunk);
   launch_to_bf16(cent, k, d, cb, cn, s);
-  launch_max_norm(cn, k, d, bmax2, s);
+  launch_cert_bounds(cn, cent, k, d, bounds, s);
   int64_t fallback = 0;
   for (int64_t r0 = 0; r0 < n; r0 += chunk) {
     const int64_t nb = std::min(chunk, n - r0);
@@ -164,7 +164,7 @@ void assign_nearest(const float* x, int64_t n, int d, const float* cent, int k, 
     launch_umma_topk(xb, nb, cb, k, d, metric, nullptr, cn, kc, nseg, nullptr,
                      osegs > 1 ? gthr : nullptr, cand, ctx->d_err.as<int>(), s);
     MV_CHECK_CUDA(cudaMemsetAsync(nflag, 0, sizeof(int), s));
-    launch_assign_certify(xr, nb, d, cent, k, metric, cand, osegs * ncp, kc, bmax2, assign + r0,
+    launch_assign_certify(xr, nb, d, cent, k, metric, cand, osegs * ncp, kc, bounds, assign + r0,
                           mind ? mind + r0 : nullptr, flagged, nflag, s);
     int h_nflag = 0;
     d2h(&h_nflag, nflag, sizeof(int), s);
@@ -406,10 +406,12 @@ int32_t mv_ctx_synchronize(mv_ctx* ctx) {
 
 int64_t mv_ctx_kernel_launches(mv_ctx* ctx) { return ctx ? ctx->launches.load() : -1; }
 
-int32_t mv_ctx_assign_stats(mv_ctx* ctx, int64_t* rows, int64_t* fallback_rows) {
-  if (!ctx) return MV_ERR_ARG;
-  if (rows) *rows = ctx->assign_rows.load();
-  if (fallback_rows) *fallback_rows = ctx->assign_fallback.load();
+int32_t mv_ctx_certify_stats(mv_ctx* ctx, int64_t* out4) {
+  if (!ctx || !out4) return MV_ERR_ARG;
+  out4[0] = ctx->assign_rows.load();
+  out4[1] = ctx->assign_fallback.load();
+  out4[2] = ctx->flat_queries.load();
+  out4[3] = ctx->flat_fallback.load();
   return MV_OK;
 }
 
@@ -1126,7 +1128,7 @@ int32_t mv_ivfpq_search(mv_ivfpq* ix, const float* x, int64_t nq, int32_t k,
 // ---------------------------------------------------------------------------
 namespace mv {
 
-void flat_search_plain(mv_flat* ix, const float* d_x, int64_t nq, int k, const uint8_t* d_filter,
+void flat_search_exact(mv_flat* ix, const float* d_x, int64_t nq, int k, const uint8_t* d_filter,
                        float* d_out, int64_t* d_lab, DevBuf& ws, cudaStream_t s) {
   if (nq == 0) return;
   const int64_t nb = ix->ntotal;
@@ -1175,10 +1177,97 @@ void ensure_flat_fast(mv_flat* ix, cudaStream_t s) {
   const int kp = umma_kpad(ix->d);
   ix->rows_bf16.ensure((size_t)ix->ntotal * kp * 2);
   ix->norms.ensure((size_t)ix->ntotal * 4);
+  ix->cert.ensure(2 * sizeof(double));
   launch_to_bf16(ix->rows.as<float>(), ix->ntotal, ix->d, ix->rows_bf16.as<__nv_bfloat16>(),
                  ix->norms.as<float>(), s);
+  launch_cert_bounds(ix->norms.as<float>(), ix->rows.as<float>(), ix->ntotal, ix->d,
+                     ix->cert.as<double>(), s);
   sync(s);
   ix->fast_ready = true;
+}
+
+// Plain Flat search (index_flat.mojo:260-325), bit-exact. Where it applies
+// it runs on the tensor cores: the BF16 top-k GEMM keeps a shortlist of R
+// rows per query, k_flat_certify computes their reference FP32 distances,
+// writes the k smallest and proves with the BF16 error bound that no other
+// row can rank ahead; queries the bound leaves open (or whose shortlist
+// overflowed) are recomputed by the exact SIMT scan. Elsewhere the exact
+// scan runs alone.
+void flat_search_plain(mv_flat* ix, const float* d_x, int64_t nq, int k, const uint8_t* d_filter,
+                       float* d_out, int64_t* d_lab, DevBuf& ws, cudaStream_t s) {
+  if (nq == 0) return;
+  const int64_t nb = ix->ntotal;
+  if (nb < 4096 || k > 128 || umma_kpad(ix->d) > 256 || nb > 0xfffffffell ||
+      flat_certify_smem(ix->d, 2 * std::max(k, 32), k) > 200 * 1024) {
+    flat_search_exact(ix, d_x, nq, k, d_filter, d_out, d_lab, ws, s);
+    return;
+  }
+  ensure_flat_fast(ix, s);
+  const int R = k <= 32 ? std::min(64, std::max(32, 2 * k)) : 2 * k;
+  const int kseg = std::min(R, UMMA_TOPK_MAX);
+  const int ncp = next_pow2(kseg);
+  const int kp = umma_kpad(ix->d);
+  const int64_t qb = std::min<int64_t>(nq, 32768);
+  int nseg = umma_topk_nseg(qb, nb, ix->d, kseg, ix->ctx->num_sms);
+  const int groups = umma_topk_groups(ix->d, kseg);
+  if (kseg < R) {  // as in the fast form: batch-independent segment counts
+    const int64_t nct = (nb + 127) / 128;
+    nseg = (int)std::min<int64_t>((R + 15) / 16 / groups + 1, std::max<int64_t>(1, nct));
+  }
+  const int osegs = nseg * groups;
+  ws.ensure(ws_bytes((size_t)qb * kp, 2) + ws_bytes((size_t)qb * osegs * ncp, 8) +
+            ws_bytes((size_t)qb * R, 8) + 2 * ws_bytes((size_t)qb, 4) + ws_bytes((size_t)qb, 8));
+  Arena ar(ws);
+  __nv_bfloat16* xq = ar.take<__nv_bfloat16>((size_t)qb * kp);
+  uint64_t* cand = ar.take<uint64_t>((size_t)qb * osegs * ncp);
+  uint64_t* skeys = ar.take<uint64_t>((size_t)qb * R);
+  int* over = ar.take<int>((size_t)qb);
+  int* flag = ar.take<int>((size_t)qb);
+  uint64_t* gthr = (kseg == R && osegs > 1) ? ar.take<uint64_t>((size_t)qb) : nullptr;
+  std::vector<int> h_flag;
+  for (int64_t q0 = 0; q0 < nq; q0 += qb) {
+    const int64_t nqb = std::min(qb, nq - q0);
+    const float* xb = d_x + q0 * ix->d;
+    {
+      StageTimer t(ix->ctx, MV_STAGE_FLAT, s);
+      launch_to_bf16(xb, nqb, ix->d, xq, nullptr, s);
+      launch_umma_topk(xq, nqb, ix->rows_bf16.as<__nv_bfloat16>(), nb, ix->d, ix->metric, nullptr,
+                       ix->norms.as<float>(), kseg, nseg, d_filter, gthr, cand,
+                       ix->ctx->d_err.as<int>(), s);
+    }
+    {
+      StageTimer t(ix->ctx, MV_STAGE_SELECT, s);
+      launch_flat_merge(cand, nqb, osegs, ncp, kseg, R, skeys, k, nullptr, ix->metric, 0.0f,
+                        nullptr, nullptr, kseg < R ? over : nullptr, s);
+      launch_flat_certify(xb, nqb, ix->d, ix->metric, ix->rows.as<float>(), nb, skeys, R, k,
+                          ix->cert.as<double>(), kseg < R ? over : nullptr, d_out + q0 * k,
+                          d_lab + q0 * k, flag, s);
+    }
+    h_flag.resize((size_t)nqb);
+    d2h(h_flag.data(), flag, sizeof(int) * nqb, s);
+    check_kernel_errors(ix->ctx, s);  // syncs
+    std::vector<int64_t> rows;
+    for (int64_t i = 0; i < nqb; ++i)
+      if (h_flag[(size_t)i]) rows.push_back(q0 + i);
+    ix->ctx->flat_queries += nqb;
+    ix->ctx->flat_fallback += (int64_t)rows.size();
+    if (rows.empty()) continue;
+    const int64_t nr = (int64_t)rows.size();
+    DevBuf tmp, tws;
+    tmp.ensure(ws_bytes((size_t)nr, 8) + ws_bytes((size_t)nr * ix->d, 4) +
+               ws_bytes((size_t)nr * k, 4) + ws_bytes((size_t)nr * k, 8));
+    Arena ta(tmp);
+    int64_t* idx = ta.take<int64_t>((size_t)nr);
+    float* tx = ta.take<float>((size_t)nr * ix->d);
+    float* td = ta.take<float>((size_t)nr * k);
+    int64_t* tl = ta.take<int64_t>((size_t)nr * k);
+    h2d(idx, rows.data(), sizeof(int64_t) * nr, s);
+    launch_gather_rows(d_x, ix->d, idx, nr, tx, 1, 0, 0, s);
+    flat_search_exact(ix, tx, nr, k, d_filter, td, tl, tws, s);
+    scatter_rows(td, nr, 4 * k, idx, d_out, s);
+    scatter_rows(tl, nr, 8 * k, idx, d_lab, s);
+    sync(s);  // tmp is freed on the next iteration
+  }
 }
 
 // Flat fast form: BF16 tensor-core distances with the per-row heap epilogue
@@ -1281,7 +1370,7 @@ void flat_search_fast(mv_flat* ix, const float* d_x, int64_t nq, int k, const ui
         int64_t* tl = ta.take<int64_t>((size_t)nr * k);
         for (int64_t i = 0; i < nr; ++i)
           d2d(tx + i * ix->d, d_x + rows[(size_t)i] * ix->d, sizeof(float) * ix->d, s);
-        flat_search_plain(ix, tx, nr, k, d_filter, td, tl, tws, s);
+        flat_search_exact(ix, tx, nr, k, d_filter, td, tl, tws, s);
         for (int64_t i = 0; i < nr; ++i) {
           d2d(d_out + rows[(size_t)i] * k, td + i * k, sizeof(float) * k, s);
           d2d(d_lab + rows[(size_t)i] * k, tl + i * k, sizeof(int64_t) * k, s);
@@ -1299,6 +1388,7 @@ void flat_search_any(mv_flat* ix, const float* d_x, int64_t nq, int k, const uin
   const int form = p ? p->form : MV_FORM_PLAIN;
   MV_REQUIRE(form == MV_FORM_PLAIN || form == MV_FORM_FAST, MV_ERR_ARG, "unknown search form");
   if (form == MV_FORM_FAST) flat_search_fast(ix, d_x, nq, k, d_filter, p, d_out, d_lab, ws, s);
+  else if (p && p->plain_scan) flat_search_exact(ix, d_x, nq, k, d_filter, d_out, d_lab, ws, s);
   else flat_search_plain(ix, d_x, nq, k, d_filter, d_out, d_lab, ws, s);
 }
 
@@ -1749,15 +1839,17 @@ static int32_t sq8_search_host(mv_sq8* ix, const float* x, int64_t nq, int32_t k
   });
 }
 
+// The plain SQ8 entry points take the tensor-core keys where they are exact
+// (they equal the integer scan's bit for bit), the integer scan elsewhere.
 int32_t mv_sq8_search(mv_sq8* ix, const float* x, int64_t nq, int32_t k, const uint8_t* filter,
                       float* distances, int64_t* labels) {
-  return sq8_search_host(ix, x, nq, k, filter, 0, distances, labels);
+  return sq8_search_host(ix, x, nq, k, filter, 0, distances, labels, true);
 }
 
 int32_t mv_sq8_search_rerank(mv_sq8* ix, const float* x, int64_t nq, int32_t k,
                              int32_t rerank_factor, float* distances, int64_t* labels) {
   if (rerank_factor < 1) return MV_ERR_ARG;
-  return sq8_search_host(ix, x, nq, k, nullptr, rerank_factor, distances, labels);
+  return sq8_search_host(ix, x, nq, k, nullptr, rerank_factor, distances, labels, true);
 }
 
 int32_t mv_sq8_search_device(mv_sq8* ix, const float* d_x, int64_t nq, int32_t k,
@@ -1774,7 +1866,7 @@ int32_t mv_sq8_search_device(mv_sq8* ix, const float* d_x, int64_t nq, int32_t k
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : lease.stream();
     lease.use(s);
     sq8_search_impl(ix, d_x, nq, k, rerank_factor, d_filter, d_distances, d_labels,
-                    lease.slot->ws, s, form == MV_FORM_FAST);
+                    lease.slot->ws, s, form == MV_FORM_FAST || !(params && params->plain_scan));
     if (!stream) check_kernel_errors(ix->ctx, s);
   });
 }
@@ -1786,7 +1878,7 @@ int32_t mv_sq8_search_ex(mv_sq8* ix, const float* x, int64_t nq, int32_t k,
   const int form = params ? params->form : MV_FORM_PLAIN;
   if (form != MV_FORM_PLAIN && form != MV_FORM_FAST) return MV_ERR_ARG;
   return sq8_search_host(ix, x, nq, k, filter, rerank_factor, distances, labels,
-                         form == MV_FORM_FAST);
+                         form == MV_FORM_FAST || !(params && params->plain_scan));
 }
 
 // ---------------------------------------------------------------------------

@@ -113,9 +113,9 @@ struct mv_ctx {
   std::atomic<int64_t> launches{0};
   cudaStream_t main_stream = nullptr;
   mv::DevBuf d_err;  // int: set by kernels whose bounded waits gave up
-  // certified nearest-centroid assignment: rows assigned, rows the bound left
-  // to the exact SIMT argmin (mv_ctx_assign_stats)
-  std::atomic<int64_t> assign_rows{0}, assign_fallback{0};
+  // certified selections (mv_ctx_certify_stats): nearest-centroid rows and
+  // plain Flat queries, and how many of each the bound left to the exact scan
+  std::atomic<int64_t> assign_rows{0}, assign_fallback{0}, flat_queries{0}, flat_fallback{0};
   // stage profiling (mv_ctx_profile)
   std::atomic<bool> profile{false};
   std::mutex prof_mu;
@@ -234,6 +234,7 @@ struct mv_flat {
   mv::DevBuf rows;       // capacity x d FP32
   mv::DevBuf rows_bf16;  // ntotal x kpad BF16 (fast form, built lazily)
   mv::DevBuf norms;      // FP32 ||x||^2 per rounded row (fast form)
+  mv::DevBuf cert;       // 2 doubles: bound on ||bf16(y)||^2, max ||y - bf16(y)|| (fast form)
   std::mutex fast_mu;
   bool fast_ready = false;
   int64_t overflow_rows = 0;  // fast-form queries recomputed exactly (shortlist overflow)

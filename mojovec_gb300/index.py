@@ -92,12 +92,19 @@ class Context:
     def kernel_launches(self) -> int:
         return int(_lib.load().mv_ctx_kernel_launches(self._h))
 
+    def certify_stats(self) -> dict:
+        """Plain-form selections settled on the tensor cores by the error
+        bound, and those recomputed by the exact FP32 scan (mv_ctx_certify_stats)."""
+        out = np.zeros(4, np.int64)
+        check(_lib.load().mv_ctx_certify_stats(self._h, _p(out)))
+        return {"assign_rows": int(out[0]), "assign_fallback": int(out[1]),
+                "flat_queries": int(out[2]), "flat_fallback": int(out[3])}
+
     def assign_stats(self) -> tuple:
-        """(rows assigned on the tensor cores with the certified recheck, rows
-        of those that took the exact FP32 scan)."""
-        rows, fb = C.c_int64(), C.c_int64()
-        check(_lib.load().mv_ctx_assign_stats(self._h, C.byref(rows), C.byref(fb)))
-        return rows.value, fb.value
+        """(rows assigned through the certified path, rows of those that took
+        the exact FP32 scan)."""
+        st = self.certify_stats()
+        return st["assign_rows"], st["assign_fallback"]
 
     def profile(self, enable: bool = True):
         """Enables (and resets) per-stage CUDA-event timing."""
@@ -112,9 +119,11 @@ class Context:
         return {name: (float(ms[i]), int(cnt[i])) for i, name in enumerate(_lib.STAGES) if cnt[i]}
 
 
-def _params(form=None, nprobe=0, rerank=0, coarse_fp32=False, lut_fp16=False, coarse_path=0):
+def _params(form=None, nprobe=0, rerank=0, coarse_fp32=False, lut_fp16=False, coarse_path=0,
+            plain_scan=False):
     p = SearchParams()
     p.coarse_path = int(coarse_path)
+    p.plain_scan = 1 if plain_scan else 0
     p.form = _lib.FORM_PLAIN if form is None else int(form)
     p.nprobe = int(nprobe)
     p.rerank = int(rerank)
@@ -380,13 +389,16 @@ class IndexFlat:
         x = _f32(x, self.d)
         check(_lib.load().mv_flat_add(self._h, _p(x), x.shape[0]))
 
-    def search(self, x, k: int, filter=None, form=None, rerank: int = 0):
+    def search(self, x, k: int, filter=None, form=None, rerank: int = 0, plain_scan: bool = False):
+        """IndexFlat.search. The plain form returns the reference's exact
+        results, from the certified tensor-core shortlist where it applies;
+        plain_scan=True runs the exact FP32 scan alone."""
         x = _f32(x, self.d)
         n = x.shape[0]
         dist = np.empty((n, k), np.float32)
         lab = np.empty((n, k), np.int64)
         flt = None if filter is None else np.ascontiguousarray(filter, dtype=np.uint8)
-        p = _params(form, 0, rerank)
+        p = _params(form, 0, rerank, plain_scan=plain_scan)
         check(_lib.load().mv_flat_search(self._h, _p(x), n, k, _p(flt), C.byref(p), _p(dist),
                                          _p(lab)))
         return dist, lab
@@ -404,8 +416,8 @@ class IndexFlat:
         return dist, lab
 
     def search_device(self, x_ptr: int, n: int, k: int, dist_ptr: int, lab_ptr: int,
-                      stream: int = 0, form=None, rerank: int = 0):
-        p = _params(form, 0, rerank)
+                      stream: int = 0, form=None, rerank: int = 0, plain_scan: bool = False):
+        p = _params(form, 0, rerank, plain_scan=plain_scan)
         check(_lib.load().mv_flat_search_device(self._h, x_ptr, n, k, None, C.byref(p), dist_ptr,
                                                 lab_ptr, stream or None))
 
@@ -462,26 +474,30 @@ class IndexFlatSQ8:
         check(_lib.load().mv_sq8_get_codes(self._h, _p(c), _p(nm)))
         return c[:n], nm[:n]
 
-    def search(self, x, k: int, filter=None, form=None, rerank_factor: int = 0):
+    def search(self, x, k: int, filter=None, form=None, rerank_factor: int = 0,
+               plain_scan: bool = False):
         """IndexFlatSQ8.search; with rerank_factor > 0 the shortlist of
-        k * rerank_factor is reranked with exact FP32 distances. form=FORM_FAST
-        takes the shortlist from the tensor cores (same results)."""
+        k * rerank_factor is reranked with exact FP32 distances. Both forms
+        take the shortlist from the tensor cores where that is exact (the
+        same results as the integer scan); plain_scan=True runs the integer
+        scan alone."""
         x = _f32(x, self.d)
         n = x.shape[0]
         dist = np.empty((n, k), np.float32)
         lab = np.empty((n, k), np.int64)
         flt = None if filter is None else np.ascontiguousarray(filter, dtype=np.uint8)
-        if form is None and rerank_factor == 0:
+        if form is None and rerank_factor == 0 and not plain_scan:
             check(_lib.load().mv_sq8_search(self._h, _p(x), n, k, _p(flt), _p(dist), _p(lab)))
         else:
-            p = _params(form)
+            p = _params(form, plain_scan=plain_scan)
             check(_lib.load().mv_sq8_search_ex(self._h, _p(x), n, k, _p(flt), rerank_factor,
                                                C.byref(p), _p(dist), _p(lab)))
         return dist, lab
 
     def search_device(self, x_ptr: int, n: int, k: int, dist_ptr: int, lab_ptr: int,
-                      stream: int = 0, form=None, rerank_factor: int = 0, filter_ptr: int = 0):
-        p = _params(form)
+                      stream: int = 0, form=None, rerank_factor: int = 0, filter_ptr: int = 0,
+                      plain_scan: bool = False):
+        p = _params(form, plain_scan=plain_scan)
         check(_lib.load().mv_sq8_search_device(self._h, x_ptr, n, k, filter_ptr or None,
                                                rerank_factor, C.byref(p), dist_ptr, lab_ptr,
                                                stream or None))
