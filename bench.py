@@ -435,6 +435,7 @@ def run_flat(args, rank, world):
         fast = dict(form=mv.FORM_FAST, rerank=rerank)
         plain = dict(form=mv.FORM_PLAIN)
         scan = dict(form=mv.FORM_PLAIN, plain_scan=True)
+        fp8 = dict(form=mv.FORM_FAST, rerank=rerank, e4m3=True)
     setup_s = time.perf_counter() - t_setup
     d_q = torch.from_numpy(queries).cuda()
     d_dist = torch.empty((nq, k), dtype=torch.float32, device="cuda")
@@ -453,8 +454,10 @@ def run_flat(args, rank, world):
     results = {}
     scan_steps = max(1, min(args.steps, 3))  # the scans alone are 7-30x slower
     cert0 = ctx.certify_stats()
-    for name, opts, steps in (("scan", scan, scan_steps), ("plain", plain, args.steps),
-                              ("fast", fast, args.steps)):
+    forms = [("scan", scan, scan_steps), ("plain", plain, args.steps), ("fast", fast, args.steps)]
+    if not sq8:
+        forms.append(("fp8", fp8, args.steps))
+    for name, opts, steps in forms:
         step = make_step(opts)
         for _ in range(args.warmup if name != "scan" else 1):
             step()
@@ -538,6 +541,10 @@ def run_flat(args, rank, world):
             "fast_form_recall_at_k": round(rec, 5),
             "fast_form": (f"SQ8 fast form (same shortlist path, rerank of {rerank})" if sq8 else
                           f"BF16 shortlist + FP32 rerank of {rerank}"),
+            **({} if sq8 else {
+                "fp8_form_qps": round(world * nq / (results["fp8"]["ms"] / 1e3), 1),
+                "fp8_form_recall_at_k": round(recall_at(gt, results["fp8"]["labels"], k), 5),
+                "fp8_form": f"E4M3 (per-row scales) tcgen05 shortlist + FP32 rerank of {rerank}"}),
             "l2_policy": "inputs larger than L2 (256 MB BF16 rows) and a 256 MiB flush per step",
             "parallelism": f"replicas x{world}",
             "setup_s": round(setup_s, 1),

@@ -73,7 +73,8 @@ typedef struct mv_search_params {
   int32_t plain_scan;  /* plain form, Flat and SQ8: 1 = the exact SIMT scan alone, without
                           the tensor-core shortlist that is proven (Flat) or exact by
                           construction (SQ8) to give the same results */
-  int32_t reserved[1];
+  int32_t flat_e4m3;   /* fast form, Flat: 1 = shortlist from an E4M3 (FP8) GEMM with
+                          per-row scales instead of BF16 (exact FP32 rerank either way) */
 } mv_search_params;
 
 /* ---- library / context ---------------------------------------------- */

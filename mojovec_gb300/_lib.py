@@ -60,7 +60,7 @@ class SearchParams(C.Structure):
         ("lut_fp16", C.c_int32),
         ("coarse_path", C.c_int32),
         ("plain_scan", C.c_int32),
-        ("reserved", C.c_int32 * 1),
+        ("flat_e4m3", C.c_int32),
     ]
 
 

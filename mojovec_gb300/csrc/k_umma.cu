@@ -29,6 +29,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 
 #include <mutex>
 
@@ -279,10 +280,12 @@ __device__ __forceinline__ void heap_replace_top(uint64_t* h, int K, uint64_t ke
   h[(size_t)i * BM] = key;
 }
 
-template <int BN, bool L2, int EG>
+template <int BN, bool L2, int EG, bool F8 = false>
 __global__ void __launch_bounds__(64 + 128 * EG, 1)
     k_umma_topk(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUtensorMap ty,
                 UmmaTopkArgs g) {
+  // A k-block is one 128-byte swizzled row: 64 BF16 or 128 E4M3 elements.
+  constexpr int KB_ELEMS = F8 ? 128 : 64;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
@@ -296,7 +299,9 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
   uint64_t* heap = reinterpret_cast<uint64_t*>(sB + STAGES * b_stage);
   uint64_t* pend = heap + (size_t)EG * g.nc * BM;
   float* cnbuf = reinterpret_cast<float*>(pend + (size_t)EG * g.pend * BM);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(cnbuf + 4 * EG * BN);
+  // E4M3: per epilogue warp also the tile's column scales (BN floats).
+  float* csbuf = cnbuf + 4 * EG * BN;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(csbuf + (F8 ? 4 * EG * BN : 0));
   uint32_t* holder = reinterpret_cast<uint32_t*>(bars + 12);
   __shared__ int s_err;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -344,7 +349,7 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
     if (lane == 0) {
       mbar_arrive_expect_tx(b_fulla, a_bytes);
       for (int kb = 0; kb < nkb; ++kb)
-        tma_load_2d(smem_u32(sA + kb * (BM * 128)), &tx, kb * 64, rb * BM, b_fulla);
+        tma_load_2d(smem_u32(sA + kb * (BM * 128)), &tx, kb * KB_ELEMS, rb * BM, b_fulla);
       int i = 0;
       for (; i < my_count; ++i) {
         const int s = i % STAGES;
@@ -356,7 +361,8 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
         uint8_t* st = sB + (size_t)s * b_stage;
         mbar_arrive_expect_tx(b_full(s), b_stage);
         for (int kb = 0; kb < nkb; ++kb)
-          tma_load_2d(smem_u32(st + kb * (BN * 128)), &ty, kb * 64, (ct0 + i) * BN, b_full(s));
+          tma_load_2d(smem_u32(st + kb * (BN * 128)), &ty, kb * KB_ELEMS, (ct0 + i) * BN,
+                      b_full(s));
       }
       // Drain: every issued load must land before the CTA exits.
       if (!mbar_wait(b_fulla, 0)) *verr = 1;
@@ -365,7 +371,7 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      const uint32_t idesc = idesc_bf16_f32(BM, BN);
+      const uint32_t idesc = F8 ? idesc_e4m3_f32(BM, BN) : idesc_bf16_f32(BM, BN);
       bool ok = mbar_wait(b_fulla, 0);
       if (!ok) *verr = 1;
       for (int i = 0; ok && i < my_count; ++i) {
@@ -384,8 +390,10 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
           const uint64_t ad = desc_k_sw128(smem_u32(sA + kb * (BM * 128)));
           const uint64_t bd = desc_k_sw128(smem_u32(st + kb * (BN * 128)));
 #pragma unroll
-          for (int kk = 0; kk < 4; ++kk)
-            umma_bf16(d, ad + 2u * kk, bd + 2u * kk, idesc, (kb | kk) ? 1u : 0u);
+          for (int kk = 0; kk < 4; ++kk) {  // 32 bytes of K per instruction
+            if (F8) umma_e4m3(d, ad + 2u * kk, bd + 2u * kk, idesc, (kb | kk) ? 1u : 0u);
+            else umma_bf16(d, ad + 2u * kk, bd + 2u * kk, idesc, (kb | kk) ? 1u : 0u);
+          }
         }
         umma_commit(b_empty(s));
         umma_commit(b_tfull(acc));
@@ -407,6 +415,10 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
     uint64_t* H = heap + (size_t)h * K * BM + rloc;      // H[j * BM]
     uint64_t* P = pend + (size_t)h * g.pend * BM + rloc;  // P[j * BM]
     float* cs = cnbuf + (h * 4 + q) * BN;  // this warp's copy of the tile's column biases
+    float* css = csbuf + (h * 4 + q) * BN;  // E4M3: its column scales
+    // E4M3: acc = <x8, y8> with x = sx x8, y = sy y8, so x.y = sx sy acc; the
+    // row's factor SCALE * sx stays in a register, the columns' sy are staged.
+    const float rsc = F8 ? SCALE * ((row_ok && g.rscale) ? g.rscale[row] : 1.0f) : SCALE;
     for (int j = 0; j < K; ++j) H[(size_t)j * BM] = KEY_NONE;
     int pc = 0;
     // Work with e = -distance (2 x.y - ||y||^2 for L2, x.y for IP): a column
@@ -438,11 +450,17 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
     // t * CPL ...) while the current tile is processed.
     constexpr int CPL = BN / 32;
     float cpre[CPL];
+    float spre[F8 ? CPL : 1];
     auto load_cn = [&](int i) {
       const int64_t base = (int64_t)(ct0 + i) * BN + lane * CPL;
 #pragma unroll
       for (int u = 0; u < CPL; ++u)
         cpre[u] = base + u >= g.ncols ? -INF : (L2 ? -__ldg(g.cnorm + base + u) : 0.0f);
+      if constexpr (F8) {
+#pragma unroll
+        for (int u = 0; u < CPL; ++u)
+          spre[u] = base + u >= g.ncols ? 0.0f : __ldg(g.cscale + base + u);
+      }
     };
     if (my_count > 0) load_cn(0);
     uint64_t gpre = KEY_NONE;  // the row's shared threshold, read one tile ahead
@@ -459,6 +477,10 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
       __syncwarp();
 #pragma unroll
       for (int u = 0; u < CPL; ++u) cs[lane * CPL + u] = cpre[u];
+      if constexpr (F8) {
+#pragma unroll
+        for (int u = 0; u < CPL; ++u) css[lane * CPL + u] = spre[u];
+      }
       __syncwarp();
       if (i + 1 < my_count) load_cn(i + 1);
       if (g.gthr && row_ok) {
@@ -475,10 +497,18 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
 #pragma unroll
         for (int j = 0; j < 32; j += 4) {
           const float4 b4 = *reinterpret_cast<const float4*>(cs + ch * 32 + j);  // broadcast
-          e[j] = fmaf(SCALE, __uint_as_float(rv[j]), b4.x);
-          e[j + 1] = fmaf(SCALE, __uint_as_float(rv[j + 1]), b4.y);
-          e[j + 2] = fmaf(SCALE, __uint_as_float(rv[j + 2]), b4.z);
-          e[j + 3] = fmaf(SCALE, __uint_as_float(rv[j + 3]), b4.w);
+          if constexpr (F8) {
+            const float4 s4 = *reinterpret_cast<const float4*>(css + ch * 32 + j);
+            e[j] = fmaf(rsc * s4.x, __uint_as_float(rv[j]), b4.x);
+            e[j + 1] = fmaf(rsc * s4.y, __uint_as_float(rv[j + 1]), b4.y);
+            e[j + 2] = fmaf(rsc * s4.z, __uint_as_float(rv[j + 2]), b4.z);
+            e[j + 3] = fmaf(rsc * s4.w, __uint_as_float(rv[j + 3]), b4.w);
+          } else {
+            e[j] = fmaf(SCALE, __uint_as_float(rv[j]), b4.x);
+            e[j + 1] = fmaf(SCALE, __uint_as_float(rv[j + 1]), b4.y);
+            e[j + 2] = fmaf(SCALE, __uint_as_float(rv[j + 2]), b4.z);
+            e[j + 3] = fmaf(SCALE, __uint_as_float(rv[j + 3]), b4.w);
+          }
         }
       };
       // Phase 1, no branches: the largest e of each chunk. All of the
@@ -583,6 +613,33 @@ __global__ void k_to_bf16(const float* __restrict__ x, int64_t n, int d, int kp,
   if (norms && lane == 0) norms[row] = acc;
 }
 
+// One warp per row: scale = max|x| / 448 (the largest finite E4M3 is 448),
+// E4M3 of x / scale (round to nearest, saturating), zero padding, and the
+// norm of the dequantized row.
+__global__ void k_to_e4m3(const float* __restrict__ x, int64_t n, int d, int kp,
+                          uint8_t* __restrict__ out, float* __restrict__ scales,
+                          float* __restrict__ norms) {
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= n) return;
+  float amax = 0.0f;
+  for (int j = lane; j < d; j += 32) amax = fmaxf(amax, fabsf(x[row * d + j]));
+  for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+  const float sc = amax > 0.0f ? amax / 448.0f : 1.0f;
+  float acc = 0.0f;
+  for (int j = lane; j < kp; j += 32) {
+    const __nv_fp8_e4m3 v(j < d ? x[row * d + j] / sc : 0.0f);
+    out[row * kp + j] = v.__x;
+    const float r = (float)v * sc;
+    acc = fmaf(r, r, acc);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) {
+    scales[row] = sc;
+    if (norms) norms[row] = acc;
+  }
+}
+
 __global__ void k_fill_keys(uint64_t* keys, int64_t n) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) keys[i] = KEY_NONE;
@@ -610,6 +667,23 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   });
   MV_REQUIRE(fn != nullptr, MV_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
   return fn;
+}
+
+// E4M3 rows of kp bytes (a multiple of 128), 128-byte boxes.
+CUtensorMap make_tmap8(const void* base, int64_t rows, int kp, int box_rows) {
+  MV_REQUIRE((reinterpret_cast<uintptr_t>(base) & 15) == 0, MV_ERR_INTERNAL, "TMA base not 16-byte aligned");
+  MV_REQUIRE(kp % 128 == 0, MV_ERR_INTERNAL, "TMA rows must be padded to 128 bytes");
+  CUtensorMap tm;
+  cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)kp};
+  cuuint32_t box[2] = {128, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode_fn()(&tm, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(base), dims,
+                           strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  MV_REQUIRE(r == CUDA_SUCCESS, MV_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return tm;
 }
 
 CUtensorMap make_tmap(const void* base, int64_t rows, int kp, int box_rows) {
@@ -644,6 +718,15 @@ void launch_bn(const UmmaArgs& g, const CUtensorMap& tx, const CUtensorMap& ty, 
 }  // namespace
 
 int umma_kpad(int d) { return (d + 63) / 64 * 64; }
+int umma_kpad8(int d) { return (d + 127) / 128 * 128; }
+
+void launch_to_e4m3(const float* x, int64_t n, int d, uint8_t* out, float* scales, float* norms,
+                    cudaStream_t s) {
+  if (n == 0) return;
+  k_to_e4m3<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(x, n, d, umma_kpad8(d), out, scales, norms);
+  count_launch();
+  MV_CHECK_CUDA(cudaGetLastError());
+}
 
 void launch_to_bf16(const float* x, int64_t n, int d, __nv_bfloat16* out, float* norms,
                     cudaStream_t s) {
@@ -704,35 +787,37 @@ namespace {
 struct TopkCfg {
   int bn, eg, pend;
 };
-size_t topk_smem_base(int nkb, int bn, int nc, int eg) {
+size_t topk_smem_base(int nkb, int bn, int nc, int eg, bool f8 = false) {
   return 1024 + (size_t)nkb * BM * 128 + (size_t)STAGES * nkb * bn * 128 +
-         (size_t)eg * nc * BM * 8 + (size_t)4 * eg * bn * 4 + 256;
+         (size_t)eg * nc * BM * 8 + (size_t)4 * eg * bn * 4 * (f8 ? 2 : 1) + 256;
 }
-int topk_pend_fit(int nkb, int bn, int nc, int eg) {
-  const size_t base = topk_smem_base(nkb, bn, nc, eg);
+int topk_pend_fit(int nkb, int bn, int nc, int eg, bool f8 = false) {
+  const size_t base = topk_smem_base(nkb, bn, nc, eg, f8);
   const size_t room = base < 227 * 1024 ? (227 * 1024 - base) / ((size_t)eg * BM * 8) : 0;
   return (int)std::min<size_t>(TOPK_PEND_MAX, room / 8 * 8);
 }
-TopkCfg topk_cfg(int nkb, int nc) {
+TopkCfg topk_cfg(int nkb, int nc, bool f8 = false) {
   const int bn = nkb <= 2 ? 128 : 64;
-  return {bn, 1, topk_pend_fit(nkb, bn, nc, 1)};
+  return {bn, 1, topk_pend_fit(nkb, bn, nc, 1, f8)};
 }
-size_t topk_smem(int nkb, const TopkCfg& c, int nc) {
-  return topk_smem_base(nkb, c.bn, nc, c.eg) + (size_t)c.eg * c.pend * BM * 8;
+size_t topk_smem(int nkb, const TopkCfg& c, int nc, bool f8 = false) {
+  return topk_smem_base(nkb, c.bn, nc, c.eg, f8) + (size_t)c.eg * c.pend * BM * 8;
 }
 }  // namespace
 
-int umma_topk_groups(int d, int nc) { return topk_cfg(umma_kpad(d) / 64, nc).eg; }
+int umma_topk_groups(int d, int nc, bool e4m3) {
+  return topk_cfg(e4m3 ? umma_kpad8(d) / 128 : umma_kpad(d) / 64, nc, e4m3).eg;
+}
 
-int umma_topk_nseg(int64_t nrows, int64_t ncols, int d, int nc, int num_sms) {
-  const int nkb = umma_kpad(d) / 64;
-  const TopkCfg c = topk_cfg(nkb, nc);
+int umma_topk_nseg(int64_t nrows, int64_t ncols, int d, int nc, int num_sms, bool e4m3) {
+  const int nkb = e4m3 ? umma_kpad8(d) / 128 : umma_kpad(d) / 64;
+  const TopkCfg c = topk_cfg(nkb, nc, e4m3);
   const int64_t nrb = (nrows + BM - 1) / BM;
   const int64_t nct = (ncols + c.bn - 1) / c.bn;
   // CTAs resident per SM (228 KB of shared memory per SM, 1 KB reserved per
   // CTA), then the fewest column segments whose CTAs fill the last wave to
   // 90%; a segment is never shorter than 16 column tiles.
-  const int64_t cps = std::max<int64_t>(1, std::min<int64_t>(4, (228 * 1024) / (topk_smem(nkb, c, nc) + 1024)));
+  const int64_t cps = std::max<int64_t>(1, std::min<int64_t>(4, (228 * 1024) / (topk_smem(nkb, c, nc, e4m3) + 1024)));
   const int64_t slots = (int64_t)std::max(num_sms, 1) * cps;
   const int64_t maxseg = std::max<int64_t>(1, std::min<int64_t>(nct / 16, 4096));
   int64_t best = 1;
@@ -795,6 +880,59 @@ void launch_umma_topk(const __nv_bfloat16* X, int64_t nx, const __nv_bfloat16* Y
     l2m ? go(k_umma_topk<128, true, 1>, 192) : go(k_umma_topk<128, false, 1>, 192);
   } else {
     l2m ? go(k_umma_topk<64, true, 1>, 192) : go(k_umma_topk<64, false, 1>, 192);
+  }
+  count_launch();
+  MV_CHECK_CUDA(cudaGetLastError());
+}
+
+void launch_umma_topk_e4m3(const uint8_t* X8, int64_t nx, const float* xscale, const uint8_t* Y8,
+                           int64_t ny, const float* yscale, int d, int metric, const float* ynorm,
+                           int nc, int nseg, const uint8_t* filter, uint64_t* gthr, uint64_t* out,
+                           int* err, cudaStream_t s) {
+  if (nx == 0) return;
+  const int kp = umma_kpad8(d);
+  MV_REQUIRE(kp <= 256, MV_ERR_UNSUPPORTED, "E4M3 GEMM supports d <= 256");
+  MV_REQUIRE(nc >= 1 && nc <= UMMA_TOPK_MAX, MV_ERR_UNSUPPORTED, "fused top-k keeps at most 64 per row");
+  MV_REQUIRE(nx < (1ll << 31) && ny < (1ll << 32) - 1, MV_ERR_UNSUPPORTED, "GEMM too large");
+  MV_REQUIRE(nseg >= 1 && nseg <= 65535, MV_ERR_INTERNAL, "fused top-k: bad segment count");
+  MV_REQUIRE(xscale && yscale, MV_ERR_INTERNAL, "E4M3 GEMM needs row and column scales");
+  UmmaTopkArgs g;
+  g.nrows = nx;
+  g.ncols = ny;
+  g.nkb = kp / 128;
+  g.metric = metric;
+  g.rnorm = nullptr;
+  g.cnorm = ynorm;
+  g.nc = nc;
+  g.ncp = next_pow2(nc);
+  g.nseg = nseg;
+  g.filter = filter;
+  g.gthr = gthr;
+  if (gthr) MV_CHECK_CUDA(cudaMemsetAsync(gthr, 0xff, sizeof(uint64_t) * nx, s));
+  g.out = out;
+  g.err = err;
+  g.rscale = xscale;
+  g.cscale = yscale;
+  const TopkCfg c = topk_cfg(g.nkb, nc, true);
+  g.pend = c.pend;
+  MV_REQUIRE(g.pend >= TOPK_PEND_MIN, MV_ERR_UNSUPPORTED, "fused top-k GEMM: nc or d too large");
+  const int64_t nct = (ny + c.bn - 1) / c.bn;
+  g.tps = (int)((nct + nseg - 1) / nseg);
+  const CUtensorMap tx = make_tmap8(X8, nx, kp, BM);
+  const CUtensorMap ty = make_tmap8(Y8, ny, kp, c.bn);
+  MV_REQUIRE((nx + BM - 1) / BM <= 65535, MV_ERR_UNSUPPORTED, "fused top-k: too many rows per launch");
+  dim3 grid((unsigned)nseg, (unsigned)((nx + BM - 1) / BM));
+  const size_t smem = topk_smem(g.nkb, c, nc, true);
+  MV_REQUIRE(smem <= 227 * 1024, MV_ERR_UNSUPPORTED, "fused top-k GEMM: nc or d too large");
+  auto go = [&](auto kernel, int threads) {
+    smem_limit(kernel, smem);
+    kernel<<<grid, threads, smem, s>>>(tx, ty, g);
+  };
+  const bool l2m = metric == MV_METRIC_L2;
+  if (c.bn == 128) {
+    l2m ? go(k_umma_topk<128, true, 1, true>, 192) : go(k_umma_topk<128, false, 1, true>, 192);
+  } else {
+    l2m ? go(k_umma_topk<64, true, 1, true>, 192) : go(k_umma_topk<64, false, 1, true>, 192);
   }
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());

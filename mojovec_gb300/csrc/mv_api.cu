@@ -1186,6 +1186,18 @@ void ensure_flat_fast(mv_flat* ix, cudaStream_t s) {
   ix->fast_ready = true;
 }
 
+void ensure_flat_e4m3(mv_flat* ix, cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(ix->fast_mu);
+  if (ix->e4m3_ready) return;
+  ix->rows_e4m3.ensure((size_t)ix->ntotal * umma_kpad8(ix->d) + 16);
+  ix->scales_e4m3.ensure((size_t)ix->ntotal * 4 + 16);
+  ix->norms_e4m3.ensure((size_t)ix->ntotal * 4 + 16);
+  launch_to_e4m3(ix->rows.as<float>(), ix->ntotal, ix->d, ix->rows_e4m3.as<uint8_t>(),
+                 ix->scales_e4m3.as<float>(), ix->norms_e4m3.as<float>(), s);
+  sync(s);
+  ix->e4m3_ready = true;
+}
+
 // Plain Flat search (index_flat.mojo:260-325), bit-exact. Where it applies
 // it runs on the tensor cores: the BF16 top-k GEMM keeps a shortlist of R
 // rows per query, k_flat_certify computes their reference FP32 distances,
@@ -1286,16 +1298,19 @@ void flat_search_fast(mv_flat* ix, const float* d_x, int64_t nq, int k, const ui
     return;
   }
   MV_REQUIRE(umma_kpad(ix->d) <= 256, MV_ERR_UNSUPPORTED, "fast flat form supports d <= 256");
-  ensure_flat_fast(ix, s);
+  const bool e4m3 = p && p->flat_e4m3;
+  MV_REQUIRE(!e4m3 || (p->rerank > 0), MV_ERR_UNSUPPORTED, "the E4M3 shortlist needs a rerank");
+  if (e4m3) ensure_flat_e4m3(ix, s);
+  else ensure_flat_fast(ix, s);
   const bool rerank = p && p->rerank > 0;
   const int R = std::max(k, rerank ? (int)p->rerank : k);
   MV_REQUIRE(R <= 4096, MV_ERR_ARG, "rerank depth must be at most 4096");
   const int kseg = std::min(R, UMMA_TOPK_MAX);
   const int ncp = next_pow2(kseg);
-  const int kp = umma_kpad(ix->d);
+  const int kp = e4m3 ? umma_kpad8(ix->d) / 2 : umma_kpad(ix->d);  // BF16 elements of a query row
   const int64_t qb = std::min<int64_t>(nq, 32768);
-  int nseg = umma_topk_nseg(qb, nb, ix->d, kseg, ix->ctx->num_sms);
-  const int groups = umma_topk_groups(ix->d, kseg);
+  int nseg = umma_topk_nseg(qb, nb, ix->d, kseg, ix->ctx->num_sms, e4m3);
+  const int groups = umma_topk_groups(ix->d, kseg, e4m3);
   if (kseg < R) {
     // About 16 shortlist keys per segment keeps overflow rare. The count
     // depends on the index and R only, never on the batch, so whether a
@@ -1322,10 +1337,20 @@ void flat_search_fast(mv_flat* ix, const float* d_x, int64_t nq, int k, const ui
     const float* xb = d_x + q0 * ix->d;
     {
       StageTimer t(ix->ctx, MV_STAGE_FLAT, s);
-      launch_to_bf16(xb, nqb, ix->d, xq, qnorm, s);
-      launch_umma_topk(xq, nqb, ix->rows_bf16.as<__nv_bfloat16>(), nb, ix->d, ix->metric, nullptr,
-                       ix->norms.as<float>(), kseg, nseg, d_filter, gthr, cand,
-                       ix->ctx->d_err.as<int>(), s);
+      if (e4m3) {
+        // the query's E4M3 bytes reuse the BF16 query buffer; qnorm holds its scales
+        uint8_t* q8 = reinterpret_cast<uint8_t*>(xq);
+        launch_to_e4m3(xb, nqb, ix->d, q8, qnorm, nullptr, s);
+        launch_umma_topk_e4m3(q8, nqb, qnorm, ix->rows_e4m3.as<uint8_t>(), nb,
+                              ix->scales_e4m3.as<float>(), ix->d, ix->metric,
+                              ix->norms_e4m3.as<float>(), kseg, nseg, d_filter, gthr, cand,
+                              ix->ctx->d_err.as<int>(), s);
+      } else {
+        launch_to_bf16(xb, nqb, ix->d, xq, qnorm, s);
+        launch_umma_topk(xq, nqb, ix->rows_bf16.as<__nv_bfloat16>(), nb, ix->d, ix->metric,
+                         nullptr, ix->norms.as<float>(), kseg, nseg, d_filter, gthr, cand,
+                         ix->ctx->d_err.as<int>(), s);
+      }
     }
     {
       StageTimer t(ix->ctx, MV_STAGE_SELECT, s);
@@ -1441,6 +1466,7 @@ int32_t mv_flat_add(mv_flat* ix, const float* x, int64_t n) {
     sync(s);
     ix->ntotal = need;
     ix->fast_ready = false;
+    ix->e4m3_ready = false;
   });
 }
 

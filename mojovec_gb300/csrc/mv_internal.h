@@ -235,6 +235,9 @@ struct mv_flat {
   mv::DevBuf rows_bf16;  // ntotal x kpad BF16 (fast form, built lazily)
   mv::DevBuf norms;      // FP32 ||x||^2 per rounded row (fast form)
   mv::DevBuf cert;       // 2 doubles: bound on ||bf16(y)||^2, max ||y - bf16(y)|| (fast form)
+  mv::DevBuf rows_e4m3;  // ntotal x umma_kpad8(d) E4M3 rows (fast form with flat_e4m3)
+  mv::DevBuf scales_e4m3, norms_e4m3;  // per row: scale, norm of the dequantized row
+  bool e4m3_ready = false;
   std::mutex fast_mu;
   bool fast_ready = false;
   int64_t overflow_rows = 0;  // fast-form queries recomputed exactly (shortlist overflow)

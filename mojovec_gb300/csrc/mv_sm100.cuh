@@ -149,6 +149,29 @@ __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a_desc, uint
       : "memory");
 }
 
+// Instruction descriptor of tcgen05.mma kind::f8f6f4: E4M3 x E4M3 -> FP32
+// (A and B format code 0 = E4M3), both operands K-major, tile M x N. Same
+// field layout as idesc_bf16_f32.
+__host__ __device__ constexpr uint32_t idesc_e4m3_f32(int m, int n) {
+  return (1u << 4)                       // D format: F32
+         | (0u << 7)                     // A format: E4M3
+         | (0u << 10)                    // B format: E4M3
+         | ((uint32_t)(n >> 3) << 17)    // N / 8
+         | ((uint32_t)(m >> 4) << 24);   // M / 16
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T with 8-bit floats (K = 32 per
+// instruction: the same 32 bytes of a 128-byte swizzled row as kind::f16).
+__device__ __forceinline__ void umma_e4m3(uint32_t tmem_d, uint64_t a_desc, uint64_t b_desc,
+                                          uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
 // Arrives on `bar` when all previously issued tcgen05.mma of this thread
 // have completed.
 __device__ __forceinline__ void umma_commit(uint32_t bar) {

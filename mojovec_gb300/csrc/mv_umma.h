@@ -37,10 +37,19 @@ struct UmmaTopkArgs {
   uint64_t* gthr;      // per-row threshold shared by the segments (may be null)
   uint64_t* out;       // nrows x nseg x ncp keys (distance, column)
   int* err;
+  const float* rscale = nullptr;  // E4M3 operands: per-row scale of X
+  const float* cscale = nullptr;  // E4M3 operands: per-column scale of Y
 };
 
 // Rows are padded to this many BF16 elements (a multiple of 64).
 int umma_kpad(int d);
+// E4M3 rows are padded to this many bytes (a multiple of 128).
+int umma_kpad8(int d);
+// FP32 rows -> E4M3 rows scaled to the format's range (x = scale * x8,
+// scale = max|x| / 448 per row, round to nearest, saturating), zero padded
+// to umma_kpad8(d); norms of the dequantized rows (may be null).
+void launch_to_e4m3(const float* x, int64_t n, int d, uint8_t* out, float* scales, float* norms,
+                    cudaStream_t s);
 // FP32 rows -> zero-padded BF16 rows (kpad wide) and FP32 norms of the
 // rounded rows (norms may be null).
 void launch_to_bf16(const float* x, int64_t n, int d, __nv_bfloat16* out, float* norms,
@@ -55,10 +64,10 @@ constexpr int UMMA_TOPK_MAX = 64;
 // Epilogue groups of the fused top-k GEMM for (d, nc): each CTA writes one
 // output segment per group, so a launch with nseg column segments leaves
 // nseg * groups segments per row.
-int umma_topk_groups(int d, int nc);
+int umma_topk_groups(int d, int nc, bool e4m3 = false);
 // Column segments for the fused top-k GEMM: enough CTAs to fill the SMs
 // in whole waves.
-int umma_topk_nseg(int64_t nrows, int64_t ncols, int d, int nc, int num_sms);
+int umma_topk_nseg(int64_t nrows, int64_t ncols, int d, int nc, int num_sms, bool e4m3 = false);
 // Per-row nc smallest (distance, column) keys of the BF16 distances, per
 // output segment: out[(row * S + s) * next_pow2(nc) + j] with
 // S = nseg * umma_topk_groups(d, nc), unsorted, KEY_NONE padded. The key
@@ -69,6 +78,14 @@ void launch_umma_topk(const __nv_bfloat16* X, int64_t nx, const __nv_bfloat16* Y
                       int d, int metric, const float* xnorm, const float* ynorm, int nc, int nseg,
                       const uint8_t* filter, uint64_t* gthr, uint64_t* out, int* err,
                       cudaStream_t s);
+// The same with E4M3 operands (kind::f8f6f4): X8 nx x umma_kpad8(d) with
+// per-row scales xscale, Y8 with per-column scales yscale and ynorm the
+// norms of the dequantized Y rows (L2). The key distance is
+// ||y||^2 - 2 sx sy <x8, y8> (L2) or -sx sy <x8, y8> (IP).
+void launch_umma_topk_e4m3(const uint8_t* X8, int64_t nx, const float* xscale, const uint8_t* Y8,
+                           int64_t ny, const float* yscale, int d, int metric, const float* ynorm,
+                           int nc, int nseg, const uint8_t* filter, uint64_t* gthr, uint64_t* out,
+                           int* err, cudaStream_t s);
 // keys -> argmin columns (and distances).
 void launch_keys_argmin(const uint64_t* keys, int64_t n, int32_t* out, float* dist, cudaStream_t s);
 

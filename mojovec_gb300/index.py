@@ -120,10 +120,11 @@ class Context:
 
 
 def _params(form=None, nprobe=0, rerank=0, coarse_fp32=False, lut_fp16=False, coarse_path=0,
-            plain_scan=False):
+            plain_scan=False, e4m3=False):
     p = SearchParams()
     p.coarse_path = int(coarse_path)
     p.plain_scan = 1 if plain_scan else 0
+    p.flat_e4m3 = 1 if e4m3 else 0
     p.form = _lib.FORM_PLAIN if form is None else int(form)
     p.nprobe = int(nprobe)
     p.rerank = int(rerank)
@@ -389,16 +390,18 @@ class IndexFlat:
         x = _f32(x, self.d)
         check(_lib.load().mv_flat_add(self._h, _p(x), x.shape[0]))
 
-    def search(self, x, k: int, filter=None, form=None, rerank: int = 0, plain_scan: bool = False):
+    def search(self, x, k: int, filter=None, form=None, rerank: int = 0, plain_scan: bool = False,
+               e4m3: bool = False):
         """IndexFlat.search. The plain form returns the reference's exact
         results, from the certified tensor-core shortlist where it applies;
-        plain_scan=True runs the exact FP32 scan alone."""
+        plain_scan=True runs the exact FP32 scan alone. The fast form takes
+        its shortlist from a BF16 GEMM, or with e4m3=True an FP8 one."""
         x = _f32(x, self.d)
         n = x.shape[0]
         dist = np.empty((n, k), np.float32)
         lab = np.empty((n, k), np.int64)
         flt = None if filter is None else np.ascontiguousarray(filter, dtype=np.uint8)
-        p = _params(form, 0, rerank, plain_scan=plain_scan)
+        p = _params(form, 0, rerank, plain_scan=plain_scan, e4m3=e4m3)
         check(_lib.load().mv_flat_search(self._h, _p(x), n, k, _p(flt), C.byref(p), _p(dist),
                                          _p(lab)))
         return dist, lab
@@ -416,8 +419,9 @@ class IndexFlat:
         return dist, lab
 
     def search_device(self, x_ptr: int, n: int, k: int, dist_ptr: int, lab_ptr: int,
-                      stream: int = 0, form=None, rerank: int = 0, plain_scan: bool = False):
-        p = _params(form, 0, rerank, plain_scan=plain_scan)
+                      stream: int = 0, form=None, rerank: int = 0, plain_scan: bool = False,
+                      e4m3: bool = False):
+        p = _params(form, 0, rerank, plain_scan=plain_scan, e4m3=e4m3)
         check(_lib.load().mv_flat_search_device(self._h, x_ptr, n, k, None, C.byref(p), dist_ptr,
                                                 lab_ptr, stream or None))
 
