@@ -923,6 +923,7 @@ def run_serve(args, rank, world):
         return out
 
     results = {}
+    clocks = ClockSampler(dev)
     for form_name in ("plain", "fast"):
         srv = mv.Server(ctx=ctx, hbm_budget=args.serve_budget_gb << 30, lanes=4,
                         max_batch_queries=4096)
@@ -932,6 +933,8 @@ def run_serve(args, rank, world):
             for k in (10, 100):
                 srv.wait(srv.submit(ids[ci], q[:64], k))
         per_rate = []
+        if form_name == "fast":
+            clocks.start()
         for rate in args.serve_rates:
             times = np.cumsum(gaps / rate)
             lat = [None] * nreq
@@ -963,6 +966,8 @@ def run_serve(args, rank, world):
                 "p50_ms": round(float(np.percentile(lat_ms, 50)), 3),
                 "p99_ms": round(float(np.percentile(lat_ms, 99)), 3),
             })
+        if form_name == "fast":
+            clk = clocks.stop()
         st = srv.stats()
         srv.close()
         results[form_name] = {"rates": per_rate, "recall_at_10": recall_of(form_name),
@@ -982,7 +987,7 @@ def run_serve(args, rank, world):
             "arrivals": "Poisson; batch size log-uniform on [1, 1024]; collection uniform; k in {10, 100}",
             "server": f"4 lanes, HBM budget {args.serve_budget_gb} GB, batches up to 4096 queries",
             "forms": {"plain": "IVF-PQ plain nprobe 8; SQ8 integer scan + FP32 rerank of 2k; "
-                               "Flat exact FP32",
+                               "Flat exact FP32 (certified tensor-core shortlist)",
                       "fast": "IVF-PQ fast nprobe 8 rerank 256; SQ8 integer scan + FP32 rerank of "
                               "2k (d = 768 is above the tensor path's 256); Flat BF16 + FP32 "
                               "rerank of max(k, 40)"},
@@ -992,6 +997,7 @@ def run_serve(args, rank, world):
         "e2e": {"value": top["sustained_queries_per_s"], "unit": "queries/s",
                 "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
         "gpu_launches": None,
+        "clocks": clk,
     }
 
 
@@ -1120,7 +1126,7 @@ def main():
     ap.add_argument("--batch-nb", type=int, default=10_000_000)
     ap.add_argument("--serve-scale", type=float, default=1.0)
     ap.add_argument("--serve-requests", type=int, default=300)
-    ap.add_argument("--serve-rates", type=float, nargs="+", default=[20.0, 80.0, 320.0])
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[20.0, 80.0, 320.0, 1280.0])
     ap.add_argument("--serve-budget-gb", type=int, default=24)
     ap.add_argument("--batch-nq", type=int, default=20_000)
     ap.add_argument("--km-n", type=int, default=1_000_000)
