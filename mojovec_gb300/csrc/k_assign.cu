@@ -172,6 +172,96 @@ __global__ void k_assign_certify(const float* __restrict__ x, int64_t n, int d,
   }
 }
 
+// In-place ascending bitonic sort of n keys (a power of two) by one warp.
+__device__ __forceinline__ void warp_sort_keys(uint64_t* a, int n) {
+  const int lane = threadIdx.x & 31;
+  for (int k = 2; k <= n; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = lane; i < n; i += 32) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const uint64_t x = a[i], y = a[ixj];
+          if ((x > y) == ((i & k) == 0)) {
+            a[i] = y;
+            a[ixj] = x;
+          }
+        }
+      }
+      __syncwarp();
+    }
+}
+
+// The P nearest centroids of each query (the coarse quantizer search with
+// k = nprobe, index/index_flat.mojo:292-310), one warp per query: the
+// candidates' reference distances, the P smallest (distance, list) keys in
+// ascending order, and the bound for the centroids outside the candidates
+// against the P-th. Open queries are appended to flagged[].
+constexpr int TP_WARPS = 4, TP_CAP = 256;
+
+template <bool IP>
+__global__ void __launch_bounds__(TP_WARPS * 32)
+    k_topp_certify(const float* __restrict__ x, int64_t n, int d, const float* __restrict__ cent,
+                   int nlist, const uint64_t* __restrict__ cand, int ncand, int kc, int P,
+                   const double* __restrict__ cert, int32_t* __restrict__ probes,
+                   int64_t* __restrict__ flagged, int* __restrict__ nflag) {
+  __shared__ uint64_t bufs[TP_WARPS][TP_CAP];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * TP_WARPS + warp;
+  if (row >= n) return;  // warps are independent
+  uint64_t* B = bufs[warp];
+  const float* xr = x + row * d;
+  const uint64_t* ck = cand + row * ncand;
+  int np2 = 32;
+  while (np2 < ncand) np2 <<= 1;
+  bool bad = false;
+  int valid = 0;
+  for (int c = lane; c < np2; c += 32) {
+    uint64_t e = KEY_NONE - (uint64_t)c;  // distinct padding keys sort last
+    if (c < ncand) {
+      const uint64_t key = ck[c];
+      if (key != KEY_NONE && key_id(key) < (uint32_t)nlist) {
+        const uint32_t ci = key_id(key);
+        const float* yr = cent + (int64_t)ci * d;
+        const float r = IP ? -ip_simd<8>(xr, yr, d) : l2_simd<8>(xr, yr, d);
+        if (!(r < 1e38f && r > -1e38f)) bad = true;  // NaN, inf or huge
+        e = make_key(r, ci);
+        ++valid;
+      }
+    }
+    B[c] = e;
+  }
+  for (int o = 16; o > 0; o >>= 1) valid += __shfl_xor_sync(0xffffffffu, valid, o);
+  bad = __any_sync(0xffffffffu, bad);
+  __syncwarp();
+  warp_sort_keys(B, np2);
+  bool ok = !bad && valid >= P;
+  if (ok && valid < nlist) {
+    uint64_t prev = 0;  // K: the kc-th smallest candidate key
+    for (int t = 0; t < kc; ++t) {
+      uint64_t m = KEY_NONE;
+      for (int c = lane; c < ncand; c += 32) {
+        const uint64_t key = ck[c];
+        if (key == KEY_NONE || key_id(key) >= (uint32_t)nlist) continue;
+        if ((t == 0 || key > prev) && key < m) m = key;
+      }
+      prev = warp_min_u64(m);
+    }
+    double xs, rs;
+    bf16_norms(xr, d, xs, rs);
+    const double B2 = cert[0], rmax = cert[1];
+    if (valid < kc || prev == KEY_NONE || !cert_inputs_ok(xs, B2, rmax)) {
+      ok = false;
+    } else {
+      const double K = (double)key_dist(prev);
+      const double lower = IP ? cert_lower_ip(sqrt(xs), sqrt(rs), B2, rmax, K, d)
+                              : cert_lower_l2(sqrt(xs), sqrt(rs), B2, rmax, K, d);
+      ok = lower > (double)key_dist(B[P - 1]);
+    }
+  }
+  for (int p = lane; p < P; p += 32) probes[row * P + p] = (int32_t)key_id(B[p]);
+  if (!ok && lane == 0) flagged[atomicAdd(nflag, 1)] = row;
+}
+
 // Flat top-k, one CTA per query over its shortlist of R approximate keys
 // (the R smallest of the GEMM's candidates, KEY_NONE padded): the rows are
 // staged in shared memory (stride d + 1, so thread t reading row t touches
@@ -315,6 +405,22 @@ void launch_assign_certify(const float* x, int64_t n, int d, const float* cent, 
   else
     k_assign_certify<false><<<grid, 256, 0, s>>>(x, n, d, cent, nlist, cand, ncand, kc, cert,
                                                  assign, mind, flagged, nflag);
+  count_launch();
+  MV_CHECK_CUDA(cudaGetLastError());
+}
+
+void launch_topp_certify(const float* x, int64_t n, int d, const float* cent, int nlist, int metric,
+                         const uint64_t* cand, int ncand, int kc, int P, const double* cert,
+                         int32_t* probes, int64_t* flagged, int* nflag, cudaStream_t s) {
+  if (n == 0) return;
+  MV_REQUIRE(ncand <= TP_CAP && P >= 1 && P <= kc, MV_ERR_INTERNAL, "top-P certify: bad sizes");
+  const unsigned grid = (unsigned)((n + TP_WARPS - 1) / TP_WARPS);
+  if (metric == MV_METRIC_IP)
+    k_topp_certify<true><<<grid, TP_WARPS * 32, 0, s>>>(x, n, d, cent, nlist, cand, ncand, kc, P,
+                                                        cert, probes, flagged, nflag);
+  else
+    k_topp_certify<false><<<grid, TP_WARPS * 32, 0, s>>>(x, n, d, cent, nlist, cand, ncand, kc, P,
+                                                         cert, probes, flagged, nflag);
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());
 }

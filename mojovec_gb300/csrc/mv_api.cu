@@ -487,6 +487,73 @@ void launch_fill(float* d, int64_t* l, int64_t n, float dv, cudaStream_t s) {
 }
 
 // Plain IVF-PQ search on device buffers (index_ivf_pq.mojo:225-360).
+void scatter_rows(const void* src, int64_t n, int width_bytes, const int64_t* pos, void* dst,
+                  cudaStream_t s);
+void ensure_coarse(mv_ivfpq* ix, cudaStream_t s);
+
+// The coarse quantizer search with k = nprobe (index_ivf_pq.mojo:264;
+// index_ivf_flat.mojo:185-194), exact: the canonical nprobe nearest lists
+// of each query in ascending (distance, list) order. Through the certified
+// tensor-core path when nprobe plus a margin fits the GEMM's per-row list
+// (`k_topp_certify`), the exact FP32 matrix + selection for the queries the
+// bound leaves open and everywhere else. Returns false when the certified
+// path does not apply (the caller runs the exact one).
+bool coarse_topp_certified(mv_ctx* ctx, const float* d_q, int64_t nq, int d, const float* cent,
+                           const __nv_bfloat16* cent_bf16, const float* cnorm, const double* ccert,
+                           int nlist, int metric, int P, int32_t* probes, cudaStream_t s) {
+  const int nc = std::min(nlist, P + std::max(16, P / 2));
+  if (nc > UMMA_TOPK_MAX || nc >= nlist || umma_kpad(d) > 256 || nq > 0x7fffffffll) return false;
+  const int kp = umma_kpad(d), ncp = next_pow2(nc);
+  const int64_t qb = std::min<int64_t>(nq, 65536);
+  const int nseg = umma_topk_nseg(qb, nlist, d, nc, ctx->num_sms);
+  const int osegs = nseg * umma_topk_groups(d, nc);
+  if ((int64_t)osegs * ncp > 256) return false;
+  DevBuf buf;
+  buf.ensure(ws_bytes((size_t)qb * kp, 2) + ws_bytes((size_t)qb * osegs * ncp, 8) +
+             2 * ws_bytes((size_t)qb, 8) + ws_bytes(1, 4));
+  Arena ar(buf);
+  __nv_bfloat16* xb = ar.take<__nv_bfloat16>((size_t)qb * kp);
+  uint64_t* cand = ar.take<uint64_t>((size_t)qb * osegs * ncp);
+  uint64_t* gthr = ar.take<uint64_t>((size_t)qb);
+  int64_t* flagged = ar.take<int64_t>((size_t)qb);
+  int* nflag = ar.take<int>(1);
+  int64_t fallback = 0;
+  for (int64_t q0 = 0; q0 < nq; q0 += qb) {
+    const int64_t nb = std::min(qb, nq - q0);
+    const float* xr = d_q + q0 * d;
+    launch_to_bf16(xr, nb, d, xb, nullptr, s);
+    launch_umma_topk(xb, nb, cent_bf16, nlist, d, metric, nullptr, cnorm, nc, nseg, nullptr,
+                     osegs > 1 ? gthr : nullptr, cand, ctx->d_err.as<int>(), s);
+    MV_CHECK_CUDA(cudaMemsetAsync(nflag, 0, sizeof(int), s));
+    launch_topp_certify(xr, nb, d, cent, nlist, metric, cand, osegs * ncp, nc, P, ccert,
+                        probes + q0 * P, flagged, nflag, s);
+    int h_nflag = 0;
+    d2h(&h_nflag, nflag, sizeof(int), s);
+    check_kernel_errors(ctx, s);  // syncs
+    if (h_nflag > 0) {  // the exact selection for the open queries
+      DevBuf tmp;
+      tmp.ensure(ws_bytes((size_t)h_nflag * d, 4) + ws_bytes((size_t)h_nflag * nlist, 4) +
+                 ws_bytes((size_t)h_nflag * P, 8) + ws_bytes((size_t)h_nflag * P, 4));
+      Arena ta(tmp);
+      float* sx = ta.take<float>((size_t)h_nflag * d);
+      float* dm = ta.take<float>((size_t)h_nflag * nlist);
+      uint64_t* keys = ta.take<uint64_t>((size_t)h_nflag * P);
+      int32_t* sp = ta.take<int32_t>((size_t)h_nflag * P);
+      launch_gather_rows(xr, d, flagged, h_nflag, sx, 1, 0, 0, s);
+      launch_exact_matrix(metric == MV_METRIC_L2 ? KIND_L2_SIMD8 : KIND_IP_SIMD8, sx, h_nflag, d,
+                          cent, nlist, d, d, dm, nlist, s);
+      launch_select_rows(dm, h_nflag, nlist, nlist, 0, P, nullptr, keys, nullptr, s);
+      launch_keys_to_ids(keys, (int64_t)h_nflag * P, sp, s);
+      scatter_rows(sp, h_nflag, 4 * P, flagged, probes + q0 * P, s);
+      sync(s);
+    }
+    fallback += h_nflag;
+  }
+  ctx->assign_rows += nq;
+  ctx->assign_fallback += fallback;
+  return true;
+}
+
 void ivfpq_search_plain(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int nprobe,
                         const uint8_t* d_filter, int64_t filter_len, float* d_out,
                         int64_t* d_lab, DevBuf& ws, cudaStream_t s) {
@@ -496,6 +563,10 @@ void ivfpq_search_plain(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int n
     return;
   }
   MV_REQUIRE(nprobe <= 8192, MV_ERR_UNSUPPORTED, "nprobe above 8192 is not supported on the GPU");
+  const bool cert_coarse = umma_kpad(ix->d) <= 256 &&
+                           std::min(ix->nlist, nprobe + std::max(16, nprobe / 2)) < ix->nlist &&
+                           nprobe + std::max(16, nprobe / 2) <= UMMA_TOPK_MAX;
+  if (cert_coarse) ensure_coarse(ix, s);
   // Query batches bound the coarse distance matrix to ~1.5 GB.
   int64_t qb = std::max<int64_t>(64, (int64_t)(1536ll * 1024 * 1024 / ((int64_t)ix->nlist * 4)));
   qb = std::min<int64_t>({qb, nq, 65535ll * 64});
@@ -510,12 +581,20 @@ void ivfpq_search_plain(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int n
     const int64_t nb = std::min(qb, nq - q0);
     const float* xq = d_x + q0 * ix->d;
     // :264 coarse quantizer search with k = nprobe
-    {
+    bool certified = false;
+    if (cert_coarse) {
       StageTimer t(ix->ctx, MV_STAGE_COARSE, s);
-      launch_exact_matrix(kind, xq, nb, ix->d, ix->centroids.as<float>(), ix->nlist, ix->d, ix->d,
-                          dmat, ix->nlist, s);
+      certified = coarse_topp_certified(ix->ctx, xq, nb, ix->d, ix->centroids.as<float>(),
+                                        ix->d_cent_bf16.as<__nv_bfloat16>(), ix->d_cnorm.as<float>(),
+                                        ix->d_ccert.as<double>(), ix->nlist, ix->metric, nprobe,
+                                        probes, s);
     }
-    {
+    if (!certified) {
+      {
+        StageTimer t(ix->ctx, MV_STAGE_COARSE, s);
+        launch_exact_matrix(kind, xq, nb, ix->d, ix->centroids.as<float>(), ix->nlist, ix->d,
+                            ix->d, dmat, ix->nlist, s);
+      }
       StageTimer t(ix->ctx, MV_STAGE_SELECT, s);
       launch_select_rows(dmat, nb, ix->nlist, ix->nlist, 0, nprobe, nullptr, ckeys, nullptr, s);
       launch_keys_to_ids(ckeys, nb * nprobe, probes, s);
@@ -560,14 +639,31 @@ void check_kernel_errors(mv_ctx* ctx, cudaStream_t s) {
 
 // Builds the fast-form side structures once per index state: BF16
 // centroids and their norms, and the per-vector term ||y||^2 + 2<c, y>.
-void ensure_fast(mv_ivfpq* ix, cudaStream_t s) {
-  std::lock_guard<std::mutex> lk(ix->fast_mu);
-  if (ix->fast_ready) return;
+// Centroid-only tensor-core state: BF16 centroids, their norms and the
+// certificate bounds (caller holds fast_mu).
+void build_coarse_locked(mv_ivfpq* ix, cudaStream_t s) {
+  if (ix->coarse_ready) return;
   const int kp = umma_kpad(ix->d);
   ix->d_cent_bf16.ensure((size_t)ix->nlist * kp * 2);
   ix->d_cnorm.ensure((size_t)ix->nlist * 4);
+  ix->d_ccert.ensure(2 * sizeof(double));
   launch_to_bf16(ix->centroids.as<float>(), ix->nlist, ix->d, ix->d_cent_bf16.as<__nv_bfloat16>(),
                  ix->d_cnorm.as<float>(), s);
+  launch_cert_bounds(ix->d_cnorm.as<float>(), ix->centroids.as<float>(), ix->nlist, ix->d,
+                     ix->d_ccert.as<double>(), s);
+  sync(s);
+  ix->coarse_ready = true;
+}
+
+void ensure_coarse(mv_ivfpq* ix, cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(ix->fast_mu);
+  build_coarse_locked(ix, s);
+}
+
+void ensure_fast(mv_ivfpq* ix, cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(ix->fast_mu);
+  if (ix->fast_ready) return;
+  build_coarse_locked(ix, s);
   const int64_t total = ix->h_off[ix->nlist];
   if (ix->metric == MV_METRIC_L2 && total > 0) {
     ix->d_vec_term.ensure((size_t)total * 4);
@@ -953,6 +1049,7 @@ int32_t mv_ivfpq_set_codebooks(mv_ivfpq* ix, const float* centroids, const float
     MV_CHECK_CUDA(cudaMemcpy(ix->pq.p, pq, sizeof(float) * 256 * ix->d, cudaMemcpyHostToDevice));
     ix->trained = true;
     ix->fast_ready = false;
+    ix->coarse_ready = false;
   });
 }
 
@@ -1035,6 +1132,7 @@ int32_t mv_ivfpq_train_ex(mv_ivfpq* ix, const float* x, int64_t n, int32_t niter
     sync(s);
     ix->trained = true;
     ix->fast_ready = false;
+    ix->coarse_ready = false;
   });
 }
 
@@ -2483,13 +2581,19 @@ void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int npr
   const int cpath = p ? p->coarse_path : 0;
   MV_REQUIRE(cpath >= 0 && cpath <= 2, MV_ERR_ARG, "coarse_path must be 0, 1 or 2");
   const bool fused = fast && nc <= 64 && (cpath == 1 || (cpath == 0 && nc <= 16));
-  if (fast) {
+  const bool cert_coarse = !fast && umma_kpad(ix->d) <= 256 &&
+                           std::min(ix->nlist, nprobe + std::max(16, nprobe / 2)) < ix->nlist &&
+                           nprobe + std::max(16, nprobe / 2) <= UMMA_TOPK_MAX;
+  if (fast || cert_coarse) {
     std::lock_guard<std::mutex> lk(ix->fast_mu);
     if (!ix->fast_ready) {
       ix->d_cent_bf16.ensure((size_t)ix->nlist * kp * 2);
       ix->d_cnorm.ensure((size_t)ix->nlist * 4);
+      ix->d_ccert.ensure(2 * sizeof(double));
       launch_to_bf16(ix->centroids.as<float>(), ix->nlist, ix->d,
                      ix->d_cent_bf16.as<__nv_bfloat16>(), ix->d_cnorm.as<float>(), s);
+      launch_cert_bounds(ix->d_cnorm.as<float>(), ix->centroids.as<float>(), ix->nlist, ix->d,
+                         ix->d_ccert.as<double>(), s);
       sync(s);
       ix->fast_ready = true;
     }
@@ -2513,7 +2617,15 @@ void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int npr
   for (int64_t q0 = 0; q0 < nq; q0 += qb) {
     const int64_t nb = std::min(qb, nq - q0);
     const float* xb = d_x + q0 * ix->d;
-    {
+    bool certified = false;
+    if (cert_coarse) {
+      StageTimer t(ix->ctx, MV_STAGE_COARSE, s);
+      certified = coarse_topp_certified(ix->ctx, xb, nb, ix->d, ix->centroids.as<float>(),
+                                        ix->d_cent_bf16.as<__nv_bfloat16>(), ix->d_cnorm.as<float>(),
+                                        ix->d_ccert.as<double>(), ix->nlist, ix->metric, nprobe,
+                                        probes, s);
+    }
+    if (!certified) {
       StageTimer t(ix->ctx, MV_STAGE_COARSE, s);
       if (!fast) {
         launch_exact_matrix(kind, xb, nb, ix->d, ix->centroids.as<float>(), ix->nlist, ix->d,
@@ -2531,7 +2643,7 @@ void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int npr
                            nullptr, ix->ctx->d_err.as<int>(), ix->ctx->num_sms, s);
       }
     }
-    {
+    if (!certified) {
       StageTimer t(ix->ctx, MV_STAGE_SELECT, s);
       if (!fast) {  // :185-194 coarse quantizer search with k = nprobe
         launch_select_rows(dmat, nb, ix->nlist, ix->nlist, 0, nprobe, nullptr, ckeys, nullptr, s);

@@ -205,6 +205,8 @@ struct mv_ivfpq {
   // Fast-form state (built lazily from the above).
   std::mutex fast_mu;
   bool fast_ready = false;
+  bool coarse_ready = false;  // d_cent_bf16, d_cnorm, d_ccert (centroid-only state)
+  mv::DevBuf d_ccert;       // 2 doubles: bound on ||bf16(c)||^2, max ||c - bf16(c)||
   mv::DevBuf d_vec_term;    // FP32 per vector: ||y||^2 + 2<c, y> (y = PQ reconstruction)
   mv::DevBuf d_cnorm;       // FP32 per centroid ||c||^2
   mv::DevBuf d_cent_bf16;   // nlist x d BF16
@@ -224,6 +226,7 @@ struct mv_ivfflat {
   std::mutex fast_mu;
   bool fast_ready = false;
   mv::DevBuf d_cent_bf16, d_cnorm;  // fast coarse step
+  mv::DevBuf d_ccert;               // 2 doubles: coarse certificate bounds
 };
 
 struct mv_flat {

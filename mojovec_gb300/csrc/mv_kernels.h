@@ -100,6 +100,11 @@ void launch_assign_certify(const float* x, int64_t n, int d, const float* cent, 
                            const uint64_t* cand, int ncand, int kc, const double* cert,
                            int32_t* assign, float* mind, int64_t* flagged, int* nflag,
                            cudaStream_t s);
+// The P nearest centroids per row (ascending (distance, list)) from the
+// GEMM's candidates; rows the bound does not settle go to flagged[].
+void launch_topp_certify(const float* x, int64_t n, int d, const float* cent, int nlist, int metric,
+                         const uint64_t* cand, int ncand, int kc, int P, const double* cert,
+                         int32_t* probes, int64_t* flagged, int* nflag, cudaStream_t s);
 // Flat top-k from each query's shortlist of R approximate keys: reference
 // distances, the k smallest written (0.0 / -1 tail, IP un-negated), flag[q]
 // = 1 when the bound (or over[q], may be null) leaves the query open.

@@ -93,3 +93,74 @@ def test_duplicated_centroids_ties_settled_exactly(mv):
     dist = (x64 * x64).sum(1)[:, None] + (c64 * c64).sum(1)[None, :] - 2 * x64 @ c64.T
     assert np.array_equal(where, dist.argmin(1))
     assert (np.diff(off)[1:40] == 0).all()
+
+
+@pytest.mark.parametrize("metric", [0, 1])
+@pytest.mark.parametrize("nprobe", [1, 8, 32])
+def test_plain_ivfpq_certified_coarse_matches_oracle(mv, orc, metric, nprobe):
+    """The plain search's coarse step (k = nprobe, index_ivf_pq.mojo:264)
+    through the certified path: probes, hence ids and distance bits, equal
+    the oracle's."""
+    from mojovec_gb300 import synth
+
+    d, nlist, M = 64, 1024, 8
+    x, q = synth.sift_like(30000, d=d, n_centers=100, seed=61, nq=300)
+    if metric == 1:
+        x = x / np.linalg.norm(x, axis=1, keepdims=True)
+        q = q / np.linalg.norm(q, axis=1, keepdims=True)
+    rng = np.random.default_rng(62)
+    cent = x[rng.choice(len(x), nlist, replace=False)] + rng.standard_normal((nlist, d)).astype(np.float32) * 0.01
+    pq = rng.standard_normal((M, 256, d // M)).astype(np.float32)
+    g = mv.IndexIVFPQ(d, nlist, M, metric)
+    g.set_codebooks(cent, pq)
+    g.add(x)
+    r = orc.IVFPQ(d, nlist, M, metric)
+    r.set_codebooks(cent, pq)
+    r.add(x)
+    r0, _ = _stats(mv)
+    gd, gl = g.search(q, 10, nprobe=nprobe)
+    rows, _ = _stats(mv)
+    assert rows - r0 == len(q)  # the coarse step went through the certified path
+    rd, rl = r.search(q, 10, nprobe)
+    assert np.array_equal(gl, rl) and np.array_equal(gd.view(np.uint32), rd.view(np.uint32))
+
+
+def test_plain_coarse_ties_fall_back(mv, orc):
+    d, nlist, M = 16, 256, 4
+    rng = np.random.default_rng(63)
+    cent = rng.integers(0, 4, size=(nlist, d)).astype(np.float32)
+    cent[:120] = cent[0]  # 120 equal centroids: ties far past the candidates
+    pq = rng.standard_normal((M, 256, d // M)).astype(np.float32)
+    x = rng.integers(0, 4, size=(20000, d)).astype(np.float32)
+    q = np.vstack([cent[:50] + rng.integers(0, 2, size=(50, d)),
+                   rng.integers(0, 4, size=(50, d))]).astype(np.float32)
+    g = mv.IndexIVFPQ(d, nlist, M)
+    g.set_codebooks(cent, pq)
+    g.add(x)
+    r = orc.IVFPQ(d, nlist, M)
+    r.set_codebooks(cent, pq)
+    r.add(x)
+    _, f0 = _stats(mv)
+    gd, gl = g.search(q, 10, nprobe=8)
+    _, f1 = _stats(mv)
+    rd, rl = r.search(q, 10, 8)
+    assert f1 > f0
+    assert np.array_equal(gl, rl) and np.array_equal(gd.view(np.uint32), rd.view(np.uint32))
+
+
+@pytest.mark.parametrize("metric", [0, 1])
+def test_plain_ivfflat_certified_coarse_matches_oracle(mv, orc, metric):
+    from mojovec_gb300 import synth
+
+    d, nlist = 32, 512
+    x, q = synth.sift_like(20000, d=d, n_centers=64, seed=64, nq=200)
+    g = mv.IndexIVFFlat(d, nlist, metric)
+    g.train(x, niter=4)
+    g.add(x)
+    r = orc.IVFFlat(d, nlist, metric)
+    r.train(x, niter=4)
+    r.add(x)
+    for nprobe in (4, 16):
+        gd, gl = g.search(q, 10, nprobe=nprobe)
+        rd, rl = r.search(q, 10, nprobe)
+        assert np.array_equal(gl, rl) and np.array_equal(gd.view(np.uint32), rd.view(np.uint32))
