@@ -265,26 +265,26 @@ __global__ void __launch_bounds__(TP_WARPS * 32)
 // Flat top-k, one CTA per query over its shortlist of R approximate keys
 // (the R smallest of the GEMM's candidates, KEY_NONE padded): the rows are
 // staged in shared memory (stride d + 1, so thread t reading row t touches
-// its own bank) in chunks of FC_CHUNK rows, each thread computes one row's
+// its own bank) in chunks of `chunk` rows, each thread computes one row's
 // reference distance, the k smallest (distance, row) keys are selected and
 // written, and the certificate compares the k-th with the bound for the
 // rows outside the shortlist. flag[q] = 1 when it does not settle the query
 // (the host recomputes those with the exact scan).
-constexpr int FC_THREADS = 128, FC_CHUNK = 64;
+constexpr int FC_THREADS = 128, FC_CHUNK_MAX = 64;
 
 template <bool IP>
 __global__ void __launch_bounds__(FC_THREADS)
     k_flat_certify(const float* __restrict__ q, int d, const float* __restrict__ rows, int64_t nb,
-                   const uint64_t* __restrict__ skeys, int R, int k,
+                   const uint64_t* __restrict__ skeys, int R, int k, int chunk,
                    const double* __restrict__ cert, const int* __restrict__ over,
                    float* __restrict__ out_d, int64_t* __restrict__ out_l,
                    int* __restrict__ flag) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int stride = d + 1;
   float* qv = reinterpret_cast<float*>(smraw);
-  float* tile = qv + d;  // FC_CHUNK x (d + 1)
+  float* tile = qv + d;  // chunk x (d + 1)
   uint64_t* ek = reinterpret_cast<uint64_t*>(
-      smraw + (((size_t)d + (size_t)FC_CHUNK * stride) * 4 + 15) / 16 * 16);  // R
+      smraw + (((size_t)d + (size_t)chunk * stride) * 4 + 15) / 16 * 16);  // R
   uint64_t* outb = ek + R;                                                  // next_pow2(k)
   __shared__ RadixScratch rs;
   __shared__ unsigned long long s_kmax;
@@ -308,8 +308,8 @@ __global__ void __launch_bounds__(FC_THREADS)
       s_rs = rsq;
     }
   }
-  for (int c0 = 0; c0 < R; c0 += FC_CHUNK) {
-    const int n = min(FC_CHUNK, R - c0);
+  for (int c0 = 0; c0 < R; c0 += chunk) {
+    const int n = min(chunk, R - c0);
     // stage the chunk's rows, one warp per row, coalesced
     for (int i = warp; i < n; i += FC_THREADS / 32) {
       const uint64_t key = sk[c0 + i];
@@ -425,8 +425,15 @@ void launch_topp_certify(const float* x, int64_t n, int d, const float* cent, in
   MV_CHECK_CUDA(cudaGetLastError());
 }
 
+// Rows staged per chunk: up to 64, fewer for long rows.
+int flat_certify_chunk(int d, int R, int k) {
+  const long room = 160l * 1024 - (long)d * 4 - (long)(R + next_pow2(k)) * 8 - 16;
+  return (int)std::max(1l, std::min((long)FC_CHUNK_MAX, room / ((long)(d + 1) * 4)));
+}
+
 size_t flat_certify_smem(int d, int R, int k) {
-  return ((size_t)d + (size_t)FC_CHUNK * (d + 1)) * 4 + 16 + (size_t)(R + next_pow2(k)) * 8;
+  return ((size_t)d + (size_t)flat_certify_chunk(d, R, k) * (d + 1)) * 4 + 16 +
+         (size_t)(R + next_pow2(k)) * 8;
 }
 
 void launch_flat_certify(const float* q, int64_t nq, int d, int metric, const float* rows,
@@ -436,14 +443,16 @@ void launch_flat_certify(const float* q, int64_t nq, int d, int metric, const fl
   if (nq == 0) return;
   const size_t smem = flat_certify_smem(d, R, k);
   MV_REQUIRE(smem <= 200 * 1024, MV_ERR_UNSUPPORTED, "flat certify: d or shortlist too large");
+  const int chunk = flat_certify_chunk(d, R, k);
   if (metric == MV_METRIC_IP) {
     smem_limit(k_flat_certify<true>, smem);
-    k_flat_certify<true><<<(unsigned)nq, FC_THREADS, smem, s>>>(q, d, rows, nb, skeys, R, k, cert,
-                                                               over, out_d, out_l, flag);
+    k_flat_certify<true><<<(unsigned)nq, FC_THREADS, smem, s>>>(q, d, rows, nb, skeys, R, k, chunk,
+                                                               cert, over, out_d, out_l, flag);
   } else {
     smem_limit(k_flat_certify<false>, smem);
     k_flat_certify<false><<<(unsigned)nq, FC_THREADS, smem, s>>>(q, d, rows, nb, skeys, R, k,
-                                                                cert, over, out_d, out_l, flag);
+                                                                chunk, cert, over, out_d, out_l,
+                                                                flag);
   }
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());

@@ -46,6 +46,10 @@ using namespace sm100;
 
 constexpr int BM = 128;
 constexpr int STAGES = 2;
+// The fused top-k GEMM keeps the X block resident up to this many k-blocks
+// (256 BF16 or E4M3 bytes of K ... 4 x 128-byte rows); longer rows stream
+// X and Y k-blocks through KS_STAGES stages.
+constexpr int KS_MAX_RESIDENT = 4, KS_STAGES = 4;
 constexpr int NUM_THREADS = 192;
 
 template <int BN>
@@ -280,7 +284,10 @@ __device__ __forceinline__ void heap_replace_top(uint64_t* h, int K, uint64_t ke
   h[(size_t)i * BM] = key;
 }
 
-template <int BN, bool L2, int EG, bool F8 = false>
+// KS (K streaming, rows longer than KS_MAX_RESIDENT k-blocks): the X block is
+// not kept resident; every stage of a KS_STAGES ring holds one k-block of X
+// and one of the Y tile, and the MMA warp walks (tile, k-block).
+template <int BN, bool L2, int EG, bool F8 = false, bool KS = false>
 __global__ void __launch_bounds__(64 + 128 * EG, 1)
     k_umma_topk(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUtensorMap ty,
                 UmmaTopkArgs g) {
@@ -290,31 +297,32 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
   const int nkb = g.nkb;
-  const uint32_t a_bytes = (uint32_t)nkb * BM * 128;
-  const uint32_t b_stage = (uint32_t)nkb * BN * 128;
+  const uint32_t a_bytes = KS ? 0u : (uint32_t)nkb * BM * 128;
+  const uint32_t b_stage = KS ? (uint32_t)(BM + BN) * 128 : (uint32_t)nkb * BN * 128;
+  constexpr int NST = KS ? KS_STAGES : STAGES;
   uint8_t* sA = smem;
   uint8_t* sB = smem + a_bytes;
   // Per epilogue group: heaps (nc x BM), pending (g.pend x BM); per
   // epilogue warp: the tile's column biases (BN floats).
-  uint64_t* heap = reinterpret_cast<uint64_t*>(sB + STAGES * b_stage);
+  uint64_t* heap = reinterpret_cast<uint64_t*>(sB + NST * b_stage);
   uint64_t* pend = heap + (size_t)EG * g.nc * BM;
   float* cnbuf = reinterpret_cast<float*>(pend + (size_t)EG * g.pend * BM);
   // E4M3: per epilogue warp also the tile's column scales (BN floats).
   float* csbuf = cnbuf + 4 * EG * BN;
   uint64_t* bars = reinterpret_cast<uint64_t*>(csbuf + (F8 ? 4 * EG * BN : 0));
-  uint32_t* holder = reinterpret_cast<uint32_t*>(bars + 12);
+  uint32_t* holder = reinterpret_cast<uint32_t*>(bars + 16);
   __shared__ int s_err;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t bar0 = smem_u32(bars);
   auto b_full = [&](int s) { return bar0 + 8u * s; };
-  auto b_empty = [&](int s) { return bar0 + 8u * (2 + s); };
-  auto b_tfull = [&](int a) { return bar0 + 8u * (4 + a); };
-  auto b_tempty = [&](int a) { return bar0 + 8u * (6 + a); };
-  const uint32_t b_done = bar0 + 8u * 8;
-  const uint32_t b_fulla = bar0 + 8u * 9;
+  auto b_empty = [&](int s) { return bar0 + 8u * (4 + s); };
+  auto b_tfull = [&](int a) { return bar0 + 8u * (8 + a); };
+  auto b_tempty = [&](int a) { return bar0 + 8u * (10 + a); };
+  const uint32_t b_done = bar0 + 8u * 12;
+  const uint32_t b_fulla = bar0 + 8u * 13;
   if (threadIdx.x == 0) {
     s_err = 0;
-    for (int s = 0; s < STAGES; ++s) {
+    for (int s = 0; s < NST; ++s) {
       mbar_init(b_full(s), 1);
       mbar_init(b_empty(s), 1);
     }
@@ -345,6 +353,70 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
   const int my_count = ct1 > ct0 ? ct1 - ct0 : 0;
   volatile int* verr = &s_err;
 
+  if constexpr (KS) {
+    if (warp == 0) {
+      if (lane == 0) {
+        int it = 0;  // k-blocks issued
+        bool stop = false;
+        for (int i = 0; i < my_count && !stop; ++i) {
+          for (int kb = 0; kb < nkb; ++kb, ++it) {
+            const int s = it % NST;
+            const uint32_t ph = (uint32_t)(it / NST) & 1u;
+            if (*verr || !mbar_wait(b_empty(s), ph ^ 1u)) {
+              *verr = 1;
+              stop = true;
+              break;
+            }
+            uint8_t* st = sB + (size_t)s * b_stage;
+            mbar_arrive_expect_tx(b_full(s), b_stage);
+            tma_load_2d(smem_u32(st), &tx, kb * KB_ELEMS, rb * BM, b_full(s));
+            tma_load_2d(smem_u32(st + BM * 128), &ty, kb * KB_ELEMS, (ct0 + i) * BN, b_full(s));
+          }
+        }
+        // Drain: every issued load must land before the CTA exits.
+        for (int j = (it > NST ? it - NST : 0); j < it; ++j)
+          if (!mbar_wait(b_full(j % NST), (uint32_t)(j / NST) & 1u)) *verr = 1;
+      }
+    } else if (warp == 1) {
+      if (lane == 0) {
+        const uint32_t idesc = F8 ? idesc_e4m3_f32(BM, BN) : idesc_bf16_f32(BM, BN);
+        int it = 0;
+        for (int i = 0; i < my_count; ++i) {
+          const int acc = i & 1;
+          const uint32_t aph = (uint32_t)(i >> 1) & 1u;
+          if (*verr || !mbar_wait(b_tempty(acc), aph ^ 1u)) {
+            *verr = 1;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t d = tmem + (uint32_t)(acc * BN);
+          bool bad = false;
+          for (int kb = 0; kb < nkb; ++kb, ++it) {
+            const int s = it % NST;
+            const uint32_t ph = (uint32_t)(it / NST) & 1u;
+            if (*verr || !mbar_wait(b_full(s), ph)) {
+              *verr = 1;
+              bad = true;
+              break;
+            }
+            tc_fence_after();
+            const uint8_t* st = sB + (size_t)s * b_stage;
+            const uint64_t ad = desc_k_sw128(smem_u32(st));
+            const uint64_t bd = desc_k_sw128(smem_u32(st + BM * 128));
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {  // 32 bytes of K per instruction
+              if (F8) umma_e4m3(d, ad + 2u * kk, bd + 2u * kk, idesc, (kb | kk) ? 1u : 0u);
+              else umma_bf16(d, ad + 2u * kk, bd + 2u * kk, idesc, (kb | kk) ? 1u : 0u);
+            }
+            umma_commit(b_empty(s));
+          }
+          if (bad) break;
+          umma_commit(b_tfull(acc));
+        }
+        umma_commit(b_done);
+      }
+    }
+  } else
   if (warp == 0) {
     if (lane == 0) {
       mbar_arrive_expect_tx(b_fulla, a_bytes);
@@ -400,7 +472,8 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
       }
       umma_commit(b_done);
     }
-  } else {
+  }
+  if (warp >= 2) {
     // Epilogue warp (q, h): TMEM lane quarter q (= warp % 4, as tcgen05.ld
     // requires) and group h, which owns chunks [h * NCHG, (h + 1) * NCHG) of
     // every tile and keeps its own heaps (an output segment of its own).
@@ -788,8 +861,10 @@ struct TopkCfg {
   int bn, eg, pend;
 };
 size_t topk_smem_base(int nkb, int bn, int nc, int eg, bool f8 = false) {
-  return 1024 + (size_t)nkb * BM * 128 + (size_t)STAGES * nkb * bn * 128 +
-         (size_t)eg * nc * BM * 8 + (size_t)4 * eg * bn * 4 * (f8 ? 2 : 1) + 256;
+  const size_t tiles = nkb > KS_MAX_RESIDENT
+                           ? (size_t)KS_STAGES * (BM + bn) * 128
+                           : (size_t)nkb * BM * 128 + (size_t)STAGES * nkb * bn * 128;
+  return 1024 + tiles + (size_t)eg * nc * BM * 8 + (size_t)4 * eg * bn * 4 * (f8 ? 2 : 1) + 256;
 }
 int topk_pend_fit(int nkb, int bn, int nc, int eg, bool f8 = false) {
   const size_t base = topk_smem_base(nkb, bn, nc, eg, f8);
@@ -797,6 +872,11 @@ int topk_pend_fit(int nkb, int bn, int nc, int eg, bool f8 = false) {
   return (int)std::min<size_t>(TOPK_PEND_MAX, room / 8 * 8);
 }
 TopkCfg topk_cfg(int nkb, int nc, bool f8 = false) {
+  if (nkb > KS_MAX_RESIDENT) {  // streamed K: 128-column tiles when the pending list fits
+    const int p128 = topk_pend_fit(nkb, 128, nc, 1, f8);
+    if (p128 >= TOPK_PEND_MIN) return {128, 1, p128};
+    return {64, 1, topk_pend_fit(nkb, 64, nc, 1, f8)};
+  }
   const int bn = nkb <= 2 ? 128 : 64;
   return {bn, 1, topk_pend_fit(nkb, bn, nc, 1, f8)};
 }
@@ -841,7 +921,7 @@ void launch_umma_topk(const __nv_bfloat16* X, int64_t nx, const __nv_bfloat16* Y
                       cudaStream_t s) {
   if (nx == 0) return;
   const int kp = umma_kpad(d);
-  MV_REQUIRE(kp <= 256, MV_ERR_UNSUPPORTED, "BF16 GEMM supports d <= 256");
+  MV_REQUIRE(kp <= UMMA_TOPK_MAX_K, MV_ERR_UNSUPPORTED, "fused top-k GEMM: d too large");
   MV_REQUIRE(nc >= 1 && nc <= UMMA_TOPK_MAX, MV_ERR_UNSUPPORTED, "fused top-k keeps at most 64 per row");
   MV_REQUIRE(nx < (1ll << 31) && ny < (1ll << 32) - 1, MV_ERR_UNSUPPORTED, "GEMM too large");
   MV_REQUIRE(nseg >= 1 && nseg <= 65535, MV_ERR_INTERNAL, "fused top-k: bad segment count");
@@ -876,7 +956,15 @@ void launch_umma_topk(const __nv_bfloat16* X, int64_t nx, const __nv_bfloat16* Y
     kernel<<<grid, threads, smem, s>>>(tx, ty, g);
   };
   const bool l2m = metric == MV_METRIC_L2;
-  if (c.bn == 128) {
+  if (g.nkb > KS_MAX_RESIDENT) {
+    if (c.bn == 128) {
+      l2m ? go(k_umma_topk<128, true, 1, false, true>, 192)
+          : go(k_umma_topk<128, false, 1, false, true>, 192);
+    } else {
+      l2m ? go(k_umma_topk<64, true, 1, false, true>, 192)
+          : go(k_umma_topk<64, false, 1, false, true>, 192);
+    }
+  } else if (c.bn == 128) {
     l2m ? go(k_umma_topk<128, true, 1>, 192) : go(k_umma_topk<128, false, 1>, 192);
   } else {
     l2m ? go(k_umma_topk<64, true, 1>, 192) : go(k_umma_topk<64, false, 1>, 192);
@@ -891,7 +979,7 @@ void launch_umma_topk_e4m3(const uint8_t* X8, int64_t nx, const float* xscale, c
                            int* err, cudaStream_t s) {
   if (nx == 0) return;
   const int kp = umma_kpad8(d);
-  MV_REQUIRE(kp <= 256, MV_ERR_UNSUPPORTED, "E4M3 GEMM supports d <= 256");
+  MV_REQUIRE(kp <= UMMA_TOPK_MAX_K, MV_ERR_UNSUPPORTED, "E4M3 GEMM: d too large");
   MV_REQUIRE(nc >= 1 && nc <= UMMA_TOPK_MAX, MV_ERR_UNSUPPORTED, "fused top-k keeps at most 64 per row");
   MV_REQUIRE(nx < (1ll << 31) && ny < (1ll << 32) - 1, MV_ERR_UNSUPPORTED, "GEMM too large");
   MV_REQUIRE(nseg >= 1 && nseg <= 65535, MV_ERR_INTERNAL, "fused top-k: bad segment count");
@@ -929,7 +1017,15 @@ void launch_umma_topk_e4m3(const uint8_t* X8, int64_t nx, const float* xscale, c
     kernel<<<grid, threads, smem, s>>>(tx, ty, g);
   };
   const bool l2m = metric == MV_METRIC_L2;
-  if (c.bn == 128) {
+  if (g.nkb > KS_MAX_RESIDENT) {
+    if (c.bn == 128) {
+      l2m ? go(k_umma_topk<128, true, 1, true, true>, 192)
+          : go(k_umma_topk<128, false, 1, true, true>, 192);
+    } else {
+      l2m ? go(k_umma_topk<64, true, 1, true, true>, 192)
+          : go(k_umma_topk<64, false, 1, true, true>, 192);
+    }
+  } else if (c.bn == 128) {
     l2m ? go(k_umma_topk<128, true, 1, true>, 192) : go(k_umma_topk<128, false, 1, true>, 192);
   } else {
     l2m ? go(k_umma_topk<64, true, 1, true>, 192) : go(k_umma_topk<64, false, 1, true>, 192);

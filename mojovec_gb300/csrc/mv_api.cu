@@ -127,7 +127,7 @@ void assign_nearest(const float* x, int64_t n, int d, const float* cent, int k, 
   const int kind = metric == MV_METRIC_IP ? KIND_IP_SIMD8
                                           : (mode == 1 && d <= 4 ? KIND_L2_SHORT4 : KIND_L2_SIMD8);
   mv_ctx* ctx = g_cur_ctx;
-  const bool cert = ctx && kind != KIND_L2_SHORT4 && umma_kpad(d) <= 256 && k > 2 * ASSIGN_KC &&
+  const bool cert = ctx && kind != KIND_L2_SHORT4 && umma_kpad(d) <= UMMA_TOPK_MAX_K && k > 2 * ASSIGN_KC &&
                     n >= 4096 && n <= 0x7fffffffll;
   if (!cert) {
     launch_exact_argmin(kind, mode, x, n, d, cent, k, d, d, assign, mind, 1, 0, 0, 0, s);
@@ -245,7 +245,7 @@ void kmeans_train_fast(const float* x, int64_t n, int d, int k, int niter, float
                        double* d_obj) {
   if (n == 0 || k <= 0) return;
   MV_REQUIRE(n <= 0x7fffffffll, MV_ERR_UNSUPPORTED, "fast k-means: too many rows");
-  MV_REQUIRE(umma_kpad(d) <= 256, MV_ERR_UNSUPPORTED, "fast k-means supports d <= 256");
+  MV_REQUIRE(umma_kpad(d) <= UMMA_TOPK_MAX_K, MV_ERR_UNSUPPORTED, "fast k-means supports d <= 2048");
   Philox gen(KMEANS_SEED);  // kmeans.mojo:70-82, as in the plain form
   uint32_t words[4];
   gen.step(words);
@@ -502,7 +502,7 @@ bool coarse_topp_certified(mv_ctx* ctx, const float* d_q, int64_t nq, int d, con
                            const __nv_bfloat16* cent_bf16, const float* cnorm, const double* ccert,
                            int nlist, int metric, int P, int32_t* probes, cudaStream_t s) {
   const int nc = std::min(nlist, P + std::max(16, P / 2));
-  if (nc > UMMA_TOPK_MAX || nc >= nlist || umma_kpad(d) > 256 || nq > 0x7fffffffll) return false;
+  if (nc > UMMA_TOPK_MAX || nc >= nlist || umma_kpad(d) > UMMA_TOPK_MAX_K || nq > 0x7fffffffll) return false;
   const int kp = umma_kpad(d), ncp = next_pow2(nc);
   const int64_t qb = std::min<int64_t>(nq, 65536);
   const int nseg = umma_topk_nseg(qb, nlist, d, nc, ctx->num_sms);
@@ -563,7 +563,7 @@ void ivfpq_search_plain(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int n
     return;
   }
   MV_REQUIRE(nprobe <= 8192, MV_ERR_UNSUPPORTED, "nprobe above 8192 is not supported on the GPU");
-  const bool cert_coarse = umma_kpad(ix->d) <= 256 &&
+  const bool cert_coarse = umma_kpad(ix->d) <= UMMA_TOPK_MAX_K &&
                            std::min(ix->nlist, nprobe + std::max(16, nprobe / 2)) < ix->nlist &&
                            nprobe + std::max(16, nprobe / 2) <= UMMA_TOPK_MAX;
   if (cert_coarse) ensure_coarse(ix, s);
@@ -745,6 +745,10 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
           launch_umma_topk(xq, nb, ix->d_cent_bf16.as<__nv_bfloat16>(), ix->nlist, ix->d,
                            ix->metric, nullptr, ix->d_cnorm.as<float>(), nc, nseg, nullptr, gthr,
                            ckeys, ix->ctx->d_err.as<int>(), s);
+        else if (kp > 256)  // the matrix GEMM keeps K resident: exact rows past d = 256
+          launch_exact_matrix(ix->metric == MV_METRIC_L2 ? KIND_L2_SIMD8 : KIND_IP_SIMD8, xb, nb,
+                              ix->d, ix->centroids.as<float>(), ix->nlist, ix->d, ix->d, dmat,
+                              ix->nlist, s);
         else
           launch_umma_dist(EPI_MATRIX, xq, nb, ix->d_cent_bf16.as<__nv_bfloat16>(), ix->nlist,
                            ix->d, ix->metric, nullptr, ix->d_cnorm.as<float>(), dmat, ix->nlist,
@@ -1114,7 +1118,7 @@ int32_t mv_ivfpq_train_ex(mv_ivfpq* ix, const float* x, int64_t n, int32_t niter
     h2d(dx.p, x, sizeof(float) * n * d, s);
     // 1. coarse k-means (:98-103)
     assign.ensure(sizeof(int32_t) * n);
-    if (form == MV_FORM_FAST && umma_kpad(d) <= 256)
+    if (form == MV_FORM_FAST && umma_kpad(d) <= UMMA_TOPK_MAX_K)
       kmeans_train_fast(dx.as<float>(), n, d, ix->nlist, niter_coarse, ix->centroids.as<float>(),
                         assign.as<int32_t>(), scratch, ix->ctx, s, nullptr);
     else
@@ -1307,7 +1311,7 @@ void flat_search_plain(mv_flat* ix, const float* d_x, int64_t nq, int k, const u
                        float* d_out, int64_t* d_lab, DevBuf& ws, cudaStream_t s) {
   if (nq == 0) return;
   const int64_t nb = ix->ntotal;
-  if (nb < 4096 || k > 128 || umma_kpad(ix->d) > 256 || nb > 0xfffffffell ||
+  if (nb < 4096 || k > 128 || umma_kpad(ix->d) > UMMA_TOPK_MAX_K || nb > 0xfffffffell ||
       flat_certify_smem(ix->d, 2 * std::max(k, 32), k) > 200 * 1024) {
     flat_search_exact(ix, d_x, nq, k, d_filter, d_out, d_lab, ws, s);
     return;
@@ -1395,7 +1399,7 @@ void flat_search_fast(mv_flat* ix, const float* d_x, int64_t nq, int k, const ui
     launch_fill(d_out, d_lab, nq * k, 0.0f, s);
     return;
   }
-  MV_REQUIRE(umma_kpad(ix->d) <= 256, MV_ERR_UNSUPPORTED, "fast flat form supports d <= 256");
+  MV_REQUIRE(umma_kpad(ix->d) <= UMMA_TOPK_MAX_K, MV_ERR_UNSUPPORTED, "fast flat form supports d <= 2048");
   const bool e4m3 = p && p->flat_e4m3;
   MV_REQUIRE(!e4m3 || (p->rerank > 0), MV_ERR_UNSUPPORTED, "the E4M3 shortlist needs a rerank");
   if (e4m3) ensure_flat_e4m3(ix, s);
@@ -1695,10 +1699,10 @@ __global__ void k_keys_to_cand(const uint64_t* __restrict__ keys, int64_t n, int
 
 // The tensor-core SQ8 scan is exact when every BF16 product and FP32
 // partial sum is an integer below 2^24: L2 (u8 codes) needs
-// 2 * d * 255^2 < 2^24 (d <= 129), IP (s8 codes) d * 127^2 < 2^24; the
-// GEMM takes d <= 256.
+// 2 * d * 255^2 < 2^24 (d <= 129), IP (s8 codes) d * 127^2 < 2^24
+// (d <= 1040).
 bool sq8_tensor_exact(const mv_sq8* ix) {
-  if (umma_kpad(ix->d) > 256) return false;
+  if (umma_kpad(ix->d) > UMMA_TOPK_MAX_K) return false;
   if (ix->metric == MV_METRIC_L2) return 2ll * ix->d * 255 * 255 < (1ll << 24);
   return (int64_t)ix->d * 127 * 127 < (1ll << 24);
 }
@@ -2575,13 +2579,13 @@ void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int npr
     return;
   }
   MV_REQUIRE(nprobe <= 8192, MV_ERR_UNSUPPORTED, "nprobe above 8192 is not supported on the GPU");
-  const bool fast = p && p->form == MV_FORM_FAST && umma_kpad(ix->d) <= 256;
+  const bool fast = p && p->form == MV_FORM_FAST && umma_kpad(ix->d) <= UMMA_TOPK_MAX_K;
   const int kp = umma_kpad(ix->d);
   const int nc = std::min(ix->nlist, nprobe + std::max(8, nprobe / 4));
   const int cpath = p ? p->coarse_path : 0;
   MV_REQUIRE(cpath >= 0 && cpath <= 2, MV_ERR_ARG, "coarse_path must be 0, 1 or 2");
   const bool fused = fast && nc <= 64 && (cpath == 1 || (cpath == 0 && nc <= 16));
-  const bool cert_coarse = !fast && umma_kpad(ix->d) <= 256 &&
+  const bool cert_coarse = !fast && umma_kpad(ix->d) <= UMMA_TOPK_MAX_K &&
                            std::min(ix->nlist, nprobe + std::max(16, nprobe / 2)) < ix->nlist &&
                            nprobe + std::max(16, nprobe / 2) <= UMMA_TOPK_MAX;
   if (fast || cert_coarse) {
@@ -2637,6 +2641,9 @@ void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int npr
                            ix->metric, nullptr, ix->d_cnorm.as<float>(), nc, nseg, nullptr,
                            ncand > next_pow2(nc) ? gthr : nullptr, fkeys, ix->ctx->d_err.as<int>(),
                            s);
+        else if (umma_kpad(ix->d) > 256)  // the matrix GEMM keeps K resident: exact past d = 256
+          launch_exact_matrix(kind, xb, nb, ix->d, ix->centroids.as<float>(), ix->nlist, ix->d,
+                              ix->d, dmat, ix->nlist, s);
         else
           launch_umma_dist(EPI_MATRIX, xq, nb, ix->d_cent_bf16.as<__nv_bfloat16>(), ix->nlist,
                            ix->d, ix->metric, nullptr, ix->d_cnorm.as<float>(), dmat, ix->nlist,
@@ -2721,7 +2728,7 @@ int32_t mv_ivfflat_train(mv_ivfflat* ix, const float* x, int64_t n, int32_t nite
     assign.ensure(sizeof(int32_t) * n);
     h2d(dx.p, x, sizeof(float) * n * ix->d, s);
     // :73-77 KMeans(d, nlist, 15)
-    if (form == MV_FORM_FAST && umma_kpad(ix->d) <= 256)
+    if (form == MV_FORM_FAST && umma_kpad(ix->d) <= UMMA_TOPK_MAX_K)
       kmeans_train_fast(dx.as<float>(), n, ix->d, ix->nlist, niter, ix->centroids.as<float>(),
                         assign.as<int32_t>(), scratch, ix->ctx, s, nullptr);
     else

@@ -61,6 +61,9 @@ void launch_umma_dist(int epi, const __nv_bfloat16* X, int64_t nx, const __nv_bf
                       cudaStream_t s);
 // Most keys the fused top-k GEMM keeps per row and column segment.
 constexpr int UMMA_TOPK_MAX = 64;
+// Longest padded row (elements) the fused top-k GEMM takes; above 256 the X
+// block streams through shared memory with the Y tiles.
+constexpr int UMMA_TOPK_MAX_K = 2048;
 // Epilogue groups of the fused top-k GEMM for (d, nc): each CTA writes one
 // output segment per group, so a launch with nseg column segments leaves
 // nseg * groups segments per row.
