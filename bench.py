@@ -137,10 +137,10 @@ NB = 1_000_000
 NQ = 10_000
 
 
-def build_workload(nb=None, nq=None):
+def build_workload(nb=None, nq=None, d=D):
     from mojovec_gb300 import synth
 
-    base, queries = synth.sift_like(nb or NB, d=D, n_centers=N_CENTERS, nq=nq or NQ)
+    base, queries = synth.sift_like(nb or NB, d=d, n_centers=N_CENTERS, nq=nq or NQ)
     return base, queries
 
 
@@ -409,18 +409,18 @@ def run_flat(args, rank, world):
 
     import mojovec_gb300 as mv
 
-    nb, nq, k = args.nb, args.nq, args.k
+    nb, nq, k, dim = args.nb, args.nq, args.k, args.dim
     sq8 = args.workload == "sq8"
     metric = mv.METRIC_L2 if args.metric == "l2" else mv.METRIC_IP
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
     ctx = mv.Context(dev)
     t_setup = time.perf_counter()
-    base, queries = build_workload(nb, nq)
-    exact = mv.IndexFlat(D, metric, ctx=ctx)
+    base, queries = build_workload(nb, nq, dim)
+    exact = mv.IndexFlat(dim, metric, ctx=ctx)
     exact.add(base)
     if sq8:
-        flat = mv.IndexFlatSQ8(D, metric, ctx=ctx)
+        flat = mv.IndexFlatSQ8(dim, metric, ctx=ctx)
         flat.add(base)
         _, gt_exact = exact.search(queries, k)
         del exact
@@ -490,7 +490,7 @@ def run_flat(args, rank, world):
     scan_qps = world * nq / (results["scan"]["ms"] / 1e3)
     fast_qps = world * nq / (results["fast"]["ms"] / 1e3)
 
-    pinned = torch.empty((nq, D), dtype=torch.float32).pin_memory()
+    pinned = torch.empty((nq, dim), dtype=torch.float32).pin_memory()
     pinned.copy_(torch.from_numpy(queries))
     hq = pinned.numpy()
     flat.search(hq, k, **plain)
@@ -511,7 +511,7 @@ def run_flat(args, rank, world):
     tc_peak = float(peaks.get("bf16_tflops", 1900.0))
     gemm_ms, gemm_n = stage.get("flat", (0.0, 0))
     per_launch_ms = gemm_ms / max(gemm_n, 1)
-    flops = 2.0 * nq * nb * D
+    flops = 2.0 * nq * nb * dim
     achieved = flops / (per_launch_ms / 1e3) / 1e12 if per_launch_ms > 0 else 0.0
     out = {
         "metric": SQ8_METRIC if sq8 else FLAT_METRIC,
@@ -527,7 +527,7 @@ def run_flat(args, rank, world):
         "dtype": "bf16+f32",
         "data": "synthetic SIFT-like (seeded Gaussian mixture, integer-valued), not SIFT1M",
         "config": {
-            "workload": f"{'sq8' if sq8 else 'flat'}_{nb}x128_{args.metric}_nq{nq}_k{k}",
+            "workload": f"{'sq8' if sq8 else 'flat'}_{nb}x{dim}_{args.metric}_nq{nq}_k{k}",
             "form": ("plain: SQ8 codes as BF16 on tcgen05 (exact integer dots) + per-row heap, "
                      f"reference formula and tie check, exact FP32 rerank of {rerank}") if sq8 else
                     ("plain: BF16 tcgen05 GEMM + per-row heap shortlist, reference FP32 distances "
@@ -545,12 +545,13 @@ def run_flat(args, rank, world):
                 "fp8_form_qps": round(world * nq / (results["fp8"]["ms"] / 1e3), 1),
                 "fp8_form_recall_at_k": round(recall_at(gt, results["fp8"]["labels"], k), 5),
                 "fp8_form": f"E4M3 (per-row scales) tcgen05 shortlist + FP32 rerank of {rerank}"}),
-            "l2_policy": "inputs larger than L2 (256 MB BF16 rows) and a 256 MiB flush per step",
+            "l2_policy": f"inputs larger than L2 ({nb * dim * 2 / 1e6:.0f} MB BF16 rows) and a "
+                         "256 MiB flush per step",
             "parallelism": f"replicas x{world}",
             "setup_s": round(setup_s, 1),
         },
         "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s",
-                "h2d_bytes_per_step": nq * D * 4, "d2h_bytes_per_step": nq * k * 12},
+                "h2d_bytes_per_step": nq * dim * 4, "d2h_bytes_per_step": nq * k * 12},
         "gpu_launches": int(launches),
         "roofline": {
             "bound": "tensor",
@@ -572,7 +573,7 @@ def run_flat(args, rank, world):
 
         sample = min(args.cpu_sample // 10, nq)
         threads = os.cpu_count() or 1
-        ref = orc.SQ8(D, metric)
+        ref = orc.SQ8(dim, metric)
         ref.add(base)
         ref.search(queries[:2], k, nthreads=threads)
         t0 = time.perf_counter()
@@ -1010,10 +1011,10 @@ def run_serve(args, rank, world):
             "workload": f"serve_ivfpq1M_sq8_2Mx768_flat500kx256_req{nreq}_scale{s}",
             "arrivals": "Poisson; batch size log-uniform on [1, 1024]; collection uniform; k in {10, 100}",
             "server": f"4 lanes, HBM budget {args.serve_budget_gb} GB, batches up to 4096 queries",
-            "forms": {"plain": "IVF-PQ plain nprobe 8; SQ8 integer scan + FP32 rerank of 2k; "
-                               "Flat exact FP32 (certified tensor-core shortlist)",
-                      "fast": "IVF-PQ fast nprobe 8 rerank 256; SQ8 integer scan + FP32 rerank of "
-                              "2k (d = 768 is above the tensor path's 256); Flat BF16 + FP32 "
+            "forms": {"plain": "IVF-PQ plain nprobe 8; SQ8 integer keys from the tensor cores "
+                               "(exact for s8 codes at d <= 1040) + FP32 rerank of 2k; Flat exact "
+                               "FP32 (certified tensor-core shortlist)",
+                      "fast": "IVF-PQ fast nprobe 8 rerank 256; SQ8 as plain; Flat BF16 + FP32 "
                               "rerank of max(k, 40)"},
             "results": results,
             "setup_s": round(setup_s, 1),
@@ -1096,12 +1097,12 @@ def run_reference_flat(args):
     from oracle import oracle as orc
 
     threads = os.cpu_count() or 1
-    base, queries = build_workload(args.nb, args.nq)
+    base, queries = build_workload(args.nb, args.nq, args.dim)
     metric = 0 if args.metric == "l2" else 1
     sample = min(max(args.cpu_sample // 10, 1), args.nq)
     q = queries[:sample]
     if args.workload == "sq8":
-        ref = orc.SQ8(D, metric)
+        ref = orc.SQ8(args.dim, metric)
         ref.add(base)
         run = lambda qq: ref.search(qq, args.k, nthreads=threads)  # noqa: E731
     else:
@@ -1120,7 +1121,7 @@ def run_reference_flat(args):
         "ms_per_step": round(1e3 * total / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic SIFT-like (seeded Gaussian mixture, integer-valued), not SIFT1M",
-        "config": {"workload": f"{args.workload}_{args.nb}x128_{args.metric}_nq{args.nq}_k{args.k}",
+        "config": {"workload": f"{args.workload}_{args.nb}x{args.dim}_{args.metric}_nq{args.nq}_k{args.k}",
                    "form": "reference CPU path (oracle port)"},
         "cpu_baseline": {"value": round(qps, 1), "unit": "queries/s", "cores": threads,
                          "kind": "port",
@@ -1150,7 +1151,7 @@ def main():
     ap.add_argument("--batch-nb", type=int, default=10_000_000)
     ap.add_argument("--serve-scale", type=float, default=1.0)
     ap.add_argument("--serve-requests", type=int, default=300)
-    ap.add_argument("--serve-rates", type=float, nargs="+", default=[20.0, 80.0, 320.0, 1280.0])
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[20.0, 80.0, 320.0, 1280.0, 5120.0])
     ap.add_argument("--serve-budget-gb", type=int, default=24)
     ap.add_argument("--batch-nq", type=int, default=20_000)
     ap.add_argument("--km-n", type=int, default=1_000_000)
@@ -1159,6 +1160,7 @@ def main():
     ap.add_argument("--rerank-factor", type=int, default=2, help="sq8 workload: shortlist k * factor")
     ap.add_argument("--k", type=int, default=K, help="flat workload: results per query")
     ap.add_argument("--metric", default="l2", choices=["l2", "ip"], help="flat workload metric")
+    ap.add_argument("--dim", type=int, default=D, help="flat/sq8 workloads: row length")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.rerank is None:

@@ -69,12 +69,18 @@ typedef struct mv_search_params {
   int32_t lut_fp16;    /* fast form: 1 = FP16 lookup tables */
   int32_t coarse_path; /* fast form, BF16 coarse step: 0 = automatic, 1 = GEMM with a
                           per-row top-k epilogue, 2 = distance matrix then one warp
-                          per query selecting its lists */
+                          per query selecting its lists, 3 = two-pass GEMM (bucket
+                          threshold, then per-row lists; nprobe + margin <= 32 and
+                          d <= 256). All keep the same lists; automatic takes 3
+                          where it applies, else 2 */
   int32_t plain_scan;  /* plain form, Flat and SQ8: 1 = the exact SIMT scan alone, without
                           the tensor-core shortlist that is proven (Flat) or exact by
                           construction (SQ8) to give the same results */
   int32_t flat_e4m3;   /* fast form, Flat: 1 = shortlist from an E4M3 (FP8) GEMM with
                           per-row scales instead of BF16 (exact FP32 rerank either way) */
+  int32_t rerank_fp32; /* fast form, IVF-PQ: 1 = every shortlisted row reranked from its FP32
+                          copy; 0 (default) = a certified BF16 prescreen first, which
+                          provably leaves the results unchanged */
 } mv_search_params;
 
 /* ---- library / context ---------------------------------------------- */

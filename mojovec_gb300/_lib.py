@@ -61,6 +61,7 @@ class SearchParams(C.Structure):
         ("coarse_path", C.c_int32),
         ("plain_scan", C.c_int32),
         ("flat_e4m3", C.c_int32),
+        ("rerank_fp32", C.c_int32),
     ]
 
 

@@ -235,6 +235,70 @@ __device__ __forceinline__ void warp_bitonic_sort(uint64_t* a, int n) {
     }
 }
 
+// B[0..nc): a query's nc smallest approximate (distance, list) keys, sorted
+// (KEY_NONE where the row has fewer). Their exact FP32 distances (as
+// k_coarse_from_keys) are sorted and the nprobe smallest written.
+__device__ void coarse_recheck_warp(uint64_t* B, int64_t row, const float* __restrict__ q, int d,
+                                    const float* __restrict__ cent, int nlist, int metric, int nc,
+                                    int nprobe, int32_t* __restrict__ probes,
+                                    float* __restrict__ term, int* __restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  const float* qr = q + row * d;
+  const int ncp = next_pow2(nc);
+  // CU candidates per round, so their row loads overlap; each distance is
+  // computed exactly as in k_coarse_from_keys (lane-strided FMAs, xor tree).
+  constexpr int CU = 8;
+  for (int c0 = 0; c0 < ncp; c0 += CU) {
+    uint32_t list[CU];
+    bool ok[CU];
+    float acc[CU];
+#pragma unroll
+    for (int u = 0; u < CU; ++u) {
+      const int c = c0 + u;
+      const uint64_t key = c < nc ? B[c] : KEY_NONE;
+      list[u] = key_id(key);
+      ok[u] = key != KEY_NONE && list[u] < (uint32_t)nlist;
+      if (key != KEY_NONE && !ok[u] && lane == 0) atomicExch(err, 106);
+      acc[u] = 0.0f;
+    }
+    for (int j = lane; j < d; j += 32) {
+      const float qj = qr[j];
+#pragma unroll
+      for (int u = 0; u < CU; ++u) {
+        if (!ok[u]) continue;
+        const float v = cent[(int64_t)list[u] * d + j];
+        if (metric == MV_METRIC_L2) {
+          const float df = qj - v;
+          acc[u] = fmaf(df, df, acc[u]);
+        } else {
+          acc[u] = fmaf(qj, v, acc[u]);
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < CU; ++u)
+      for (int o = 16; o > 0; o >>= 1) acc[u] += __shfl_xor_sync(0xffffffffu, acc[u], o);
+    __syncwarp();
+    if (lane == 0) {
+#pragma unroll
+      for (int u = 0; u < CU; ++u) {
+        const int c = c0 + u;
+        if (c < ncp)
+          B[c] = ok[u] ? make_key(metric == MV_METRIC_L2 ? acc[u] : -acc[u], list[u])
+                       : KEY_NONE - (uint64_t)c;
+      }
+    }
+    __syncwarp();
+  }
+  warp_bitonic_sort(B, ncp);
+  for (int p = lane; p < nprobe; p += 32) {
+    const uint64_t key = B[p];
+    const bool ok = key < KEY_NONE - (uint64_t)ncp;
+    probes[row * nprobe + p] = ok ? (int32_t)key_id(key) : -1;
+    term[row * nprobe + p] = ok ? key_dist(key) : 0.0f;
+  }
+}
+
 __global__ void __launch_bounds__(CR_WARPS * 32)
     k_coarse_rows(const float* __restrict__ approx, int64_t nq, int nlist, const float* __restrict__ q,
                   int d, const float* __restrict__ cent, int metric, int nc, int nprobe,
@@ -299,41 +363,124 @@ __global__ void __launch_bounds__(CR_WARPS * 32)
   for (int i = cnt + lane; i < np2; i += 32) B[i] = KEY_NONE;
   __syncwarp();
   warp_bitonic_sort(B, np2);
-  // 3. exact FP32 distances of the nc smallest (as k_coarse_from_keys)
-  const float* qr = q + row * d;
-  const int ncp = next_pow2(nc);
-  for (int c = 0; c < ncp; ++c) {
-    uint64_t out = KEY_NONE - (uint64_t)c;
-    if (c < nc) {
-      const uint32_t list = key_id(B[c]);
-      if (list < (uint32_t)nlist) {
-        const float* cp = cent + (int64_t)list * d;
-        float acc = 0.0f;
-        for (int j = lane; j < d; j += 32) {
-          if (metric == MV_METRIC_L2) {
-            const float df = qr[j] - cp[j];
-            acc = fmaf(df, df, acc);
-          } else {
-            acc = fmaf(qr[j], cp[j], acc);
-          }
+  coarse_recheck_warp(B, row, q, d, cent, nlist, metric, nc, nprobe, probes, term, err);
+}
+
+// Ascending bitonic sort of the warp's 32 * RR keys held in registers,
+// element r * 32 + lane in v[r] of that lane: cross-lane steps by xor
+// shuffles, in-lane steps between registers (all indices static).
+template <int RR>
+__device__ __forceinline__ void warp_sort_regs(uint64_t (&v)[RR]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 2; k <= 32 * RR; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j >= 32) {
+        const int jr = j >> 5;
+#pragma unroll
+        for (int r = 0; r < RR; ++r) {
+          if (r & jr) continue;
+          const int r2 = r | jr;
+          const bool up = (((r << 5) | lane) & k) == 0;
+          const uint64_t a = v[r], b = v[r2];
+          const bool sw = (a > b) == up;
+          v[r] = sw ? b : a;
+          v[r2] = sw ? a : b;
         }
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        out = make_key(metric == MV_METRIC_L2 ? acc : -acc, list);
-      } else if (lane == 0) {
-        atomicExch(err, 106);
+      } else {
+        const bool low = (lane & j) == 0;
+#pragma unroll
+        for (int r = 0; r < RR; ++r) {
+          const bool up = (((r << 5) | lane) & k) == 0;
+          const uint64_t a = v[r];
+          const uint64_t b = __shfl_xor_sync(0xffffffffu, a, j);
+          const bool keep_min = low == up;
+          v[r] = keep_min ? (a < b ? a : b) : (a < b ? b : a);
+        }
       }
     }
-    __syncwarp();
-    if (lane == 0) B[c] = out;
-    __syncwarp();
   }
-  warp_bitonic_sort(B, ncp);
-  for (int p = lane; p < nprobe; p += 32) {
-    const uint64_t key = B[p];
-    const bool ok = key < KEY_NONE - (uint64_t)ncp;
-    probes[row * nprobe + p] = ok ? (int32_t)key_id(key) : -1;
-    term[row * nprobe + p] = ok ? key_dist(key) : 0.0f;
+}
+
+// Sorts a bitonic sequence of 32 keys (one per lane) ascending.
+__device__ __forceinline__ uint64_t warp_bitonic_merge32(uint64_t a) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 16; j > 0; j >>= 1) {
+    const uint64_t b = __shfl_xor_sync(0xffffffffu, a, j);
+    const bool low = (lane & j) == 0;
+    a = low ? (a < b ? a : b) : (a < b ? b : a);
   }
+  return a;
+}
+
+// best (ascending across lanes) <- the 32 smallest of best and v (any order).
+__device__ __forceinline__ uint64_t warp_merge_smallest32(uint64_t best, uint64_t v) {
+  const int lane = threadIdx.x & 31;
+  uint64_t t[1] = {v};
+  warp_sort_regs<1>(t);
+  const uint64_t r = __shfl_sync(0xffffffffu, t[0], 31 - lane);
+  return warp_bitonic_merge32(best < r ? best : r);
+}
+
+// The row's candidate keys (segment lists concatenated) sorted in registers;
+// the nc <= 32 smallest end up in v[0] of lanes 0 .. nc - 1.
+template <int RR>
+__device__ __forceinline__ uint64_t coarse_lists_smallest(const uint64_t* __restrict__ lists,
+                                                          int64_t row, int nseg, int cap, int n,
+                                                          int o1, int o2, int o3) {
+  const int lane = threadIdx.x & 31;
+  uint64_t v[RR];
+#pragma unroll
+  for (int r = 0; r < RR; ++r) {
+    const int i = (r << 5) | lane;
+    uint64_t key = KEY_NONE;
+    if (i < n) {
+      const int sg = (i >= o1) + (i >= o2) + (i >= o3);
+      const int base = sg == 0 ? 0 : sg == 1 ? o1 : sg == 2 ? o2 : o3;
+      key = lists[((int64_t)row * nseg + sg) * cap + (i - base)];
+    }
+    v[r] = key;
+  }
+  warp_sort_regs<RR>(v);
+  return v[0];
+}
+
+// Per-row lists of the two-pass coarse GEMM -> the nc smallest keys, their
+// exact FP32 distances and the nprobe nearest lists, one warp per query (the
+// same selection and recheck as k_coarse_rows; nseg <= 4, nseg * cap <= 256,
+// nc <= 32).
+__global__ void __launch_bounds__(CR_WARPS * 32)
+    k_coarse_lists(const uint64_t* __restrict__ lists, const int* __restrict__ counts, int nseg,
+                   int cap, int64_t nq, int nlist, const float* __restrict__ q, int d,
+                   const float* __restrict__ cent, int metric, int nc, int nprobe,
+                   int32_t* __restrict__ probes, float* __restrict__ term, int* __restrict__ err) {
+  __shared__ uint64_t bufs[CR_WARPS][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * CR_WARPS + warp;
+  if (row >= nq) return;  // warps are independent: no block-wide barrier below
+  const int c = lane < nseg ? min(max(counts[row * nseg + lane], 0), cap) : 0;
+  int incl = c;  // inclusive prefix over the (at most 4) segments
+#pragma unroll
+  for (int o = 1; o < 4; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int o1 = __shfl_sync(0xffffffffu, incl, 0);
+  const int o2 = nseg > 1 ? __shfl_sync(0xffffffffu, incl, 1) : 1 << 30;
+  const int o3 = nseg > 2 ? __shfl_sync(0xffffffffu, incl, 2) : 1 << 30;
+  const int n = __shfl_sync(0xffffffffu, incl, nseg - 1);
+  const int p1 = nseg > 1 ? o1 : 1 << 30;
+  uint64_t best;
+  if (n <= 32) best = coarse_lists_smallest<1>(lists, row, nseg, cap, n, p1, o2, o3);
+  else if (n <= 64) best = coarse_lists_smallest<2>(lists, row, nseg, cap, n, p1, o2, o3);
+  else if (n <= 128) best = coarse_lists_smallest<4>(lists, row, nseg, cap, n, p1, o2, o3);
+  else best = coarse_lists_smallest<8>(lists, row, nseg, cap, n, p1, o2, o3);
+  uint64_t* B = bufs[warp];
+  B[lane] = best;
+  __syncwarp();
+  coarse_recheck_warp(B, row, q, d, cent, nlist, metric, nc, nprobe, probes, term, err);
 }
 
 // Per-query table lut[m][k] = scale * <q_m, C[m][k]>: warp w builds
@@ -598,101 +745,375 @@ __global__ void __launch_bounds__(NT) k_ivfpq_scan_fast(FastScanArgs a) {
   }  // queries
 }
 
-// Exact FP32 rerank of the shortlist against the raw rows (CSR order), one
-// CTA per query: a warp per candidate row (float4 loads), radix select of
-// the k smallest (distance, id), sorted.
-__global__ void __launch_bounds__(FT) k_rerank_fast(RerankArgs a) {
-  extern __shared__ __align__(16) unsigned char smraw[];
+// FP32 distances of U shortlisted rows (positions pos, 0xffffffff = none)
+// to the query qv, accumulated per lane in acc: float4 loads of the lane's
+// 4-element slices (scalar elements when d is not a multiple of 4). The
+// warp's sum of acc (xor tree) is the distance; every exact rerank path
+// uses this arithmetic.
+template <int U>
+__device__ __forceinline__ void rerank_rows_fp32(const RerankArgs& a, const float* qv,
+                                                 const uint32_t* pos, float* acc) {
   const int d = a.d;
-  float* qv = reinterpret_cast<float*>(smraw);
-  uint64_t* ck = reinterpret_cast<uint64_t*>(smraw + (((size_t)d * 4 + 15) & ~size_t(15)));
-  uint64_t* outb = ck + a.R;  // kp (power of two >= k)
-  __shared__ RadixScratch rs;
-  const int64_t row = blockIdx.x;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int j = threadIdx.x; j < d; j += FT) qv[j] = a.q[row * d + j];
-  __syncthreads();
-  const uint64_t* cand = a.cand + row * a.R;
-  // Each warp takes U candidates at a time and issues all of their row loads
-  // before reducing, so U rows per warp are in flight.
-  constexpr int U = 4;
-  for (int c0 = warp * U; c0 < a.R; c0 += (FT / 32) * U) {
-    uint32_t pos[U];
-    float acc[U];
+  const int lane = threadIdx.x & 31;
+  if ((d & 3) == 0) {
+    for (int j = lane * 4; j < d; j += 128) {
+      float4 v[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int c = c0 + u;
-      const uint64_t key = c < a.R ? cand[c] : KEY_NONE;
-      pos[u] = key == KEY_NONE ? 0xffffffffu : key_id(key);
-      if (pos[u] != 0xffffffffu && (int64_t)pos[u] >= a.ntotal) {
-        atomicExch(a.err, 105);
-        pos[u] = 0xffffffffu;
-      }
-      acc[u] = 0.0f;
-    }
-    if ((d & 3) == 0) {
-      for (int j = lane * 4; j < d; j += 128) {
-        float4 v[U];
+      for (int u = 0; u < U; ++u)
+        v[u] = pos[u] != 0xffffffffu ? *reinterpret_cast<const float4*>(a.raw + (int64_t)pos[u] * d + j)
+                                     : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float q0 = qv[j], q1 = qv[j + 1], q2 = qv[j + 2], q3 = qv[j + 3];
 #pragma unroll
-        for (int u = 0; u < U; ++u)
-          v[u] = pos[u] != 0xffffffffu
-                     ? *reinterpret_cast<const float4*>(a.raw + (int64_t)pos[u] * d + j)
-                     : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float q0 = qv[j], q1 = qv[j + 1], q2 = qv[j + 2], q3 = qv[j + 3];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          if (a.metric == MV_METRIC_L2) {
-            const float d0 = q0 - v[u].x, d1 = q1 - v[u].y, d2 = q2 - v[u].z, d3 = q3 - v[u].w;
-            acc[u] = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, acc[u]))));
-          } else {
-            acc[u] = fmaf(q0, v[u].x, fmaf(q1, v[u].y, fmaf(q2, v[u].z, fmaf(q3, v[u].w, acc[u]))));
-          }
-        }
-      }
-    } else {
-      for (int j = lane; j < d; j += 32) {
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          if (pos[u] == 0xffffffffu) continue;
-          const float x = a.raw[(int64_t)pos[u] * d + j];
-          if (a.metric == MV_METRIC_L2) {
-            const float df = qv[j] - x;
-            acc[u] = fmaf(df, df, acc[u]);
-          } else {
-            acc[u] = fmaf(qv[j], x, acc[u]);
-          }
+      for (int u = 0; u < U; ++u) {
+        if (a.metric == MV_METRIC_L2) {
+          const float d0 = q0 - v[u].x, d1 = q1 - v[u].y, d2 = q2 - v[u].z, d3 = q3 - v[u].w;
+          acc[u] = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, acc[u]))));
+        } else {
+          acc[u] = fmaf(q0, v[u].x, fmaf(q1, v[u].y, fmaf(q2, v[u].z, fmaf(q3, v[u].w, acc[u]))));
         }
       }
     }
+  } else {
+    for (int j = lane; j < d; j += 32) {
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      float t = acc[u];
-      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-      const int c = c0 + u;
-      if (lane == 0 && c < a.R) {
-        ck[c] = pos[u] == 0xffffffffu
-                    ? KEY_NONE - (uint64_t)c  // distinct keys for empty slots
-                    : make_key(a.metric == MV_METRIC_L2 ? t : -t, a.ids ? a.ids[pos[u]] : pos[u]);
+      for (int u = 0; u < U; ++u) {
+        if (pos[u] == 0xffffffffu) continue;
+        const float x = a.raw[(int64_t)pos[u] * d + j];
+        if (a.metric == MV_METRIC_L2) {
+          const float df = qv[j] - x;
+          acc[u] = fmaf(df, df, acc[u]);
+        } else {
+          acc[u] = fmaf(qv[j], x, acc[u]);
+        }
       }
     }
   }
-  __syncthreads();
-  const int r = block_radix_select<FT>(ck, a.R, a.k, outb, rs);
-  for (int j = r + threadIdx.x; j < a.kp; j += FT) outb[j] = KEY_NONE;
-  __syncthreads();
-  block_bitonic_sort(outb, a.kp);
+}
+
+// Results of one query from its k smallest keys outb[0, k) (sorted;
+// padding keys above KEY_NONE - R become unfilled slots).
+__device__ __forceinline__ void rerank_write(const RerankArgs& a, int64_t row, const uint64_t* outb,
+                                             int t0, int nt) {
   const int kq = a.k_q ? min(max(a.k_q[row], 0), a.k) : a.k;
-  for (int i = threadIdx.x; i < a.k; i += FT) {
+  for (int i = t0; i < a.k; i += nt) {
     const uint64_t key = outb[i];
     float dd = a.fill_d;
     int64_t ll = -1;
-    if (i < kq && key < KEY_NONE - (uint64_t)a.R) {  // padding keys are the top R values
+    if (i < kq && key < KEY_NONE - (uint64_t)a.R) {
       dd = key_dist(key);
       if (a.metric != MV_METRIC_L2) dd = -dd;
       ll = (int64_t)key_id(key);
     }
     a.out_d[row * a.k + i] = dd;
     a.out_l[row * a.k + i] = ll;
+  }
+}
+
+// Exact FP32 rerank of the shortlist against the raw rows (CSR order), one
+// CTA per query: a warp per candidate row (float4 loads, U rows in flight per
+// warp; keys and ids of a warp's 32 candidates loaded once, a lane each),
+// then the k smallest (distance, id) keys, sorted.
+__global__ void __launch_bounds__(FT) k_rerank_fast(RerankArgs a) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int d = a.d;
+  float* qv = reinterpret_cast<float*>(smraw);
+  uint64_t* ck = reinterpret_cast<uint64_t*>(smraw + (((size_t)d * 4 + 15) & ~size_t(15)));
+  uint64_t* outb = ck + a.R;     // kp (power of two >= k)
+  uint64_t* part = outb + a.kp;  // FT keys (k <= 32 selection)
+  __shared__ RadixScratch rs;
+  const int64_t row = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int j = threadIdx.x; j < d; j += FT) qv[j] = a.q[row * d + j];
+  __syncthreads();
+  const uint64_t* cand = a.cand + row * a.R;
+  constexpr int U = 8;
+  for (int c0 = warp * 32; c0 < a.R; c0 += FT) {
+    uint32_t mpos = 0xffffffffu, mid = 0;
+    if (c0 + lane < a.R) {
+      const uint64_t key = cand[c0 + lane];
+      if (key != KEY_NONE) {
+        mpos = key_id(key);
+        if ((int64_t)mpos >= a.ntotal) {
+          atomicExch(a.err, 105);
+          mpos = 0xffffffffu;
+        } else {
+          mid = a.ids ? a.ids[mpos] : mpos;
+        }
+      }
+    }
+    const int nloc = min(32, a.R - c0);
+    for (int u0 = 0; u0 < nloc; u0 += U) {
+      uint32_t pos[U];
+      float acc[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const uint32_t p = __shfl_sync(0xffffffffu, mpos, (u0 + u) & 31);
+        pos[u] = u0 + u < nloc ? p : 0xffffffffu;
+        acc[u] = 0.0f;
+      }
+      rerank_rows_fp32<U>(a, qv, pos, acc);
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        float t = acc[u];
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        const uint32_t id = __shfl_sync(0xffffffffu, mid, (u0 + u) & 31);
+        const int c = c0 + u0 + u;
+        if (lane == 0 && u0 + u < nloc) {
+          ck[c] = pos[u] == 0xffffffffu
+                      ? KEY_NONE - (uint64_t)c  // distinct keys for empty slots
+                      : make_key(a.metric == MV_METRIC_L2 ? t : -t, id);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (a.k <= 32) {
+    // The k smallest keys: every warp keeps the 32 smallest of its share in
+    // registers, warp 0 merges the warps' sets (keys are distinct, so this
+    // is the same set as a radix select).
+    uint64_t best = KEY_NONE;
+    for (int c0 = warp * 32; c0 < a.R; c0 += FT)
+      best = warp_merge_smallest32(best, c0 + lane < a.R ? ck[c0 + lane] : KEY_NONE);
+    part[warp * 32 + lane] = best;
+    __syncthreads();
+    if (warp == 0) {
+      best = part[lane];
+      for (int w = 1; w < FT / 32; ++w) best = warp_merge_smallest32(best, part[w * 32 + lane]);
+      if (lane < a.kp) outb[lane] = best;
+    }
+    __syncthreads();
+  } else {
+    const int r = block_radix_select<FT>(ck, a.R, a.k, outb, rs);
+    for (int j = r + threadIdx.x; j < a.kp; j += FT) outb[j] = KEY_NONE;
+    __syncthreads();
+    block_bitonic_sort(outb, a.kp);
+  }
+  rerank_write(a, row, outb, threadIdx.x, FT);
+}
+
+// Certified rerank (k <= 32), one warp per query. Every shortlisted row's
+// distance is first computed from its BF16 copy (half the bytes; 32 rows
+// per warp in flight, lane-owned partial sums reduced by a transposing
+// butterfly) and turned into an interval that provably holds the FP32
+// distance the exact pass computes: the BF16 value's own summation error,
+// the triangle inequality with the row's rounding radius r >=
+// ||y - bf16(y)|| (L2), or Cauchy-Schwarz with ||q|| and ||bf16(y)|| (IP),
+// and the exact pass's summation error (both bounded by
+// gamma = (d + 64) * 2^-24 relative to the sum of |terms|), with 2^-20 of
+// slack for the bound arithmetic. The k-th smallest upper end of any group
+// of candidates bounds the query's k-th smallest key; a candidate whose
+// lower end exceeds it has k candidates strictly closer and is dropped. The
+// survivors are computed in FP32 with k_rerank_fast's arithmetic, so the
+// results are the ones the full FP32 pass gives.
+constexpr int RC_WARPS = 8;
+__global__ void __launch_bounds__(RC_WARPS * 32, 2) k_rerank_cert(RerankArgs a) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int d = a.d;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * RC_WARPS + warp;
+  if (row >= a.nq) return;  // warps are independent: no block-wide barrier below
+  const size_t qbytes = ((size_t)d * 4 + 15) & ~size_t(15);
+  unsigned char* base = smraw + (size_t)warp * (qbytes + (size_t)a.R * 24);
+  float* qv = reinterpret_cast<float*>(base);
+  uint64_t* sk = reinterpret_cast<uint64_t*>(base + qbytes);  // R: survivors' keys
+  float* blo = reinterpret_cast<float*>(sk + a.R);             // R lower ends
+  uint32_t* spos = reinterpret_cast<uint32_t*>(blo + a.R);     // R positions
+  uint32_t* sid = spos + a.R;                                  // R ids
+  int* slist = reinterpret_cast<int*>(sid + a.R);              // R survivors
+  const float INF = __int_as_float(0x7f800000);
+  const float gam = (float)(d + 64) * 5.9604645e-08f;  // (d + 64) * 2^-24
+  const float up = 1.0f + 9.5367432e-07f, dn = 1.0f - 9.5367432e-07f;  // 1 +- 2^-20
+  for (int j = lane; j < d; j += 32) qv[j] = a.q[row * d + j];
+  __syncwarp();
+  float qn = 0.0f;  // IP: upper bound on ||q||
+  if (a.metric != MV_METRIC_L2) {
+    for (int j = lane; j < d; j += 32) qn = fmaf(qv[j], qv[j], qn);
+    for (int o = 16; o > 0; o >>= 1) qn += __shfl_xor_sync(0xffffffffu, qn, o);
+    qn = sqrtf(qn * (1.0f + 2.0f * gam)) * up;
+  }
+  const uint64_t* cand = a.cand + row * a.R;
+  uint32_t hk = 0xffffffffu;  // ordered bits of the smallest group bound so far
+  for (int c0 = 0; c0 < a.R; c0 += 32) {
+    const int c = c0 + lane;
+    uint32_t mpos = 0xffffffffu, mid = 0;
+    if (c < a.R) {
+      const uint64_t key = cand[c];
+      if (key != KEY_NONE) {
+        mpos = key_id(key);
+        if ((int64_t)mpos >= a.ntotal) {
+          atomicExch(a.err, 105);
+          mpos = 0xffffffffu;
+        }
+      }
+    }
+    float mrad = 0.0f, mn16 = 0.0f;
+    if (mpos != 0xffffffffu) {
+      mid = a.ids ? a.ids[mpos] : mpos;
+      mrad = a.rad[mpos];
+      if (a.metric != MV_METRIC_L2) mn16 = a.n16[mpos];
+    }
+    float acc[32];
+#pragma unroll
+    for (int u = 0; u < 32; ++u) acc[u] = 0.0f;
+    if ((d & 3) == 0) {
+      for (int j0 = 0; j0 < d; j0 += 128) {
+        const int j = j0 + lane * 4;
+        const bool jin = j < d;
+        uint2 v[32];
+#pragma unroll
+        for (int u = 0; u < 32; ++u) {
+          const uint32_t p = __shfl_sync(0xffffffffu, mpos, u);
+          v[u] = jin && p != 0xffffffffu ? *reinterpret_cast<const uint2*>(a.raw16 + (int64_t)p * d + j)
+                                         : make_uint2(0u, 0u);
+        }
+        const float q0 = jin ? qv[j] : 0.0f, q1 = jin ? qv[j + 1] : 0.0f;
+        const float q2 = jin ? qv[j + 2] : 0.0f, q3 = jin ? qv[j + 3] : 0.0f;
+#pragma unroll
+        for (int u = 0; u < 32; ++u) {
+          const float y0 = __uint_as_float(v[u].x << 16), y1 = __uint_as_float(v[u].x & 0xffff0000u);
+          const float y2 = __uint_as_float(v[u].y << 16), y3 = __uint_as_float(v[u].y & 0xffff0000u);
+          if (a.metric == MV_METRIC_L2) {
+            const float d0 = jin ? q0 - y0 : 0.0f, d1 = jin ? q1 - y1 : 0.0f;
+            const float d2 = jin ? q2 - y2 : 0.0f, d3 = jin ? q3 - y3 : 0.0f;
+            acc[u] = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, acc[u]))));
+          } else {
+            acc[u] = fmaf(q0, y0, fmaf(q1, y1, fmaf(q2, y2, fmaf(q3, y3, acc[u]))));
+          }
+        }
+      }
+    } else {
+      for (int j0 = 0; j0 < d; j0 += 32) {  // every lane runs the same trips
+        const int j = j0 + lane;
+        const bool jin = j < d;
+        const float qj = jin ? qv[j] : 0.0f;
+#pragma unroll
+        for (int u = 0; u < 32; ++u) {
+          const uint32_t p = __shfl_sync(0xffffffffu, mpos, u);
+          const float y = jin && p != 0xffffffffu ? __bfloat162float(a.raw16[(int64_t)p * d + j]) : 0.0f;
+          if (a.metric == MV_METRIC_L2) {
+            const float df = jin ? qj - y : 0.0f;
+            acc[u] = fmaf(df, df, acc[u]);
+          } else {
+            acc[u] = fmaf(qj, y, acc[u]);
+          }
+        }
+      }
+    }
+    // transposing butterfly: lane l ends with candidate l's sum
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+      const bool upper = (lane & w) != 0;
+#pragma unroll
+      for (int i = 0; i < w; ++i) {
+        const float send = upper ? acc[i] : acc[i + w];
+        const float keep = upper ? acc[i + w] : acc[i];
+        acc[i] = keep + __shfl_xor_sync(0xffffffffu, send, w);
+      }
+    }
+    float lo = INF, hi = INF;  // empty slots never survive
+    if (mpos != 0xffffffffu) {
+      const float t = acc[0];
+      const float r = mrad, yn = mn16;
+      if (!(fabsf(t) < INF)) {  // not finite: always computed exactly
+        lo = -INF;
+        hi = INF;
+      } else if (a.metric == MV_METRIC_L2) {
+        const float slo = sqrtf(t * (1.0f - 2.0f * gam)) * dn - r * up;
+        const float shi = sqrtf(t * (1.0f + 2.0f * gam)) * up + r * up;
+        const float m = fmaxf(slo, 0.0f);
+        lo = m * m * (1.0f - 2.0f * gam) * dn;
+        hi = shi * shi * (1.0f + 2.0f * gam) * up;
+      } else {
+        const float e = qn * (gam * yn + r + gam * (yn + r)) * up;
+        lo = (-t - e) * (-t - e < 0.0f ? up : dn);
+        hi = (-t + e) * (-t + e < 0.0f ? dn : up);
+      }
+    }
+    if (c < a.R) {
+      blo[c] = lo;
+      spos[c] = mpos;
+      sid[c] = mid;
+    }
+    uint64_t hv[1] = {c < a.R ? ((uint64_t)float_to_ordered(hi) << 32) | (uint32_t)lane : KEY_NONE};
+    warp_sort_regs<1>(hv);
+    const uint64_t kth = __shfl_sync(0xffffffffu, hv[0], a.k - 1);
+    if (kth != KEY_NONE) hk = min(hk, (uint32_t)(kth >> 32));
+  }
+  __syncwarp();
+  const float hkf = hk == 0xffffffffu ? INF : ordered_to_float(hk);
+  int ns = 0;
+  for (int c0 = 0; c0 < a.R; c0 += 32) {
+    const int c = c0 + lane;
+    const bool keep = c < a.R && blo[c] <= hkf;
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (keep) slist[ns + __popc(m & ((1u << lane) - 1u))] = c;
+    ns += __popc(m);
+  }
+  __syncwarp();
+  // exact FP32 keys of the survivors (k_rerank_fast's arithmetic)
+  constexpr int U = 8;
+  for (int i0 = 0; i0 < ns; i0 += U) {
+    uint32_t pos[U];
+    float acc[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      pos[u] = i0 + u < ns ? spos[slist[i0 + u]] : 0xffffffffu;
+      acc[u] = 0.0f;
+    }
+    rerank_rows_fp32<U>(a, qv, pos, acc);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      float t = acc[u];
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (lane == 0 && i0 + u < ns) {
+        const int c = slist[i0 + u];
+        sk[i0 + u] = pos[u] == 0xffffffffu ? KEY_NONE - (uint64_t)c
+                                           : make_key(a.metric == MV_METRIC_L2 ? t : -t, sid[c]);
+      }
+    }
+  }
+  __syncwarp();
+  // the k smallest keys are the survivors' smallest (every other key is
+  // padding, above all real keys)
+  uint64_t best = KEY_NONE;
+  for (int i0 = 0; i0 < ns; i0 += 32)
+    best = warp_merge_smallest32(best, i0 + lane < ns ? sk[i0 + lane] : KEY_NONE);
+  uint64_t* outb = sk;  // reuse: 32 sorted keys
+  __syncwarp();
+  outb[lane] = best;
+  __syncwarp();
+  rerank_write(a, row, outb, lane, 32);
+}
+
+// BF16 copy of each row, an upper bound on ||y - bf16(y)|| and on
+// ||bf16(y)||, one warp per row. The squared sums carry a relative error of
+// at most (d + 2) 2^-24 (non-negative terms), covered by the (d + 64) 2^-23
+// inflation, and 2^-21 more covers the square root.
+__global__ void k_rerank_rows(const float* __restrict__ raw, int64_t n, int d,
+                              __nv_bfloat16* __restrict__ raw16, float* __restrict__ rad,
+                              float* __restrict__ n16) {
+  const int lane = threadIdx.x & 31;
+  const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= n) return;
+  float e2 = 0.0f, y2 = 0.0f;
+  for (int j = lane; j < d; j += 32) {
+    const float y = raw[r * d + j];
+    const __nv_bfloat16 b = __float2bfloat16_rn(y);
+    const float yb = __bfloat162float(b);
+    raw16[r * d + j] = b;
+    const float df = y - yb;  // exact
+    e2 = fmaf(df, df, e2);
+    y2 = fmaf(yb, yb, y2);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+    y2 += __shfl_xor_sync(0xffffffffu, y2, o);
+  }
+  if (lane == 0) {
+    const float infl = 1.0f + (float)(d + 64) * 1.1920929e-07f;
+    const float up = 1.0f + 4.7683716e-07f;  // 1 + 2^-21
+    rad[r] = sqrtf(e2 * infl) * up;
+    n16[r] = sqrtf(y2 * infl) * up;
   }
 }
 
@@ -756,6 +1177,20 @@ void launch_coarse_rows(const float* approx, int64_t nq, int nlist, const float*
   MV_CHECK_CUDA(cudaGetLastError());
 }
 
+void launch_coarse_lists(const uint64_t* lists, const int* counts, int nseg, int cap, int64_t nq,
+                         int nlist, const float* q, int d, const float* cent, int metric, int nc,
+                         int nprobe, int32_t* probes, float* term, int* err, cudaStream_t s) {
+  if (nq == 0) return;
+  MV_REQUIRE(nc >= 1 && nc <= 64 && nc <= nlist && nprobe <= nc, MV_ERR_UNSUPPORTED,
+             "coarse lists: nc must be in [nprobe, min(64, nlist)]");
+  MV_REQUIRE((int64_t)nseg * cap <= CR_CAP && nseg <= 4 && nc <= 32, MV_ERR_INTERNAL,
+             "coarse lists: too many keys per row");
+  k_coarse_lists<<<(unsigned)((nq + CR_WARPS - 1) / CR_WARPS), CR_WARPS * 32, 0, s>>>(
+      lists, counts, nseg, cap, nq, nlist, q, d, cent, metric, nc, nprobe, probes, term, err);
+  count_launch();
+  MV_CHECK_CUDA(cudaGetLastError());
+}
+
 void launch_coarse_from_keys(const uint64_t* cand, int64_t nq, int ncand, const float* q, int d,
                              const float* cent, int nlist, int metric, int nc, int nprobe,
                              int32_t* probes, float* term, int* err, cudaStream_t s) {
@@ -809,10 +1244,27 @@ void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s, int nt, int persiste
 void launch_rerank_fast(RerankArgs a, cudaStream_t s) {
   if (a.nq == 0) return;
   a.kp = next_pow2(a.k);
-  const size_t smem = (((size_t)a.d * 4 + 15) & ~size_t(15)) + (size_t)(a.R + a.kp) * 8;
+  const size_t qbytes = ((size_t)a.d * 4 + 15) & ~size_t(15);
+  const size_t csmem = (size_t)RC_WARPS * (qbytes + (size_t)a.R * 24);
+  if (a.raw16 && a.rad && a.n16 && a.k <= 32 && a.R >= 32 && csmem <= 100 * 1024) {
+    smem_attr(k_rerank_cert, csmem);
+    k_rerank_cert<<<(unsigned)((a.nq + RC_WARPS - 1) / RC_WARPS), RC_WARPS * 32, csmem, s>>>(a);
+    count_launch();
+    MV_CHECK_CUDA(cudaGetLastError());
+    return;
+  }
+  const size_t smem = qbytes + (size_t)(a.R + a.kp + FT) * 8;
   MV_REQUIRE(smem <= 220 * 1024, MV_ERR_UNSUPPORTED, "rerank: d or shortlist too large");
   smem_attr(k_rerank_fast, smem);
   k_rerank_fast<<<(unsigned)a.nq, FT, smem, s>>>(a);
+  count_launch();
+  MV_CHECK_CUDA(cudaGetLastError());
+}
+
+void launch_rerank_rows(const float* raw, int64_t n, int d, __nv_bfloat16* raw16, float* rad,
+                        float* n16, cudaStream_t s) {
+  if (n == 0) return;
+  k_rerank_rows<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(raw, n, d, raw16, rad, n16);
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());
 }

@@ -669,6 +669,317 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
   if (threadIdx.x == 0 && *verr && g.err) atomicExch(g.err, 1);
 }
 
+// Descending bitonic network over N register values (static indices).
+template <int N>
+__device__ __forceinline__ void sort_desc_regs(float* v) {
+#pragma unroll
+  for (int k = 2; k <= N; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const int l = i ^ j;
+        if (l > i) {
+          const float a = v[i], b = v[l];
+          const bool desc = (i & k) == 0;
+          v[i] = desc ? fmaxf(a, b) : fminf(a, b);
+          v[l] = desc ? fminf(a, b) : fmaxf(a, b);
+        }
+      }
+    }
+  }
+}
+
+// Keeps the K smallest of the n keys of a per-row list in lst[0..K)
+// (selection in place; only reached when a row has more keys at or above
+// its threshold than the list holds) and returns the largest of them.
+__device__ __noinline__ uint64_t coarse_list_compact(uint64_t* lst, int n, int K) {
+  for (int t = 0; t < K; ++t) {
+    int best = t;
+    uint64_t bv = lst[t];
+    for (int i = t + 1; i < n; ++i) {
+      const uint64_t v = lst[i];
+      if (v < bv) {
+        bv = v;
+        best = i;
+      }
+    }
+    lst[best] = lst[t];
+    lst[t] = bv;
+  }
+  return lst[K - 1];
+}
+
+// Coarse top-nc in two passes over a segment of centroid tiles (few columns
+// per row: the IVF coarse quantizer). Same pipeline as k_umma_topk with the
+// query block resident; the producer streams the segment's tiles twice and
+// the MMA warp computes them twice with the same instructions, so both
+// passes see the same accumulators.
+// Pass 1, branch-free: per row, the largest e = -distance of every column
+// bucket (column mod NBK). The nc-th largest bucket maximum T has at least
+// nc columns with e >= T, so each of the row's nc smallest keys has e >= T.
+// Pass 2 appends the keys (distance, column) with e >= T to the row's list
+// in global memory (the thread owns the row: no atomics), per 32-column
+// chunk from a bit mask with positions by population count (no serial
+// dependence, no divergence). A chunk that would overflow the list first
+// compacts it to its nc smallest keys and raises T to the e of the largest
+// of them (later columns have larger ids, so a key they tie with that one
+// cannot be among the nc smallest); the list always contains the segment's
+// nc smallest keys, whatever the data.
+// With gthr, the segments of a row share their pass-1 thresholds (atomicMax
+// on the ordered e): the segment holding the largest T has nc columns at or
+// above it, so no column below it is among the row's nc smallest keys, and
+// every segment may use it (read again at every pass-2 tile). Output: lists[(row * nseg + seg) * cap + j] for
+// j < counts[row * nseg + seg], unsorted.
+template <bool L2, int NBK>
+__global__ void __launch_bounds__(192, 2)
+    k_coarse_topk2(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUtensorMap ty,
+                   CoarseTopkArgs g) {
+  constexpr int BN = 128;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  const int nkb = g.nkb;
+  const uint32_t a_bytes = (uint32_t)nkb * BM * 128;
+  const uint32_t b_stage = (uint32_t)nkb * BN * 128;
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + a_bytes;
+  float* cnbuf = reinterpret_cast<float*>(sB + STAGES * b_stage);  // 4 warps x BN biases
+  uint64_t* bars = reinterpret_cast<uint64_t*>(cnbuf + 4 * BN);
+  uint32_t* holder = reinterpret_cast<uint32_t*>(bars + 16);
+  __shared__ int s_err;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t bar0 = smem_u32(bars);
+  auto b_full = [&](int s) { return bar0 + 8u * s; };
+  auto b_empty = [&](int s) { return bar0 + 8u * (4 + s); };
+  auto b_tfull = [&](int a) { return bar0 + 8u * (8 + a); };
+  auto b_tempty = [&](int a) { return bar0 + 8u * (10 + a); };
+  const uint32_t b_done = bar0 + 8u * 12;
+  const uint32_t b_fulla = bar0 + 8u * 13;
+  if (threadIdx.x == 0) {
+    s_err = 0;
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(b_full(s), 1);
+      mbar_init(b_empty(s), 1);
+    }
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(b_tfull(a), 1);
+      mbar_init(b_tempty(a), 128);
+    }
+    mbar_init(b_done, 1);
+    mbar_init(b_fulla, 1);
+    fence_mbar_init();
+  }
+  if (warp == 0 && lane == 0) {
+    prefetch_tmap(&tx);
+    prefetch_tmap(&ty);
+  }
+  if (warp == 1) tmem_alloc(smem_u32(holder), 2 * BN);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(holder);
+  const int seg = blockIdx.x;
+  const int rb = blockIdx.y;
+  const int nct = (int)((g.ncols + BN - 1) / BN);
+  const int ct0 = seg * g.tps;
+  const int ct1 = min(ct0 + g.tps, nct);
+  const int my_count = ct1 > ct0 ? ct1 - ct0 : 0;
+  const int total = 2 * my_count;  // both passes
+  volatile int* verr = &s_err;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      mbar_arrive_expect_tx(b_fulla, a_bytes);
+      for (int kb = 0; kb < nkb; ++kb)
+        tma_load_2d(smem_u32(sA + kb * (BM * 128)), &tx, kb * 64, rb * BM, b_fulla);
+      int it = 0;
+      for (; it < total; ++it) {
+        const int s = it % STAGES;
+        const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+        if (*verr || !mbar_wait(b_empty(s), ph ^ 1u)) {
+          *verr = 1;
+          break;
+        }
+        const int tile = ct0 + (it < my_count ? it : it - my_count);
+        uint8_t* st = sB + (size_t)s * b_stage;
+        mbar_arrive_expect_tx(b_full(s), b_stage);
+        for (int kb = 0; kb < nkb; ++kb)
+          tma_load_2d(smem_u32(st + kb * (BN * 128)), &ty, kb * 64, tile * BN, b_full(s));
+      }
+      // Drain: every issued load must land before the CTA exits.
+      if (!mbar_wait(b_fulla, 0)) *verr = 1;
+      for (int j = (it > STAGES ? it - STAGES : 0); j < it; ++j)
+        if (!mbar_wait(b_full(j % STAGES), (uint32_t)(j / STAGES) & 1u)) *verr = 1;
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_f32(BM, BN);
+      bool ok = mbar_wait(b_fulla, 0);
+      if (!ok) *verr = 1;
+      for (int it = 0; ok && it < total; ++it) {
+        const int s = it % STAGES;
+        const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+        const int acc = it & 1;
+        const uint32_t aph = (uint32_t)(it >> 1) & 1u;
+        if (*verr || !mbar_wait(b_tempty(acc), aph ^ 1u) || !mbar_wait(b_full(s), ph)) {
+          *verr = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint8_t* st = sB + (size_t)s * b_stage;
+        const uint32_t d = tmem + (uint32_t)(acc * BN);
+        for (int kb = 0; kb < nkb; ++kb) {
+          const uint64_t ad = desc_k_sw128(smem_u32(sA + kb * (BM * 128)));
+          const uint64_t bd = desc_k_sw128(smem_u32(st + kb * (BN * 128)));
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk)
+            umma_bf16(d, ad + 2u * kk, bd + 2u * kk, idesc, (kb | kk) ? 1u : 0u);
+        }
+        umma_commit(b_empty(s));
+        umma_commit(b_tfull(acc));
+      }
+      umma_commit(b_done);
+    }
+  } else {
+    const int q = warp & 3;  // TMEM lane quarter (warp % 4, as tcgen05.ld requires)
+    const int rloc = q * 32 + lane;
+    const int64_t row = (int64_t)rb * BM + rloc;
+    const bool row_ok = row < g.nrows;
+    const float INF = __int_as_float(0x7f800000);
+    constexpr float SCALE = L2 ? 2.0f : 1.0f;
+    constexpr int BO = NBK == 64 ? 32 : 0;  // bucket offset of the odd chunks
+    constexpr int CL = 1;                   // chunks loaded from TMEM per wait
+    float* cs = cnbuf + q * BN;
+    float bm[NBK];
+#pragma unroll
+    for (int j = 0; j < NBK; ++j) bm[j] = -INF;
+    float thr = INF;  // pass 2: e >= thr enters (never for rows past the end)
+    int cnt = 0;
+    uint32_t* grow = g.gthr && row_ok ? g.gthr + row : nullptr;
+    uint64_t* lst = g.lists + ((size_t)(row_ok ? row : 0) * g.nseg + seg) * g.cap;
+    float cpre[4];
+    auto load_cn = [&](int ti) {
+      const int64_t base = (int64_t)(ct0 + ti) * BN + lane * 4;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        cpre[u] = base + u >= g.ncols ? -INF : (L2 ? -__ldg(g.cnorm + base + u) : 0.0f);
+    };
+    if (my_count > 0) load_cn(0);
+    for (int it = 0; it < total; ++it) {
+      const bool pass2 = it >= my_count;
+      const int ti = pass2 ? it - my_count : it;
+      if (it == my_count && row_ok) {
+        sort_desc_regs<NBK>(bm);
+        // bm[nc - 1] without a dynamic register index: after the descending
+        // sort it is the largest value at positions >= nc - 1.
+        float t = -INF;
+#pragma unroll
+        for (int j = 0; j < NBK; ++j) t = fmaxf(t, j >= g.nc - 1 ? bm[j] : -INF);
+        thr = t;
+        if (grow) atomicMax(grow, float_to_ordered(t));
+      }
+      if (pass2 && grow) thr = fmaxf(thr, ordered_to_float(*reinterpret_cast<volatile uint32_t*>(grow)));
+      const int acc = it & 1;
+      const uint32_t aph = (uint32_t)(it >> 1) & 1u;
+      bool ok = !*verr && mbar_wait(b_tfull(acc), aph);
+      if (!__all_sync(0xffffffffu, ok)) {
+        *verr = 1;
+        break;
+      }
+      tc_fence_after();
+      __syncwarp();
+#pragma unroll
+      for (int u = 0; u < 4; ++u) cs[lane * 4 + u] = cpre[u];
+      __syncwarp();
+      if (it + 1 < total) load_cn(it + 1 < my_count ? it + 1 : it + 1 - my_count);
+      const int64_t tile0 = (int64_t)(ct0 + ti) * BN;
+      const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN);
+      // e = -distance of the 32 columns of chunk ch (-inf past the end), from
+      // the chunk's raw accumulators (the TMEM loads of CL chunks are issued
+      // before one wait).
+      auto chunk_e = [&](const uint32_t* rv, int ch, float* e) {
+#pragma unroll
+        for (int j = 0; j < 32; j += 4) {
+          const float4 b4 = *reinterpret_cast<const float4*>(cs + ch * 32 + j);  // broadcast
+          e[j] = fmaf(SCALE, __uint_as_float(rv[j]), b4.x);
+          e[j + 1] = fmaf(SCALE, __uint_as_float(rv[j + 1]), b4.y);
+          e[j + 2] = fmaf(SCALE, __uint_as_float(rv[j + 2]), b4.z);
+          e[j + 3] = fmaf(SCALE, __uint_as_float(rv[j + 3]), b4.w);
+        }
+      };
+      if (!pass2) {
+#pragma unroll
+        for (int c2 = 0; c2 < 4; c2 += CL) {
+          uint32_t rr[CL][32];
+#pragma unroll
+          for (int h2 = 0; h2 < CL; ++h2) tmem_ld32_issue(tbase + (uint32_t)((c2 + h2) * 32), rr[h2]);
+#pragma unroll
+          for (int h2 = 0; h2 < CL; ++h2) tmem_ld32_wait(rr[h2]);
+#pragma unroll
+          for (int h2 = 0; h2 < CL; ++h2) {
+            const int ch = c2 + h2;
+            float e[32];
+            chunk_e(rr[h2], ch, e);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) bm[(ch & 1) * BO + j] = fmaxf(bm[(ch & 1) * BO + j], e[j]);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int c2 = 0; c2 < 4; c2 += CL) {
+          uint32_t rr[CL][32];
+#pragma unroll
+          for (int h2 = 0; h2 < CL; ++h2) tmem_ld32_issue(tbase + (uint32_t)((c2 + h2) * 32), rr[h2]);
+#pragma unroll
+          for (int h2 = 0; h2 < CL; ++h2) tmem_ld32_wait(rr[h2]);
+#pragma unroll
+          for (int h2 = 0; h2 < CL; ++h2) {
+            const int ch = c2 + h2;
+            float e[32];
+            chunk_e(rr[h2], ch, e);
+            const int64_t col0 = tile0 + ch * 32;
+            const int64_t left = g.ncols - col0;
+            const uint32_t valid = left >= 32 ? 0xffffffffu : left <= 0 ? 0u : (1u << left) - 1u;
+            uint32_t mk = 0;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) mk |= e[j] >= thr ? (1u << j) : 0u;
+            mk &= valid;
+            if (!__any_sync(0xffffffffu, mk != 0u)) continue;
+            if (cnt + __popc(mk) > g.cap) {  // rare
+              const uint64_t km = coarse_list_compact(lst, cnt, g.nc);
+              cnt = g.nc;
+              thr = fmaxf(thr, -key_dist(km));
+              mk = 0;
+#pragma unroll
+              for (int j = 0; j < 32; ++j) mk |= e[j] >= thr ? (1u << j) : 0u;
+              mk &= valid;
+            }
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+              if (mk & (1u << j))
+                lst[cnt + __popc(mk & ((1u << j) - 1u))] = make_key(-e[j], (uint32_t)(col0 + j));
+            cnt += __popc(mk);
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(b_tempty(acc));
+    }
+    if (row_ok) g.counts[(size_t)row * g.nseg + seg] = cnt;
+  }
+  __syncthreads();
+  if (warp == 1) {
+    bool done = true;
+    if (lane == 0) done = mbar_wait(b_done, 0);
+    done = __shfl_sync(0xffffffffu, done, 0);
+    if (!done && lane == 0) *verr = 1;
+    tc_fence_after();
+    tmem_dealloc(tmem, 2 * BN);
+  }
+  if (threadIdx.x == 0 && *verr && g.err) atomicExch(g.err, 1);
+}
+
 __global__ void k_to_bf16(const float* __restrict__ x, int64_t n, int d, int kp,
                           __nv_bfloat16* __restrict__ out, float* __restrict__ norms) {
   const int lane = threadIdx.x & 31;
@@ -969,6 +1280,80 @@ void launch_umma_topk(const __nv_bfloat16* X, int64_t nx, const __nv_bfloat16* Y
   } else {
     l2m ? go(k_umma_topk<64, true, 1>, 192) : go(k_umma_topk<64, false, 1>, 192);
   }
+  count_launch();
+  MV_CHECK_CUDA(cudaGetLastError());
+}
+
+namespace {
+size_t coarse_topk2_smem(int nkb) {
+  return 1024 + (size_t)nkb * BM * 128 + (size_t)STAGES * nkb * 128 * 128 + 4 * 128 * 4 + 256;
+}
+}  // namespace
+
+int coarse_topk2_cap(int nc) { return nc <= 16 ? 64 : 128; }
+
+int coarse_topk2_nseg(int64_t nrows, int64_t ncols, int d, int nc, int num_sms) {
+  const int nkb = umma_kpad(d) / 64;
+  const int64_t nrb = (nrows + BM - 1) / BM;
+  const int64_t nct = (ncols + 127) / 128;
+  // CTAs resident per SM (shared memory; 1 KB reserved per CTA), then the
+  // fewest column segments (at least 4 tiles each) whose CTAs fill the last
+  // wave to 90 %; the select kernel takes at most 256 keys per row.
+  const int64_t cps = std::max<int64_t>(1, std::min<int64_t>(2, (228 * 1024) / (coarse_topk2_smem(nkb) + 1024)));
+  const int64_t slots = (int64_t)std::max(num_sms, 1) * cps;
+  const int64_t maxseg = std::max<int64_t>(1, std::min<int64_t>(nct / 4, 256 / coarse_topk2_cap(nc)));
+  int64_t best = 1;
+  double best_eff = 0.0;
+  for (int64_t ns = 1; ns <= maxseg; ++ns) {
+    const int64_t ctas = nrb * ns;
+    const int64_t waves = (ctas + slots - 1) / slots;
+    const double eff = (double)ctas / (double)(waves * slots);
+    if (eff > best_eff + 1e-9) {
+      best_eff = eff;
+      best = ns;
+    }
+    if (eff >= 0.9) break;
+  }
+  return (int)best;
+}
+
+void launch_coarse_topk2(const __nv_bfloat16* X, int64_t nx, const __nv_bfloat16* Y, int64_t ny,
+                         int d, int metric, const float* ynorm, int nc, int nseg, uint64_t* lists,
+                         int* counts, uint32_t* gthr, int* err, cudaStream_t s) {
+  if (nx == 0) return;
+  const int kp = umma_kpad(d);
+  MV_REQUIRE(kp <= 256, MV_ERR_UNSUPPORTED, "two-pass coarse GEMM: d must be at most 256");
+  MV_REQUIRE(nc >= 1 && nc <= 32 && nc <= ny, MV_ERR_UNSUPPORTED, "two-pass coarse GEMM keeps 1..32 lists");
+  MV_REQUIRE(nx < (1ll << 31) && ny < (1ll << 32) - 1, MV_ERR_UNSUPPORTED, "GEMM too large");
+  MV_REQUIRE((nx + BM - 1) / BM <= 65535, MV_ERR_UNSUPPORTED, "two-pass coarse GEMM: too many rows");
+  const int cap = coarse_topk2_cap(nc);
+  MV_REQUIRE(nseg >= 1 && (int64_t)nseg * cap <= 256, MV_ERR_INTERNAL, "two-pass coarse GEMM: bad segment count");
+  CoarseTopkArgs g;
+  g.nrows = nx;
+  g.ncols = ny;
+  g.nkb = kp / 64;
+  g.cnorm = ynorm;
+  g.nc = nc;
+  g.nseg = nseg;
+  const int64_t nct = (ny + 127) / 128;
+  g.tps = (int)((nct + nseg - 1) / nseg);
+  g.cap = cap;
+  g.lists = lists;
+  g.counts = counts;
+  g.gthr = nseg > 1 ? gthr : nullptr;
+  if (g.gthr) MV_CHECK_CUDA(cudaMemsetAsync(g.gthr, 0, sizeof(uint32_t) * nx, s));
+  g.err = err;
+  const CUtensorMap tx = make_tmap(X, nx, kp, BM);
+  const CUtensorMap ty = make_tmap(Y, ny, kp, 128);
+  dim3 grid((unsigned)nseg, (unsigned)((nx + BM - 1) / BM));
+  const size_t smem = coarse_topk2_smem(g.nkb);
+  auto go = [&](auto kernel) {
+    smem_limit(kernel, smem);
+    kernel<<<grid, 192, smem, s>>>(tx, ty, g);
+  };
+  const bool l2m = metric == MV_METRIC_L2;
+  if (nc <= 16) l2m ? go(k_coarse_topk2<true, 32>) : go(k_coarse_topk2<false, 32>);
+  else l2m ? go(k_coarse_topk2<true, 64>) : go(k_coarse_topk2<false, 64>);
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());
 }

@@ -671,6 +671,13 @@ void ensure_fast(mv_ivfpq* ix, cudaStream_t s) {
                      ix->pq.as<float>(), ix->centroids.as<float>(), ix->d, ix->M,
                      ix->d_vec_term.as<float>(), s);
   }
+  if (ix->has_raw && total > 0) {
+    ix->d_raw16.ensure((size_t)total * ix->d * 2);
+    ix->d_rad.ensure((size_t)total * 4);
+    ix->d_n16.ensure((size_t)total * 4);
+    launch_rerank_rows(ix->d_raw.as<float>(), total, ix->d, ix->d_raw16.as<__nv_bfloat16>(),
+                       ix->d_rad.as<float>(), ix->d_n16.as<float>(), s);
+  }
   sync(s);
   ix->fast_ready = true;
 }
@@ -702,31 +709,42 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
   MV_REQUIRE(nprobe <= 8192, MV_ERR_UNSUPPORTED, "nprobe above 8192 is not supported on the GPU");
   const int nc = fp32_coarse ? nprobe : std::min(ix->nlist, nprobe + std::max(8, nprobe / 4));
   const int kp = umma_kpad(ix->d);
-  // Fused coarse (tensor-core GEMM keeping each query's best nc lists) when
-  // nc fits the epilogue's per-row list; otherwise the distance matrix path.
+  // BF16 coarse step, three kinds that keep the same approximate top-nc
+  // lists per query: the two-pass GEMM with per-row lists (nc <= 32,
+  // d <= 256; coarse_path 3), the GEMM with a per-row heap epilogue
+  // (nc <= 64; coarse_path 1) and the distance matrix with one warp per
+  // query selecting (coarse_path 2). Automatic: two-pass where it applies,
+  // else the matrix.
   const int cpath = p ? p->coarse_path : 0;
-  MV_REQUIRE(cpath >= 0 && cpath <= 2, MV_ERR_ARG, "coarse_path must be 0, 1 or 2");
-  // Automatic: the fused epilogue up to 16 candidates per row; above that
-  // the distance matrix with one warp per query selecting is faster.
-  const bool fused = !fp32_coarse && nc <= 64 &&
-                     (batch ? !batch->coarse_matrix : (cpath == 1 || (cpath == 0 && nc <= 16)));
+  MV_REQUIRE(cpath >= 0 && cpath <= 3, MV_ERR_ARG, "coarse_path must be 0, 1, 2 or 3");
+  const bool twopass_ok = !fp32_coarse && nc <= 32 && kp <= 256;
+  const bool gemm = !fp32_coarse && (batch ? !batch->coarse_matrix : cpath != 2);
+  const bool twopass = gemm && twopass_ok && cpath != 1;
+  const bool fused = gemm && !twopass && nc <= 64 && (batch || cpath == 1);
   int64_t qb = std::max<int64_t>(128, (int64_t)(1536ll * 1024 * 1024 / ((int64_t)ix->nlist * 4)));
   qb = std::min<int64_t>({qb, nq, 65535ll * 64});
   if (batch) {
     MV_REQUIRE(nq <= 65535ll * 64, MV_ERR_UNSUPPORTED, "batch too large for one launch");
     qb = nq;
   }
-  const int nseg = fused ? umma_topk_nseg(qb, ix->nlist, ix->d, nc, ix->ctx->num_sms) : 1;
+  const int nseg = fused ? umma_topk_nseg(qb, ix->nlist, ix->d, nc, ix->ctx->num_sms)
+                 : twopass ? coarse_topk2_nseg(qb, ix->nlist, ix->d, nc, ix->ctx->num_sms) : 1;
   const int ncand = nseg * (fused ? umma_topk_groups(ix->d, nc) : 1) * next_pow2(nc);
+  const int lcap = twopass ? coarse_topk2_cap(nc) : 0;
   ws.ensure(ws_bytes((size_t)qb * kp, 2) +
-            (fused ? ws_bytes((size_t)qb * ncand, 8) + ws_bytes((size_t)qb, 8)
-                   : ws_bytes((size_t)qb * ix->nlist, 4)) +
+            (fused     ? ws_bytes((size_t)qb * ncand, 8) + ws_bytes((size_t)qb, 8)
+             : twopass ? ws_bytes((size_t)qb * nseg * lcap, 8) + ws_bytes((size_t)qb * nseg, 4) +
+                            ws_bytes((size_t)qb, 4)
+                       : ws_bytes((size_t)qb * ix->nlist, 4)) +
             ws_bytes((size_t)qb * nprobe, 4) * 2 + ws_bytes((size_t)qb * R, 8));
   Arena ar(ws);
   __nv_bfloat16* xq = ar.take<__nv_bfloat16>((size_t)qb * kp);
-  float* dmat = fused ? nullptr : ar.take<float>((size_t)qb * ix->nlist);
+  float* dmat = fused || twopass ? nullptr : ar.take<float>((size_t)qb * ix->nlist);
   uint64_t* ckeys = fused ? ar.take<uint64_t>((size_t)qb * ncand) : nullptr;
   uint64_t* gthr = fused && ncand > next_pow2(nc) ? ar.take<uint64_t>((size_t)qb) : nullptr;
+  uint64_t* clists = twopass ? ar.take<uint64_t>((size_t)qb * nseg * lcap) : nullptr;
+  int* ccounts = twopass ? ar.take<int>((size_t)qb * nseg) : nullptr;
+  uint32_t* cthr = twopass ? ar.take<uint32_t>((size_t)qb) : nullptr;
   int32_t* probes = ar.take<int32_t>((size_t)qb * nprobe);
   float* term = ar.take<float>((size_t)qb * nprobe);
   uint64_t* skeys = ar.take<uint64_t>((size_t)qb * R);
@@ -741,7 +759,11 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
                             ix->nlist, s);
       } else {
         launch_to_bf16(xb, nb, ix->d, xq, nullptr, s);
-        if (fused)
+        if (twopass)
+          launch_coarse_topk2(xq, nb, ix->d_cent_bf16.as<__nv_bfloat16>(), ix->nlist, ix->d,
+                              ix->metric, ix->d_cnorm.as<float>(), nc, nseg, clists, ccounts,
+                              cthr, ix->ctx->d_err.as<int>(), s);
+        else if (fused)
           launch_umma_topk(xq, nb, ix->d_cent_bf16.as<__nv_bfloat16>(), ix->nlist, ix->d,
                            ix->metric, nullptr, ix->d_cnorm.as<float>(), nc, nseg, nullptr, gthr,
                            ckeys, ix->ctx->d_err.as<int>(), s);
@@ -757,7 +779,11 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
     }
     {
       StageTimer t(ix->ctx, MV_STAGE_SELECT, s);
-      if (fused)
+      if (twopass)
+        launch_coarse_lists(clists, ccounts, nseg, lcap, nb, ix->nlist, xb, ix->d,
+                            ix->centroids.as<float>(), ix->metric, nc, nprobe, probes, term,
+                            ix->ctx->d_err.as<int>(), s);
+      else if (fused)
         launch_coarse_from_keys(ckeys, nb, ncand, xb, ix->d, ix->centroids.as<float>(), ix->nlist,
                                 ix->metric, nc, nprobe, probes, term, ix->ctx->d_err.as<int>(), s);
       else if (nc <= 64)
@@ -821,6 +847,11 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
       r.ntotal = ix->h_off[ix->nlist];
       r.err = ix->ctx->d_err.as<int>();
       r.k_q = batch ? batch->k_q : nullptr;
+      if (!(p && p->rerank_fp32) && ix->d_raw16.p) {
+        r.raw16 = ix->d_raw16.as<__nv_bfloat16>();
+        r.rad = ix->d_rad.as<float>();
+        r.n16 = ix->d_n16.as<float>();
+      }
       launch_rerank_fast(r, s);
     } else {
       launch_short_to_results(skeys, nb, R, k, ix->d_ids.as<uint32_t>(), ix->metric,
@@ -2403,8 +2434,8 @@ int32_t mv_ivfpq_plan_create(mv_ivfpq* ix, int64_t max_nq, int32_t nprobe_max, i
     pl->params.form = MV_FORM_FAST;
     // the tuner may change it
     const int nc = std::min(ix->nlist, nprobe_max + std::max(8, nprobe_max / 4));
-    pl->cfg.coarse_matrix =
-        pl->params.coarse_path == 2 || (pl->params.coarse_path == 0 && nc > 16);
+    pl->cfg.coarse_matrix = pl->params.coarse_path == 2 ||
+                            (pl->params.coarse_path == 0 && !(nc <= 32 && umma_kpad(ix->d) <= 256));
     MV_CHECK_CUDA(cudaStreamCreateWithFlags(&pl->stream, cudaStreamNonBlocking));
     pl->x.ensure(sizeof(float) * max_nq * ix->d);
     pl->nprobe_q.ensure(sizeof(int32_t) * max_nq);
@@ -2583,8 +2614,12 @@ void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int npr
   const int kp = umma_kpad(ix->d);
   const int nc = std::min(ix->nlist, nprobe + std::max(8, nprobe / 4));
   const int cpath = p ? p->coarse_path : 0;
-  MV_REQUIRE(cpath >= 0 && cpath <= 2, MV_ERR_ARG, "coarse_path must be 0, 1 or 2");
-  const bool fused = fast && nc <= 64 && (cpath == 1 || (cpath == 0 && nc <= 16));
+  MV_REQUIRE(cpath >= 0 && cpath <= 3, MV_ERR_ARG, "coarse_path must be 0, 1, 2 or 3");
+  // As in the fast IVF-PQ search: two-pass GEMM + lists where it applies
+  // (automatic, or coarse_path 3), the heap epilogue on request, else the
+  // distance matrix.
+  const bool twopass = fast && nc <= 32 && kp <= 256 && (cpath == 0 || cpath == 3);
+  const bool fused = fast && !twopass && nc <= 64 && cpath == 1;
   const bool cert_coarse = !fast && umma_kpad(ix->d) <= UMMA_TOPK_MAX_K &&
                            std::min(ix->nlist, nprobe + std::max(16, nprobe / 2)) < ix->nlist &&
                            nprobe + std::max(16, nprobe / 2) <= UMMA_TOPK_MAX;
@@ -2604,11 +2639,15 @@ void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int npr
   }
   int64_t qb = std::max<int64_t>(64, (int64_t)(1536ll * 1024 * 1024 / ((int64_t)ix->nlist * 4)));
   qb = std::min<int64_t>({qb, nq, 65535ll * 64});
-  const int nseg = fused ? umma_topk_nseg(qb, ix->nlist, ix->d, nc, ix->ctx->num_sms) : 1;
+  const int nseg = fused ? umma_topk_nseg(qb, ix->nlist, ix->d, nc, ix->ctx->num_sms)
+                 : twopass ? coarse_topk2_nseg(qb, ix->nlist, ix->d, nc, ix->ctx->num_sms) : 1;
   const int ncand = nseg * (fused ? umma_topk_groups(ix->d, nc) : 1) * next_pow2(nc);
+  const int lcap = twopass ? coarse_topk2_cap(nc) : 0;
   ws.ensure(ws_bytes((size_t)qb * ix->nlist, 4) + ws_bytes((size_t)qb * nprobe, 8) +
             ws_bytes((size_t)qb * nprobe, 4) * 2 + ws_bytes((size_t)qb * kp, 2) +
-            ws_bytes((size_t)qb * ncand, 8) + ws_bytes((size_t)qb, 8));
+            ws_bytes((size_t)qb * ncand, 8) + ws_bytes((size_t)qb, 8) +
+            ws_bytes((size_t)qb * nseg * lcap, 8) + ws_bytes((size_t)qb * nseg, 4) +
+            ws_bytes((size_t)qb, 4));
   Arena ar(ws);
   float* dmat = ar.take<float>((size_t)qb * ix->nlist);
   uint64_t* ckeys = ar.take<uint64_t>((size_t)qb * nprobe);
@@ -2617,6 +2656,9 @@ void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int npr
   __nv_bfloat16* xq = ar.take<__nv_bfloat16>((size_t)qb * kp);
   uint64_t* fkeys = ar.take<uint64_t>((size_t)qb * ncand);
   uint64_t* gthr = ar.take<uint64_t>((size_t)qb);
+  uint64_t* clists = ar.take<uint64_t>((size_t)qb * nseg * lcap);
+  int* ccounts = ar.take<int>((size_t)qb * nseg);
+  uint32_t* cthr = ar.take<uint32_t>((size_t)qb);
   const int kind = ix->metric == MV_METRIC_L2 ? KIND_L2_SIMD8 : KIND_IP_SIMD8;
   for (int64_t q0 = 0; q0 < nq; q0 += qb) {
     const int64_t nb = std::min(qb, nq - q0);
@@ -2636,7 +2678,11 @@ void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int npr
                             ix->d, dmat, ix->nlist, s);
       } else {
         launch_to_bf16(xb, nb, ix->d, xq, nullptr, s);
-        if (fused)
+        if (twopass)
+          launch_coarse_topk2(xq, nb, ix->d_cent_bf16.as<__nv_bfloat16>(), ix->nlist, ix->d,
+                              ix->metric, ix->d_cnorm.as<float>(), nc, nseg, clists, ccounts,
+                              cthr, ix->ctx->d_err.as<int>(), s);
+        else if (fused)
           launch_umma_topk(xq, nb, ix->d_cent_bf16.as<__nv_bfloat16>(), ix->nlist, ix->d,
                            ix->metric, nullptr, ix->d_cnorm.as<float>(), nc, nseg, nullptr,
                            ncand > next_pow2(nc) ? gthr : nullptr, fkeys, ix->ctx->d_err.as<int>(),
@@ -2655,6 +2701,10 @@ void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int npr
       if (!fast) {  // :185-194 coarse quantizer search with k = nprobe
         launch_select_rows(dmat, nb, ix->nlist, ix->nlist, 0, nprobe, nullptr, ckeys, nullptr, s);
         launch_keys_to_ids(ckeys, nb * nprobe, probes, s);
+      } else if (twopass) {
+        launch_coarse_lists(clists, ccounts, nseg, lcap, nb, ix->nlist, xb, ix->d,
+                            ix->centroids.as<float>(), ix->metric, nc, nprobe, probes, term,
+                            ix->ctx->d_err.as<int>(), s);
       } else if (fused) {
         launch_coarse_from_keys(fkeys, nb, ncand, xb, ix->d, ix->centroids.as<float>(), ix->nlist,
                                 ix->metric, nc, nprobe, probes, term, ix->ctx->d_err.as<int>(), s);

@@ -1,6 +1,8 @@
 // Host interface of the fast-form IVF-PQ kernels (k_ivfpq_fast.cu).
 #pragma once
 
+#include <cuda_bf16.h>
+
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -50,8 +52,24 @@ struct RerankArgs {
   float fill_d = 1e38f;   // distance of an unfilled slot (label -1)
   const int32_t* k_q = nullptr;  // per-query k (<= k; the row keeps k slots), may be null
   int kp;                 // set by the launcher
+  // Certified prescreen (k <= 32; all null: every candidate is computed in
+  // FP32): BF16 copies of the rows, per row an upper bound on
+  // ||y - bf16(y)|| and (IP) on ||bf16(y)||.
+  const __nv_bfloat16* raw16 = nullptr;
+  const float* rad = nullptr;
+  const float* n16 = nullptr;
 };
 
+// BF16 copies of FP32 rows (CSR order) for the certified rerank prescreen,
+// with per row upper bounds on ||y - bf16(y)|| and ||bf16(y)||.
+void launch_rerank_rows(const float* raw, int64_t n, int d, __nv_bfloat16* raw16, float* rad,
+                        float* n16, cudaStream_t s);
+
+// Two-pass coarse GEMM lists (launch_coarse_topk2) -> the nprobe nearest
+// lists, as launch_coarse_rows (one warp per query; nseg * cap <= 256).
+void launch_coarse_lists(const uint64_t* lists, const int* counts, int nseg, int cap, int64_t nq,
+                         int nlist, const float* q, int d, const float* cent, int metric, int nc,
+                         int nprobe, int32_t* probes, float* term, int* err, cudaStream_t s);
 void launch_vec_terms(const int64_t* off, int nlist, const uint8_t* codes, const float* pq,
                       const float* cent, int d, int M, float* out, cudaStream_t s);
 // Top-nc of the approximate coarse distances, exact FP32 recheck, top-nprobe.

@@ -208,6 +208,9 @@ struct mv_ivfpq {
   bool coarse_ready = false;  // d_cent_bf16, d_cnorm, d_ccert (centroid-only state)
   mv::DevBuf d_ccert;       // 2 doubles: bound on ||bf16(c)||^2, max ||c - bf16(c)||
   mv::DevBuf d_vec_term;    // FP32 per vector: ||y||^2 + 2<c, y> (y = PQ reconstruction)
+  mv::DevBuf d_raw16;       // BF16 rows per entry (certified rerank prescreen)
+  mv::DevBuf d_rad;         // FP32 per entry: bound on ||y - bf16(y)||
+  mv::DevBuf d_n16;         // FP32 per entry: bound on ||bf16(y)||
   mv::DevBuf d_cnorm;       // FP32 per centroid ||c||^2
   mv::DevBuf d_cent_bf16;   // nlist x d BF16
 };

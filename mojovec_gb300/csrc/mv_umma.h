@@ -41,6 +41,19 @@ struct UmmaTopkArgs {
   const float* cscale = nullptr;  // E4M3 operands: per-column scale of Y
 };
 
+struct CoarseTopkArgs {
+  int64_t nrows, ncols;
+  int nkb;
+  const float* cnorm;  // ||y||^2 per column (L2)
+  int nc;              // keys kept per row
+  int nseg, tps;       // column segments (grid.x) and 128-column tiles per segment
+  int cap;             // list slots per row and segment (> nc)
+  uint64_t* lists;     // nrows x nseg x cap keys (distance, column)
+  int* counts;         // nrows x nseg
+  uint32_t* gthr;      // per-row threshold shared by the segments (may be null)
+  int* err;
+};
+
 // Rows are padded to this many BF16 elements (a multiple of 64).
 int umma_kpad(int d);
 // E4M3 rows are padded to this many bytes (a multiple of 128).
@@ -89,6 +102,18 @@ void launch_umma_topk_e4m3(const uint8_t* X8, int64_t nx, const float* xscale, c
                            int64_t ny, const float* yscale, int d, int metric, const float* ynorm,
                            int nc, int nseg, const uint8_t* filter, uint64_t* gthr, uint64_t* out,
                            int* err, cudaStream_t s);
+// Two-pass coarse top-nc GEMM (d <= 256, nc <= 32): per row and column
+// segment, a list of at most coarse_topk2_cap(nc) unsorted keys
+// lists[(row * nseg + seg) * cap + j], j < counts[row * nseg + seg], that
+// contains the segment's nc smallest (distance, column) keys of the BF16
+// distances (the keys launch_umma_topk keeps; the key distance leaves out
+// the row's own ||x||^2).
+int coarse_topk2_cap(int nc);
+int coarse_topk2_nseg(int64_t nrows, int64_t ncols, int d, int nc, int num_sms);
+// gthr: nx words of scratch (used when nseg > 1).
+void launch_coarse_topk2(const __nv_bfloat16* X, int64_t nx, const __nv_bfloat16* Y, int64_t ny,
+                         int d, int metric, const float* ynorm, int nc, int nseg, uint64_t* lists,
+                         int* counts, uint32_t* gthr, int* err, cudaStream_t s);
 // keys -> argmin columns (and distances).
 void launch_keys_argmin(const uint64_t* keys, int64_t n, int32_t* out, float* dist, cudaStream_t s);
 

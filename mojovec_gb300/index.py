@@ -120,8 +120,9 @@ class Context:
 
 
 def _params(form=None, nprobe=0, rerank=0, coarse_fp32=False, lut_fp16=False, coarse_path=0,
-            plain_scan=False, e4m3=False):
+            plain_scan=False, e4m3=False, rerank_fp32=False):
     p = SearchParams()
+    p.rerank_fp32 = 1 if rerank_fp32 else 0
     p.coarse_path = int(coarse_path)
     p.plain_scan = 1 if plain_scan else 0
     p.flat_e4m3 = 1 if e4m3 else 0
@@ -264,13 +265,15 @@ class IndexIVFPQ:
         return self
 
     def search(self, x, k: int, filter=None, form=None, nprobe: int = 0, rerank: int = 0,
-               coarse_fp32: bool = False, lut_fp16: bool = False, coarse_path: int = 0):
+               coarse_fp32: bool = False, lut_fp16: bool = False, coarse_path: int = 0,
+               rerank_fp32: bool = False):
         x = _f32(x, self.d)
         n = x.shape[0]
         dist = np.empty((n, k), np.float32)
         lab = np.empty((n, k), np.int64)
         flt = None if filter is None else np.ascontiguousarray(filter, dtype=np.uint8)
-        p = _params(form, nprobe, rerank, coarse_fp32, lut_fp16, coarse_path)
+        p = _params(form, nprobe, rerank, coarse_fp32, lut_fp16, coarse_path,
+                    rerank_fp32=rerank_fp32)
         check(_lib.load().mv_ivfpq_search(self._h, _p(x), n, k, _p(flt),
                                           0 if flt is None else flt.size, C.byref(p), _p(dist),
                                           _p(lab)))

@@ -160,18 +160,45 @@ def test_fast_fused_coarse_matches_matrix_coarse(mv):
         assert agree > 0.97, (nprobe, agree)
 
 
-def test_fast_paths_pick_the_same_lists(mv):
-    """coarse_path 1 (fused GEMM + per-row heap) and 2 (distance matrix + one
-    warp per query) keep the same approximate top-nc lists, so the searches
-    agree exactly."""
+@pytest.mark.parametrize("metric", [0, 1])
+def test_fast_paths_pick_the_same_lists(mv, metric):
+    """coarse_path 1 (fused GEMM + per-row heap), 2 (distance matrix + one
+    warp per query) and 3 (two-pass GEMM + per-row lists, also the automatic
+    choice up to 32 lists per query) keep the same approximate top-nc
+    lists, so the searches agree exactly."""
     from mojovec_gb300 import synth
 
     base, q = synth.sift_like(40000, d=96, n_centers=64, nq=300, seed=34)
-    g = _index(mv, base, 96, 512, 24)
-    for nprobe in (4, 16, 48):
+    g = _index(mv, base, 96, 512, 24, metric)
+    for nprobe in (1, 4, 16, 24, 48):
         a = g.search(q, 10, form=mv.FORM_FAST, nprobe=nprobe, rerank=64, coarse_path=1)
-        b = g.search(q, 10, form=mv.FORM_FAST, nprobe=nprobe, rerank=64, coarse_path=2)
-        assert np.array_equal(a[1], b[1]) and np.array_equal(a[0], b[0]), nprobe
+        for cpath in (0, 2, 3):
+            b = g.search(q, 10, form=mv.FORM_FAST, nprobe=nprobe, rerank=64, coarse_path=cpath)
+            assert np.array_equal(a[1], b[1]) and np.array_equal(a[0], b[0]), (nprobe, cpath)
+
+
+@pytest.mark.parametrize("d", [64, 200])
+def test_two_pass_coarse_lists_compact_exactly(mv, d):
+    """200 identical centroids nearest to every query tie at the two-pass
+    threshold: each row's list overflows its slots and is compacted, and the
+    kept lists (the smallest list ids among the ties) must still equal the
+    heap and matrix paths'."""
+    rng = np.random.default_rng(35)
+    nlist, M = 1024, 8
+    cent = rng.standard_normal((nlist, d)).astype(np.float32) * 4
+    cent[100:300] = cent[100]
+    base = cent[rng.integers(0, nlist, 30000)] + rng.standard_normal((30000, d)).astype(np.float32)
+    q = cent[100] + 0.01 * rng.standard_normal((257, d)).astype(np.float32)
+    g = mv.IndexIVFPQ(d, nlist, M)
+    g.train(base[:8000], niter_coarse=2, niter_pq=2)
+    _, pq = g.codebooks()
+    g.set_codebooks(cent, pq)
+    g.add(base)
+    for nprobe in (8, 24):
+        a = g.search(q, 10, form=mv.FORM_FAST, nprobe=nprobe, rerank=50, coarse_path=1)
+        for cpath in (2, 3):
+            b = g.search(q, 10, form=mv.FORM_FAST, nprobe=nprobe, rerank=50, coarse_path=cpath)
+            assert np.array_equal(a[1], b[1]) and np.array_equal(a[0], b[0]), (nprobe, cpath)
 
 
 @pytest.mark.parametrize("rerank", [0, 128])
@@ -198,3 +225,28 @@ def test_fast_filter_equals_index_without_filtered_rows(mv, rerank):
     hit = a_l[(a_l >= 0) & (a_l < len(filt))]
     assert not filt[hit].any()
     assert np.array_equal(a_l, b_l) and np.array_equal(a_d, b_d)
+
+
+@pytest.mark.parametrize("metric", [0, 1])
+@pytest.mark.parametrize("d", [64, 96, 130])
+def test_certified_rerank_prescreen_is_exact(mv, metric, d):
+    """The BF16 prescreen of the rerank (default) must return the bits of the
+    rerank that computes every shortlisted row in FP32 (rerank_fp32): on
+    real-valued rows, on SIFT-like integer rows, with duplicated rows (exact
+    ties across the k-th boundary) and with k from 1 to 32."""
+    from mojovec_gb300 import synth
+
+    rng = np.random.default_rng(36 + d)
+    if d == 96:
+        base, q = synth.sift_like(20000, d=d, n_centers=64, nq=150, seed=37)
+    else:
+        base = rng.standard_normal((20000, d)).astype(np.float32)
+        base[5000:5400] = base[5000]  # 400 identical rows
+        q = np.vstack([base[5000:5020] + 1e-3 * rng.standard_normal((20, d)).astype(np.float32),
+                       rng.standard_normal((130, d)).astype(np.float32)])
+    g = _index(mv, base, d, 64, 8 if d != 130 else 10, metric)
+    for k, R in ((1, 16), (10, 256), (32, 100)):
+        a = g.search(q, k, form=mv.FORM_FAST, nprobe=6, rerank=R)
+        b = g.search(q, k, form=mv.FORM_FAST, nprobe=6, rerank=R, rerank_fp32=True)
+        assert np.array_equal(a[1], b[1]), (k, R)
+        assert np.array_equal(a[0].view(np.uint32), b[0].view(np.uint32)), (k, R)
