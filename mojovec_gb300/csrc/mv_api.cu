@@ -671,6 +671,33 @@ void ensure_fast(mv_ivfpq* ix, cudaStream_t s) {
                      ix->pq.as<float>(), ix->centroids.as<float>(), ix->d, ix->M,
                      ix->d_vec_term.as<float>(), s);
   }
+  // FP16 codebook for the fast form's per-query tables, scaled by 2^e so
+  // the largest magnitude lies in [2^13, 2^14): no overflow, and the scale
+  // divides out exactly.
+  ix->pq16_inv = 0.0f;
+  const int dsub = ix->d / ix->M;
+  if (dsub == 4 || dsub == 8) {
+    const size_t npq = (size_t)ix->M * 256 * dsub;
+    std::vector<float> h(npq);
+    d2h(h.data(), ix->pq.p, sizeof(float) * npq, s);
+    sync(s);
+    float amax = 0.0f;
+    bool finite = true;
+    for (float v : h) {
+      finite = finite && std::isfinite(v);
+      amax = std::max(amax, std::fabs(v));
+    }
+    if (finite && amax > 0.0f && amax < 1e30f && amax > 1e-30f) {
+      const int e = 13 - std::ilogb(amax);
+      const float scale = std::ldexp(1.0f, e);
+      std::vector<__half> h16(npq);
+      for (size_t i = 0; i < npq; ++i) h16[i] = __float2half_rn(h[i] * scale);
+      ix->d_pq16.ensure(npq * sizeof(__half));
+      h2d(ix->d_pq16.p, h16.data(), npq * sizeof(__half), s);
+      sync(s);  // the host copy goes out of scope
+      ix->pq16_inv = std::ldexp(1.0f, -e);
+    }
+  }
   if (ix->has_raw && total > 0) {
     ix->d_raw16.ensure((size_t)total * ix->d * 2);
     ix->d_rad.ensure((size_t)total * 4);
@@ -802,6 +829,10 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
       a.M = ix->M;
       a.metric = ix->metric;
       a.pq = ix->pq.as<float>();
+      if (ix->pq16_inv > 0.0f) {
+        a.pq16 = ix->d_pq16.as<__half>();
+        a.pq16_inv = ix->pq16_inv;
+      }
       a.list_off = ix->d_off.as<int64_t>();
       a.codes = ix->d_codes.as<uint8_t>();
       a.vterm = ix->metric == MV_METRIC_L2 ? ix->d_vec_term.as<float>() : nullptr;

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <cuda_runtime.h>
 
@@ -14,6 +15,11 @@ struct FastScanArgs {
   int64_t nq;
   int d, M, metric;
   const float* pq;
+  // FP16 codebook scaled by a power of two (pq16 = pq / pq16_inv; dsub 4 or
+  // 8), read instead of pq when set: the table values differ from FP32 ones
+  // by the FP16 rounding of the codewords.
+  const __half* pq16 = nullptr;
+  float pq16_inv = 1.0f;
   const int64_t* list_off;
   const uint8_t* codes;
   const float* vterm;     // per CSR entry, null for IP

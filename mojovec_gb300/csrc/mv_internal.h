@@ -211,6 +211,8 @@ struct mv_ivfpq {
   mv::DevBuf d_raw16;       // BF16 rows per entry (certified rerank prescreen)
   mv::DevBuf d_rad;         // FP32 per entry: bound on ||y - bf16(y)||
   mv::DevBuf d_n16;         // FP32 per entry: bound on ||bf16(y)||
+  mv::DevBuf d_pq16;        // FP16 codebook * pq16_scale (fast-form tables; dsub 4 or 8)
+  float pq16_inv = 0.0f;    // 1 / scale; 0 = no FP16 codebook
   mv::DevBuf d_cnorm;       // FP32 per centroid ||c||^2
   mv::DevBuf d_cent_bf16;   // nlist x d BF16
 };
