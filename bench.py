@@ -337,7 +337,8 @@ def run_gpu(args, rank, world):
         "data": "synthetic SIFT-like (seeded Gaussian mixture, integer-valued), not SIFT1M",
         "config": {
             "workload": workload,
-            "form": "fast: BF16 tcgen05 coarse + FP32 recheck, per-query LUT, exact FP32 rerank"
+            "form": ("fast: two-pass BF16 tcgen05 coarse GEMM + FP32 recheck, per-query table from the "
+                     "FP16 codebook, certified rerank (the full FP32 rerank's results)")
                     if fast_form else "plain FP32 (reference algorithm, bit-exact)",
             "nprobe": nprobe,
             "rerank": args.rerank if fast_form else 0,
