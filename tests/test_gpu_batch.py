@@ -83,3 +83,16 @@ def test_batch_fused_coarse_and_argument_checks(mv):
     assert (l >= 0).all() and np.isfinite(d).all()
     with pytest.raises(mv.MojoVecGPUError):
         ix.search_batch(q[:4], np.array([0, 1, 2, 3], np.int32), k[:4], rerank=40)
+
+
+def test_batch_certified_rerank_per_query_k(mv):
+    """k <= 32 takes the certified rerank (BF16 prescreen) with per-query k:
+    the batch must still equal per-query searches, and the prescreen-free
+    rerank of the same batch."""
+    ix, q = _index(mv)
+    nprobe = RNG.integers(1, 30, size=len(q)).astype(np.int32)
+    k = RNG.choice([1, 5, 20, 32], size=len(q)).astype(np.int32)
+    d, l = ix.search_batch(q, nprobe, k, rerank=96, coarse_fp32=True)
+    rd, rl = _reference_rows(mv, ix, q, nprobe, k, 96)
+    assert np.array_equal(l, rl)
+    assert np.array_equal(d, rd)

@@ -250,3 +250,23 @@ def test_certified_rerank_prescreen_is_exact(mv, metric, d):
         b = g.search(q, k, form=mv.FORM_FAST, nprobe=6, rerank=R, rerank_fp32=True)
         assert np.array_equal(a[1], b[1]), (k, R)
         assert np.array_equal(a[0].view(np.uint32), b[0].view(np.uint32)), (k, R)
+
+
+@pytest.mark.parametrize("metric", [0, 1])
+def test_certified_rerank_odd_queries(mv, metric):
+    """Queries with a NaN component, all zeros, or huge values: the certified
+    rerank keeps such candidates (non-finite intervals always survive) and
+    must return the full FP32 rerank's bits."""
+    rng = np.random.default_rng(38)
+    d = 64
+    base = rng.standard_normal((8000, d)).astype(np.float32)
+    q = rng.standard_normal((8, d)).astype(np.float32)
+    q[0, 3] = np.nan
+    q[1] = 0.0
+    q[2] *= 1e18
+    q[3] *= 1e-20
+    g = _index(mv, base, d, 32, 8, metric)
+    a = g.search(q, 10, form=mv.FORM_FAST, nprobe=32, rerank=64, coarse_fp32=True)
+    b = g.search(q, 10, form=mv.FORM_FAST, nprobe=32, rerank=64, coarse_fp32=True, rerank_fp32=True)
+    assert np.array_equal(a[1], b[1])
+    assert np.array_equal(a[0].view(np.uint32), b[0].view(np.uint32))
