@@ -1098,6 +1098,301 @@ def run_curve(args, rank, world):
     }
 
 
+IVFFLAT_METRIC = ("IVF-Flat QPS (1Mx128 SIFT-like, nlist 4096, nprobe 8, 10k queries, k 10): exact "
+                  "per-list FP32 scan; plain bit-exact (certified tensor-core coarse step)")
+IVFFLAT_TRAIN, IVFFLAT_NITER = 65536, 8
+RERANK_METRIC = ("Shortlist rerank QPS (1Mx128 SIFT-like FP32 rows, 10k queries, 2k = 20 candidates "
+                 "each, k 10), exact FP32 l2_distance_simd[64] semantics")
+
+
+def _build_ivfflat(mv, base, ctx=None):
+    ix = mv.IndexIVFFlat(D, NLIST, mv.METRIC_L2, **({"ctx": ctx} if ctx else {}))
+    ix.train(base[:IVFFLAT_TRAIN], niter=IVFFLAT_NITER)
+    ix.add(base)
+    return ix
+
+
+def run_ivfflat(args, rank, world):
+    """IVF-Flat search (index/index_ivf_flat.mojo:149-243): the plain form
+    (bit-exact, certified coarse step) is the line's value, the fast form
+    (BF16 two-pass coarse step) is timed beside it."""
+    import torch
+
+    import mojovec_gb300 as mv
+
+    nb, nq, k, nprobe = args.nb, args.nq, K, args.nprobe
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    ctx = mv.Context(dev)
+    t0 = time.perf_counter()
+    base, queries = build_workload(nb, nq)
+    ix = _build_ivfflat(mv, base, ctx)
+    flat = mv.IndexFlat(D, mv.METRIC_L2, ctx=ctx)
+    flat.add(base)
+    _, gt = flat.search(queries, k)
+    del flat
+    setup_s = time.perf_counter() - t0
+    d_q = torch.from_numpy(queries).cuda()
+    d_dist = torch.empty((nq, k), dtype=torch.float32, device="cuda")
+    d_lab = torch.empty((nq, k), dtype=torch.int64, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    res = {}
+    for name, form in (("fast", mv.FORM_FAST), ("plain", mv.FORM_PLAIN)):
+        def step(form=form):
+            ix.search_device(d_q.data_ptr(), nq, k, d_dist.data_ptr(), d_lab.data_ptr(),
+                             stream=stream.cuda_stream, nprobe=nprobe, form=form)
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        lab = d_lab.cpu().numpy()
+        if name == "plain":
+            clocks = ClockSampler(dev)
+            clocks.start()
+            launches0 = ctx.kernel_launches()
+        torch.cuda.nvtx.range_push(f"timed_ivfflat_{name}")
+        ms = _timed_steps(torch, step, args.steps, stream, flush) / args.steps
+        torch.cuda.nvtx.range_pop()
+        if name == "plain":
+            launches = ctx.kernel_launches() - launches0
+            clk = clocks.stop()
+            ctx.profile(True)
+            _timed_steps(torch, step, args.steps, stream, flush)
+            stage = ctx.stage_times()
+            ctx.profile(False)
+        res[name] = {"ms": _max_over_ranks(torch, world, ms), "labels": lab}
+    value = world * nq / (res["plain"]["ms"] / 1e3)
+    pinned = torch.empty((nq, D), dtype=torch.float32).pin_memory()
+    pinned.copy_(torch.from_numpy(queries))
+    hq = pinned.numpy()
+    ix.search(hq, k, nprobe=nprobe)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _, elab = ix.search(hq, k, nprobe=nprobe)
+    e2e_qps = world * nq * args.steps / _max_over_ranks(torch, world, time.perf_counter() - t0)
+    assert np.array_equal(elab, res["plain"]["labels"]), "host and device searches disagree"
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    scan_ms, scan_n = stage.get("scan", (0.0, 0))
+    per_launch = scan_ms / max(scan_n, 1)
+    mean_list = nb / NLIST
+    alg_bytes = nq * nprobe * mean_list * D * 4
+    achieved = alg_bytes / (per_launch / 1e3) / 1e9 if per_launch > 0 else 0.0
+    out = {
+        "metric": IVFFLAT_METRIC, "value": round(value, 1), "unit": "queries/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(res["plain"]["ms"], 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic SIFT-like (seeded Gaussian mixture, integer-valued), not SIFT1M",
+        "config": {
+            "workload": f"ivfflat_{nb}x128_nlist{NLIST}_nprobe{nprobe}_nq{nq}_k{k}",
+            "train_rows": IVFFLAT_TRAIN, "train_niter": IVFFLAT_NITER,
+            "recall_at_10_vs_exact": round(recall_at(gt, res["plain"]["labels"], k), 4),
+            "fast_form_qps": round(world * nq / (res["fast"]["ms"] / 1e3), 1),
+            "fast_form_recall_at_10": round(recall_at(gt, res["fast"]["labels"], k), 4),
+            "fast_form": "BF16 two-pass tcgen05 coarse + FP32 recheck, same exact list scan",
+            "l2_policy": "rows (512 MB) larger than L2, plus a 256 MiB flush per step",
+            "parallelism": f"replicas x{world}", "setup_s": round(setup_s, 1),
+        },
+        "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s",
+                "h2d_bytes_per_step": nq * D * 4, "d2h_bytes_per_step": nq * k * 12},
+        "gpu_launches": int(launches),
+        "roofline": {
+            "bound": "hbm", "kernel": "k_ivfflat_scan (exact FP32 list scan)",
+            "achieved": round(achieved, 1), "peak": hbm,
+            "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "unit": "GB/s",
+            "frac": round(achieved / hbm, 4), "traffic": None,
+            "algorithmic_bytes_per_launch": int(alg_bytes),
+            "note": "row bytes of the probed lists, mean-list approximation (nb / nlist rows each)",
+            "launch_ms": round(per_launch, 4),
+        },
+        "stages_ms_per_step": {kk: round(v[0] / args.steps, 4) for kk, v in stage.items()},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as orc
+
+        threads = os.cpu_count() or 1
+        ref = orc.IVFFlat(D, NLIST, 0)
+        ref.train(base[:IVFFLAT_TRAIN], niter=IVFFLAT_NITER, nthreads=threads)
+        ref.add(base, nthreads=threads)
+        sample = min(args.cpu_sample // 2, nq)
+        ref.search(queries[:4], k, nprobe, nthreads=threads)
+        t0 = time.perf_counter()
+        _, clab = ref.search(queries[:sample], k, nprobe, nthreads=threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {
+            "value": round(sample / dt, 1), "unit": "queries/s", "cores": threads, "kind": "port",
+            "sample": f"{sample} of the {nq} queries; index trained and filled by the oracle on "
+                      f"the CPU; query-parallel on {threads} threads",
+            "ids_equal_to_gpu_plain": bool(np.array_equal(clab, res["plain"]["labels"][:sample])),
+        }
+    return out
+
+
+def _rerank_workload(mv, nb, nq, k, ctx=None):
+    base, queries = build_workload(nb, nq)
+    flat = mv.IndexFlat(D, mv.METRIC_L2, **({"ctx": ctx} if ctx else {}))
+    flat.add(base)
+    rng = np.random.default_rng(np.random.SeedSequence(20261203).spawn(8)[5])
+    # the shortlist: the 2k nearest rows in a random order (as a graph walk
+    # would hand them over)
+    _, cand = flat.search(queries, 2 * k)
+    cand = np.take_along_axis(cand, rng.permuted(np.tile(np.arange(2 * k), (nq, 1)), axis=1), 1)
+    return base, queries, flat, np.ascontiguousarray(cand, np.int64)
+
+
+def run_rerank(args, rank, world):
+    """The exact rerank service for a shortlist (index/index_hnsw.mojo:433-497)."""
+    import torch
+
+    import mojovec_gb300 as mv
+
+    nq, k = args.nq, K
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    ctx = mv.Context(dev)
+    base, queries, flat, cand = _rerank_workload(mv, args.nb, nq, k, ctx)
+    ncand = cand.shape[1]
+    d_q = torch.from_numpy(queries).cuda()
+    d_c = torch.from_numpy(cand).cuda()
+    d_dist = torch.empty((nq, k), dtype=torch.float32, device="cuda")
+    d_lab = torch.empty((nq, k), dtype=torch.int64, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step():
+        flat.rerank_device(d_q.data_ptr(), nq, d_c.data_ptr(), ncand, k, d_dist.data_ptr(),
+                           d_lab.data_ptr(), stream=stream.cuda_stream)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    lab = d_lab.cpu().numpy()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    l0 = ctx.kernel_launches()
+    torch.cuda.nvtx.range_push("timed_rerank")
+    ms = _timed_steps(torch, step, args.steps, stream, flush) / args.steps
+    torch.cuda.nvtx.range_pop()
+    launches = ctx.kernel_launches() - l0
+    clk = clocks.stop()
+    ms = _max_over_ranks(torch, world, ms)
+    hd, hl = flat.rerank(queries, cand, k)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        hd, hl = flat.rerank(queries, cand, k)
+    e2e_qps = world * nq * args.steps / _max_over_ranks(torch, world, time.perf_counter() - t0)
+    assert np.array_equal(hl, lab), "host and device reranks disagree"
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    alg = nq * ncand * D * 4
+    achieved = alg / (ms / 1e3) / 1e9
+    out = {
+        "metric": RERANK_METRIC, "value": round(world * nq / (ms / 1e3), 1), "unit": "queries/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic SIFT-like rows; shortlists are each query's 20 nearest rows, shuffled",
+        "config": {"workload": f"rerank_{args.nb}x128_nq{nq}_ncand{ncand}_k{k}",
+                   "parallelism": f"replicas x{world}",
+                   "l2_policy": "rows (512 MB) larger than L2, plus a 256 MiB flush per step"},
+        "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s",
+                "h2d_bytes_per_step": nq * D * 4 + nq * ncand * 8, "d2h_bytes_per_step": nq * k * 12},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "k_rerank_simd64 (whole step)",
+                     "achieved": round(achieved, 1), "peak": hbm,
+                     "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                     "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": None,
+                     "algorithmic_bytes_per_launch": int(alg),
+                     "note": "candidate rows gathered (nq x 2k x d x 4 bytes); latency-bound at this size"},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as orc
+
+        threads = os.cpu_count() or 1
+        sample = min(nq, 2000)
+        orc.rerank(base, queries[:4], cand[:4], k, nthreads=threads)
+        t0 = time.perf_counter()
+        _, clab = orc.rerank(base, queries[:sample], cand[:sample], k, nthreads=threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {
+            "value": round(sample / dt, 1), "unit": "queries/s", "cores": threads, "kind": "port",
+            "sample": f"{sample} of the {nq} queries, query-parallel on {threads} threads",
+            "ids_equal_to_gpu": bool(np.array_equal(clab, lab[:sample])),
+        }
+    return out
+
+
+def run_reference_ivfflat(args):
+    """The oracle's IVF-Flat (same training recipe) on a bounded query sample."""
+    from oracle import oracle as orc
+
+    threads = os.cpu_count() or 1
+    base, queries = build_workload(args.nb, args.nq)
+    ref = orc.IVFFlat(D, NLIST, 0)
+    ref.train(base[:IVFFLAT_TRAIN], niter=IVFFLAT_NITER, nthreads=threads)
+    ref.add(base, nthreads=threads)
+    sample = min(max(args.cpu_sample // 2, 1), args.nq)
+    for _ in range(args.warmup):
+        ref.search(queries[:4], K, args.nprobe, nthreads=threads)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        ref.search(queries[:sample], K, args.nprobe, nthreads=threads)
+    total = time.perf_counter() - t
+    qps = sample * args.steps / total
+    return _reference_line(args, IVFFLAT_METRIC, qps, total, threads,
+                           f"ivfflat_{args.nb}x128_nlist{NLIST}_nprobe{args.nprobe}_nq{args.nq}_k{K}",
+                           f"{sample} queries per step, query-parallel on {threads} threads")
+
+
+def run_reference_rerank(args):
+    """The oracle's rerank (l2_distance_simd[64] semantics) on a bounded sample."""
+    import mojovec_gb300  # noqa: F401  (synthetic data generator only)
+    from oracle import oracle as orc
+
+    threads = os.cpu_count() or 1
+    base, queries = build_workload(args.nb, args.nq)
+    rng = np.random.default_rng(np.random.SeedSequence(20261203).spawn(8)[5])
+    sample = min(args.nq, 2000)
+    q = queries[:sample]
+    # shortlists: the 20 nearest rows by the oracle's exact search, shuffled
+    _, cand = orc.flat_search(base, q, 2 * K, nthreads=threads)
+    cand = np.ascontiguousarray(np.take_along_axis(
+        cand, rng.permuted(np.tile(np.arange(2 * K), (sample, 1)), axis=1), 1), np.int64)
+    for _ in range(args.warmup):
+        orc.rerank(base, q[:4], cand[:4], K, nthreads=threads)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        orc.rerank(base, q, cand, K, nthreads=threads)
+    total = time.perf_counter() - t
+    qps = sample * args.steps / total
+    return _reference_line(args, RERANK_METRIC, qps, total, threads,
+                           f"rerank_{args.nb}x128_nq{args.nq}_ncand{2 * K}_k{K}",
+                           f"{sample} queries per step, query-parallel on {threads} threads")
+
+
+def _reference_line(args, metric, qps, total, threads, workload, sample):
+    return {
+        "metric": metric, "impl": "reference", "value": round(qps, 1), "unit": "queries/s",
+        "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * total / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic SIFT-like (seeded Gaussian mixture, integer-valued), not SIFT1M",
+        "config": {"workload": workload, "form": "reference CPU path (oracle port)"},
+        "cpu_baseline": {"value": round(qps, 1), "unit": "queries/s", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(qps, 1), "unit": "queries/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
 def run_reference_flat(args):
     """The oracle's IndexFlat search over all rows for a bounded query sample."""
     from oracle import oracle as orc
@@ -1153,7 +1448,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=500)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="ivfpq",
-                    choices=["ivfpq", "flat", "sq8", "kmeans", "batch", "serve", "curve"])
+                    choices=["ivfpq", "flat", "sq8", "kmeans", "batch", "serve", "curve", "ivfflat",
+                             "rerank"])
     ap.add_argument("--batch-nb", type=int, default=10_000_000)
     ap.add_argument("--serve-scale", type=float, default=1.0)
     ap.add_argument("--serve-requests", type=int, default=300)
@@ -1176,7 +1472,14 @@ def main():
 
     if args.impl == "reference":
         if rank == 0:
-            ref = run_reference_flat(args) if args.workload in ("flat", "sq8") else run_reference(args)
+            if args.workload in ("flat", "sq8"):
+                ref = run_reference_flat(args)
+            elif args.workload == "ivfflat":
+                ref = run_reference_ivfflat(args)
+            elif args.workload == "rerank":
+                ref = run_reference_rerank(args)
+            else:
+                ref = run_reference(args)
             print(json.dumps(ref), flush=True)
         return
 
@@ -1194,6 +1497,10 @@ def main():
         out = run_curve(args, rank, world)
     elif args.workload in ("flat", "sq8"):
         out = run_flat(args, rank, world)
+    elif args.workload == "ivfflat":
+        out = run_ivfflat(args, rank, world)
+    elif args.workload == "rerank":
+        out = run_rerank(args, rank, world)
     else:
         out = run_gpu(args, rank, world)
     if rank == 0:

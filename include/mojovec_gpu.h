@@ -294,6 +294,11 @@ int32_t mv_ivfflat_add_with_ids(mv_ivfflat* index, const float* x, const int64_t
  * bit-exact; FAST takes the probes from the BF16 coarse step. */
 int32_t mv_ivfflat_search(mv_ivfflat* index, const float* x, int64_t nq, int32_t k,
                           const mv_search_params* params, float* distances, int64_t* labels);
+/* Same with device buffers, enqueued on `stream` (null: the call's own
+ * stream, synchronised). */
+int32_t mv_ivfflat_search_device(mv_ivfflat* index, const float* d_x, int64_t nq, int32_t k,
+                                 const mv_search_params* params, float* d_distances,
+                                 int64_t* d_labels, void* stream);
 
 /* ---- Flat index: replaces IndexFlat (index/index_flat.mojo:117-330) ---- */
 int32_t mv_flat_create(mv_ctx* ctx, int32_t d, int32_t metric, mv_flat** out);
@@ -313,6 +318,12 @@ int32_t mv_flat_search(mv_flat* index, const float* x, int64_t nq, int32_t k,
  * 0.0 / -1, IP un-negated. */
 int32_t mv_flat_rerank(mv_flat* index, const float* x, int64_t nq, const int64_t* cand,
                        int32_t ncand, int32_t k, float* distances, int64_t* labels);
+/* mv_flat_rerank with device buffers (index_hnsw.mojo:433-497 semantics),
+ * enqueued on `stream` (null: synchronised). Candidate ids outside
+ * [0, ntotal) count as empty slots (the host variant rejects them). */
+int32_t mv_flat_rerank_device(mv_flat* index, const float* d_x, int64_t nq, const int64_t* d_cand,
+                              int32_t ncand, int32_t k, float* d_distances, int64_t* d_labels,
+                              void* stream);
 int32_t mv_flat_search_device(mv_flat* index, const float* d_x, int64_t nq, int32_t k,
                               const uint8_t* d_filter, const mv_search_params* params,
                               float* d_distances, int64_t* d_labels, void* stream);

@@ -106,6 +106,7 @@ SIGNATURES = {
     "mv_flat_ntotal": (_i64, [_vp]),
     "mv_flat_search": (_i32, [_vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp]),
     "mv_flat_rerank": (_i32, [_vp, _vp, _i64, _vp, _i32, _i32, _vp, _vp]),
+    "mv_flat_rerank_device": (_i32, [_vp, _vp, _i64, _vp, _i32, _i32, _vp, _vp, _vp]),
     "mv_flat_search_device": (_i32, [_vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _vp]),
     "mv_sq8_create": (_i32, [_vp, _i32, _i32, C.POINTER(_vp)]),
     "mv_sq8_destroy": (_i32, [_vp]),
@@ -135,6 +136,7 @@ SIGNATURES = {
     "mv_ivfflat_add": (_i32, [_vp, _vp, _i64]),
     "mv_ivfflat_add_with_ids": (_i32, [_vp, _vp, _vp, _i64]),
     "mv_ivfflat_search": (_i32, [_vp, _vp, _i64, _i32, _vp, _vp, _vp]),
+    "mv_ivfflat_search_device": (_i32, [_vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp]),
     "mv_server_create": (_i32, [_vp, _i64, _i32, _i64, _vp]),
     "mv_server_destroy": (_i32, [_vp]),
     "mv_server_add_ivfpq": (_i32, [_vp, _vp, _vp, _vp]),

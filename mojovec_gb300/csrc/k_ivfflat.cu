@@ -4,10 +4,13 @@
 // widths), into the canonical top-k (distance, then the smaller id); tail
 // 1e38 / -1 and IP un-negated (:199-203, :241-243).
 //
-// One CTA per query. Candidate rows are staged through shared memory in
-// tiles of TR rows loaded with coalesced reads (row stride d + 1 floats, so
-// thread t reading row t touches its own bank); thread t then computes row
-// t's distance with the same per-thread, in-order routine as the oracle.
+// One CTA of FT threads per query (several CTAs per SM, so one CTA's loads
+// overlap another's arithmetic). Candidate rows are staged through shared
+// memory in tiles of up to FT rows, each warp reading 8 rows at a time with
+// coalesced (float4 where d allows) loads all issued before the stores, at a
+// row stride of d + 1 floats so that thread t
+// reading row t touches its own bank; thread t then computes row t's
+// distance with the same per-thread, in-order routine as the oracle.
 #include "mv_exact.cuh"
 #include "mv_internal.h"
 #include "mv_kernels.h"
@@ -16,8 +19,8 @@
 namespace mv {
 namespace {
 
-constexpr int FT = 256;
-constexpr int TOP_BUF = 512;
+constexpr int FT = 64;
+constexpr int TOP_BUF = 256;
 
 template <bool IP>
 __global__ void __launch_bounds__(FT)
@@ -46,9 +49,36 @@ __global__ void __launch_bounds__(FT)
       const int nr = ls - j0 < tr ? (int)(ls - j0) : tr;
       __syncthreads();  // the previous tile is consumed
       const float* src = rows + (off + j0) * d;
-      for (int e = threadIdx.x; e < nr * d; e += FT) {
-        const int r = e / d;
-        tile[r * stride + (e - r * d)] = src[e];
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      if ((d & 3) == 0) {
+        // UR rows per warp per step: all of their loads are issued before
+        // the stores, so each warp keeps UR row slices in flight.
+        constexpr int UR = 8;
+        for (int r0 = warp * UR; r0 < nr; r0 += (FT / 32) * UR) {
+          for (int c4 = lane; c4 < (d >> 2); c4 += 32) {
+            float4 v[UR];
+#pragma unroll
+            for (int u = 0; u < UR; ++u)
+              v[u] = r0 + u < nr ? __ldg(reinterpret_cast<const float4*>(src + (int64_t)(r0 + u) * d) + c4)
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int u = 0; u < UR; ++u) {
+              if (r0 + u < nr) {
+                float* t = tile + (r0 + u) * stride + 4 * c4;
+                t[0] = v[u].x;
+                t[1] = v[u].y;
+                t[2] = v[u].z;
+                t[3] = v[u].w;
+              }
+            }
+          }
+        }
+      } else {
+        for (int r = warp; r < nr; r += FT / 32) {
+          const float* sr = src + (int64_t)r * d;
+          float* t = tile + r * stride;
+          for (int c = lane; c < d; c += 32) t[c] = __ldg(sr + c);
+        }
       }
       __syncthreads();
       for (int r0 = 0; r0 < nr; r0 += FT) {

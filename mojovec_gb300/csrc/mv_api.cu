@@ -1650,6 +1650,29 @@ int32_t mv_flat_search_device(mv_flat* ix, const float* d_x, int64_t nq, int32_t
   });
 }
 
+int32_t mv_flat_rerank_device(mv_flat* ix, const float* d_x, int64_t nq, const int64_t* d_cand,
+                              int32_t ncand, int32_t k, float* d_distances, int64_t* d_labels,
+                              void* stream) {
+  if (!ix || nq < 0 || ncand < 0 || (nq > 0 && (!d_x || !d_distances || !d_labels)) ||
+      (nq > 0 && ncand > 0 && !d_cand))
+    return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    check_search_args(nq, k);
+    if (nq == 0) return;
+    SlotLease lease(ix->ctx);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : lease.stream();
+    lease.use(s);
+    DevBuf& ws = lease.slot->ws;
+    ws.ensure(ws_bytes((size_t)nq * k, 8));
+    Arena ar(ws);
+    uint64_t* keys = ar.take<uint64_t>((size_t)nq * k);
+    launch_rerank_simd64(d_x, nq, ix->d, ix->rows.as<float>(), ix->ntotal, ix->metric, d_cand,
+                         ncand, k, keys, s);
+    launch_keys_to_results(keys, nq, k, 0.0f, ix->metric == MV_METRIC_IP, d_distances, d_labels, s);
+    if (!stream) check_kernel_errors(ix->ctx, s);
+  });
+}
+
 int32_t mv_flat_rerank(mv_flat* ix, const float* x, int64_t nq, const int64_t* cand,
                        int32_t ncand, int32_t k, float* distances, int64_t* labels) {
   if (!ix || nq < 0 || ncand < 0 || (nq > 0 && (!x || !distances || !labels)) ||
@@ -2869,6 +2892,23 @@ int32_t mv_ivfflat_search(mv_ivfflat* ix, const float* x, int64_t nq, int32_t k,
     d2h(distances, dd, sizeof(float) * nq * k, s);
     d2h(labels, dl, sizeof(int64_t) * nq * k, s);
     check_kernel_errors(ix->ctx, s);
+  });
+}
+
+int32_t mv_ivfflat_search_device(mv_ivfflat* ix, const float* d_x, int64_t nq, int32_t k,
+                                 const mv_search_params* params, float* d_distances,
+                                 int64_t* d_labels, void* stream) {
+  if (!ix || (nq > 0 && (!d_x || !d_distances || !d_labels))) return MV_ERR_ARG;
+  return guard(ix->ctx, [&] {
+    check_search_args(nq, k);
+    if (nq == 0) return;
+    int nprobe = params && params->nprobe > 0 ? params->nprobe : ix->nprobe;
+    nprobe = std::min(nprobe, ix->nlist);
+    SlotLease lease(ix->ctx);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : lease.stream();
+    lease.use(s);
+    ivfflat_search(ix, d_x, nq, k, nprobe, params, d_distances, d_labels, lease.slot->ws, s);
+    if (!stream) check_kernel_errors(ix->ctx, s);
   });
 }
 

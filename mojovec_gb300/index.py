@@ -364,6 +364,12 @@ class IndexIVFFlat:
         check(_lib.load().mv_ivfflat_search(self._h, _p(x), n, k, C.byref(p), _p(dist), _p(lab)))
         return dist, lab
 
+    def search_device(self, x_ptr: int, n: int, k: int, dist_ptr: int, lab_ptr: int,
+                      stream: int = 0, nprobe: int = 0, form=None):
+        p = _params(form, nprobe)
+        check(_lib.load().mv_ivfflat_search_device(self._h, x_ptr, n, k, C.byref(p), dist_ptr,
+                                                   lab_ptr, stream or None))
+
 
 class IndexFlat:
     """Exact index over raw FP32 rows (index/index_flat.mojo:117)."""
@@ -426,6 +432,12 @@ class IndexFlat:
                       e4m3: bool = False):
         p = _params(form, 0, rerank, plain_scan=plain_scan, e4m3=e4m3)
         check(_lib.load().mv_flat_search_device(self._h, x_ptr, n, k, None, C.byref(p), dist_ptr,
+                                                lab_ptr, stream or None))
+
+    def rerank_device(self, x_ptr: int, n: int, cand_ptr: int, ncand: int, k: int, dist_ptr: int,
+                      lab_ptr: int, stream: int = 0):
+        """rerank with device buffers (n x ncand int64 candidate ids)."""
+        check(_lib.load().mv_flat_rerank_device(self._h, x_ptr, n, cand_ptr, ncand, k, dist_ptr,
                                                 lab_ptr, stream or None))
 
 

@@ -96,3 +96,33 @@ def test_ivfflat_reference_known_answers(mv):
     d, l = t.search(z, 5)
     assert l[0].tolist() == [42, -1, -1, -1, -1]
     assert d[0, 0] == 0.0 and (d[0, 1:] == 1e38).all()
+
+
+def test_device_entry_points_match_host_calls(mv):
+    """mv_ivfflat_search_device and mv_flat_rerank_device (device buffers,
+    caller stream) return the host-buffer calls' bits."""
+    torch = pytest.importorskip("torch")
+    x = (RNG.standard_normal((6000, 48)) * 2).astype(np.float32)
+    q = (RNG.standard_normal((70, 48)) * 2).astype(np.float32)
+    g = mv.IndexIVFFlat(48, 32, 0)
+    g.train(x[:3000])
+    g.add(x)
+    dq = torch.from_numpy(q).cuda()
+    dd = torch.empty((70, 10), dtype=torch.float32, device="cuda")
+    dl = torch.empty((70, 10), dtype=torch.int64, device="cuda")
+    s = torch.cuda.current_stream()
+    for form in (mv.FORM_PLAIN, mv.FORM_FAST):
+        hd, hl = g.search(q, 10, nprobe=5, form=form)
+        g.search_device(dq.data_ptr(), 70, 10, dd.data_ptr(), dl.data_ptr(), stream=s.cuda_stream,
+                        nprobe=5, form=form)
+        torch.cuda.synchronize()
+        assert np.array_equal(dl.cpu().numpy(), hl) and _same(dd.cpu().numpy(), hd)
+    f = mv.IndexFlat(48, 1)
+    f.add(x)
+    cand = RNG.integers(-1, 6000, size=(70, 24)).astype(np.int64)
+    hd, hl = f.rerank(q, cand, 10)
+    dc = torch.from_numpy(cand).cuda()
+    f.rerank_device(dq.data_ptr(), 70, dc.data_ptr(), 24, 10, dd.data_ptr(), dl.data_ptr(),
+                    stream=s.cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(dl.cpu().numpy(), hl) and _same(dd.cpu().numpy(), hd)
