@@ -447,6 +447,35 @@ __device__ __forceinline__ uint64_t coarse_lists_smallest(const uint64_t* __rest
   return v[0];
 }
 
+// Per-row lists of the two-pass coarse GEMM -> the row's nc smallest keys,
+// sorted, in out[row * ncp + j] (KEY_NONE past nc or past the row's keys),
+// one warp per row.
+__global__ void __launch_bounds__(CR_WARPS * 32)
+    k_lists_smallest(const uint64_t* __restrict__ lists, const int* __restrict__ counts, int nseg,
+                     int cap, int64_t nq, int nc, int ncp, uint64_t* __restrict__ out) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * CR_WARPS + warp;
+  if (row >= nq) return;
+  const int c = lane < nseg ? min(max(counts[row * nseg + lane], 0), cap) : 0;
+  int incl = c;
+#pragma unroll
+  for (int o = 1; o < 4; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int o1 = __shfl_sync(0xffffffffu, incl, 0);
+  const int o2 = nseg > 1 ? __shfl_sync(0xffffffffu, incl, 1) : 1 << 30;
+  const int o3 = nseg > 2 ? __shfl_sync(0xffffffffu, incl, 2) : 1 << 30;
+  const int n = __shfl_sync(0xffffffffu, incl, nseg - 1);
+  const int p1 = nseg > 1 ? o1 : 1 << 30;
+  uint64_t best;
+  if (n <= 32) best = coarse_lists_smallest<1>(lists, row, nseg, cap, n, p1, o2, o3);
+  else if (n <= 64) best = coarse_lists_smallest<2>(lists, row, nseg, cap, n, p1, o2, o3);
+  else if (n <= 128) best = coarse_lists_smallest<4>(lists, row, nseg, cap, n, p1, o2, o3);
+  else best = coarse_lists_smallest<8>(lists, row, nseg, cap, n, p1, o2, o3);
+  if (lane < ncp) out[row * ncp + lane] = lane < nc ? best : KEY_NONE;
+}
+
 // Per-row lists of the two-pass coarse GEMM -> the nc smallest keys, their
 // exact FP32 distances and the nprobe nearest lists, one warp per query (the
 // same selection and recheck as k_coarse_rows; nseg <= 4, nseg * cap <= 256,
@@ -1229,6 +1258,17 @@ void launch_coarse_rows(const float* approx, int64_t nq, int nlist, const float*
              "coarse rows: nc must be in [nprobe, min(64, nlist)]");
   k_coarse_rows<<<(unsigned)((nq + CR_WARPS - 1) / CR_WARPS), CR_WARPS * 32, 0, s>>>(
       approx, nq, nlist, q, d, cent, metric, nc, nprobe, probes, term, err);
+  count_launch();
+  MV_CHECK_CUDA(cudaGetLastError());
+}
+
+void launch_lists_smallest(const uint64_t* lists, const int* counts, int nseg, int cap, int64_t nq,
+                           int nc, uint64_t* out, cudaStream_t s) {
+  if (nq == 0) return;
+  MV_REQUIRE((int64_t)nseg * cap <= CR_CAP && nseg <= 4 && nc >= 1 && nc <= 32, MV_ERR_INTERNAL,
+             "lists smallest: too many keys per row");
+  k_lists_smallest<<<(unsigned)((nq + CR_WARPS - 1) / CR_WARPS), CR_WARPS * 32, 0, s>>>(
+      lists, counts, nseg, cap, nq, nc, next_pow2(nc), out);
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());
 }

@@ -505,25 +505,46 @@ bool coarse_topp_certified(mv_ctx* ctx, const float* d_q, int64_t nq, int d, con
   if (nc > UMMA_TOPK_MAX || nc >= nlist || umma_kpad(d) > UMMA_TOPK_MAX_K || nq > 0x7fffffffll) return false;
   const int kp = umma_kpad(d), ncp = next_pow2(nc);
   const int64_t qb = std::min<int64_t>(nq, 65536);
-  const int nseg = umma_topk_nseg(qb, nlist, d, nc, ctx->num_sms);
-  const int osegs = nseg * umma_topk_groups(d, nc);
+  // Candidates: the two-pass GEMM's lists reduced to each row's nc smallest
+  // keys (nc <= 32, d <= 256), else the heap epilogue's per-segment keys;
+  // either way a superset of the row's nc smallest approximate keys.
+  const bool twopass = nc <= 32 && kp <= 256;
+  const int nseg = twopass ? coarse_topk2_nseg(qb, nlist, d, nc, ctx->num_sms)
+                           : umma_topk_nseg(qb, nlist, d, nc, ctx->num_sms);
+  const int osegs = twopass ? 1 : nseg * umma_topk_groups(d, nc);
+  const int lcap = twopass ? coarse_topk2_cap(nc) : 0;
   if ((int64_t)osegs * ncp > 256) return false;
-  DevBuf buf;
+  // Scratch from a leased slot (grow-only, reused across calls), bound to s.
+  SlotLease lease(ctx);
+  lease.use(s);
+  DevBuf& buf = lease.slot->ws;
   buf.ensure(ws_bytes((size_t)qb * kp, 2) + ws_bytes((size_t)qb * osegs * ncp, 8) +
-             2 * ws_bytes((size_t)qb, 8) + ws_bytes(1, 4));
+             2 * ws_bytes((size_t)qb, 8) + ws_bytes(1, 4) +
+             (twopass ? ws_bytes((size_t)qb * nseg * lcap, 8) + ws_bytes((size_t)qb * nseg, 4) +
+                            ws_bytes((size_t)qb, 4)
+                      : 0));
   Arena ar(buf);
   __nv_bfloat16* xb = ar.take<__nv_bfloat16>((size_t)qb * kp);
   uint64_t* cand = ar.take<uint64_t>((size_t)qb * osegs * ncp);
   uint64_t* gthr = ar.take<uint64_t>((size_t)qb);
   int64_t* flagged = ar.take<int64_t>((size_t)qb);
   int* nflag = ar.take<int>(1);
+  uint64_t* lists = twopass ? ar.take<uint64_t>((size_t)qb * nseg * lcap) : nullptr;
+  int* counts = twopass ? ar.take<int>((size_t)qb * nseg) : nullptr;
+  uint32_t* lthr = twopass ? ar.take<uint32_t>((size_t)qb) : nullptr;
   int64_t fallback = 0;
   for (int64_t q0 = 0; q0 < nq; q0 += qb) {
     const int64_t nb = std::min(qb, nq - q0);
     const float* xr = d_q + q0 * d;
     launch_to_bf16(xr, nb, d, xb, nullptr, s);
-    launch_umma_topk(xb, nb, cent_bf16, nlist, d, metric, nullptr, cnorm, nc, nseg, nullptr,
-                     osegs > 1 ? gthr : nullptr, cand, ctx->d_err.as<int>(), s);
+    if (twopass) {
+      launch_coarse_topk2(xb, nb, cent_bf16, nlist, d, metric, cnorm, nc, nseg, lists, counts, lthr,
+                          ctx->d_err.as<int>(), s);
+      launch_lists_smallest(lists, counts, nseg, lcap, nb, nc, cand, s);
+    } else {
+      launch_umma_topk(xb, nb, cent_bf16, nlist, d, metric, nullptr, cnorm, nc, nseg, nullptr,
+                       osegs > 1 ? gthr : nullptr, cand, ctx->d_err.as<int>(), s);
+    }
     MV_CHECK_CUDA(cudaMemsetAsync(nflag, 0, sizeof(int), s));
     launch_topp_certify(xr, nb, d, cent, nlist, metric, cand, osegs * ncp, nc, P, ccert,
                         probes + q0 * P, flagged, nflag, s);

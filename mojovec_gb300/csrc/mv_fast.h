@@ -73,6 +73,10 @@ void launch_rerank_rows(const float* raw, int64_t n, int d, __nv_bfloat16* raw16
 
 // Two-pass coarse GEMM lists (launch_coarse_topk2) -> the nprobe nearest
 // lists, as launch_coarse_rows (one warp per query; nseg * cap <= 256).
+// The same lists -> each row's nc (<= 32) smallest keys, sorted, padded with
+// KEY_NONE to next_pow2(nc) per row.
+void launch_lists_smallest(const uint64_t* lists, const int* counts, int nseg, int cap, int64_t nq,
+                           int nc, uint64_t* out, cudaStream_t s);
 void launch_coarse_lists(const uint64_t* lists, const int* counts, int nseg, int cap, int64_t nq,
                          int nlist, const float* q, int d, const float* cent, int metric, int nc,
                          int nprobe, int32_t* probes, float* term, int* err, cudaStream_t s);
