@@ -269,7 +269,9 @@ __device__ int block_radix_select(const uint64_t* keys, int n, int R, uint64_t* 
 }
 
 // Same selection over keys stored as two word arrays, key = (hi << 32) | lo
-// (hi: ordered distance, lo: payload). Histogram passes whose digit lies in
+// (hi: ordered distance, lo: payload), with 8-bit digits: 256-bin passes are
+// cheaper to clear and scan than 2048-bin ones, and measured faster for the
+// fast IVF-PQ shortlist (256 of about 2 000 keys). Histogram passes whose digit lies in
 // the high word read 4 bytes per key; the low word is read only when
 // distances tie down to the last bit. Histogram updates are aggregated per
 // warp (one atomic per distinct digit).
@@ -315,7 +317,7 @@ __device__ int block_radix_select_soa(const uint32_t* khi, const uint32_t* klo, 
   unsigned long long prefix = shift >= 64 ? 0ull : (lo >> shift) << shift;
   int need = R;
   while (shift > 0) {
-    const int bits = shift < 11 ? shift : 11;
+    const int bits = shift < 8 ? shift : 8;
     const int nb = 1 << bits;
     shift -= bits;
     const int top = shift + bits;
