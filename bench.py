@@ -1201,12 +1201,14 @@ def run_ivfflat(args, rank, world):
                 "h2d_bytes_per_step": nq * D * 4, "d2h_bytes_per_step": nq * k * 12},
         "gpu_launches": int(launches),
         "roofline": {
-            "bound": "hbm", "kernel": "k_ivfflat_scan (exact FP32 list scan)",
+            "bound": "hbm", "kernel": "k_lm_scan (exact FP32 list-major scan) + count/place/merge",
             "achieved": round(achieved, 1), "peak": hbm,
             "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "unit": "GB/s",
             "frac": round(achieved / hbm, 4), "traffic": None,
             "algorithmic_bytes_per_launch": int(alg_bytes),
-            "note": "row bytes of the probed lists, mean-list approximation (nb / nlist rows each)",
+            "note": ("row bytes of the probed lists per query, mean-list approximation (nb / nlist "
+                     "rows each); the list-major scan reads each list once per 8 of its queries, "
+                     "so DRAM traffic is below these algorithmic bytes"),
             "launch_ms": round(per_launch, 4),
         },
         "stages_ms_per_step": {kk: round(v[0] / args.steps, 4) for kk, v in stage.items()},

@@ -366,64 +366,6 @@ __global__ void __launch_bounds__(CR_WARPS * 32)
   coarse_recheck_warp(B, row, q, d, cent, nlist, metric, nc, nprobe, probes, term, err);
 }
 
-// Ascending bitonic sort of the warp's 32 * RR keys held in registers,
-// element r * 32 + lane in v[r] of that lane: cross-lane steps by xor
-// shuffles, in-lane steps between registers (all indices static).
-template <int RR>
-__device__ __forceinline__ void warp_sort_regs(uint64_t (&v)[RR]) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int k = 2; k <= 32 * RR; k <<= 1) {
-#pragma unroll
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      if (j >= 32) {
-        const int jr = j >> 5;
-#pragma unroll
-        for (int r = 0; r < RR; ++r) {
-          if (r & jr) continue;
-          const int r2 = r | jr;
-          const bool up = (((r << 5) | lane) & k) == 0;
-          const uint64_t a = v[r], b = v[r2];
-          const bool sw = (a > b) == up;
-          v[r] = sw ? b : a;
-          v[r2] = sw ? a : b;
-        }
-      } else {
-        const bool low = (lane & j) == 0;
-#pragma unroll
-        for (int r = 0; r < RR; ++r) {
-          const bool up = (((r << 5) | lane) & k) == 0;
-          const uint64_t a = v[r];
-          const uint64_t b = __shfl_xor_sync(0xffffffffu, a, j);
-          const bool keep_min = low == up;
-          v[r] = keep_min ? (a < b ? a : b) : (a < b ? b : a);
-        }
-      }
-    }
-  }
-}
-
-// Sorts a bitonic sequence of 32 keys (one per lane) ascending.
-__device__ __forceinline__ uint64_t warp_bitonic_merge32(uint64_t a) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int j = 16; j > 0; j >>= 1) {
-    const uint64_t b = __shfl_xor_sync(0xffffffffu, a, j);
-    const bool low = (lane & j) == 0;
-    a = low ? (a < b ? a : b) : (a < b ? b : a);
-  }
-  return a;
-}
-
-// best (ascending across lanes) <- the 32 smallest of best and v (any order).
-__device__ __forceinline__ uint64_t warp_merge_smallest32(uint64_t best, uint64_t v) {
-  const int lane = threadIdx.x & 31;
-  uint64_t t[1] = {v};
-  warp_sort_regs<1>(t);
-  const uint64_t r = __shfl_sync(0xffffffffu, t[0], 31 - lane);
-  return warp_bitonic_merge32(best < r ? best : r);
-}
-
 // The row's candidate keys (segment lists concatenated) sorted in registers;
 // the nc <= 32 smallest end up in v[0] of lanes 0 .. nc - 1.
 template <int RR>

@@ -2718,11 +2718,13 @@ void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int npr
                  : twopass ? coarse_topk2_nseg(qb, ix->nlist, ix->d, nc, ix->ctx->num_sms) : 1;
   const int ncand = nseg * (fused ? umma_topk_groups(ix->d, nc) : 1) * next_pow2(nc);
   const int lcap = twopass ? coarse_topk2_cap(nc) : 0;
+  const bool list_major = ivfflat_lm_supported(qb, ix->d, nprobe, k);
+  const size_t lm_bytes = list_major ? ivfflat_lm_scratch_bytes(qb, nprobe, ix->nlist, k) : 0;
   ws.ensure(ws_bytes((size_t)qb * ix->nlist, 4) + ws_bytes((size_t)qb * nprobe, 8) +
             ws_bytes((size_t)qb * nprobe, 4) * 2 + ws_bytes((size_t)qb * kp, 2) +
             ws_bytes((size_t)qb * ncand, 8) + ws_bytes((size_t)qb, 8) +
             ws_bytes((size_t)qb * nseg * lcap, 8) + ws_bytes((size_t)qb * nseg, 4) +
-            ws_bytes((size_t)qb, 4));
+            ws_bytes((size_t)qb, 4) + ws_bytes(lm_bytes, 1));
   Arena ar(ws);
   float* dmat = ar.take<float>((size_t)qb * ix->nlist);
   uint64_t* ckeys = ar.take<uint64_t>((size_t)qb * nprobe);
@@ -2734,6 +2736,7 @@ void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int npr
   uint64_t* clists = ar.take<uint64_t>((size_t)qb * nseg * lcap);
   int* ccounts = ar.take<int>((size_t)qb * nseg);
   uint32_t* cthr = ar.take<uint32_t>((size_t)qb);
+  unsigned char* lm_scratch = list_major ? ar.take<unsigned char>(lm_bytes) : nullptr;
   const int kind = ix->metric == MV_METRIC_L2 ? KIND_L2_SIMD8 : KIND_IP_SIMD8;
   for (int64_t q0 = 0; q0 < nq; q0 += qb) {
     const int64_t nb = std::min(qb, nq - q0);
@@ -2792,9 +2795,15 @@ void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int npr
       }
     }
     StageTimer t(ix->ctx, MV_STAGE_SCAN, s);
-    launch_ivfflat_scan(xb, nb, ix->d, ix->metric, probes, nprobe, ix->nlist,
-                        ix->d_off.as<int64_t>(), ix->d_rows.as<float>(), ix->d_ids.as<uint32_t>(),
-                        k, d_out + q0 * k, d_lab + q0 * k, s);
+    if (list_major)
+      launch_ivfflat_scan_lm(xb, nb, ix->d, ix->metric, probes, nprobe, ix->nlist,
+                             ix->d_off.as<int64_t>(), ix->d_rows.as<float>(),
+                             ix->d_ids.as<uint32_t>(), k, d_out + q0 * k, d_lab + q0 * k,
+                             lm_scratch, s);
+    else
+      launch_ivfflat_scan(xb, nb, ix->d, ix->metric, probes, nprobe, ix->nlist,
+                          ix->d_off.as<int64_t>(), ix->d_rows.as<float>(), ix->d_ids.as<uint32_t>(),
+                          k, d_out + q0 * k, d_lab + q0 * k, s);
   }
 }
 

@@ -158,6 +158,15 @@ void launch_sum_fp64(const float* v, int64_t n, double* part256, double* out, cu
 void launch_ivfflat_scan(const float* q, int64_t nq, int d, int metric, const int32_t* probes,
                          int nprobe, int nlist, const int64_t* list_off, const float* rows,
                          const uint32_t* ids, int k, float* out_d, int64_t* out_l, cudaStream_t s);
+// List-major form of the same scan (k <= 32): (query, probe) pairs grouped
+// by list, each list read once per 8 of its queries; same results.
+// scratch: ivfflat_lm_scratch_bytes() bytes of device memory.
+size_t ivfflat_lm_scratch_bytes(int64_t nq, int nprobe, int nlist, int k);
+bool ivfflat_lm_supported(int64_t nq, int d, int nprobe, int k);
+void launch_ivfflat_scan_lm(const float* q, int64_t nq, int d, int metric, const int32_t* probes,
+                            int nprobe, int nlist, const int64_t* list_off, const float* rows,
+                            const uint32_t* ids, int k, float* out_d, int64_t* out_l, void* scratch,
+                            cudaStream_t s);
 
 // SQ8 codes as BF16 rows (kp wide) and FP32 norms, for the tensor-core scan.
 void launch_sq8_codes_to_bf16(const uint8_t* codes, int64_t n, int d, int dpad, int kp,
