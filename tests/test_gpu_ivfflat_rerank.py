@@ -126,3 +126,26 @@ def test_device_entry_points_match_host_calls(mv):
                     stream=s.cuda_stream)
     torch.cuda.synchronize()
     assert np.array_equal(dl.cpu().numpy(), hl) and _same(dd.cpu().numpy(), hd)
+
+
+@pytest.mark.parametrize("metric", [0, 1])
+def test_ivfflat_list_major_chunks_and_k_limits(mv, orc, metric):
+    """The list-major scan (k <= 32) and its fallback (k > 32) against the
+    oracle: clustered queries put hundreds of queries on the same few lists
+    (many 8-query chunks per list), k at both sides of the limit."""
+    d = 37  # not a multiple of 4: the scalar staging path
+    cent = (RNG.standard_normal((12, d)) * 6).astype(np.float32)
+    x = (cent[RNG.integers(0, 12, 5000)] + RNG.standard_normal((5000, d))).astype(np.float32)
+    q = (cent[RNG.integers(0, 3, 300)] + 0.5 * RNG.standard_normal((300, d))).astype(np.float32)
+    g = mv.IndexIVFFlat(d, 40, metric)
+    g.train(x[:3000])
+    o = orc.IVFFlat(d, 40, metric)
+    o.train(x[:3000])
+    g.add(x)
+    o.add(x)
+    for k in (1, 32, 33):
+        for nprobe in (3, 12):
+            gd, gl = g.search(q, k, nprobe=nprobe)
+            od, ol = o.search(q, k, nprobe)
+            assert np.array_equal(gl, ol), (k, nprobe)
+            assert _same(gd, od), (k, nprobe)
