@@ -1290,7 +1290,8 @@ size_t coarse_topk2_smem(int nkb) {
 }
 }  // namespace
 
-int coarse_topk2_cap(int nc) { return nc <= 16 ? 64 : 128; }
+// A list must take nc keys plus one chunk's 32 after a compaction.
+int coarse_topk2_cap(int nc) { return nc <= 16 ? 48 : 128; }
 
 int coarse_topk2_nseg(int64_t nrows, int64_t ncols, int d, int nc, int num_sms) {
   const int nkb = umma_kpad(d) / 64;
@@ -1301,7 +1302,8 @@ int coarse_topk2_nseg(int64_t nrows, int64_t ncols, int d, int nc, int num_sms) 
   // wave to 90 %; the select kernel takes at most 256 keys per row.
   const int64_t cps = std::max<int64_t>(1, std::min<int64_t>(2, (228 * 1024) / (coarse_topk2_smem(nkb) + 1024)));
   const int64_t slots = (int64_t)std::max(num_sms, 1) * cps;
-  const int64_t maxseg = std::max<int64_t>(1, std::min<int64_t>(nct / 4, 256 / coarse_topk2_cap(nc)));
+  const int64_t maxseg =
+      std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(nct / 4, 256 / coarse_topk2_cap(nc)), 4));
   int64_t best = 1;
   double best_eff = 0.0;
   for (int64_t ns = 1; ns <= maxseg; ++ns) {

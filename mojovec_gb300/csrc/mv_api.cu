@@ -137,7 +137,10 @@ void assign_nearest(const float* x, int64_t n, int d, const float* cent, int k, 
   const int64_t chunk = std::min<int64_t>(n, 1 << 19);
   const int nseg = umma_topk_nseg(chunk, k, d, kc, ctx->num_sms);
   const int osegs = nseg * umma_topk_groups(d, kc);
-  DevBuf buf;
+  // Scratch from a leased slot (grow-only, reused across calls), bound to s.
+  SlotLease lease(ctx);
+  lease.use(s);
+  DevBuf& buf = lease.slot->ws;
   buf.ensure(ws_bytes((size_t)k * kp, 2) + ws_bytes(k, 4) + ws_bytes(2, 8) +
              ws_bytes((size_t)chunk * kp, 2) + ws_bytes((size_t)chunk * osegs * ncp, 8) +
              2 * ws_bytes(chunk, 8) + ws_bytes(1, 4) + ws_bytes((size_t)chunk * d, 4) +
@@ -178,7 +181,6 @@ void assign_nearest(const float* x, int64_t n, int d, const float* cent, int k, 
     }
     fallback += h_nflag;
   }
-  sync(s);  // the scratch is freed on return
   ctx->assign_rows += n;
   ctx->assign_fallback += fallback;
 }
