@@ -1207,7 +1207,7 @@ def run_ivfflat(args, rank, world):
             "frac": round(achieved / hbm, 4), "traffic": None,
             "algorithmic_bytes_per_launch": int(alg_bytes),
             "note": ("row bytes of the probed lists per query, mean-list approximation (nb / nlist "
-                     "rows each); the list-major scan reads each list once per 8 of its queries, "
+                     "rows each); the list-major scan reads each list once per 4 of its queries, "
                      "so DRAM traffic is below these algorithmic bytes"),
             "launch_ms": round(per_launch, 4),
         },

@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(FT)
 // union of the per-list k smallest holds the query's k smallest keys, so the
 // results equal the query-major scan's.
 constexpr int LM_T = 64;   // threads per CTA = rows per tile
-constexpr int LM_QC = 8;   // queries per CTA
+constexpr int LM_QC = 4;   // queries per CTA (measured: 2, 8 and 16 are slower)
 
 __global__ void k_lm_count(const int32_t* __restrict__ probes, int64_t npairs, int nlist,
                            int* __restrict__ cnt) {

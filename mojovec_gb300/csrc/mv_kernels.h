@@ -159,7 +159,7 @@ void launch_ivfflat_scan(const float* q, int64_t nq, int d, int metric, const in
                          int nprobe, int nlist, const int64_t* list_off, const float* rows,
                          const uint32_t* ids, int k, float* out_d, int64_t* out_l, cudaStream_t s);
 // List-major form of the same scan (k <= 32): (query, probe) pairs grouped
-// by list, each list read once per 8 of its queries; same results.
+// by list, each list read once per 4 of its queries; same results.
 // scratch: ivfflat_lm_scratch_bytes() bytes of device memory.
 size_t ivfflat_lm_scratch_bytes(int64_t nq, int nprobe, int nlist, int k);
 bool ivfflat_lm_supported(int64_t nq, int d, int nprobe, int k);
