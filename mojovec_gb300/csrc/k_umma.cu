@@ -955,11 +955,23 @@ __global__ void __launch_bounds__(192, 2)
               for (int j = 0; j < 32; ++j) mk |= e[j] >= thr ? (1u << j) : 0u;
               mk &= valid;
             }
+            // One store per set bit, in ascending column order; e[j] for the
+            // lane's own j comes from a select tree (static register indices).
+            while (mk) {
+              const int j = __ffs(mk) - 1;
+              mk &= mk - 1u;
+              float t16[16], t8[8], t4[4], t2[2];
 #pragma unroll
-            for (int j = 0; j < 32; ++j)
-              if (mk & (1u << j))
-                lst[cnt + __popc(mk & ((1u << j) - 1u))] = make_key(-e[j], (uint32_t)(col0 + j));
-            cnt += __popc(mk);
+              for (int i = 0; i < 16; ++i) t16[i] = (j & 1) ? e[2 * i + 1] : e[2 * i];
+#pragma unroll
+              for (int i = 0; i < 8; ++i) t8[i] = (j & 2) ? t16[2 * i + 1] : t16[2 * i];
+#pragma unroll
+              for (int i = 0; i < 4; ++i) t4[i] = (j & 4) ? t8[2 * i + 1] : t8[2 * i];
+#pragma unroll
+              for (int i = 0; i < 2; ++i) t2[i] = (j & 8) ? t4[2 * i + 1] : t4[2 * i];
+              const float ej = (j & 16) ? t2[1] : t2[0];
+              lst[cnt++] = make_key(-ej, (uint32_t)(col0 + j));
+            }
           }
         }
       }

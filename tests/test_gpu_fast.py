@@ -108,6 +108,28 @@ def test_fast_recall_and_determinism(mv):
     assert abs(recall(lc) - r_rerank) < 0.02
 
 
+@pytest.mark.parametrize("nprobe", [3, 12])
+def test_fast_shortlist_select_is_exact(mv, nprobe):
+    """With rerank 0 the shortlist is the answer, sorted by (table distance,
+    position). At nprobe 3 most queries have fewer than 2048 candidates, so
+    k = 2048 returns every candidate with no radix select; a smaller k runs
+    the block radix select and must return exactly that list's first k
+    entries. At nprobe 12 queries stage more keys than the staging area
+    holds, so intermediate selects run first; the k smallest must still be
+    a prefix of the 2048 smallest."""
+    from mojovec_gb300 import synth
+
+    base, q = synth.sift_like(24000, d=32, n_centers=64, nq=150, seed=23)
+    g = _index(mv, base, 32, 64, 8)
+    fd, fl = g.search(q, 2048, form=mv.FORM_FAST, nprobe=nprobe)
+    if nprobe == 3:
+        assert np.mean((fl == -1).any(axis=1)) > 0.5  # complete candidate lists
+    for k in (10, 100, 256, 700):
+        d, l = g.search(q, k, form=mv.FORM_FAST, nprobe=nprobe)
+        assert np.array_equal(l, fl[:, :k]), k
+        assert np.array_equal(d.view(np.uint32), fd[:, :k].view(np.uint32)), k
+
+
 def test_fast_untrained_and_small_lists(mv):
     g = mv.IndexIVFPQ(16, 8, 4)
     d, l = g.search(np.zeros((2, 16), np.float32), 5, form=mv.FORM_FAST, nprobe=4)
