@@ -720,8 +720,8 @@ __device__ __noinline__ uint64_t coarse_list_compact(uint64_t* lst, int n, int K
 // nc columns with e >= T, so each of the row's nc smallest keys has e >= T.
 // Pass 2 appends the keys (distance, column) with e >= T to the row's list
 // in global memory (the thread owns the row: no atomics), per 32-column
-// chunk from a bit mask with positions by population count (no serial
-// dependence, no divergence). A chunk that would overflow the list first
+// chunk one store per set bit of the row's mask, in column order. A chunk
+// that would overflow the list first
 // compacts it to its nc smallest keys and raises T to the e of the largest
 // of them (later columns have larger ids, so a key they tie with that one
 // cannot be among the nc smallest); the list always contains the segment's
