@@ -17,7 +17,8 @@ nprobe and reported beside it.
 events on the launching stream, L2 flushed with a 256 MiB write before each
 step, outside the timed interval); `e2e` times the public host-buffer C-ABI
 call (mv_ivfpq_search) including the host->device copy of the queries from
-pinned memory and the device->host copy of distances and ids.
+pinned memory and the device->host copy of distances and ids into
+caller-provided pinned result arrays.
 
 `--impl reference` times the oracle (the C++ restatement of the reference's
 CPU path) on the host cores over a bounded query sample of the same
@@ -199,6 +200,15 @@ def _timed_steps(torch, step, steps, stream, flush):
     return float(sum(a.elapsed_time(b) for a, b in evs))
 
 
+def _pinned_results(torch, nq, k):
+    """Caller-provided result arrays in pinned host memory, allocated once
+    (the search writes distances and labels into them every call, as the
+    reference's search writes into the caller's spans)."""
+    d = torch.empty((nq, k), dtype=torch.float32).pin_memory()
+    lab = torch.empty((nq, k), dtype=torch.int64).pin_memory()
+    return (d, lab), {"distances": d.numpy(), "labels": lab.numpy()}
+
+
 def _max_over_ranks(torch, world, v, device="cuda"):
     """The slowest rank's time: all ranks' work counts as done only when the
     last rank finishes."""
@@ -292,12 +302,13 @@ def run_gpu(args, rank, world):
     pinned = torch.empty((nq, D), dtype=torch.float32).pin_memory()
     pinned.copy_(torch.from_numpy(queries))
     hq = pinned.numpy()
-    index.search(hq, K, **headline)
+    keep, outs = _pinned_results(torch, nq, K)
+    index.search(hq, K, **headline, **outs)
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        _, elab = index.search(hq, K, **headline)
+        _, elab = index.search(hq, K, **headline, **outs)
     e2e_s = _max_over_ranks(torch, world, time.perf_counter() - t0)
     e2e_qps = world * nq * args.steps / e2e_s
     assert np.array_equal(elab, labels), "host-buffer and device-buffer searches disagree"
@@ -499,12 +510,13 @@ def run_flat(args, rank, world):
     pinned = torch.empty((nq, dim), dtype=torch.float32).pin_memory()
     pinned.copy_(torch.from_numpy(queries))
     hq = pinned.numpy()
-    flat.search(hq, k, **plain)
+    keep, outs = _pinned_results(torch, nq, k)
+    flat.search(hq, k, **plain, **outs)
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        _, elab = flat.search(hq, k, **plain)
+        _, elab = flat.search(hq, k, **plain, **outs)
     e2e_s = _max_over_ranks(torch, world, time.perf_counter() - t0)
     e2e_qps = world * nq * args.steps / e2e_s
     assert np.array_equal(elab, results["plain"]["labels"]), "host and device searches disagree"
@@ -1165,10 +1177,11 @@ def run_ivfflat(args, rank, world):
     pinned = torch.empty((nq, D), dtype=torch.float32).pin_memory()
     pinned.copy_(torch.from_numpy(queries))
     hq = pinned.numpy()
-    ix.search(hq, k, nprobe=nprobe)
+    keep, outs = _pinned_results(torch, nq, k)
+    ix.search(hq, k, nprobe=nprobe, **outs)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        _, elab = ix.search(hq, k, nprobe=nprobe)
+        _, elab = ix.search(hq, k, nprobe=nprobe, **outs)
     e2e_qps = world * nq * args.steps / _max_over_ranks(torch, world, time.perf_counter() - t0)
     assert np.array_equal(elab, res["plain"]["labels"]), "host and device searches disagree"
     peaks = {}

@@ -62,6 +62,21 @@ def _p(a):
     return None if a is None else a.ctypes.data
 
 
+def _out(a, n, k, dtype, name):
+    """Result array of a search: a new (n, k) array, or the caller's own
+    (the reference's search writes into caller-provided distances and
+    labels spans, index/index_ivf_pq.mojo:215-232). A caller's array must
+    be C-contiguous with that shape and dtype (pinned host memory, e.g.
+    from torch's pin_memory(), lets the device copy straight into it)."""
+    if a is None:
+        return np.empty((n, k), dtype)
+    if (not isinstance(a, np.ndarray) or a.dtype != dtype or a.shape != (n, k)
+            or not a.flags.c_contiguous or not a.flags.writeable):
+        raise ValueError(f"{name} must be a writable C-contiguous {np.dtype(dtype).name} "
+                         f"array of shape ({n}, {k})")
+    return a
+
+
 class Context:
     """One CUDA device (mv_ctx)."""
 
@@ -266,11 +281,11 @@ class IndexIVFPQ:
 
     def search(self, x, k: int, filter=None, form=None, nprobe: int = 0, rerank: int = 0,
                coarse_fp32: bool = False, lut_fp16: bool = False, coarse_path: int = 0,
-               rerank_fp32: bool = False):
+               rerank_fp32: bool = False, distances=None, labels=None):
         x = _f32(x, self.d)
         n = x.shape[0]
-        dist = np.empty((n, k), np.float32)
-        lab = np.empty((n, k), np.int64)
+        dist = _out(distances, n, k, np.float32, "distances")
+        lab = _out(labels, n, k, np.int64, "labels")
         flt = None if filter is None else np.ascontiguousarray(filter, dtype=np.uint8)
         p = _params(form, nprobe, rerank, coarse_fp32, lut_fp16, coarse_path,
                     rerank_fp32=rerank_fp32)
@@ -355,11 +370,11 @@ class IndexIVFFlat:
             ids = np.ascontiguousarray(ids, dtype=np.int64)
             check(_lib.load().mv_ivfflat_add_with_ids(self._h, _p(x), _p(ids), x.shape[0]))
 
-    def search(self, x, k: int, nprobe: int = 0, form=None):
+    def search(self, x, k: int, nprobe: int = 0, form=None, distances=None, labels=None):
         x = _f32(x, self.d)
         n = x.shape[0]
-        dist = np.empty((n, k), np.float32)
-        lab = np.empty((n, k), np.int64)
+        dist = _out(distances, n, k, np.float32, "distances")
+        lab = _out(labels, n, k, np.int64, "labels")
         p = _params(form, nprobe)
         check(_lib.load().mv_ivfflat_search(self._h, _p(x), n, k, C.byref(p), _p(dist), _p(lab)))
         return dist, lab
@@ -400,15 +415,16 @@ class IndexFlat:
         check(_lib.load().mv_flat_add(self._h, _p(x), x.shape[0]))
 
     def search(self, x, k: int, filter=None, form=None, rerank: int = 0, plain_scan: bool = False,
-               e4m3: bool = False):
+               e4m3: bool = False, distances=None, labels=None):
         """IndexFlat.search. The plain form returns the reference's exact
         results, from the certified tensor-core shortlist where it applies;
         plain_scan=True runs the exact FP32 scan alone. The fast form takes
-        its shortlist from a BF16 GEMM, or with e4m3=True an FP8 one."""
+        its shortlist from a BF16 GEMM, or with e4m3=True an FP8 one.
+        distances / labels: optional caller-provided result arrays."""
         x = _f32(x, self.d)
         n = x.shape[0]
-        dist = np.empty((n, k), np.float32)
-        lab = np.empty((n, k), np.int64)
+        dist = _out(distances, n, k, np.float32, "distances")
+        lab = _out(labels, n, k, np.int64, "labels")
         flt = None if filter is None else np.ascontiguousarray(filter, dtype=np.uint8)
         p = _params(form, 0, rerank, plain_scan=plain_scan, e4m3=e4m3)
         check(_lib.load().mv_flat_search(self._h, _p(x), n, k, _p(flt), C.byref(p), _p(dist),

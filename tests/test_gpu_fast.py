@@ -130,6 +130,31 @@ def test_fast_shortlist_select_is_exact(mv, nprobe):
         assert np.array_equal(d.view(np.uint32), fd[:, :k].view(np.uint32)), k
 
 
+def test_search_into_caller_arrays(mv):
+    """Results written into caller-provided pinned arrays equal the
+    allocating call's, for IVF-PQ (both forms), IVF-Flat and Flat."""
+    import torch
+    from mojovec_gb300 import synth
+
+    base, q = synth.sift_like(20000, d=64, n_centers=64, nq=300, seed=24)
+    g = _index(mv, base, 64, 64, 8)
+    f = mv.IndexIVFFlat(64, 64, 0)
+    f.train(base[:8000], niter=4)
+    f.add(base)
+    fl = mv.IndexFlat(64, 0)
+    fl.add(base)
+    hq = torch.from_numpy(q).pin_memory().numpy()
+    cases = [(g, dict(nprobe=8)), (g, dict(form=mv.FORM_FAST, nprobe=8, rerank=64)),
+             (f, dict(nprobe=8)), (fl, {})]
+    for ix, kw in cases:
+        dt = torch.full((len(q), 10), -7.0).pin_memory()
+        lt = torch.full((len(q), 10), -7, dtype=torch.int64).pin_memory()
+        rd, rl = ix.search(hq, 10, **kw, distances=dt.numpy(), labels=lt.numpy())
+        assert rd.ctypes.data == dt.data_ptr() and rl.ctypes.data == lt.data_ptr()
+        ed, el = ix.search(q, 10, **kw)
+        assert np.array_equal(lt.numpy(), el) and np.array_equal(dt.numpy(), ed), kw
+
+
 def test_fast_untrained_and_small_lists(mv):
     g = mv.IndexIVFPQ(16, 8, 4)
     d, l = g.search(np.zeros((2, 16), np.float32), 5, form=mv.FORM_FAST, nprobe=4)

@@ -60,3 +60,24 @@ def test_collection_validation_before_device_work(kwargs, match):
 
     with pytest.raises(ValueError, match=match):
         IVFPQCollection(**kwargs)
+
+
+def test_search_result_arrays_checked():
+    """Caller-provided result arrays (the reference's search writes into the
+    caller's distances / labels spans): the exact shape, dtype and a
+    writable C-contiguous layout, else ValueError; None allocates."""
+    import numpy as np
+    import pytest as _pytest
+    from mojovec_gb300.index import _out
+
+    a = _out(None, 3, 4, np.float32, "distances")
+    assert a.shape == (3, 4) and a.dtype == np.float32
+    mine = np.zeros((3, 4), np.int64)
+    assert _out(mine, 3, 4, np.int64, "labels") is mine
+    bad = [np.zeros((3, 5), np.int64), np.zeros((3, 4), np.int32),
+           np.zeros((4, 3), np.int64).T, [[0] * 4] * 3]
+    ro = np.zeros((3, 4), np.int64)
+    ro.flags.writeable = False
+    for b in bad + [ro]:
+        with _pytest.raises(ValueError):
+            _out(b, 3, 4, np.int64, "labels")
