@@ -510,16 +510,17 @@ class IndexFlatSQ8:
         return c[:n], nm[:n]
 
     def search(self, x, k: int, filter=None, form=None, rerank_factor: int = 0,
-               plain_scan: bool = False):
+               plain_scan: bool = False, distances=None, labels=None):
         """IndexFlatSQ8.search; with rerank_factor > 0 the shortlist of
         k * rerank_factor is reranked with exact FP32 distances. Both forms
         take the shortlist from the tensor cores where that is exact (the
         same results as the integer scan); plain_scan=True runs the integer
-        scan alone."""
+        scan alone. distances / labels: optional caller-provided result
+        arrays."""
         x = _f32(x, self.d)
         n = x.shape[0]
-        dist = np.empty((n, k), np.float32)
-        lab = np.empty((n, k), np.int64)
+        dist = _out(distances, n, k, np.float32, "distances")
+        lab = _out(labels, n, k, np.int64, "labels")
         flt = None if filter is None else np.ascontiguousarray(filter, dtype=np.uint8)
         if form is None and rerank_factor == 0 and not plain_scan:
             check(_lib.load().mv_sq8_search(self._h, _p(x), n, k, _p(flt), _p(dist), _p(lab)))

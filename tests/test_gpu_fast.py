@@ -132,7 +132,7 @@ def test_fast_shortlist_select_is_exact(mv, nprobe):
 
 def test_search_into_caller_arrays(mv):
     """Results written into caller-provided pinned arrays equal the
-    allocating call's, for IVF-PQ (both forms), IVF-Flat and Flat."""
+    allocating call's, for IVF-PQ (both forms), IVF-Flat, Flat and SQ8."""
     import torch
     from mojovec_gb300 import synth
 
@@ -143,9 +143,11 @@ def test_search_into_caller_arrays(mv):
     f.add(base)
     fl = mv.IndexFlat(64, 0)
     fl.add(base)
+    sq = mv.IndexFlatSQ8(64, 0)
+    sq.add(base)
     hq = torch.from_numpy(q).pin_memory().numpy()
     cases = [(g, dict(nprobe=8)), (g, dict(form=mv.FORM_FAST, nprobe=8, rerank=64)),
-             (f, dict(nprobe=8)), (fl, {})]
+             (f, dict(nprobe=8)), (fl, {}), (sq, {}), (sq, dict(rerank_factor=2))]
     for ix, kw in cases:
         dt = torch.full((len(q), 10), -7.0).pin_memory()
         lt = torch.full((len(q), 10), -7, dtype=torch.int64).pin_memory()
