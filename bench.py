@@ -168,6 +168,33 @@ def recall_at(gt, labels, k=10):
     return hits / (gt.shape[0] * k)
 
 
+def distance_error_vs_fp64(base, queries, dist, labels, metric="l2", sample=256):
+    """Relative error of each returned distance against the FP64 distance of
+    the same (query, row) pair, over the first `sample` queries (computed on
+    the host, outside every timed region). metric "l2": squared L2; "ip":
+    the inner product (the index returns it un-negated). Labels are row
+    numbers of `base`; -1 slots are skipped. For PQ forms without a rerank
+    the returned value is the ADC approximation, so its error is the
+    quantization error, not arithmetic error."""
+    n = min(sample, len(queries))
+    lab = np.asarray(labels[:n])
+    ok = lab >= 0
+    if not ok.any():
+        return {"max_rel": None, "mean_rel": None, "results": 0, "queries": n}
+    qi = np.nonzero(ok)[0]
+    rows = base[lab[ok]].astype(np.float64)
+    qs = queries[:n][qi].astype(np.float64)
+    if metric == "l2":
+        ref = ((qs - rows) ** 2).sum(1)
+    else:
+        ref = (qs * rows).sum(1)
+    got = np.asarray(dist[:n], np.float64)[ok]
+    rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-30)
+    return {"max_rel": float(f"{rel.max():.3e}"), "mean_rel": float(f"{rel.mean():.3e}"),
+            "results": int(ok.sum()), "queries": n,
+            "definition": "|returned - FP64(query, returned row)| / |FP64|, per result"}
+
+
 def cpu_baseline(index, queries, nprobe, threads, sample):
     """The oracle searching the same index (codebooks and lists loaded from
     the GPU index) on a bounded sample of queries."""
@@ -272,7 +299,8 @@ def run_gpu(args, rank, world):
             step()
         torch.cuda.synchronize()
         labels = d_lab.cpu().numpy()
-        results[name] = {"recall": recall_at(gt, labels, K), "labels": labels}
+        results[name] = {"recall": recall_at(gt, labels, K), "labels": labels,
+                         "derr": distance_error_vs_fp64(base, queries, d_dist.cpu().numpy(), labels)}
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
@@ -389,7 +417,9 @@ def run_gpu(args, rank, world):
         },
         "stages_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in stage.items()},
         "clocks": clk,
+        "distance_error_vs_fp64": results["headline"]["derr"],
     }
+    out["config"]["plain_fp32_distance_error_vs_fp64"] = results["plain"]["derr"]
     if rank == 0 and not args.no_cpu:
         sample = min(args.cpu_sample, nq)
         threads = os.cpu_count() or 1
@@ -478,6 +508,8 @@ def run_flat(args, rank, world):
             step()
         torch.cuda.synchronize()
         results[name] = {"labels": d_lab.cpu().numpy(), "dist": d_dist.cpu().numpy()}
+        results[name]["derr"] = distance_error_vs_fp64(base, queries, results[name]["dist"],
+                                                       results[name]["labels"], args.metric)
         if world > 1:
             torch.distributed.barrier()
         if name == "plain":
@@ -585,7 +617,11 @@ def run_flat(args, rank, world):
         },
         "stages_ms_per_step": {kk: round(v[0] / args.steps, 4) for kk, v in stage.items()},
         "clocks": clk,
+        "distance_error_vs_fp64": results["plain"]["derr"],
     }
+    out["config"]["fast_form_distance_error_vs_fp64"] = results["fast"]["derr"]
+    if not sq8:
+        out["config"]["fp8_form_distance_error_vs_fp64"] = results["fp8"]["derr"]
     if rank == 0 and not args.no_cpu and sq8:
         from oracle import oracle as orc
 
@@ -639,11 +675,13 @@ def run_reference(args):
     times = []
     for _ in range(args.steps):
         t = time.perf_counter()
-        ref.search(q, K, args.nprobe, nthreads=threads, lut_threads=threads)
+        rd, rl = ref.search(q, K, args.nprobe, nthreads=threads, lut_threads=threads)
         times.append(time.perf_counter() - t)
     total = sum(times)
     qps = sample * args.steps / total
+    derr = distance_error_vs_fp64(base, q, rd, rl) if args.steps else None
     return {
+        "distance_error_vs_fp64": derr,
         "metric": METRIC,
         "impl": "reference",
         "value": round(qps, 1),
@@ -786,6 +824,7 @@ def run_batch(args, rank, world):
                      "achieved": round(achieved, 1), "peak": hbm_peak,
                      "frac": round(achieved / hbm_peak, 4), "unit": "GB/s", "traffic": None},
         "clocks": clk,
+        "distance_error_vs_fp64": distance_error_vs_fp64(base, queries, dist, lab, "ip"),
     }
     if not args.no_cpu:
         # The oracle (plain IVF-PQ restatement) over the same lists, on a
@@ -853,6 +892,14 @@ def run_kmeans(args, rank, world):
                      "launches": ctx.kernel_launches() - l0, "clocks": clocks.stop()}
     f, p = out["fast"], out["plain"]
     rel = abs(f["km"].objective[-1] - p["km"].objective[-1]) / p["km"].objective[-1]
+    # The fast form's final objective against the same sum recomputed in FP64
+    # on the host from its centroids and assignments.
+    obj64 = 0.0
+    for r0 in range(0, n, 1 << 17):
+        xa = x[r0:r0 + (1 << 17)].astype(np.float64)
+        ca = f["km"].centroids[f["km"].assignments[r0:r0 + (1 << 17)]].astype(np.float64)
+        obj64 += float(((xa - ca) ** 2).sum())
+    obj_rel = abs(f["km"].objective[-1] - obj64) / obj64
     value = niter / (f["dev_ms"] / 1e3)
     peaks = {}
     try:
@@ -887,6 +934,11 @@ def run_kmeans(args, rank, world):
                      "achieved": round(achieved, 1), "peak": tc_peak, "unit": "TFLOP/s",
                      "frac": round(achieved / tc_peak, 4), "traffic": None},
         "clocks": f["clocks"],
+        "distance_error_vs_fp64": {"max_rel": float(f"{obj_rel:.3e}"), "mean_rel": None,
+                                   "definition": "final objective (sum of squared distances to "
+                                                 "the assigned centroids) against its FP64 "
+                                                 "recomputation from the same centroids and "
+                                                 "assignments"},
     }
 
 
@@ -945,7 +997,7 @@ def run_serve(args, rank, world):
     gaps = rng.exponential(1.0, size=nreq)
 
     def recall_of(form_name):
-        out = {}
+        out, err = {}, {}
         for ci, (name, idx, q) in enumerate(colls):
             qq = q[:200]
             opts = dict(forms[form_name][ci])
@@ -962,8 +1014,10 @@ def run_serve(args, rank, world):
                 gt_idx = flat
             _, gt = gt_idx.search(qq, 10)
             out[name] = round(recall_at(gt, l_, 10), 4)
+            rows = a_base if ci == 0 else (b_base if ci == 1 else c_base)
+            err[name] = distance_error_vs_fp64(rows, qq, d_, l_, "l2" if ci == 0 else "ip")
             del gt_idx
-        return out
+        return out, err
 
     results = {}
     clocks = ClockSampler(dev)
@@ -1013,7 +1067,9 @@ def run_serve(args, rank, world):
             clk = clocks.stop()
         st = srv.stats()
         srv.close()
-        results[form_name] = {"rates": per_rate, "recall_at_10": recall_of(form_name),
+        rec, derr = recall_of(form_name)
+        results[form_name] = {"rates": per_rate, "recall_at_10": rec,
+                              "distance_error_vs_fp64": derr,
                               "batches": st["batches"], "batched_queries": st["batched_queries"],
                               "peak_inflight_gb": round(st["peak_inflight_bytes"] / 2**30, 2)}
     top = results["fast"]["rates"][-1]
@@ -1039,6 +1095,11 @@ def run_serve(args, rank, world):
         },
         "e2e": {"value": top["sustained_queries_per_s"], "unit": "queries/s",
                 "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
+        "distance_error_vs_fp64": {
+            "max_rel": max(v["max_rel"] for v in results["fast"]["distance_error_vs_fp64"].values()),
+            "mean_rel": None,
+            "definition": "largest over the collections, fast form; per collection and form in "
+                          "config.results"},
         "gpu_launches": None,
         "clocks": clk,
     }
@@ -1090,11 +1151,15 @@ def run_curve(args, rank, world):
                                         stream=stream.cuda_stream, nprobe=nprobe, **opts)
                 step()
                 torch.cuda.synchronize()
-                rec = recall_at(gt, d_lab.cpu().numpy(), K)
+                lab = d_lab.cpu().numpy()
+                rec = recall_at(gt, lab, K)
+                derr = distance_error_vs_fp64(base, queries, d_dist.cpu().numpy(), lab)
                 steps = 3 if name == "plain" else 5
                 ms = _timed_steps(torch, step, steps, stream, flush) / steps
                 curve.append({"M": m, "nprobe": nprobe, "variant": name,
-                              "qps": round(nq / (ms / 1e3), 1), "recall_at_10": round(rec, 4)})
+                              "qps": round(nq / (ms / 1e3), 1), "recall_at_10": round(rec, 4),
+                              "dist_err_max_rel": derr["max_rel"],
+                              "dist_err_mean_rel": derr["mean_rel"]})
         del index
     head = [c for c in curve if c["M"] == 16 and c["nprobe"] == 16 and
             c["variant"] == "fast_bf16coarse_fp32lut_rerank40"][0]
@@ -1106,6 +1171,9 @@ def run_curve(args, rank, world):
         "config": {"workload": f"ivfpq_curve_{args.nb}x128_nlist4096_nq{nq}_k10",
                    "value_is": "M 16, nprobe 16, BF16 coarse, FP32 tables, rerank 40",
                    "curve": curve},
+        "distance_error_vs_fp64": {"max_rel": head["dist_err_max_rel"],
+                                   "mean_rel": head["dist_err_mean_rel"],
+                                   "definition": "per point of the curve in config.curve"},
         "e2e": None, "gpu_launches": None,
     }
 
@@ -1158,6 +1226,7 @@ def run_ivfflat(args, rank, world):
             step()
         torch.cuda.synchronize()
         lab = d_lab.cpu().numpy()
+        derr = distance_error_vs_fp64(base, queries, d_dist.cpu().numpy(), lab)
         if name == "plain":
             clocks = ClockSampler(dev)
             clocks.start()
@@ -1172,7 +1241,7 @@ def run_ivfflat(args, rank, world):
             _timed_steps(torch, step, args.steps, stream, flush)
             stage = ctx.stage_times()
             ctx.profile(False)
-        res[name] = {"ms": _max_over_ranks(torch, world, ms), "labels": lab}
+        res[name] = {"ms": _max_over_ranks(torch, world, ms), "labels": lab, "derr": derr}
     value = world * nq / (res["plain"]["ms"] / 1e3)
     pinned = torch.empty((nq, D), dtype=torch.float32).pin_memory()
     pinned.copy_(torch.from_numpy(queries))
@@ -1226,7 +1295,9 @@ def run_ivfflat(args, rank, world):
         },
         "stages_ms_per_step": {kk: round(v[0] / args.steps, 4) for kk, v in stage.items()},
         "clocks": clk,
+        "distance_error_vs_fp64": res["plain"]["derr"],
     }
+    out["config"]["fast_form_distance_error_vs_fp64"] = res["fast"]["derr"]
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as orc
 
@@ -1327,6 +1398,7 @@ def run_rerank(args, rank, world):
                      "algorithmic_bytes_per_launch": int(alg),
                      "note": "candidate rows gathered (nq x 2k x d x 4 bytes); latency-bound at this size"},
         "clocks": clk,
+        "distance_error_vs_fp64": distance_error_vs_fp64(base, queries, hd, hl),
     }
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as orc
@@ -1359,12 +1431,13 @@ def run_reference_ivfflat(args):
         ref.search(queries[:4], K, args.nprobe, nthreads=threads)
     t = time.perf_counter()
     for _ in range(args.steps):
-        ref.search(queries[:sample], K, args.nprobe, nthreads=threads)
+        rd, rl = ref.search(queries[:sample], K, args.nprobe, nthreads=threads)
     total = time.perf_counter() - t
     qps = sample * args.steps / total
     return _reference_line(args, IVFFLAT_METRIC, qps, total, threads,
                            f"ivfflat_{args.nb}x128_nlist{NLIST}_nprobe{args.nprobe}_nq{args.nq}_k{K}",
-                           f"{sample} queries per step, query-parallel on {threads} threads")
+                           f"{sample} queries per step, query-parallel on {threads} threads",
+                           distance_error_vs_fp64(base, queries[:sample], rd, rl))
 
 
 def run_reference_rerank(args):
@@ -1385,16 +1458,18 @@ def run_reference_rerank(args):
         orc.rerank(base, q[:4], cand[:4], K, nthreads=threads)
     t = time.perf_counter()
     for _ in range(args.steps):
-        orc.rerank(base, q, cand, K, nthreads=threads)
+        rd, rl = orc.rerank(base, q, cand, K, nthreads=threads)
     total = time.perf_counter() - t
     qps = sample * args.steps / total
     return _reference_line(args, RERANK_METRIC, qps, total, threads,
                            f"rerank_{args.nb}x128_nq{args.nq}_ncand{2 * K}_k{K}",
-                           f"{sample} queries per step, query-parallel on {threads} threads")
+                           f"{sample} queries per step, query-parallel on {threads} threads",
+                           distance_error_vs_fp64(base, q, rd, rl))
 
 
-def _reference_line(args, metric, qps, total, threads, workload, sample):
+def _reference_line(args, metric, qps, total, threads, workload, sample, derr=None):
     return {
+        "distance_error_vs_fp64": derr,
         "metric": metric, "impl": "reference", "value": round(qps, 1), "unit": "queries/s",
         "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1e3 * total / args.steps, 3), "higher_is_better": True,
@@ -1427,10 +1502,11 @@ def run_reference_flat(args):
         run(q[:2])
     t = time.perf_counter()
     for _ in range(args.steps):
-        run(q)
+        rd, rl = run(q)
     total = time.perf_counter() - t
     qps = sample * args.steps / total
     return {
+        "distance_error_vs_fp64": distance_error_vs_fp64(base, q, rd, rl, args.metric),
         "metric": SQ8_METRIC if args.workload == "sq8" else FLAT_METRIC, "impl": "reference",
         "value": round(qps, 1), "unit": "queries/s",
         "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,

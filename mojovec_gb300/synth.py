@@ -69,6 +69,13 @@ def cos_mixture(n: int, d: int = 96, n_centers: int = 4096, std: float = 0.05,
     return base, queries
 
 
+def sample_rows(n: int, m: int, seed: int = BASE_SEED + 3) -> np.ndarray:
+    """Row indices of a training sample: the first m of a seeded permutation
+    of range(n), in permutation order."""
+    g = np.random.Generator(np.random.PCG64(np.random.SeedSequence(seed)))
+    return g.permutation(n)[:m]
+
+
 def grid_vectors(count: int = 256, dimension: int = 8) -> np.ndarray:
     """The integer-pattern rows used by the reference's IVF-PQ tests
     (tests/test_ivf_pq.mojo:30-38): ((r*17 + c*29) % 251) / 251 + 2*[c == r % d]."""

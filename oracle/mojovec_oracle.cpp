@@ -564,8 +564,10 @@ void pq_train(PQ& pq, const float* x, int64_t n, int niter, int nthreads) {
 }
 
 // pq.mojo:178-219
-void pq_compute_codes(const PQ& pq, const float* x, int64_t n, uint8_t* codes) {
-  for (int64_t i = 0; i < n; ++i) {
+// Rows are encoded independently (the reference loops over them serially);
+// nthreads only splits the rows, so the codes do not depend on it.
+void pq_compute_codes(const PQ& pq, const float* x, int64_t n, uint8_t* codes, int nthreads = 1) {
+  parallel_for(n, nthreads, [&](int64_t i) {
     const float* xp = x + i * pq.d;
     for (int m = 0; m < pq.M; ++m) {
       float min_dist = 1e38f;
@@ -582,7 +584,7 @@ void pq_compute_codes(const PQ& pq, const float* x, int64_t n, uint8_t* codes) {
       }
       codes[i * pq.M + m] = (uint8_t)best;  // UInt8(-1) wraps to 255
     }
-  }
+  });
 }
 
 // pq.mojo:221-250
@@ -686,7 +688,7 @@ void ivfpq_add_with_ids(IVFPQ& ix, const float* x, int64_t n, const int64_t* ids
     for (int j = 0; j < ix.d; ++j) res[i * ix.d + j] = x[i * ix.d + j] - ix.centroids[l * ix.d + j];
   }
   std::vector<uint8_t> codes((size_t)n * ix.M);
-  pq_compute_codes(ix.pq, res.data(), n, codes.data());
+  pq_compute_codes(ix.pq, res.data(), n, codes.data(), nthreads);
   for (int64_t i = 0; i < n; ++i) {
     int64_t l = lab[i];
     if (l < 0 || l >= ix.nlist) continue;
