@@ -195,6 +195,18 @@ def distance_error_vs_fp64(base, queries, dist, labels, metric="l2", sample=256)
             "definition": "|returned - FP64(query, returned row)| / |FP64|, per result"}
 
 
+def smem_roofline(lookups, launch_ms, peaks, clk, sms=152):
+    """The ADC scan's shared-memory bound: one table lookup per code byte,
+    at most 32 lookups (one conflict-free wavefront) per SM per clock."""
+    mhz = (clk or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    peak = 32.0 * sms * float(mhz) * 1e6
+    achieved = lookups / (launch_ms / 1e3) if launch_ms > 0 else 0.0
+    return {"achieved": round(achieved / 1e9, 1), "peak": round(peak / 1e9, 1),
+            "unit": "G lookups/s", "frac": round(achieved / peak, 4),
+            "peak_basis": f"32 lookups per SM per clock x {sms} SMs x {float(mhz):.0f} MHz "
+                          "(median SM clock of the timed region)"}
+
+
 def cpu_baseline(index, queries, nprobe, threads, sample):
     """The oracle searching the same index (codebooks and lists loaded from
     the GPU index) on a bounded sample of queries."""
@@ -279,14 +291,29 @@ def run_gpu(args, rank, world):
 
     fast = dict(form=mv.FORM_FAST, nprobe=nprobe, rerank=args.rerank)
     plain = dict(form=mv.FORM_PLAIN, nprobe=nprobe)
-    headline = fast if args.form == "fast" else plain
+    batched = args.form == "batched"
+    headline = plain if args.form == "plain" else fast
+    plan, tuned = None, None
+    if batched:
+        # The batched form: one plan (device buffers, persistent scan, tuned
+        # launch shapes) replayed as a CUDA graph, every query at this nprobe / k.
+        plan = mv.IVFPQBatchPlan(index, nq, nprobe, K, rerank=args.rerank)
+        npv = np.full(nq, nprobe, np.int32)
+        kv = np.full(nq, K, np.int32)
+        plan.set_queries(queries, npv, kv)
+        tuned = plan.tune(nq)
     d_q = torch.from_numpy(queries).cuda()
     d_dist = torch.empty((nq, K), dtype=torch.float32, device="cuda")
     d_lab = torch.empty((nq, K), dtype=torch.int64, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
 
-    def make_step(opts):
+    def make_step(opts, graph=True):
+        if batched and opts is headline:
+            def step():
+                plan.run(nq, use_graph=graph, stream=stream.cuda_stream)
+            return step
+
         def step():
             index.search_device(d_q.data_ptr(), nq, K, d_dist.data_ptr(), d_lab.data_ptr(),
                                 stream=stream.cuda_stream, **opts)
@@ -298,9 +325,12 @@ def run_gpu(args, rank, world):
         for _ in range(args.warmup):
             step()
         torch.cuda.synchronize()
-        labels = d_lab.cpu().numpy()
+        if batched and name == "headline":
+            dists, labels = plan.results(nq)
+        else:
+            dists, labels = d_dist.cpu().numpy(), d_lab.cpu().numpy()
         results[name] = {"recall": recall_at(gt, labels, K), "labels": labels,
-                         "derr": distance_error_vs_fp64(base, queries, d_dist.cpu().numpy(), labels)}
+                         "derr": distance_error_vs_fp64(base, queries, dists, labels)}
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
@@ -316,8 +346,10 @@ def run_gpu(args, rank, world):
             clk = clocks.stop()
             # Per-stage times (CUDA events around each stage) from a separate,
             # untimed pass of the same steps: the events are not part of the job.
+            # (graph replays run no host code: the batched form's stages are
+            # timed on direct runs of the same plan)
             ctx.profile(True)
-            _timed_steps(torch, step, args.steps, stream, flush)
+            _timed_steps(torch, make_step(opts, graph=False), args.steps, stream, flush)
             stage = ctx.stage_times()
             ctx.profile(False)
         results[name]["ms"] = _max_over_ranks(torch, world, ms)
@@ -331,12 +363,21 @@ def run_gpu(args, rank, world):
     pinned.copy_(torch.from_numpy(queries))
     hq = pinned.numpy()
     keep, outs = _pinned_results(torch, nq, K)
-    index.search(hq, K, **headline, **outs)
+    if batched:
+        # the plan's public calls: host queries in, graph replay, results out
+        def e2e_step():
+            plan.set_queries(hq, npv, kv)
+            plan.run(nq, use_graph=True)
+            return plan.results(nq, **outs)
+    else:
+        def e2e_step():
+            return index.search(hq, K, **headline, **outs)
+    e2e_step()
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        _, elab = index.search(hq, K, **headline, **outs)
+        _, elab = e2e_step()
     e2e_s = _max_over_ranks(torch, world, time.perf_counter() - t0)
     e2e_qps = world * nq * args.steps / e2e_s
     assert np.array_equal(elab, labels), "host-buffer and device-buffer searches disagree"
@@ -353,7 +394,7 @@ def run_gpu(args, rank, world):
     code_bytes = probed_code_bytes(index, queries, nprobe)
     per_launch_ms = scan_ms / max(scan_n, 1)
     achieved = code_bytes / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
-    fast_form = args.form == "fast"
+    fast_form = args.form in ("fast", "batched")
     workload = f"ivfpq_{nb}x128_nlist4096_M16_nq{nq}_k10"
     traffic = None  # DRAM bytes per launch from the committed ncu capture of this config
     try:
@@ -380,8 +421,12 @@ def run_gpu(args, rank, world):
         "config": {
             "workload": workload,
             "form": ("fast: two-pass BF16 tcgen05 coarse GEMM + FP32 recheck, per-query table from the "
-                     "FP16 codebook, certified rerank (the full FP32 rerank's results)")
+                     "FP16 codebook, list pieces staged in shared memory by bulk copies, histogram "
+                     "select, certified rerank (the full FP32 rerank's results)"
+                     + ("; batched: one plan (persistent scan, tuned launch shapes) replayed as a "
+                        "CUDA graph" if batched else ""))
                     if fast_form else "plain FP32 (reference algorithm, bit-exact)",
+            **({"batch_tuned": tuned} if batched else {}),
             "nprobe": nprobe,
             "rerank": args.rerank if fast_form else 0,
             "nb": nb, "d": D, "nlist": NLIST, "M": M, "nq": nq, "k": K,
@@ -397,7 +442,7 @@ def run_gpu(args, rank, world):
         "e2e": {
             "value": round(e2e_qps, 1),
             "unit": "queries/s",
-            "h2d_bytes_per_step": nq * D * 4,
+            "h2d_bytes_per_step": nq * D * 4 + (nq * 12 if batched else 0),  # + nprobe, k, order
             "d2h_bytes_per_step": nq * K * (4 + 8),
         },
         "gpu_launches": int(launches),
@@ -412,8 +457,9 @@ def run_gpu(args, rank, world):
             "traffic": traffic,
             "algorithmic_bytes_per_launch": code_bytes,
             "note": "codes (16 MB) are L2-resident at this size: DRAM traffic is far below the "
-                    "algorithmic bytes; the limiter is the shared-memory LUT (see profiles/)",
+                    "algorithmic bytes; the limiter is the shared-memory table (smem_lookups)",
             "launch_ms": round(per_launch_ms, 4),
+            "smem_lookups": smem_roofline(code_bytes, per_launch_ms, peaks, clk),
         },
         "stages_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in stage.items()},
         "clocks": clk,
@@ -1530,7 +1576,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--form", default="fast", choices=["plain", "fast"])
+    ap.add_argument("--form", default="fast", choices=["plain", "fast", "batched"])
     ap.add_argument("--nprobe", type=int, default=8)
     ap.add_argument("--rerank", type=int, default=None,
                     help="shortlist depth (IVF-PQ default 256, flat default k * 4)")

@@ -66,7 +66,11 @@ typedef struct mv_search_params {
   int32_t rerank;      /* fast form: shortlist depth for the exact FP32 rerank
                           (0 = no rerank) */
   int32_t coarse_fp32; /* fast form: 1 = FP32 SIMT coarse instead of BF16 */
-  int32_t lut_fp16;    /* fast form: 1 = FP16 lookup tables */
+  int32_t lut_fp16;    /* fast form, table and scan variant: 0 or 2 = FP32 tables,
+                          1 = FP16 tables, 3 = bank-rotated 32-bit fixed-point tables
+                          (M a multiple of 4 and at least 8; else FP32), 4 = FP32
+                          tables with the probed lists staged in shared memory by
+                          bulk copies. 0, 2 and 4 return the same bits */
   int32_t coarse_path; /* fast form, BF16 coarse step: 0 = automatic, 1 = GEMM with a
                           per-row top-k epilogue, 2 = distance matrix then one warp
                           per query selecting its lists, 3 = two-pass GEMM (bucket
@@ -96,6 +100,15 @@ int32_t mv_ctx_destroy(mv_ctx* ctx);
 int32_t mv_ctx_synchronize(mv_ctx* ctx);
 /* Number of kernels this context launched since creation (for reports). */
 int64_t mv_ctx_kernel_launches(mv_ctx* ctx);
+/* Failure detection. Every wait inside a tensor-core kernel is bounded; when
+ * one gives up, the kernel stops, lets its issued copies and MMAs finish,
+ * frees its tensor memory, and the call returns MV_ERR_TIMEOUT with the
+ * context still usable. `cycles` is how long a pipeline wait may take (SM
+ * clock cycles; default 4e9, about 2 s at 2.07 GHz); 0 makes every wait that
+ * is not already satisfied give up at once (a diagnostic setting that tests
+ * the timeout path); negative restores the default. No reference
+ * counterpart: the reference runs on the CPU and has no device waits. */
+int32_t mv_ctx_set_wait_limit(mv_ctx* ctx, int64_t cycles);
 
 /* Stage profiling: when enabled, each search stage is bracketed by CUDA
  * events on the stream it runs on. Stage ids (MV_STAGE_*) index the arrays
@@ -266,7 +279,10 @@ int32_t mv_server_add_flat(mv_server* server, mv_flat* index, const mv_search_pa
 int32_t mv_server_add_sq8(mv_server* server, mv_sq8* index, int32_t rerank_factor,
                           const mv_search_params* params, int32_t* id);
 /* Queues nq query rows (copied; x is free on return) for collection `id`;
- * distances / labels (nq x k) are written before mv_server_wait returns. */
+ * distances / labels (nq x k) are written before mv_server_wait returns. A
+ * request above the server's max_batch_queries is split into parts of at
+ * most that many rows; it completes when its last part does. MV_ERR_ARG when
+ * one part's memory estimate exceeds the HBM budget. */
 int32_t mv_server_submit(mv_server* server, int32_t id, const float* x, int64_t nq, int32_t k,
                          float* distances, int64_t* labels, int64_t* request_id);
 /* Blocks until the request is done; returns its status and the latency from
@@ -275,6 +291,12 @@ int32_t mv_server_wait(mv_server* server, int64_t request_id, double* latency_s)
 /* [completed requests, batches, queries in batches, peak in-flight device
  * bytes (estimate)]. */
 int32_t mv_server_stats(mv_server* server, int64_t* out4);
+/* [peak number of batches that were on the device at the same instant, number
+ * of batches recorded]: each batch's device interval runs from its input
+ * copy to its result copy (CUDA events on its lane's stream); the most recent
+ * few thousand batches are kept. Shows that lanes overlap on the device. No
+ * reference counterpart (the reference has no serving loop). */
+int32_t mv_server_device_overlap(mv_server* server, int64_t* out2);
 
 /* ---- IVF-Flat (index/index_ivf_flat.mojo:10-243) ----------------------- */
 int32_t mv_ivfflat_create(mv_ctx* ctx, int32_t d, int32_t nlist, int32_t metric, mv_ivfflat** out);

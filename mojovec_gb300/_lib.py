@@ -79,6 +79,7 @@ SIGNATURES = {
     "mv_ctx_destroy": (_i32, [_vp]),
     "mv_ctx_synchronize": (_i32, [_vp]),
     "mv_ctx_kernel_launches": (_i64, [_vp]),
+    "mv_ctx_set_wait_limit": (_i32, [_vp, _i64]),
     "mv_ctx_profile": (_i32, [_vp, _i32]),
     "mv_ctx_stage_times": (_i32, [_vp, _vp, _vp, _i32]),
     "mv_ivfpq_create": (_i32, [_vp, _i32, _i32, _i32, _i32, C.POINTER(_vp)]),
@@ -144,6 +145,7 @@ SIGNATURES = {
     "mv_server_add_sq8": (_i32, [_vp, _vp, _i32, _vp, _vp]),
     "mv_server_submit": (_i32, [_vp, _i32, _vp, _i64, _i32, _vp, _vp, _vp]),
     "mv_server_wait": (_i32, [_vp, _i64, _vp]),
+    "mv_server_device_overlap": (_i32, [_vp, _vp]),
     "mv_server_stats": (_i32, [_vp, _vp]),
     "mv_kmeans_train_ex": (_i32, [_vp, _vp, _i64, _i32, _i32, _i32, _vp, _vp, _vp, _vp]),
     "mv_pq_train": (_i32, [_vp, _vp, _i64, _i32, _i32, _i32, _vp]),

@@ -23,49 +23,50 @@ namespace mv {
 namespace {
 
 // cert[0] = B^2 bound: max of the FP32 norms of the BF16 rows with the
-// summation slack, or -1 when a norm is NaN or infinite.
+// summation slack (rounded up), or -1 when a norm is NaN or infinite.
 __global__ void k_max_norm(const float* __restrict__ norms, int64_t n, int d,
-                           double* __restrict__ out) {
-  __shared__ double part[32];
-  double m = 0.0;
+                           float* __restrict__ out) {
+  __shared__ float part[32];
+  float m = 0.0f;
   bool bad = false;
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
     const float v = norms[i];
     if (!(v <= 3.0e38f)) bad = true;  // NaN or inf
-    m = fmax(m, (double)v);
+    else m = fmaxf(m, v);
   }
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   bad = __any_sync(0xffffffffu, bad);
-  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = bad ? -1.0 : m;
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = bad ? -1.0f : m;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double r = 0.0;
+    float r = 0.0f;
     bool anybad = false;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-      if (part[w] < 0.0) anybad = true;
-      r = fmax(r, part[w]);
+      if (part[w] < 0.0f) anybad = true;
+      r = fmaxf(r, part[w]);
     }
-    *out = anybad ? -1.0 : r * (1.0 + (d + 1) * 0x1p-23);
+    *out = anybad ? -1.0f : __fmul_ru(r, __fadd_ru(1.0f, __fmul_ru((float)(d + 1), 0x1p-23f)));
   }
 }
 
-// out = max over rows of ||y - bf16(y)|| (bits of a non-negative double,
-// zeroed by the caller), one warp per row.
+// out = max over rows of an upper bound on ||y - bf16(y)|| (bits of a
+// non-negative float, zeroed by the caller), one warp per row: the
+// differences are exact in FP32, their squares and sums rounded up.
 __global__ void k_resid_max(const float* __restrict__ rows, int64_t n, int d,
-                            unsigned long long* __restrict__ out) {
+                            unsigned* __restrict__ out) {
   const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (row >= n) return;
-  double s = 0.0;
+  float s = 0.0f;
   for (int j = lane; j < d; j += 32) {
     const float v = rows[row * d + j];
-    const double r = (double)v - (double)__bfloat162float(__float2bfloat16_rn(v));
-    s = fma(r, r, s);
+    const float r = __fsub_rn(v, __bfloat162float(__float2bfloat16_rn(v)));
+    s = __fadd_ru(s, __fmul_ru(r, r));
   }
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  for (int o = 16; o > 0; o >>= 1) s = __fadd_ru(s, __shfl_xor_sync(0xffffffffu, s, o));
   if (lane == 0) {
-    const double v = s != s ? 1e300 : sqrt(s) * (1.0 + 1e-12);
-    atomicMax(out, (unsigned long long)__double_as_longlong(v));
+    const float v = s != s ? 1e30f : __fsqrt_ru(s);  // NaN: no certificate
+    atomicMax(out, __float_as_uint(v));
   }
 }
 
@@ -77,34 +78,12 @@ __device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
   return v;
 }
 
-// X^2 = ||bx||^2 and rq^2 = ||x - bx||^2 of one row, in double (one warp).
-__device__ __forceinline__ void bf16_norms(const float* x, int d, double& xs, double& rs) {
-  const int lane = threadIdx.x & 31;
-  xs = 0.0;
-  rs = 0.0;
-  for (int j = lane; j < d; j += 32) {
-    const float v = x[j];
-    const double b = (double)__bfloat162float(__float2bfloat16_rn(v));
-    const double r = (double)v - b;
-    xs = fma(b, b, xs);
-    rs = fma(r, r, rs);
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    xs += __shfl_xor_sync(0xffffffffu, xs, o);
-    rs += __shfl_xor_sync(0xffffffffu, rs, o);
-  }
-}
-
-__device__ __forceinline__ bool cert_inputs_ok(double xs, double B2, double rmax) {
-  return B2 >= 1e-30 && B2 <= 1e300 && xs >= 1e-30 && xs <= 1e300 && rmax <= 1e150;
-}
-
 // Nearest centroid, one warp per row.
 template <bool IP>
 __global__ void k_assign_certify(const float* __restrict__ x, int64_t n, int d,
                                  const float* __restrict__ cent, int nlist,
                                  const uint64_t* __restrict__ cand, int ncand, int kc,
-                                 const double* __restrict__ cert, int32_t* __restrict__ assign,
+                                 const float* __restrict__ cert, int32_t* __restrict__ assign,
                                  float* __restrict__ mind, int64_t* __restrict__ flagged,
                                  int* __restrict__ nflag) {
   const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -153,16 +132,14 @@ __global__ void k_assign_certify(const float* __restrict__ x, int64_t n, int d,
       }
       prev = warp_min_u64(m);
     }
-    double xs, rs;
-    bf16_norms(xr, d, xs, rs);
-    const double B2 = cert[0], rmax = cert[1];
-    if (valid < kc || prev == KEY_NONE || !cert_inputs_ok(xs, B2, rmax)) {
+    const CertNorms cn = cert_norms(xr, d);
+    const float B2 = cert[0], rmax = cert[1];
+    if (valid < kc || prev == KEY_NONE || !cert_inputs_ok(cn, B2, rmax)) {
       ok = false;
     } else {
-      const double K = (double)key_dist(prev);
-      const double lower = IP ? cert_lower_ip(sqrt(xs), sqrt(rs), B2, rmax, K, d)
-                              : cert_lower_l2(sqrt(xs), sqrt(rs), B2, rmax, K, d);
-      ok = lower > (double)best;
+      const float K = key_dist(prev);
+      const float lower = IP ? cert_lower_ip(cn, B2, rmax, K, d) : cert_lower_l2(cn, B2, rmax, K, d);
+      ok = lower > best;
     }
   }
   if (lane == 0) {
@@ -202,7 +179,7 @@ template <bool IP>
 __global__ void __launch_bounds__(TP_WARPS * 32)
     k_topp_certify(const float* __restrict__ x, int64_t n, int d, const float* __restrict__ cent,
                    int nlist, const uint64_t* __restrict__ cand, int ncand, int kc, int P,
-                   const double* __restrict__ cert, int32_t* __restrict__ probes,
+                   const float* __restrict__ cert, int32_t* __restrict__ probes,
                    int64_t* __restrict__ flagged, int* __restrict__ nflag) {
   __shared__ uint64_t bufs[TP_WARPS][TP_CAP];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -246,16 +223,14 @@ __global__ void __launch_bounds__(TP_WARPS * 32)
       }
       prev = warp_min_u64(m);
     }
-    double xs, rs;
-    bf16_norms(xr, d, xs, rs);
-    const double B2 = cert[0], rmax = cert[1];
-    if (valid < kc || prev == KEY_NONE || !cert_inputs_ok(xs, B2, rmax)) {
+    const CertNorms cn = cert_norms(xr, d);
+    const float B2 = cert[0], rmax = cert[1];
+    if (valid < kc || prev == KEY_NONE || !cert_inputs_ok(cn, B2, rmax)) {
       ok = false;
     } else {
-      const double K = (double)key_dist(prev);
-      const double lower = IP ? cert_lower_ip(sqrt(xs), sqrt(rs), B2, rmax, K, d)
-                              : cert_lower_l2(sqrt(xs), sqrt(rs), B2, rmax, K, d);
-      ok = lower > (double)key_dist(B[P - 1]);
+      const float K = key_dist(prev);
+      const float lower = IP ? cert_lower_ip(cn, B2, rmax, K, d) : cert_lower_l2(cn, B2, rmax, K, d);
+      ok = lower > key_dist(B[P - 1]);
     }
   }
   for (int p = lane; p < P; p += 32) probes[row * P + p] = (int32_t)key_id(B[p]);
@@ -276,7 +251,7 @@ template <bool IP>
 __global__ void __launch_bounds__(FC_THREADS)
     k_flat_certify(const float* __restrict__ q, int d, const float* __restrict__ rows, int64_t nb,
                    const uint64_t* __restrict__ skeys, int R, int k, int chunk,
-                   const double* __restrict__ cert, const int* __restrict__ over,
+                   const float* __restrict__ cert, const int* __restrict__ over,
                    float* __restrict__ out_d, int64_t* __restrict__ out_l,
                    int* __restrict__ flag) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -289,7 +264,7 @@ __global__ void __launch_bounds__(FC_THREADS)
   __shared__ RadixScratch rs;
   __shared__ unsigned long long s_kmax;
   __shared__ int s_valid, s_bad;
-  __shared__ double s_xs, s_rs;
+  __shared__ CertNorms s_cn;
   const int64_t row = blockIdx.x;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint64_t* sk = skeys + row * R;
@@ -301,12 +276,8 @@ __global__ void __launch_bounds__(FC_THREADS)
   }
   __syncthreads();
   if (warp == 0) {
-    double xs, rsq;
-    bf16_norms(qv, d, xs, rsq);
-    if (lane == 0) {
-      s_xs = xs;
-      s_rs = rsq;
-    }
+    const CertNorms cn = cert_norms(qv, d);
+    if (lane == 0) s_cn = cn;
   }
   for (int c0 = 0; c0 < R; c0 += chunk) {
     const int n = min(chunk, R - c0);
@@ -355,15 +326,14 @@ __global__ void __launch_bounds__(FC_THREADS)
   if (tid == 0) {
     bool ok = !s_bad && !(over && over[row]);
     if (ok && valid >= R) {  // rows outside the shortlist exist: bound them
-      const double B2 = cert[0], rmax = cert[1];
-      if (!cert_inputs_ok(s_xs, B2, rmax) || valid < k) {
+      const float B2 = cert[0], rmax = cert[1];
+      const CertNorms cn = s_cn;
+      if (!cert_inputs_ok(cn, B2, rmax) || valid < k) {
         ok = false;
       } else {
-        const double K = (double)key_dist((uint64_t)s_kmax);
-        const double X = sqrt(s_xs), rq = sqrt(s_rs);
-        const double lower = IP ? cert_lower_ip(X, rq, B2, rmax, K, d)
-                                : cert_lower_l2(X, rq, B2, rmax, K, d);
-        ok = lower > (double)key_dist(outb[k - 1]);
+        const float K = key_dist((uint64_t)s_kmax);
+        const float lower = IP ? cert_lower_ip(cn, B2, rmax, K, d) : cert_lower_l2(cn, B2, rmax, K, d);
+        ok = lower > key_dist(outb[k - 1]);
       }
     }
     flag[row] = ok ? 0 : 1;
@@ -381,20 +351,20 @@ __global__ void k_scatter_assign(const int32_t* __restrict__ sub, const float* _
 
 }  // namespace
 
-void launch_cert_bounds(const float* norms, const float* rows, int64_t n, int d, double* cert,
+void launch_cert_bounds(const float* norms, const float* rows, int64_t n, int d, float* cert,
                         cudaStream_t s) {
   k_max_norm<<<1, 1024, 0, s>>>(norms, n, d, cert);
-  MV_CHECK_CUDA(cudaMemsetAsync(cert + 1, 0, sizeof(double), s));
+  MV_CHECK_CUDA(cudaMemsetAsync(cert + 1, 0, sizeof(float), s));
   if (n > 0)
-    k_resid_max<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(
-        rows, n, d, reinterpret_cast<unsigned long long*>(cert + 1));
+    k_resid_max<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(rows, n, d,
+                                                         reinterpret_cast<unsigned*>(cert + 1));
   count_launch();
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());
 }
 
 void launch_assign_certify(const float* x, int64_t n, int d, const float* cent, int nlist, int metric,
-                           const uint64_t* cand, int ncand, int kc, const double* cert,
+                           const uint64_t* cand, int ncand, int kc, const float* cert,
                            int32_t* assign, float* mind, int64_t* flagged, int* nflag,
                            cudaStream_t s) {
   if (n == 0) return;
@@ -410,7 +380,7 @@ void launch_assign_certify(const float* x, int64_t n, int d, const float* cent, 
 }
 
 void launch_topp_certify(const float* x, int64_t n, int d, const float* cent, int nlist, int metric,
-                         const uint64_t* cand, int ncand, int kc, int P, const double* cert,
+                         const uint64_t* cand, int ncand, int kc, int P, const float* cert,
                          int32_t* probes, int64_t* flagged, int* nflag, cudaStream_t s) {
   if (n == 0) return;
   MV_REQUIRE(ncand <= TP_CAP && P >= 1 && P <= kc, MV_ERR_INTERNAL, "top-P certify: bad sizes");
@@ -437,7 +407,7 @@ size_t flat_certify_smem(int d, int R, int k) {
 }
 
 void launch_flat_certify(const float* q, int64_t nq, int d, int metric, const float* rows,
-                         int64_t nb, const uint64_t* skeys, int R, int k, const double* cert,
+                         int64_t nb, const uint64_t* skeys, int R, int k, const float* cert,
                          const int* over, float* out_d, int64_t* out_l, int* flag,
                          cudaStream_t s) {
   if (nq == 0) return;

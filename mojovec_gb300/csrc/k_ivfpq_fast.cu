@@ -25,6 +25,7 @@
 #include "mv_kernels.h"
 #include "mv_fast.h"
 #include "mv_select.cuh"
+#include "mv_adc.cuh"
 
 #include <algorithm>
 
@@ -110,41 +111,6 @@ __global__ void __launch_bounds__(FT)
     probes[row * nprobe + p] = ok ? (int32_t)key_id(key) : -1;
     term[row * nprobe + p] = ok ? key_dist(key) : 0.0f;
   }
-}
-
-// Sum of the M table entries of one code; four partial sums break the
-// dependency chain (the fast form does not reproduce the reference's order).
-template <typename T>
-__device__ __forceinline__ float lut_val(const T* lut, int i) {
-  if constexpr (sizeof(T) == 2) return __half2float(lut[i]);
-  else return lut[i];
-}
-
-template <typename T>
-__device__ __forceinline__ float adc_fast(const T* lut, const uint8_t* code, int M, float acc) {
-  float p[4] = {acc, 0.0f, 0.0f, 0.0f};
-  if ((M & 15) == 0) {
-    for (int m0 = 0; m0 < M; m0 += 16) {
-      const uint4 v = *reinterpret_cast<const uint4*>(code + m0);
-      const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) p[b] += lut_val(lut, ((m0 + 4 * i + b) << 8) + ((w[i] >> (8 * b)) & 255u));
-    }
-  } else if ((M & 7) == 0) {
-    for (int m0 = 0; m0 < M; m0 += 8) {
-      const uint2 v = *reinterpret_cast<const uint2*>(code + m0);
-      const uint32_t w[2] = {v.x, v.y};
-#pragma unroll
-      for (int i = 0; i < 2; ++i)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) p[b] += lut_val(lut, ((m0 + 4 * i + b) << 8) + ((w[i] >> (8 * b)) & 255u));
-    }
-  } else {
-    for (int m = 0; m < M; ++m) p[m & 3] += lut_val(lut, (m << 8) + code[m]);
-  }
-  return (p[0] + p[1]) + (p[2] + p[3]);
 }
 
 // Coarse step from the fused GEMM's per-segment candidates: the nc
@@ -454,109 +420,185 @@ __global__ void __launch_bounds__(CR_WARPS * 32)
   coarse_recheck_warp(B, row, q, d, cent, nlist, metric, nc, nprobe, probes, term, err);
 }
 
-// Per-query table lut[m][k] = scale * <q_m, C[m][k]>: warp w builds
-// subspaces w, w + 8, ...; each lane owns 8 codewords and keeps q_m in
-// registers, with the codeword rows read as float4 when dsub is 4 or 8.
-// Emits value v of entry (mm, k) through put(index, v).
-template <int NT, typename Put>
-__device__ __forceinline__ void build_lut(Put put, const float* qv, const float* pq, int M,
-                                          int dsub, float scale) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int mm = warp; mm < M; mm += NT / 32) {
-    const float* cm = pq + (int64_t)mm * 256 * dsub;
-    const float* xm = qv + mm * dsub;
-    if (dsub == 8) {
-      const float4 qa = *reinterpret_cast<const float4*>(xm);
-      const float4 qb = *reinterpret_cast<const float4*>(xm + 4);
-      float4 ca[8], cb[8];
+// ---------------------------------------------------------------------------
+// Bank-rotated tables. A warp that looks up one subspace's 256-entry table
+// for 32 candidates at once sends 32 random codes to random banks (about 3.5
+// wavefronts per lookup instruction, more with repeats). Here every
+// subspace's table lives in one bank per copy: in a pass of S subspaces
+// (S = 8, 16 or 32) with C = 32 / S copies, entry (m, c) of subspace
+// m = p S + j sits at word (c + 256 p) * 32 + j + S h for copy h. Lane l
+// (r = l mod S, h = l / S) looks up subspace (r + s) mod S at step s, in copy
+// h, so the 32 lanes of a step read 32 different banks whatever the codes:
+// one wavefront per lookup instruction. Each lane rotates its candidate's
+// code bytes by r first (a word barrel shift and a funnel shift), so step s
+// reads byte s of the rotated code. Subspaces past M (M not a multiple of S)
+// are zero tables read with zero code bytes.
+//
+// Entries are integers: the query's table values times 2^e, rounded, with e
+// chosen from a Cauchy-Schwarz bound (sum over m of ||q_m|| times the
+// largest codeword norm of m) so that every sum stays below 2^30. Integer
+// sums do not depend on the order of the terms, so a candidate's distance
+// does not depend on the lane (the rotation) that computes it.
+// ---------------------------------------------------------------------------
+template <int WS>
+__device__ __forceinline__ void load_code_words(const uint8_t* __restrict__ row, int M, int p,
+                                                uint32_t (&w)[WS]) {
+  const int nw = M >> 2, w0 = p * WS;
+  if ((M & 15) == 0 && (WS & 3) == 0) {
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const float* c = cm + (lane + 32 * u) * 8;
-        ca[u] = __ldg(reinterpret_cast<const float4*>(c));
-        cb[u] = __ldg(reinterpret_cast<const float4*>(c + 4));
-      }
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        float dot = qa.x * ca[u].x;
-        dot = fmaf(qa.y, ca[u].y, dot);
-        dot = fmaf(qa.z, ca[u].z, dot);
-        dot = fmaf(qa.w, ca[u].w, dot);
-        dot = fmaf(qb.x, cb[u].x, dot);
-        dot = fmaf(qb.y, cb[u].y, dot);
-        dot = fmaf(qb.z, cb[u].z, dot);
-        dot = fmaf(qb.w, cb[u].w, dot);
-        put((mm << 8) + lane + 32 * u, scale * dot);
-      }
-    } else if (dsub == 4) {
-      const float4 qa = *reinterpret_cast<const float4*>(xm);
-      float4 ca[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) ca[u] = __ldg(reinterpret_cast<const float4*>(cm + (lane + 32 * u) * 4));
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        float dot = qa.x * ca[u].x;
-        dot = fmaf(qa.y, ca[u].y, dot);
-        dot = fmaf(qa.z, ca[u].z, dot);
-        dot = fmaf(qa.w, ca[u].w, dot);
-        put((mm << 8) + lane + 32 * u, scale * dot);
-      }
-    } else {
-      for (int u = 0; u < 8; ++u) {
-        const float* c = cm + (lane + 32 * u) * dsub;
-        float dot = 0.0f;
-        for (int t = 0; t < dsub; ++t) dot = fmaf(xm[t], c[t], dot);
-        put((mm << 8) + lane + 32 * u, scale * dot);
-      }
+    for (int i = 0; i < WS; i += 4) {
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (w0 + i < nw) v = *reinterpret_cast<const uint4*>(row + 4 * (w0 + i));
+      w[i] = v.x;
+      w[i + 1] = v.y;
+      w[i + 2] = v.z;
+      w[i + 3] = v.w;
     }
+  } else if ((M & 7) == 0 && (WS & 1) == 0) {
+#pragma unroll
+    for (int i = 0; i < WS; i += 2) {
+      uint2 v = make_uint2(0u, 0u);
+      if (w0 + i < nw) v = *reinterpret_cast<const uint2*>(row + 4 * (w0 + i));
+      w[i] = v.x;
+      w[i + 1] = v.y;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < WS; ++i)
+      w[i] = w0 + i < nw ? *reinterpret_cast<const uint32_t*>(row + 4 * (w0 + i)) : 0u;
   }
 }
 
-// The same table from an FP16 copy of the codebook scaled by a power of two
-// (pq16 = s * pq, inv = 1 / s; dsub 4 or 8): half the bytes read per query.
-template <int NT, typename Put>
-__device__ __forceinline__ void build_lut16(Put put, const float* qv, const __half* pq16, int M,
-                                            int dsub, float scale) {
+// Per-lane state of the rotated lookups.
+template <int S>
+struct RotLane {
+  static constexpr int WS = S / 4;
+  int boff[S];  // byte offset, within a 128-byte table row, of step s's bank
+  int qw, rb8;  // word rotation and bit shift of the lane's code bytes
+  __device__ __forceinline__ void init(int lane) {
+    const int r = lane & (S - 1), h = lane / S;
+#pragma unroll
+    for (int s = 0; s < S; ++s) boff[s] = 4 * (((r + s) & (S - 1)) + S * h);
+    qw = r >> 2;
+    rb8 = 8 * (r & 3);
+  }
+  // Sum of the table entries of one pass of a code (words w, zero past M).
+  __device__ __forceinline__ int sum(const int* tab, const uint32_t (&w)[WS]) const {
+    uint32_t L[WS];
+#pragma unroll
+    for (int i = 0; i < WS; ++i) L[i] = w[i];
+#pragma unroll
+    for (int b = 1; b < WS; b <<= 1) {
+      const bool f = (qw & b) != 0;
+      uint32_t T[WS];
+#pragma unroll
+      for (int i = 0; i < WS; ++i) T[i] = f ? L[(i + b) % WS] : L[i];
+#pragma unroll
+      for (int i = 0; i < WS; ++i) L[i] = T[i];
+    }
+    uint32_t o[WS];
+#pragma unroll
+    for (int i = 0; i < WS; ++i) o[i] = __funnelshift_r(L[i], L[(i + 1) % WS], rb8);
+    const char* tb = reinterpret_cast<const char*>(tab);
+    int a0 = 0, a1 = 0;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      const uint32_t c = (o[s >> 2] >> (8 * (s & 3))) & 255u;
+      const int v = *reinterpret_cast<const int*>(tb + (c << 7) + boff[s]);
+      if (s & 1) a1 += v;
+      else a0 += v;
+    }
+    return a0 + a1;
+  }
+};
+
+// The query's integer tables in the rotated layout: entry (m, c) =
+// rint(mul * <q_m, C[m][c]>), with mul = table scale * 2^e (and the FP16
+// codebook's power-of-two scale when pq16 is used). Lane l computes
+// subspace p S + (l mod S) for code j C + l / S and the C lanes of a slot
+// swap values so each writes all C codes of the group into its own bank.
+template <int NT, int S>
+__device__ __forceinline__ void build_rot_tables(int* tab, const float* qv, const float* pq,
+                                                 const __half* pq16, int M, int dsub, float mul) {
+  constexpr int C = 32 / S;
+  constexpr int GROUPS = 256 / C;
+  constexpr int NW = NT / 32;
+  constexpr int U = 4;  // codeword loads in flight per lane
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int mm = warp; mm < M; mm += NT / 32) {
-    const __half* cm = pq16 + (int64_t)mm * 256 * dsub;
-    const float* xm = qv + mm * dsub;
-    if (dsub == 8) {
-      const float4 qa = *reinterpret_cast<const float4*>(xm);
-      const float4 qb = *reinterpret_cast<const float4*>(xm + 4);
-      uint4 cw[8];
+  const int slot = lane & (S - 1), h = lane / S;
+  const int P = (M + S - 1) / S;
+  const int total = P * GROUPS;
+  auto store = [&](int it, int vi) {
+    const int p = it / GROUPS, j = it - p * GROUPS;
 #pragma unroll
-      for (int u = 0; u < 8; ++u) cw[u] = __ldg(reinterpret_cast<const uint4*>(cm + (lane + 32 * u) * 8));
+    for (int hh = 0; hh < C; ++hh) {
+      const int vv = C == 1 ? vi : __shfl_sync(0xffffffffu, vi, slot + S * hh);
+      tab[((j * C + hh) + 256 * p) * 32 + lane] = vv;
+    }
+  };
+  if (pq16 && (dsub == 8 || dsub == 4)) {
+    // Work item it = (pass p, group j): this lane's entry (m, c) with
+    // m = p S + slot, c = j C + h. U items per lane are loaded, then used.
+    for (int it0 = warp; it0 < total; it0 += NW * U) {
+      uint4 cw[U];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const float2 c0 = __half22float2(*reinterpret_cast<const __half2*>(&cw[u].x));
-        const float2 c1 = __half22float2(*reinterpret_cast<const __half2*>(&cw[u].y));
-        const float2 c2 = __half22float2(*reinterpret_cast<const __half2*>(&cw[u].z));
-        const float2 c3 = __half22float2(*reinterpret_cast<const __half2*>(&cw[u].w));
-        float dot = qa.x * c0.x;
-        dot = fmaf(qa.y, c0.y, dot);
-        dot = fmaf(qa.z, c1.x, dot);
-        dot = fmaf(qa.w, c1.y, dot);
-        dot = fmaf(qb.x, c2.x, dot);
-        dot = fmaf(qb.y, c2.y, dot);
-        dot = fmaf(qb.z, c3.x, dot);
-        dot = fmaf(qb.w, c3.y, dot);
-        put((mm << 8) + lane + 32 * u, scale * dot);
+      for (int u = 0; u < U; ++u) {
+        const int it = it0 + u * NW;
+        const int p = it / GROUPS, j = it - p * GROUPS;
+        const int m = p * S + slot, c = j * C + h;
+        cw[u] = make_uint4(0u, 0u, 0u, 0u);
+        if (it < total && m < M) {
+          if (dsub == 8) {
+            cw[u] = __ldg(reinterpret_cast<const uint4*>(pq16 + ((int64_t)m * 256 + c) * 8));
+          } else {
+            const uint2 v = __ldg(reinterpret_cast<const uint2*>(pq16 + ((int64_t)m * 256 + c) * 4));
+            cw[u].x = v.x;
+            cw[u].y = v.y;
+          }
+        }
       }
-    } else {  // dsub == 4
-      const float4 qa = *reinterpret_cast<const float4*>(xm);
-      uint2 cw[8];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) cw[u] = __ldg(reinterpret_cast<const uint2*>(cm + (lane + 32 * u) * 4));
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const float2 c0 = __half22float2(*reinterpret_cast<const __half2*>(&cw[u].x));
-        const float2 c1 = __half22float2(*reinterpret_cast<const __half2*>(&cw[u].y));
-        float dot = qa.x * c0.x;
-        dot = fmaf(qa.y, c0.y, dot);
-        dot = fmaf(qa.z, c1.x, dot);
-        dot = fmaf(qa.w, c1.y, dot);
-        put((mm << 8) + lane + 32 * u, scale * dot);
+      for (int u = 0; u < U; ++u) {
+        const int it = it0 + u * NW;
+        if (it >= total) break;  // warp-uniform
+        const int m = (it / GROUPS) * S + slot;
+        int vi = 0;
+        if (m < M) {
+          const float* xm = qv + m * dsub;
+          const float4 qa = *reinterpret_cast<const float4*>(xm);
+          const float2 c0 = __half22float2(*reinterpret_cast<const __half2*>(&cw[u].x));
+          const float2 c1 = __half22float2(*reinterpret_cast<const __half2*>(&cw[u].y));
+          float dot = qa.x * c0.x;
+          dot = fmaf(qa.y, c0.y, dot);
+          dot = fmaf(qa.z, c1.x, dot);
+          dot = fmaf(qa.w, c1.y, dot);
+          if (dsub == 8) {
+            const float4 qb = *reinterpret_cast<const float4*>(xm + 4);
+            const float2 c2 = __half22float2(*reinterpret_cast<const __half2*>(&cw[u].z));
+            const float2 c3 = __half22float2(*reinterpret_cast<const __half2*>(&cw[u].w));
+            dot = fmaf(qb.x, c2.x, dot);
+            dot = fmaf(qb.y, c2.y, dot);
+            dot = fmaf(qb.z, c3.x, dot);
+            dot = fmaf(qb.w, c3.y, dot);
+          }
+          vi = __float2int_rn(dot * mul);
+        }
+        store(it, vi);
       }
+    }
+  } else {
+    for (int it = warp; it < total; it += NW) {
+      const int p = it / GROUPS, j = it - p * GROUPS;
+      const int m = p * S + slot, c = j * C + h;
+      int vi = 0;
+      if (m < M) {
+        const float* xm = qv + m * dsub;
+        const float* cp = pq + ((int64_t)m * 256 + c) * dsub;
+        float dot = 0.0f;
+        for (int t = 0; t < dsub; ++t) dot = fmaf(xm[t], __ldg(cp + t), dot);
+        vi = __float2int_rn(dot * mul);
+      }
+      store(it, vi);
     }
   }
 }
@@ -568,17 +610,24 @@ __device__ __forceinline__ void build_lut16(Put put, const float* qv, const __ha
 // would overflow the staging area, and once at the end, a radix select keeps
 // the R smallest. The shortlist is written unsorted (the rerank orders it),
 // or sorted when it is the final answer.
-template <int NT, bool HALF>
-__global__ void __launch_bounds__(NT) k_ivfpq_scan_fast(FastScanArgs a) {
+// MODE 0: FP32 tables, 1: FP16 tables, 8 / 16 / 32: bank-rotated integer
+// tables with S = MODE subspaces per pass.
+template <int NT, int MODE>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_ivfpq_scan_fast(FastScanArgs a) {
   constexpr int FT = NT;
+  constexpr bool HALF = MODE == 1;
+  constexpr int S = MODE >= 8 ? MODE : 8;  // rotated modes only
+  constexpr bool ROT = MODE >= 8;
   using LutT = typename std::conditional<HALF, __half, float>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int M = a.M, d = a.d, dsub = d / M;
-  // The table region is sized for FP32 entries either way.
+  const int tab_words = ROT ? ((M + S - 1) / S) * 256 * 32 : M * 256;
+  // The table region is sized for 4-byte entries in every mode.
   LutT* lut = reinterpret_cast<LutT*>(smraw);
-  float* qv = reinterpret_cast<float*>(smraw) + M * 256;
+  int* tab = reinterpret_cast<int*>(smraw);
+  float* qv = reinterpret_cast<float*>(smraw) + tab_words;
   uint64_t* outb =
-      reinterpret_cast<uint64_t*>(smraw + (((size_t)(M * 256 + d) * 4 + 15) & ~size_t(15)));
+      reinterpret_cast<uint64_t*>(smraw + (((size_t)(tab_words + d) * 4 + 15) & ~size_t(15)));
   uint32_t* khi = reinterpret_cast<uint32_t*>(outb + a.Rp);
   uint32_t* klo = khi + a.cap;
   int64_t* poff = reinterpret_cast<int64_t*>(klo + a.cap);  // nprobe list offsets
@@ -588,6 +637,8 @@ __global__ void __launch_bounds__(NT) k_ivfpq_scan_fast(FastScanArgs a) {
   __shared__ int s_fill;
   __shared__ int s_q;
   __shared__ unsigned s_amax;  // FP16 tables: largest |entry| (float bits)
+  __shared__ int s_e;          // rotated tables: entries are in units of 2^-s_e
+  __shared__ int s_bad;        // rotated tables: non-finite query or codebook bound
   const int lane = threadIdx.x & 31;
   // One query per CTA, or (with a.counter) a persistent CTA that takes
   // queries from a global counter in a.order until none are left.
@@ -642,7 +693,31 @@ __global__ void __launch_bounds__(NT) k_ivfpq_scan_fast(FastScanArgs a) {
   // FP16 tables carry a per-query power-of-two scale so no entry overflows
   // (a first pass finds the largest magnitude); sums stay in FP32.
   float lscale = 1.0f;
-  if constexpr (HALF) {
+  if constexpr (ROT) {
+    // e from sum_m ||q_m|| * max_c ||C[m][c]|| (with slack for the FP16
+    // codebook's rounding and the FP32 dot products): |sum| < 2^30.
+    if (threadIdx.x < 32) {
+      float b = 0.0f;
+      for (int m = lane; m < M; m += 32) {
+        float s2 = 0.0f;
+        for (int t = 0; t < dsub; ++t) s2 = fmaf(qv[m * dsub + t], qv[m * dsub + t], s2);
+        b += sqrtf(s2) * a.pq_cn[m];
+      }
+      for (int o = 16; o > 0; o >>= 1) b += __shfl_xor_sync(0xffffffffu, b, o);
+      if (lane == 0) {
+        b *= fabsf(scale) * 1.0625f;
+        const bool bad = !(b <= 3.0e38f);  // NaN or infinite
+        int e = 0;
+        if (!bad && b > 0.0f) e = min(max(29 - (ilogbf(b) + 1), -120), 120);
+        s_e = e;
+        s_bad = bad ? 1 : 0;
+      }
+    }
+    __syncthreads();
+    const float mul = scale * (a.pq16 ? a.pq16_inv : 1.0f) * __int_as_float((s_e + 127) << 23);
+    build_rot_tables<NT, S>(tab, qv, a.pq, a.pq16, M, dsub, mul);
+    lscale = __int_as_float((127 - s_e) << 23);  // 2^-e
+  } else if constexpr (HALF) {
     if (threadIdx.x == 0) s_amax = 0u;
     __syncthreads();
     float mx = 0.0f;
@@ -665,6 +740,8 @@ __global__ void __launch_bounds__(NT) k_ivfpq_scan_fast(FastScanArgs a) {
     else build_lut<NT>([&](int i, float v) { lut[i] = v; }, qv, a.pq, M, dsub, scale);
   }
   __syncthreads();
+  RotLane<S> rl;  // set up after the tables so its registers are not live during the build
+  if constexpr (ROT) rl.init(lane);
   const int total = pbeg[nprobe];
   const int chunk = a.cap - a.R;
   int m = 0;
@@ -729,7 +806,21 @@ __global__ void __launch_bounds__(NT) k_ivfpq_scan_fast(FastScanArgs a) {
       const float v0 = a.vterm ? a.vterm[pos0c] : 0.0f;
       const float v1 = a.vterm ? a.vterm[pos1] : 0.0f;
       float d0, d1;
-      if constexpr (HALF) {
+      if constexpr (ROT) {
+        constexpr int WS = S / 4;
+        const int P = (M + S - 1) / S;
+        int s0 = 0, s1 = 0;
+        for (int pp = 0; pp < P; ++pp) {
+          uint32_t w0[WS], w1[WS];
+          load_code_words<WS>(a.codes + pos0c * M, M, pp, w0);
+          load_code_words<WS>(a.codes + pos1 * M, M, pp, w1);
+          s0 += rl.sum(tab + pp * 256 * 32, w0);
+          s1 += rl.sum(tab + pp * 256 * 32, w1);
+        }
+        d0 = fmaf((float)s0, lscale, t0 + v0);
+        d1 = fmaf((float)s1, lscale, t1 + v1);
+        if (s_bad) d0 = d1 = __int_as_float(0x7fc00000);
+      } else if constexpr (HALF) {
         d0 = fmaf(lscale, adc_fast(lut, a.codes + pos0c * M, M, 0.0f), t0 + v0);
         d1 = fmaf(lscale, adc_fast(lut, a.codes + pos1 * M, M, 0.0f), t1 + v1);
       } else {
@@ -1245,8 +1336,17 @@ void launch_coarse_from_keys(const uint64_t* cand, int64_t nq, int ncand, const 
 
 int fast_scan_cap(int R) { return std::max(2048, 2 * R + 1024); }
 
+// Pass width of the bank-rotated tables for M subspaces, 0 when the scan
+// keeps the plain layout.
+int fast_scan_rot(const FastScanArgs& a, int lut) {
+  if (lut != 3 || !a.pq_cn || (a.M & 3) != 0 || a.M < 8) return 0;
+  return a.M <= 8 ? 8 : (a.M <= 16 ? 16 : 32);
+}
+
 size_t fast_scan_smem(const FastScanArgs& a) {
-  return (((size_t)(a.M * 256 + a.d) * 4 + 15) & ~size_t(15)) + (size_t)next_pow2(a.R) * 8 +
+  const size_t tab_words =
+      a.rot ? (size_t)((a.M + a.rot - 1) / a.rot) * 256 * 32 : (size_t)a.M * 256;
+  return (((size_t)(tab_words + a.d) * 4 + 15) & ~size_t(15)) + (size_t)next_pow2(a.R) * 8 +
          (size_t)fast_scan_cap(a.R) * 8 + (size_t)a.nprobe * 8 + (size_t)(a.nprobe + 1) * 4 +
          (size_t)a.nprobe * 4;
 }
@@ -1254,10 +1354,12 @@ size_t fast_scan_smem(const FastScanArgs& a) {
 // Threads per CTA nt (128, 256 or 512); grid: one CTA per query, or with
 // a.counter a persistent grid of `persistent_ctas` CTAs.
 void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s, int nt, int persistent_ctas,
-                            bool lut_fp16) {
+                            int lut) {
   if (a.nq == 0) return;
+  if (lut == 4 && launch_ivfpq_scan_staged(a, s, nt, persistent_ctas, a.stage_entries)) return;
   a.cap = fast_scan_cap(a.R);
   a.Rp = next_pow2(a.R);
+  a.rot = fast_scan_rot(a, lut);
   const size_t smem = fast_scan_smem(a);
   MV_REQUIRE(smem <= 220 * 1024, MV_ERR_UNSUPPORTED, "fast IVF-PQ scan: M, d or shortlist too large");
   MV_REQUIRE(!a.counter || persistent_ctas > 0, MV_ERR_INTERNAL, "persistent scan without a grid");
@@ -1266,15 +1368,17 @@ void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s, int nt, int persiste
     smem_attr(kernel, smem);
     kernel<<<grid, threads, smem, s>>>(a);
   };
-  if (lut_fp16) {
-    if (nt == 128) go(k_ivfpq_scan_fast<128, true>, 128);
-    else if (nt == 512) go(k_ivfpq_scan_fast<512, true>, 512);
-    else go(k_ivfpq_scan_fast<256, true>, 256);
-  } else {
-    if (nt == 128) go(k_ivfpq_scan_fast<128, false>, 128);
-    else if (nt == 512) go(k_ivfpq_scan_fast<512, false>, 512);
-    else go(k_ivfpq_scan_fast<256, false>, 256);
-  }
+  auto pick = [&](auto mode) {
+    constexpr int MODE = decltype(mode)::value;
+    if (nt == 128) go(k_ivfpq_scan_fast<128, MODE>, 128);
+    else if (nt == 512) go(k_ivfpq_scan_fast<512, MODE>, 512);
+    else go(k_ivfpq_scan_fast<256, MODE>, 256);
+  };
+  if (a.rot == 8) pick(std::integral_constant<int, 8>());
+  else if (a.rot == 16) pick(std::integral_constant<int, 16>());
+  else if (a.rot == 32) pick(std::integral_constant<int, 32>());
+  else if (lut == 1) pick(std::integral_constant<int, 1>());  // 0, 2 (and 4 unstaged): FP32
+  else pick(std::integral_constant<int, 0>());
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());
 }

@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       for (; i < my_count; ++i) {
         const int s = i % STAGES;
         const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
-        if (*verr || !mbar_wait(b_empty(s), ph ^ 1u)) {
+        if (*verr || !mbar_wait(b_empty(s), ph ^ 1u, g.wait_limit)) {
           *verr = 1;
           break;
         }
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
         const int acc = i & 1;
         const uint32_t aph = (uint32_t)(i >> 1) & 1u;
-        if (*verr || !mbar_wait(b_tempty(acc), aph ^ 1u) || !mbar_wait(b_full(s), ph)) {
+        if (*verr || !mbar_wait(b_tempty(acc), aph ^ 1u, g.wait_limit) || !mbar_wait(b_full(s), ph, g.wait_limit)) {
           *verr = 1;
           break;
         }
@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     for (int i = 0; i < my_count; ++i) {
       const int acc = i & 1;
       const uint32_t aph = (uint32_t)(i >> 1) & 1u;
-      bool ok = !*verr && mbar_wait(b_tfull(acc), aph);
+      bool ok = !*verr && mbar_wait(b_tfull(acc), aph, g.wait_limit);
       if (!__all_sync(0xffffffffu, ok)) {
         *verr = 1;
         break;
@@ -362,7 +362,7 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
           for (int kb = 0; kb < nkb; ++kb, ++it) {
             const int s = it % NST;
             const uint32_t ph = (uint32_t)(it / NST) & 1u;
-            if (*verr || !mbar_wait(b_empty(s), ph ^ 1u)) {
+            if (*verr || !mbar_wait(b_empty(s), ph ^ 1u, g.wait_limit)) {
               *verr = 1;
               stop = true;
               break;
@@ -384,7 +384,7 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
         for (int i = 0; i < my_count; ++i) {
           const int acc = i & 1;
           const uint32_t aph = (uint32_t)(i >> 1) & 1u;
-          if (*verr || !mbar_wait(b_tempty(acc), aph ^ 1u)) {
+          if (*verr || !mbar_wait(b_tempty(acc), aph ^ 1u, g.wait_limit)) {
             *verr = 1;
             break;
           }
@@ -394,7 +394,7 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
           for (int kb = 0; kb < nkb; ++kb, ++it) {
             const int s = it % NST;
             const uint32_t ph = (uint32_t)(it / NST) & 1u;
-            if (*verr || !mbar_wait(b_full(s), ph)) {
+            if (*verr || !mbar_wait(b_full(s), ph, g.wait_limit)) {
               *verr = 1;
               bad = true;
               break;
@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
       for (; i < my_count; ++i) {
         const int s = i % STAGES;
         const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
-        if (*verr || !mbar_wait(b_empty(s), ph ^ 1u)) {
+        if (*verr || !mbar_wait(b_empty(s), ph ^ 1u, g.wait_limit)) {
           *verr = 1;
           break;
         }
@@ -444,14 +444,14 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       const uint32_t idesc = F8 ? idesc_e4m3_f32(BM, BN) : idesc_bf16_f32(BM, BN);
-      bool ok = mbar_wait(b_fulla, 0);
+      bool ok = mbar_wait(b_fulla, 0, g.wait_limit);
       if (!ok) *verr = 1;
       for (int i = 0; ok && i < my_count; ++i) {
         const int s = i % STAGES;
         const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
         const int acc = i & 1;
         const uint32_t aph = (uint32_t)(i >> 1) & 1u;
-        if (*verr || !mbar_wait(b_tempty(acc), aph ^ 1u) || !mbar_wait(b_full(s), ph)) {
+        if (*verr || !mbar_wait(b_tempty(acc), aph ^ 1u, g.wait_limit) || !mbar_wait(b_full(s), ph, g.wait_limit)) {
           *verr = 1;
           break;
         }
@@ -541,7 +541,7 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
     for (int i = 0; i < my_count; ++i) {
       const int acc = i & 1;
       const uint32_t aph = (uint32_t)(i >> 1) & 1u;
-      bool ok = !*verr && mbar_wait(b_tfull(acc), aph);
+      bool ok = !*verr && mbar_wait(b_tfull(acc), aph, g.wait_limit);
       if (!__all_sync(0xffffffffu, ok)) {
         *verr = 1;
         break;
@@ -797,7 +797,7 @@ __global__ void __launch_bounds__(192, 2)
       for (; it < total; ++it) {
         const int s = it % STAGES;
         const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
-        if (*verr || !mbar_wait(b_empty(s), ph ^ 1u)) {
+        if (*verr || !mbar_wait(b_empty(s), ph ^ 1u, g.wait_limit)) {
           *verr = 1;
           break;
         }
@@ -815,14 +815,14 @@ __global__ void __launch_bounds__(192, 2)
   } else if (warp == 1) {
     if (lane == 0) {
       const uint32_t idesc = idesc_bf16_f32(BM, BN);
-      bool ok = mbar_wait(b_fulla, 0);
+      bool ok = mbar_wait(b_fulla, 0, g.wait_limit);
       if (!ok) *verr = 1;
       for (int it = 0; ok && it < total; ++it) {
         const int s = it % STAGES;
         const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
         const int acc = it & 1;
         const uint32_t aph = (uint32_t)(it >> 1) & 1u;
-        if (*verr || !mbar_wait(b_tempty(acc), aph ^ 1u) || !mbar_wait(b_full(s), ph)) {
+        if (*verr || !mbar_wait(b_tempty(acc), aph ^ 1u, g.wait_limit) || !mbar_wait(b_full(s), ph, g.wait_limit)) {
           *verr = 1;
           break;
         }
@@ -882,7 +882,7 @@ __global__ void __launch_bounds__(192, 2)
       if (pass2 && grow) thr = fmaxf(thr, ordered_to_float(*reinterpret_cast<volatile uint32_t*>(grow)));
       const int acc = it & 1;
       const uint32_t aph = (uint32_t)(it >> 1) & 1u;
-      bool ok = !*verr && mbar_wait(b_tfull(acc), aph);
+      bool ok = !*verr && mbar_wait(b_tfull(acc), aph, g.wait_limit);
       if (!__all_sync(0xffffffffu, ok)) {
         *verr = 1;
         break;
@@ -1141,6 +1141,7 @@ void launch_umma_dist(int epi, const __nv_bfloat16* X, int64_t nx, const __nv_bf
   MV_REQUIRE(kp <= 256, MV_ERR_UNSUPPORTED, "BF16 GEMM supports d <= 256");
   MV_REQUIRE(nx < (1ll << 31) && ny < (1ll << 31), MV_ERR_UNSUPPORTED, "GEMM too large");
   UmmaArgs g;
+  g.wait_limit = current_wait_limit();
   g.nrows = nx;
   g.ncols = ny;
   g.nkb = kp / 64;
@@ -1249,6 +1250,7 @@ void launch_umma_topk(const __nv_bfloat16* X, int64_t nx, const __nv_bfloat16* Y
   MV_REQUIRE(nx < (1ll << 31) && ny < (1ll << 32) - 1, MV_ERR_UNSUPPORTED, "GEMM too large");
   MV_REQUIRE(nseg >= 1 && nseg <= 65535, MV_ERR_INTERNAL, "fused top-k: bad segment count");
   UmmaTopkArgs g;
+  g.wait_limit = current_wait_limit();
   g.nrows = nx;
   g.ncols = ny;
   g.nkb = kp / 64;
@@ -1343,6 +1345,7 @@ void launch_coarse_topk2(const __nv_bfloat16* X, int64_t nx, const __nv_bfloat16
   const int cap = coarse_topk2_cap(nc);
   MV_REQUIRE(nseg >= 1 && (int64_t)nseg * cap <= 256, MV_ERR_INTERNAL, "two-pass coarse GEMM: bad segment count");
   CoarseTopkArgs g;
+  g.wait_limit = current_wait_limit();
   g.nrows = nx;
   g.ncols = ny;
   g.nkb = kp / 64;
@@ -1384,6 +1387,7 @@ void launch_umma_topk_e4m3(const uint8_t* X8, int64_t nx, const float* xscale, c
   MV_REQUIRE(nseg >= 1 && nseg <= 65535, MV_ERR_INTERNAL, "fused top-k: bad segment count");
   MV_REQUIRE(xscale && yscale, MV_ERR_INTERNAL, "E4M3 GEMM needs row and column scales");
   UmmaTopkArgs g;
+  g.wait_limit = current_wait_limit();
   g.nrows = nx;
   g.ncols = ny;
   g.nkb = kp / 128;

@@ -6,6 +6,7 @@
 // their inputs to the device on a per-call stream, run, copy the results
 // back and synchronise that stream before returning.
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <limits>
 #include <memory>
@@ -26,14 +27,22 @@ static thread_local mv_ctx* g_cur_ctx = nullptr;
 
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 
+// cudaFuncSetAttribute applies to the current device, so the highest limit
+// set so far is remembered per (device, kernel).
 void raise_smem_limit(const void* kernel, size_t bytes) {
   static std::mutex mu;
-  static std::unordered_map<const void*, size_t> high;
+  static std::map<std::pair<int, const void*>, size_t> high;
+  int dev = 0;
+  MV_CHECK_CUDA(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> lk(mu);
-  size_t& h = high[kernel];
+  size_t& h = high[{dev, kernel}];
   if (bytes <= h) return;
   MV_CHECK_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   h = bytes;
+}
+
+long long current_wait_limit() {
+  return g_cur_ctx ? g_cur_ctx->wait_limit.load(std::memory_order_relaxed) : 4000000000ll;
 }
 
 void count_launch() {
@@ -66,6 +75,8 @@ int32_t guard(mv_ctx* ctx, F&& f) {
     return MV_ERR_INTERNAL;
   }
 }
+
+int32_t guarded(mv_ctx* ctx, const std::function<void()>& f) { return guard(ctx, f); }
 
 void h2d(void* dst, const void* src, size_t bytes, cudaStream_t s) {
   if (bytes) MV_CHECK_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
@@ -148,7 +159,7 @@ void assign_nearest(const float* x, int64_t n, int d, const float* cent, int k, 
   Arena ar(buf);
   __nv_bfloat16* cb = ar.take<__nv_bfloat16>((size_t)k * kp);
   float* cn = ar.take<float>(k);
-  double* bounds = ar.take<double>(2);
+  float* bounds = ar.take<float>(2);
   __nv_bfloat16* xb = ar.take<__nv_bfloat16>((size_t)chunk * kp);
   uint64_t* cand = ar.take<uint64_t>((size_t)chunk * osegs * ncp);
   uint64_t* gthr = ar.take<uint64_t>(chunk);
@@ -408,6 +419,12 @@ int32_t mv_ctx_synchronize(mv_ctx* ctx) {
 
 int64_t mv_ctx_kernel_launches(mv_ctx* ctx) { return ctx ? ctx->launches.load() : -1; }
 
+int32_t mv_ctx_set_wait_limit(mv_ctx* ctx, int64_t cycles) {
+  if (!ctx) return MV_ERR_ARG;
+  ctx->wait_limit.store(cycles < 0 ? 4000000000ll : (long long)cycles, std::memory_order_relaxed);
+  return MV_OK;
+}
+
 int32_t mv_ctx_certify_stats(mv_ctx* ctx, int64_t* out4) {
   if (!ctx || !out4) return MV_ERR_ARG;
   out4[0] = ctx->assign_rows.load();
@@ -501,7 +518,7 @@ void ensure_coarse(mv_ivfpq* ix, cudaStream_t s);
 // bound leaves open and everywhere else. Returns false when the certified
 // path does not apply (the caller runs the exact one).
 bool coarse_topp_certified(mv_ctx* ctx, const float* d_q, int64_t nq, int d, const float* cent,
-                           const __nv_bfloat16* cent_bf16, const float* cnorm, const double* ccert,
+                           const __nv_bfloat16* cent_bf16, const float* cnorm, const float* ccert,
                            int nlist, int metric, int P, int32_t* probes, cudaStream_t s) {
   const int nc = std::min(nlist, P + std::max(16, P / 2));
   if (nc > UMMA_TOPK_MAX || nc >= nlist || umma_kpad(d) > UMMA_TOPK_MAX_K || nq > 0x7fffffffll) return false;
@@ -609,7 +626,7 @@ void ivfpq_search_plain(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int n
       StageTimer t(ix->ctx, MV_STAGE_COARSE, s);
       certified = coarse_topp_certified(ix->ctx, xq, nb, ix->d, ix->centroids.as<float>(),
                                         ix->d_cent_bf16.as<__nv_bfloat16>(), ix->d_cnorm.as<float>(),
-                                        ix->d_ccert.as<double>(), ix->nlist, ix->metric, nprobe,
+                                        ix->d_ccert.as<float>(), ix->nlist, ix->metric, nprobe,
                                         probes, s);
     }
     if (!certified) {
@@ -669,11 +686,11 @@ void build_coarse_locked(mv_ivfpq* ix, cudaStream_t s) {
   const int kp = umma_kpad(ix->d);
   ix->d_cent_bf16.ensure((size_t)ix->nlist * kp * 2);
   ix->d_cnorm.ensure((size_t)ix->nlist * 4);
-  ix->d_ccert.ensure(2 * sizeof(double));
+  ix->d_ccert.ensure(2 * sizeof(float));
   launch_to_bf16(ix->centroids.as<float>(), ix->nlist, ix->d, ix->d_cent_bf16.as<__nv_bfloat16>(),
                  ix->d_cnorm.as<float>(), s);
   launch_cert_bounds(ix->d_cnorm.as<float>(), ix->centroids.as<float>(), ix->nlist, ix->d,
-                     ix->d_ccert.as<double>(), s);
+                     ix->d_ccert.as<float>(), s);
   sync(s);
   ix->coarse_ready = true;
 }
@@ -689,7 +706,7 @@ void ensure_fast(mv_ivfpq* ix, cudaStream_t s) {
   build_coarse_locked(ix, s);
   const int64_t total = ix->h_off[ix->nlist];
   if (ix->metric == MV_METRIC_L2 && total > 0) {
-    ix->d_vec_term.ensure((size_t)total * 4);
+    ix->d_vec_term.ensure((size_t)total * 4 + 16);  // staged scans copy 16-byte supersets
     launch_vec_terms(ix->d_off.as<int64_t>(), ix->nlist, ix->d_codes.as<uint8_t>(),
                      ix->pq.as<float>(), ix->centroids.as<float>(), ix->d, ix->M,
                      ix->d_vec_term.as<float>(), s);
@@ -698,7 +715,38 @@ void ensure_fast(mv_ivfpq* ix, cudaStream_t s) {
   // the largest magnitude lies in [2^13, 2^14): no overflow, and the scale
   // divides out exactly.
   ix->pq16_inv = 0.0f;
+  ix->has_pq_cn = false;
   const int dsub = ix->d / ix->M;
+  {
+    // Per subspace, the largest codeword norm (in double, rounded up): the
+    // bound that scales the rotated-table scan's integer tables.
+    const size_t npq = (size_t)ix->M * 256 * dsub;
+    std::vector<float> h(npq);
+    d2h(h.data(), ix->pq.p, sizeof(float) * npq, s);
+    sync(s);
+    std::vector<float> cn(ix->M);
+    bool ok = true;
+    for (int m = 0; m < ix->M; ++m) {
+      double mx = 0.0;
+      for (int c = 0; c < 256; ++c) {
+        double s2 = 0.0;
+        for (int t = 0; t < dsub; ++t) {
+          const double v = h[((size_t)m * 256 + c) * dsub + t];
+          s2 += v * v;
+        }
+        mx = std::max(mx, s2);
+      }
+      const double nrm = std::sqrt(mx) * (1.0 + 1e-6);
+      ok = ok && std::isfinite(nrm) && nrm < 1e37;
+      cn[m] = (float)nrm;
+    }
+    if (ok) {
+      ix->d_pq_cn.ensure((size_t)ix->M * 4);
+      h2d(ix->d_pq_cn.p, cn.data(), (size_t)ix->M * 4, s);
+      sync(s);
+      ix->has_pq_cn = true;
+    }
+  }
   if (dsub == 4 || dsub == 8) {
     const size_t npq = (size_t)ix->M * 256 * dsub;
     std::vector<float> h(npq);
@@ -856,6 +904,7 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
         a.pq16 = ix->d_pq16.as<__half>();
         a.pq16_inv = ix->pq16_inv;
       }
+      if (ix->has_pq_cn) a.pq_cn = ix->d_pq_cn.as<float>();
       a.list_off = ix->d_off.as<int64_t>();
       a.codes = ix->d_codes.as<uint8_t>();
       a.vterm = ix->metric == MV_METRIC_L2 ? ix->d_vec_term.as<float>() : nullptr;
@@ -879,9 +928,9 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
         a.counter = batch->scan_ctas_per_sm > 0 ? batch->counter : nullptr;
         if (a.counter) MV_CHECK_CUDA(cudaMemsetAsync(a.counter, 0, sizeof(int), s));
         launch_ivfpq_scan_fast(a, s, batch->scan_threads,
-                               batch->scan_ctas_per_sm * ix->ctx->num_sms, p && p->lut_fp16);
+                               batch->scan_ctas_per_sm * ix->ctx->num_sms, p ? p->lut_fp16 : 0);
       } else {
-        launch_ivfpq_scan_fast(a, s, 256, 0, p && p->lut_fp16);
+        launch_ivfpq_scan_fast(a, s, 256, 0, p ? p->lut_fp16 : 0);
       }
     }
     if (p && p->rerank > 0) {
@@ -1364,11 +1413,11 @@ void ensure_flat_fast(mv_flat* ix, cudaStream_t s) {
   const int kp = umma_kpad(ix->d);
   ix->rows_bf16.ensure((size_t)ix->ntotal * kp * 2);
   ix->norms.ensure((size_t)ix->ntotal * 4);
-  ix->cert.ensure(2 * sizeof(double));
+  ix->cert.ensure(2 * sizeof(float));
   launch_to_bf16(ix->rows.as<float>(), ix->ntotal, ix->d, ix->rows_bf16.as<__nv_bfloat16>(),
                  ix->norms.as<float>(), s);
   launch_cert_bounds(ix->norms.as<float>(), ix->rows.as<float>(), ix->ntotal, ix->d,
-                     ix->cert.as<double>(), s);
+                     ix->cert.as<float>(), s);
   sync(s);
   ix->fast_ready = true;
 }
@@ -1439,7 +1488,7 @@ void flat_search_plain(mv_flat* ix, const float* d_x, int64_t nq, int k, const u
       launch_flat_merge(cand, nqb, osegs, ncp, kseg, R, skeys, k, nullptr, ix->metric, 0.0f,
                         nullptr, nullptr, kseg < R ? over : nullptr, s);
       launch_flat_certify(xb, nqb, ix->d, ix->metric, ix->rows.as<float>(), nb, skeys, R, k,
-                          ix->cert.as<double>(), kseg < R ? over : nullptr, d_out + q0 * k,
+                          ix->cert.as<float>(), kseg < R ? over : nullptr, d_out + q0 * k,
                           d_lab + q0 * k, flag, s);
     }
     h_flag.resize((size_t)nqb);
@@ -2705,11 +2754,11 @@ void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int npr
     if (!ix->fast_ready) {
       ix->d_cent_bf16.ensure((size_t)ix->nlist * kp * 2);
       ix->d_cnorm.ensure((size_t)ix->nlist * 4);
-      ix->d_ccert.ensure(2 * sizeof(double));
+      ix->d_ccert.ensure(2 * sizeof(float));
       launch_to_bf16(ix->centroids.as<float>(), ix->nlist, ix->d,
                      ix->d_cent_bf16.as<__nv_bfloat16>(), ix->d_cnorm.as<float>(), s);
       launch_cert_bounds(ix->d_cnorm.as<float>(), ix->centroids.as<float>(), ix->nlist, ix->d,
-                         ix->d_ccert.as<double>(), s);
+                         ix->d_ccert.as<float>(), s);
       sync(s);
       ix->fast_ready = true;
     }
@@ -2748,7 +2797,7 @@ void ivfflat_search(mv_ivfflat* ix, const float* d_x, int64_t nq, int k, int npr
       StageTimer t(ix->ctx, MV_STAGE_COARSE, s);
       certified = coarse_topp_certified(ix->ctx, xb, nb, ix->d, ix->centroids.as<float>(),
                                         ix->d_cent_bf16.as<__nv_bfloat16>(), ix->d_cnorm.as<float>(),
-                                        ix->d_ccert.as<double>(), ix->nlist, ix->metric, nprobe,
+                                        ix->d_ccert.as<float>(), ix->nlist, ix->metric, nprobe,
                                         probes, s);
     }
     if (!certified) {

@@ -22,25 +22,77 @@
 //     (d + 16) 2^-23 (X + rq)(B + rmax).
 // Every margin is widened by 1 %; the caller compares strictly, so a row at
 // exactly the bound cannot tie its way in.
+//
+// The bound arithmetic itself is FP32 with directed rounding: every
+// quantity that enters as an upper bound is computed rounding up
+// (__f*_ru), every lower bound rounding down (__f*_rd), so the computed
+// bound is never above the exact one. Inputs outside cert_inputs_ok's range
+// (where FP32 products could overflow or lose the bound) take the exact
+// path instead.
 #pragma once
+
+#include <cuda_bf16.h>
 
 namespace mv {
 
-__device__ __forceinline__ double cert_lower_l2(double X, double rq, double B2, double rmax,
-                                                double K, int d) {
-  const double B = sqrt(B2);
-  const double eps = ((d + 1) * 0x1p-23 * B2 + (d + 1) * 0x1p-20 * X * B) * 1.01 + d * 1e-36;
-  const double sb = X * X + K - eps;
-  const double s = (sb > 0.0 ? sqrt(sb) : 0.0) - (rq + rmax) * 1.01 - 1e-30;
-  return s > 0.0 ? s * s * (1.0 - (d + 16) * 0x1p-23) : -1.0;
+// Upper and lower bounds on ||bq||^2 and an upper bound on ||q - bq||^2 for
+// one row (bq = the row rounded to BF16), one warp; every lane gets them.
+struct CertNorms {
+  float xs_lo, xs_hi, rs_hi;
+};
+
+__device__ __forceinline__ CertNorms cert_norms(const float* x, int d) {
+  const int lane = threadIdx.x & 31;
+  float lo = 0.0f, hi = 0.0f, rs = 0.0f;
+  for (int j = lane; j < d; j += 32) {
+    const float v = x[j];
+    const float b = __bfloat162float(__float2bfloat16_rn(v));
+    const float r = __fsub_rn(v, b);  // exact: b is v rounded to 8 significant bits
+    lo = __fadd_rd(lo, __fmul_rd(b, b));
+    hi = __fadd_ru(hi, __fmul_ru(b, b));
+    rs = __fadd_ru(rs, __fmul_ru(r, r));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = __fadd_rd(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = __fadd_ru(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    rs = __fadd_ru(rs, __shfl_xor_sync(0xffffffffu, rs, o));
+  }
+  return {lo, hi, rs};
 }
 
-__device__ __forceinline__ double cert_lower_ip(double X, double rq, double B2, double rmax,
-                                                double K, int d) {
-  const double B = sqrt(B2);
-  const double m = (d + 1) * 0x1p-20 * X * B + rq * (B + rmax) + X * rmax +
-                   (d + 16) * 0x1p-23 * (X + rq) * (B + rmax);
-  return K - m * 1.01 - d * 1e-36;
+// Ranges where every FP32 product of the bounds stays finite; rows outside
+// them (and NaN) take the exact scan.
+__device__ __forceinline__ bool cert_inputs_ok(const CertNorms& n, float B2, float rmax) {
+  return B2 >= 1e-30f && B2 <= 1e30f && n.xs_lo >= 1e-30f && n.xs_hi <= 1e30f &&
+         n.rs_hi <= 1e30f && rmax <= 1e15f;
+}
+
+__device__ __forceinline__ float cert_lower_l2(const CertNorms& n, float B2, float rmax, float K,
+                                               int d) {
+  const float B = __fsqrt_ru(B2), X = __fsqrt_ru(n.xs_hi), rq = __fsqrt_ru(n.rs_hi);
+  const float c1 = __fmul_ru((float)(d + 1), 0x1p-23f), c2 = __fmul_ru((float)(d + 1), 0x1p-20f);
+  const float eps = __fadd_ru(__fmul_ru(__fadd_ru(__fmul_ru(c1, B2), __fmul_ru(c2, __fmul_ru(X, B))),
+                                        1.01f),
+                              __fmul_ru((float)d, 1e-36f));
+  const float sb = __fsub_rd(__fadd_rd(n.xs_lo, K), eps);
+  const float s = __fsub_rd(__fsub_rd(sb > 0.0f ? __fsqrt_rd(sb) : 0.0f,
+                                      __fmul_ru(__fadd_ru(rq, rmax), 1.01f)),
+                            1e-30f);
+  if (!(s > 0.0f)) return -1.0f;
+  const float f = __fsub_rd(1.0f, __fmul_ru((float)(d + 16), 0x1p-23f));
+  return __fmul_rd(__fmul_rd(s, s), f);
+}
+
+__device__ __forceinline__ float cert_lower_ip(const CertNorms& n, float B2, float rmax, float K,
+                                               int d) {
+  const float B = __fsqrt_ru(B2), X = __fsqrt_ru(n.xs_hi), rq = __fsqrt_ru(n.rs_hi);
+  const float Br = __fadd_ru(B, rmax);
+  const float c2 = __fmul_ru((float)(d + 1), 0x1p-20f), c3 = __fmul_ru((float)(d + 16), 0x1p-23f);
+  float m = __fmul_ru(c2, __fmul_ru(X, B));
+  m = __fadd_ru(m, __fmul_ru(rq, Br));
+  m = __fadd_ru(m, __fmul_ru(X, rmax));
+  m = __fadd_ru(m, __fmul_ru(c3, __fmul_ru(__fadd_ru(X, rq), Br)));
+  return __fsub_rd(__fsub_rd(K, __fmul_ru(m, 1.01f)), __fmul_ru((float)d, 1e-36f));
 }
 
 }  // namespace mv

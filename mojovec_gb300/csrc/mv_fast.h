@@ -20,6 +20,9 @@ struct FastScanArgs {
   // by the FP16 rounding of the codewords.
   const __half* pq16 = nullptr;
   float pq16_inv = 1.0f;
+  // Per subspace, an upper bound on the largest codeword norm; when set the
+  // scan uses the bank-rotated integer tables (M a multiple of 4, M >= 8).
+  const float* pq_cn = nullptr;
   const int64_t* list_off;
   const uint8_t* codes;
   const float* vterm;     // per CSR entry, null for IP
@@ -41,6 +44,8 @@ struct FastScanArgs {
   int64_t filter_len = 0;
   const uint32_t* ids = nullptr;
   int cap, Rp;            // set by the launcher
+  int rot = 0;            // set by the launcher: rotated-table pass width (0: none)
+  int stage_entries = 0;  // staged scan: candidates per staged round (0: automatic)
 };
 
 struct RerankArgs {
@@ -95,9 +100,16 @@ void launch_coarse_from_keys(const uint64_t* cand, int64_t nq, int ncand, const 
                              const float* cent, int nlist, int metric, int nc, int nprobe,
                              int32_t* probes, float* term, int* err, cudaStream_t s);
 size_t fast_scan_smem(const FastScanArgs& a);
-// lut_fp16: FP16 tables with a per-query power-of-two scale (FP32 sums).
+// The staged scan (k_ivfpq_scan.cu); returns false, launching nothing, when
+// its shared memory would not fit (the caller runs the unstaged kernel).
+bool launch_ivfpq_scan_staged(FastScanArgs a, cudaStream_t s, int nt, int persistent_ctas, int E);
+// lut: 0 or 2 = FP32 tables read with codes from global memory, 1 = FP16
+// tables with a per-query power-of-two scale (FP32 sums), 3 = bank-rotated
+// fixed-point tables where M allows (else FP32), 4 = FP32 tables with codes
+// and terms staged in shared memory by bulk copies (the unstaged kernel when
+// that does not fit).
 void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s, int nt = 256, int persistent_ctas = 0,
-                            bool lut_fp16 = false);
+                            int lut = 0);
 // Flat fast form: merge nseg x ncp per-segment keys (kseg kept per segment)
 // into the R-key shortlist per query. With out_keys the shortlist is
 // written (unsorted) for the rerank; otherwise the k smallest become the

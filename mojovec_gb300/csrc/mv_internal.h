@@ -2,6 +2,7 @@
 // per-call stream/workspace pool and the index objects behind the C ABI.
 #pragma once
 
+#include <functional>
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -86,6 +87,13 @@ inline size_t ws_bytes(size_t count, size_t elem) { return (count * elem + 255) 
 // launch that needs more is never undercut by one that needs less. Needed
 // whenever static + dynamic shared memory exceeds 48 KB.
 void raise_smem_limit(const void* kernel, size_t bytes);
+// Runs f with ctx as the calling thread's current context (its device set,
+// its launch counter counting) and turns exceptions into status codes and
+// the thread's last error message, as every entry point does.
+int32_t guarded(mv_ctx* ctx, const std::function<void()>& f);
+// The pipeline-wait limit (cycles) of the calling thread's current context
+// (the default when there is none), copied into each tensor-core launch.
+long long current_wait_limit();
 template <typename K>
 inline void smem_limit(K kernel, size_t bytes) {
   raise_smem_limit(reinterpret_cast<const void*>(kernel), bytes);
@@ -113,6 +121,9 @@ struct mv_ctx {
   std::atomic<int64_t> launches{0};
   cudaStream_t main_stream = nullptr;
   mv::DevBuf d_err;  // int: set by kernels whose bounded waits gave up
+  // cycles a tensor-core kernel's pipeline wait may take before it gives up
+  // (mv_ctx_set_wait_limit); 0 = give up at once unless already complete
+  std::atomic<long long> wait_limit{4000000000ll};
   // certified selections (mv_ctx_certify_stats): nearest-centroid rows and
   // plain Flat queries, and how many of each the bound left to the exact scan
   std::atomic<int64_t> assign_rows{0}, assign_fallback{0}, flat_queries{0}, flat_fallback{0};
@@ -206,13 +217,15 @@ struct mv_ivfpq {
   std::mutex fast_mu;
   bool fast_ready = false;
   bool coarse_ready = false;  // d_cent_bf16, d_cnorm, d_ccert (centroid-only state)
-  mv::DevBuf d_ccert;       // 2 doubles: bound on ||bf16(c)||^2, max ||c - bf16(c)||
+  mv::DevBuf d_ccert;       // 2 floats: bound on ||bf16(c)||^2, max ||c - bf16(c)||
   mv::DevBuf d_vec_term;    // FP32 per vector: ||y||^2 + 2<c, y> (y = PQ reconstruction)
   mv::DevBuf d_raw16;       // BF16 rows per entry (certified rerank prescreen)
   mv::DevBuf d_rad;         // FP32 per entry: bound on ||y - bf16(y)||
   mv::DevBuf d_n16;         // FP32 per entry: bound on ||bf16(y)||
   mv::DevBuf d_pq16;        // FP16 codebook * pq16_scale (fast-form tables; dsub 4 or 8)
   float pq16_inv = 0.0f;    // 1 / scale; 0 = no FP16 codebook
+  mv::DevBuf d_pq_cn;       // FP32 per subspace: bound on its largest codeword norm
+  bool has_pq_cn = false;
   mv::DevBuf d_cnorm;       // FP32 per centroid ||c||^2
   mv::DevBuf d_cent_bf16;   // nlist x d BF16
 };
@@ -231,7 +244,7 @@ struct mv_ivfflat {
   std::mutex fast_mu;
   bool fast_ready = false;
   mv::DevBuf d_cent_bf16, d_cnorm;  // fast coarse step
-  mv::DevBuf d_ccert;               // 2 doubles: coarse certificate bounds
+  mv::DevBuf d_ccert;               // 2 floats: coarse certificate bounds
 };
 
 struct mv_flat {
@@ -242,7 +255,7 @@ struct mv_flat {
   mv::DevBuf rows;       // capacity x d FP32
   mv::DevBuf rows_bf16;  // ntotal x kpad BF16 (fast form, built lazily)
   mv::DevBuf norms;      // FP32 ||x||^2 per rounded row (fast form)
-  mv::DevBuf cert;       // 2 doubles: bound on ||bf16(y)||^2, max ||y - bf16(y)|| (fast form)
+  mv::DevBuf cert;       // 2 floats: bound on ||bf16(y)||^2, max ||y - bf16(y)|| (fast form)
   mv::DevBuf rows_e4m3;  // ntotal x umma_kpad8(d) E4M3 rows (fast form with flat_e4m3)
   mv::DevBuf scales_e4m3, norms_e4m3;  // per row: scale, norm of the dequantized row
   bool e4m3_ready = false;

@@ -90,27 +90,27 @@ void launch_list_append_layout(const int32_t* assign, int64_t n, int nlist, cons
 // cert[0] = bound on ||bf16(y)||^2 over the n rows (from their FP32 norms of
 // the BF16 rows; -1 when one is NaN or infinite), cert[1] = max over rows of
 // ||y - bf16(y)||.
-void launch_cert_bounds(const float* norms, const float* rows, int64_t n, int d, double* cert,
+void launch_cert_bounds(const float* norms, const float* rows, int64_t n, int d, float* cert,
                         cudaStream_t s);
 // Exact recheck of the top-k GEMM candidates (cand: n x ncand keys) with the
 // reference distance (l2_simd<8> / -ip_simd<8>), best candidate to assign[],
 // and rows the error bound does not settle appended to flagged[] (count in
 // *nflag).
 void launch_assign_certify(const float* x, int64_t n, int d, const float* cent, int nlist, int metric,
-                           const uint64_t* cand, int ncand, int kc, const double* cert,
+                           const uint64_t* cand, int ncand, int kc, const float* cert,
                            int32_t* assign, float* mind, int64_t* flagged, int* nflag,
                            cudaStream_t s);
 // The P nearest centroids per row (ascending (distance, list)) from the
 // GEMM's candidates; rows the bound does not settle go to flagged[].
 void launch_topp_certify(const float* x, int64_t n, int d, const float* cent, int nlist, int metric,
-                         const uint64_t* cand, int ncand, int kc, int P, const double* cert,
+                         const uint64_t* cand, int ncand, int kc, int P, const float* cert,
                          int32_t* probes, int64_t* flagged, int* nflag, cudaStream_t s);
 // Flat top-k from each query's shortlist of R approximate keys: reference
 // distances, the k smallest written (0.0 / -1 tail, IP un-negated), flag[q]
 // = 1 when the bound (or over[q], may be null) leaves the query open.
 size_t flat_certify_smem(int d, int R, int k);
 void launch_flat_certify(const float* q, int64_t nq, int d, int metric, const float* rows,
-                         int64_t nb, const uint64_t* skeys, int R, int k, const double* cert,
+                         int64_t nb, const uint64_t* skeys, int R, int k, const float* cert,
                          const int* over, float* out_d, int64_t* out_l, int* flag,
                          cudaStream_t s);
 // assign[idx[i]] = sub[i] (and mind[idx[i]] = sub_d[i] when mind is not null).

@@ -74,18 +74,24 @@ extern "C" int32_t mv_ivfpq_search_noalloc(mv_ivfpq* ix, const float* d_x, int64
                                            int32_t nprobe, float* d_distances, int64_t* d_labels,
                                            void* stream) {
   using namespace mv;
-  if (!ix || nq < 0 || (nq > 0 && (!d_x || !d_distances || !d_labels))) return MV_ERR_ARG;
-  try {
-    ix->ctx->set_device();
+  if (!ix) {
+    set_last_error("mv_ivfpq_search_noalloc: null index");
+    return MV_ERR_ARG;
+  }
+  return guarded(ix->ctx, [&] {
+    MV_REQUIRE(nq >= 0, MV_ERR_ARG, "mv_ivfpq_search_noalloc: negative query count");
+    MV_REQUIRE(nq == 0 || (d_x && d_distances && d_labels), MV_ERR_ARG,
+               "mv_ivfpq_search_noalloc: null query or result pointer");
     MV_REQUIRE(k >= 1 && k <= 2048, MV_ERR_ARG, "n_results must be between 1 and 2048.");
     MV_REQUIRE(nprobe >= 0, MV_ERR_ARG, "nprobe must be non-negative");
-    if (nq == 0) return MV_OK;
+    if (nq == 0) return;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     unsigned char* scratch = noalloc_scratch();
     if (!ix->trained || ix->ntotal == 0) {  // index/index_ivf_pq.mojo:247-251
       k_fill_noalloc<<<(unsigned)((nq * k + 255) / 256), 256, 0, s>>>(d_distances, d_labels, nq * k);
+      count_launch();
       MV_CHECK_CUDA(cudaGetLastError());
-      return MV_OK;
+      return;
     }
     const int np = std::min(nprobe > 0 ? (int)nprobe : ix->nprobe, ix->nlist);
     MV_REQUIRE(np <= 8192, MV_ERR_UNSUPPORTED, "nprobe above 8192 is not supported on the GPU");
@@ -130,12 +136,5 @@ extern "C" int32_t mv_ivfpq_search_noalloc(mv_ivfpq* ix, const float* d_x, int64
       a.out_l = d_labels + q0 * k;
       launch_ivfpq_scan_plain(a, s);
     }
-    return MV_OK;
-  } catch (const Error& e) {
-    set_last_error(e.what());
-    return e.code;
-  } catch (const std::exception& e) {
-    set_last_error(e.what());
-    return MV_ERR_INTERNAL;
-  }
+  });
 }

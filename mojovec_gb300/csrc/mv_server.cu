@@ -11,11 +11,19 @@
 // and device buffers, so admitted batches overlap on the device while new
 // requests keep arriving. Results are copied back through the lane's pinned
 // buffer and scattered to the requests' output buffers; each request
-// records its latency from submit to completion.
+// records its latency from submit to completion. A request with more rows
+// than a batch may hold is split into parts of at most that many rows,
+// queued together; it completes when its last part does.
+//
+// Each batch's device interval (events recorded on its lane's stream before
+// the input copy and after the result copy) is kept, so the peak number of
+// batches that were on the device at the same instant can be read back
+// (mv_server_device_overlap).
 //
 // Every search path is deterministic per query (the selections do not
 // depend on the other queries of a batch), so a request gets the same bits
 // alone and in any mix.
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cstring>
@@ -54,6 +62,10 @@ struct Req {
   clk::time_point t_submit, t_done;
   int32_t status = 0;
   bool done = false;
+  // A split request: the parent is not queued; its parts point at it and
+  // it completes when parts_left reaches zero.
+  Req* parent = nullptr;
+  int parts_left = 0;
 };
 
 struct Batch {
@@ -71,6 +83,7 @@ struct Lane {
   int64_t* h_l = nullptr;
   size_t cap_x = 0, cap_d = 0, cap_l = 0;  // elements
   mv::DevBuf d_x, d_d, d_l;
+  cudaEvent_t ev_a = nullptr, ev_b = nullptr;  // the batch's device interval
   std::unique_ptr<Batch> job;
   bool busy = false;
 };
@@ -94,6 +107,9 @@ struct mv_server {
   std::vector<std::unique_ptr<Lane>> lanes;
   std::deque<Req*> queue;
   std::unordered_map<int64_t, std::unique_ptr<Req>> reqs;
+  std::vector<std::unique_ptr<Req>> parts;  // parts of split requests in flight
+  cudaEvent_t ev_origin = nullptr;          // time base of the device intervals
+  std::vector<std::pair<float, float>> intervals;  // device intervals of recent batches (ms)
   std::mutex mu;
   std::condition_variable cv_sched, cv_lane, cv_done;
   std::thread sched;
@@ -104,6 +120,7 @@ struct mv_server {
 
   void lane_loop(Lane* ln);
   void sched_loop();
+  void finish(Req* r, int32_t st, clk::time_point now);
   size_t estimate(const Coll& c, int64_t nq, int k) const {
     return (size_t)nq * (c.d * 4 + (size_t)k * 12) + c.ws_fixed + (size_t)nq * c.ws_per_query;
   }
@@ -182,6 +199,7 @@ void mv_server::lane_loop(Lane* ln) {
       ln->d_x.ensure(sizeof(float) * nx);
       ln->d_d.ensure(sizeof(float) * nr);
       ln->d_l.ensure(sizeof(int64_t) * nr);
+      MV_CHECK_CUDA(cudaEventRecord(ln->ev_a, ln->s));
       MV_CHECK_CUDA(cudaMemcpyAsync(ln->d_x.p, ln->h_x, sizeof(float) * nx, cudaMemcpyHostToDevice, ln->s));
       if (co.kind == 0)
         st = mv_ivfpq_search_device(static_cast<mv_ivfpq*>(co.handle), ln->d_x.as<float>(), b->nq,
@@ -198,7 +216,15 @@ void mv_server::lane_loop(Lane* ln) {
       if (st == MV_OK) {
         MV_CHECK_CUDA(cudaMemcpyAsync(ln->h_d, ln->d_d.p, sizeof(float) * nr, cudaMemcpyDeviceToHost, ln->s));
         MV_CHECK_CUDA(cudaMemcpyAsync(ln->h_l, ln->d_l.p, sizeof(int64_t) * nr, cudaMemcpyDeviceToHost, ln->s));
+        MV_CHECK_CUDA(cudaEventRecord(ln->ev_b, ln->s));
         MV_CHECK_CUDA(cudaStreamSynchronize(ln->s));
+        float t0 = 0.0f, t1 = 0.0f;
+        if (cudaEventElapsedTime(&t0, ev_origin, ln->ev_a) == cudaSuccess &&
+            cudaEventElapsedTime(&t1, ev_origin, ln->ev_b) == cudaSuccess) {
+          std::lock_guard<std::mutex> lk(mu);
+          if (intervals.size() >= 4096) intervals.erase(intervals.begin(), intervals.begin() + 2048);
+          intervals.emplace_back(t0, t1);
+        }
         size_t ro = 0;
         for (Req* r : b->reqs) {
           std::memcpy(r->out_d, ln->h_d + ro, sizeof(float) * r->nq * b->k);
@@ -216,18 +242,31 @@ void mv_server::lane_loop(Lane* ln) {
     {
       std::lock_guard<std::mutex> lk(mu);
       const auto now = clk::now();
-      for (Req* r : b->reqs) {
-        r->status = st;
-        r->t_done = now;
-        r->done = true;
-        ++completed;
-      }
+      for (Req* r : b->reqs) finish(r, st, now);
       in_flight_bytes -= (int64_t)b->bytes;
       ln->busy = false;
     }
     cv_done.notify_all();
     cv_sched.notify_all();
   }
+}
+
+// Completes r (a whole request or a part of one); called with mu held.
+void mv_server::finish(Req* r, int32_t st, clk::time_point now) {
+  r->status = st;
+  r->t_done = now;
+  r->done = true;
+  if (r->parent) {
+    Req* p = r->parent;
+    if (st != MV_OK && p->status == MV_OK) p->status = st;  // the first failure
+    if (--p->parts_left > 0) return;
+    p->t_done = now;
+    p->done = true;
+    // every part of p is finished: drop them (r among them; not used after)
+    for (auto it = parts.begin(); it != parts.end();)
+      it = (*it)->parent == p ? parts.erase(it) : it + 1;
+  }
+  ++completed;
 }
 
 extern "C" {
@@ -246,8 +285,13 @@ int32_t mv_server_create(mv_ctx* ctx, int64_t hbm_budget_bytes, int32_t lanes,
     for (int i = 0; i < lanes; ++i) {
       auto ln = std::make_unique<Lane>();
       MV_CHECK_CUDA(cudaStreamCreateWithFlags(&ln->s, cudaStreamNonBlocking));
+      MV_CHECK_CUDA(cudaEventCreate(&ln->ev_a));
+      MV_CHECK_CUDA(cudaEventCreate(&ln->ev_b));
       srv->lanes.push_back(std::move(ln));
     }
+    MV_CHECK_CUDA(cudaEventCreate(&srv->ev_origin));
+    MV_CHECK_CUDA(cudaEventRecord(srv->ev_origin, srv->lanes[0]->s));
+    MV_CHECK_CUDA(cudaEventSynchronize(srv->ev_origin));
     mv_server* p = srv.get();
     for (auto& ln : p->lanes) {
       Lane* l = ln.get();
@@ -286,8 +330,11 @@ int32_t mv_server_destroy(mv_server* srv) {
     if (l->h_x) cudaFreeHost(l->h_x);
     if (l->h_d) cudaFreeHost(l->h_d);
     if (l->h_l) cudaFreeHost(l->h_l);
+    cudaEventDestroy(l->ev_a);
+    cudaEventDestroy(l->ev_b);
     cudaStreamDestroy(l->s);
   }
+  if (srv->ev_origin) cudaEventDestroy(srv->ev_origin);
   delete srv;
   return MV_OK;
 }
@@ -347,15 +394,21 @@ int32_t mv_server_submit(mv_server* srv, int32_t coll, const float* x, int64_t n
   if (!srv || !x || nq <= 0 || k <= 0 || k > 4096 || !distances || !labels || !request_id)
     return MV_ERR_ARG;
   std::unique_ptr<Req> r(new Req());
+  std::vector<std::unique_ptr<Req>> parts;
+  int d = 0;
   {
     std::lock_guard<std::mutex> lk(srv->mu);
-    if (coll < 0 || coll >= (int32_t)srv->colls.size()) return MV_ERR_ARG;
-    const Coll& c = srv->colls[coll];
-    if (nq > srv->max_batch || (int64_t)srv->estimate(c, nq, k) > srv->budget) {
-      mv::set_last_error("request larger than the server's batch or memory budget");
+    if (coll < 0 || coll >= (int32_t)srv->colls.size()) {
+      mv::set_last_error("no such collection");
       return MV_ERR_ARG;
     }
-    r->x.assign(x, x + (size_t)nq * c.d);
+    const Coll& c = srv->colls[coll];
+    d = c.d;
+    const int64_t part = std::min(nq, srv->max_batch);
+    if ((int64_t)srv->estimate(c, part, k) > srv->budget) {
+      mv::set_last_error("request larger than the server's memory budget");
+      return MV_ERR_ARG;
+    }
   }
   r->coll = coll;
   r->k = k;
@@ -363,11 +416,39 @@ int32_t mv_server_submit(mv_server* srv, int32_t coll, const float* x, int64_t n
   r->out_d = distances;
   r->out_l = labels;
   r->t_submit = clk::now();
+  if (nq <= srv->max_batch) {
+    r->x.assign(x, x + (size_t)nq * d);
+  } else {
+    // Parts of at most max_batch rows, each writing its own rows of the
+    // caller's result arrays.
+    for (int64_t q0 = 0; q0 < nq; q0 += srv->max_batch) {
+      const int64_t n = std::min(srv->max_batch, nq - q0);
+      std::unique_ptr<Req> pr(new Req());
+      pr->coll = coll;
+      pr->k = k;
+      pr->nq = n;
+      pr->x.assign(x + (size_t)q0 * d, x + (size_t)(q0 + n) * d);
+      pr->out_d = distances + q0 * k;
+      pr->out_l = labels + q0 * k;
+      pr->t_submit = r->t_submit;
+      pr->parent = r.get();
+      parts.push_back(std::move(pr));
+    }
+    r->parts_left = (int)parts.size();
+  }
   {
     std::lock_guard<std::mutex> lk(srv->mu);
     r->id = srv->next_id++;
     *request_id = r->id;
-    srv->queue.push_back(r.get());
+    if (parts.empty()) {
+      srv->queue.push_back(r.get());
+    } else {
+      for (auto& pr : parts) {
+        pr->id = -r->id;
+        srv->queue.push_back(pr.get());
+        srv->parts.push_back(std::move(pr));
+      }
+    }
     srv->reqs.emplace(r->id, std::move(r));
   }
   srv->cv_sched.notify_all();
@@ -387,6 +468,31 @@ int32_t mv_server_wait(mv_server* srv, int64_t request_id, double* latency_s) {
   const int32_t st = r->status;
   srv->reqs.erase(it);
   return st;
+}
+
+// Peak number of batches whose device intervals (input copy to result copy)
+// overlapped at one instant, over the recorded batches, and how many
+// batches are recorded (the most recent few thousand).
+int32_t mv_server_device_overlap(mv_server* srv, int64_t* out2) {
+  if (!srv || !out2) return MV_ERR_ARG;
+  std::vector<std::pair<float, int>> ev;
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    for (const auto& iv : srv->intervals) {
+      ev.emplace_back(iv.first, 1);
+      ev.emplace_back(iv.second, -1);
+    }
+    out2[1] = (int64_t)srv->intervals.size();
+  }
+  // ends before starts at equal times: touching intervals do not overlap
+  std::sort(ev.begin(), ev.end());
+  int64_t cur = 0, peak = 0;
+  for (const auto& e : ev) {
+    cur += e.second;
+    peak = std::max(peak, cur);
+  }
+  out2[0] = peak;
+  return MV_OK;
 }
 
 int32_t mv_server_stats(mv_server* srv, int64_t* out4) {

@@ -60,14 +60,20 @@ __device__ __forceinline__ bool mbar_try_wait_suspend(uint32_t bar, uint32_t par
   return ok != 0;
 }
 
-// Waits until the phase with the given parity completed. Returns false on
-// timeout.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// Waits until the phase with the given parity completed. Returns false
+// once `limit` cycles have passed. A limit of 0 or less gives up at once
+// when the phase is not already complete (the context's test setting that
+// makes pipeline waits expire). Kernels pass their launch's limit to the
+// pipeline waits and keep the default for the waits of their unwind (issued
+// TMA loads landing, issued MMAs retiring), which must not be cut short.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
+                                          long long limit = kWaitLimitCycles) {
   if (mbar_try_wait(bar, parity)) return true;
+  if (limit <= 0) return false;
   const long long t0 = clock64();
   while (true) {
     if (mbar_try_wait_suspend(bar, parity)) return true;
-    if (clock64() - t0 > kWaitLimitCycles) return false;
+    if (clock64() - t0 > limit) return false;
   }
 }
 
@@ -89,6 +95,18 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const void* tmap, int 
       "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
       " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
       "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// 1-D bulk copy global -> shared (cp.async.bulk, the TMA engine without a
+// tensor map), completion signalled on `bar` as transaction bytes. dst and
+// src must be 16-byte aligned and bytes a multiple of 16.
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes,
+                                          uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(bar)
       : "memory");
 }
 

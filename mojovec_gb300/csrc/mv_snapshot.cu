@@ -240,8 +240,11 @@ int32_t mv_ivfpq_load_snapshot(mv_ctx* ctx, const char* path, mv_ivfpq** out) {
     MV_REQUIRE(pq_trained == trained, MV_ERR_ARG, "IndexIVFPQ training state mismatch.");
     MV_REQUIRE(r.pos == payload, MV_ERR_ARG, "IVF-PQ snapshot contains unexpected payload data.");
     // collection checks (api/collection_ivfpq.mojo:420-470)
-    MV_REQUIRE(nlist > 0, MV_ERR_ARG, "nlist must be between 1 and 1000000.");
-    MV_REQUIRE(nprobe <= 65536, MV_ERR_ARG, "nprobe must be between 1 and nlist.");
+    // (the index header's checks above already bound both; these restate the
+    // collection's own range checks with its messages)
+    MV_REQUIRE(nlist > 0 && nlist <= 1000000, MV_ERR_ARG, "nlist must be between 1 and 1000000.");
+    MV_REQUIRE(nprobe > 0 && nprobe <= nlist && nprobe <= 65536, MV_ERR_ARG,
+               "nprobe must be between 1 and nlist.");
     MV_REQUIRE(d == dim && ntotal == nids, MV_ERR_ARG,
                "IVF-PQ snapshot dimensions or record count mismatch.");
     MV_REQUIRE(mi == (index_metric == MV_METRIC_IP ? 1 : 0), MV_ERR_ARG, "IVF-PQ snapshot metric mismatch.");

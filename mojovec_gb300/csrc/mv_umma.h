@@ -23,6 +23,7 @@ struct UmmaArgs {
   int64_t ldo;
   uint64_t* keys;    // EPI_ARGMIN output, one per row
   int* err;          // set to 1 when a bounded wait gave up
+  long long wait_limit = 4000000000ll;  // cycles per pipeline wait (the context's setting)
 };
 
 struct UmmaTopkArgs {
@@ -39,6 +40,7 @@ struct UmmaTopkArgs {
   int* err;
   const float* rscale = nullptr;  // E4M3 operands: per-row scale of X
   const float* cscale = nullptr;  // E4M3 operands: per-column scale of Y
+  long long wait_limit = 4000000000ll;  // cycles per pipeline wait (the context's setting)
 };
 
 struct CoarseTopkArgs {
@@ -52,6 +54,7 @@ struct CoarseTopkArgs {
   int* counts;         // nrows x nseg
   uint32_t* gthr;      // per-row threshold shared by the segments (may be null)
   int* err;
+  long long wait_limit = 4000000000ll;  // cycles per pipeline wait (the context's setting)
 };
 
 // Rows are padded to this many BF16 elements (a multiple of 64).

@@ -107,6 +107,12 @@ class Context:
     def kernel_launches(self) -> int:
         return int(_lib.load().mv_ctx_kernel_launches(self._h))
 
+    def set_wait_limit(self, cycles: int | None):
+        """Cycles a tensor-core kernel's pipeline wait may take before the call
+        gives up with MV_ERR_TIMEOUT (mv_ctx_set_wait_limit); 0 gives up at
+        once unless the wait is already satisfied, None restores the default."""
+        check(_lib.load().mv_ctx_set_wait_limit(self._h, -1 if cycles is None else int(cycles)))
+
     def certify_stats(self) -> dict:
         """Plain-form selections settled on the tensor cores by the error
         bound, and those recomputed by the exact FP32 scan (mv_ctx_certify_stats)."""
@@ -135,7 +141,9 @@ class Context:
 
 
 def _params(form=None, nprobe=0, rerank=0, coarse_fp32=False, lut_fp16=False, coarse_path=0,
-            plain_scan=False, e4m3=False, rerank_fp32=False):
+            plain_scan=False, e4m3=False, rerank_fp32=False, lut=None):
+    """lut: fast-form table / scan variant (0 or 2 FP32, 1 FP16, 3 bank-rotated
+    fixed point, 4 FP32 with staged lists); None takes it from lut_fp16."""
     p = SearchParams()
     p.rerank_fp32 = 1 if rerank_fp32 else 0
     p.coarse_path = int(coarse_path)
@@ -145,7 +153,7 @@ def _params(form=None, nprobe=0, rerank=0, coarse_fp32=False, lut_fp16=False, co
     p.nprobe = int(nprobe)
     p.rerank = int(rerank)
     p.coarse_fp32 = 1 if coarse_fp32 else 0
-    p.lut_fp16 = 1 if lut_fp16 else 0
+    p.lut_fp16 = int(lut) if lut is not None else (1 if lut_fp16 else 0)
     return p
 
 
@@ -281,14 +289,14 @@ class IndexIVFPQ:
 
     def search(self, x, k: int, filter=None, form=None, nprobe: int = 0, rerank: int = 0,
                coarse_fp32: bool = False, lut_fp16: bool = False, coarse_path: int = 0,
-               rerank_fp32: bool = False, distances=None, labels=None):
+               rerank_fp32: bool = False, distances=None, labels=None, lut=None):
         x = _f32(x, self.d)
         n = x.shape[0]
         dist = _out(distances, n, k, np.float32, "distances")
         lab = _out(labels, n, k, np.int64, "labels")
         flt = None if filter is None else np.ascontiguousarray(filter, dtype=np.uint8)
         p = _params(form, nprobe, rerank, coarse_fp32, lut_fp16, coarse_path,
-                    rerank_fp32=rerank_fp32)
+                    rerank_fp32=rerank_fp32, lut=lut)
         check(_lib.load().mv_ivfpq_search(self._h, _p(x), n, k, _p(flt),
                                           0 if flt is None else flt.size, C.byref(p), _p(dist),
                                           _p(lab)))
@@ -312,9 +320,10 @@ class IndexIVFPQ:
 
     def search_device(self, x_ptr: int, n: int, k: int, dist_ptr: int, lab_ptr: int,
                       stream: int = 0, form=None, nprobe: int = 0, rerank: int = 0,
-                      coarse_fp32: bool = False, lut_fp16: bool = False, coarse_path: int = 0):
+                      coarse_fp32: bool = False, lut_fp16: bool = False, coarse_path: int = 0,
+                      lut=None):
         """Device-pointer search (e.g. torch tensors' data_ptr())."""
-        p = _params(form, nprobe, rerank, coarse_fp32, lut_fp16, coarse_path)
+        p = _params(form, nprobe, rerank, coarse_fp32, lut_fp16, coarse_path, lut=lut)
         check(_lib.load().mv_ivfpq_search_device(self._h, x_ptr, n, k, None, 0, C.byref(p),
                                                  dist_ptr, lab_ptr, stream or None))
 
@@ -659,11 +668,11 @@ class IVFPQBatchPlan:
     (mv_ivfpq_plan_*): per-query nprobe and k, persistent scan, tuner."""
 
     def __init__(self, index: IndexIVFPQ, max_nq: int, nprobe_max: int, kmax: int,
-                 rerank: int = 0, coarse_fp32: bool = False):
+                 rerank: int = 0, coarse_fp32: bool = False, lut=None):
         self.index = index
         self.max_nq, self.kmax, self.d = max_nq, kmax, index.d
         h = C.c_void_p()
-        p = _params(FORM_FAST, 0, rerank, coarse_fp32)
+        p = _params(FORM_FAST, 0, rerank, coarse_fp32, lut=lut)
         check(_lib.load().mv_ivfpq_plan_create(index._h, max_nq, nprobe_max, kmax, C.byref(p),
                                                C.byref(h)))
         self._h = h
@@ -704,10 +713,11 @@ class IVFPQBatchPlan:
     def run(self, n: int, use_graph: bool = True, stream: int = 0):
         check(_lib.load().mv_ivfpq_plan_run(self._h, n, 1 if use_graph else 0, stream or None))
 
-    def results(self, n: int):
-        """Copies the first n result rows to the host (synchronous)."""
-        dist = np.empty((n, self.kmax), np.float32)
-        lab = np.empty((n, self.kmax), np.int64)
+    def results(self, n: int, distances=None, labels=None):
+        """Copies the first n result rows to the host (synchronous), into the
+        caller's (n, kmax) arrays when given (pinned memory copies fastest)."""
+        dist = _out(distances, n, self.kmax, np.float32, "distances")
+        lab = _out(labels, n, self.kmax, np.int64, "labels")
         check(_lib.load().mv_ivfpq_plan_results(self._h, n, _p(dist), _p(lab)))
         return dist, lab
 
@@ -772,6 +782,12 @@ class Server:
         dist, lab = self._pending.pop(rid)
         check(st)
         return dist, lab, lat.value
+
+    def device_overlap(self):
+        """(peak batches on the device at one instant, batches recorded)."""
+        out = np.zeros(2, np.int64)
+        check(_lib.load().mv_server_device_overlap(self._h, _p(out)))
+        return int(out[0]), int(out[1])
 
     def stats(self):
         out = np.zeros(4, np.int64)

@@ -3,7 +3,8 @@ collections (IVF-PQ, Flat, SQ8). Every request must get the same bits when
 it runs alone and when it is batched with concurrent requests of other
 sizes, and the same as a direct search call; requests are batched
 (fewer batches than requests) and the in-flight memory stays within the
-budget.
+budget; requests larger than a batch are split; lanes' batches overlap on
+the device.
 """
 
 import threading
@@ -83,14 +84,43 @@ def test_alone_equals_mix_and_direct(mv):
     srv.close()
 
 
+def test_large_requests_split_and_lanes_overlap(mv):
+    """Requests above max_batch_queries are split into parts (batches of at
+    most that many rows) and still equal the direct search; four large
+    requests submitted together keep several lanes' batches on the device
+    at the same instant (device intervals from CUDA events per batch)."""
+    ivf, flat, sq8 = _collections(mv)
+    srv = mv.Server(hbm_budget=8 << 30, lanes=4, max_batch_queries=256)
+    cid = srv.add(ivf, form=mv.FORM_FAST, nprobe=8, rerank=64)
+    rng = np.random.default_rng(9)
+    reqs = [rng.standard_normal((n, 64)).astype(np.float32) * 30 for n in (1000, 700, 1024, 300)]
+    b0 = srv.stats()["batches"]
+    rids = [srv.submit(cid, x, 10) for x in reqs]
+    outs = [srv.wait(r) for r in rids]
+    st = srv.stats()
+    # parts hold at most 256 rows (the last parts of different requests may share a batch)
+    assert st["batches"] - b0 >= -(-sum(len(x) for x in reqs) // 256)
+    for x, (d, l, _) in zip(reqs, outs):
+        dd, ll = _direct(mv, ivf, x, 10)
+        assert np.array_equal(ll, l) and np.array_equal(dd, d)
+    peak, recorded = srv.device_overlap()
+    assert recorded >= 4 and peak >= 2, (peak, recorded)
+    srv.close()
+
+
 def test_rejects_bad_requests(mv):
     ivf, flat, sq8 = _collections(mv)
+    tiny = mv.Server(hbm_budget=1 << 20, lanes=1, max_batch_queries=64)
+    tid = tiny.add(flat, form=mv.FORM_FAST, rerank=40)
+    with pytest.raises(mv.MojoVecGPUError):
+        tiny.submit(tid, np.zeros((10, 32), np.float32), 10)  # above the memory budget
+    tiny.close()
     srv = mv.Server(hbm_budget=2 << 30, lanes=2, max_batch_queries=64)
     cid = srv.add(flat, form=mv.FORM_FAST, rerank=40)
-    with pytest.raises(mv.MojoVecGPUError):
-        srv.submit(cid, np.zeros((65, 32), np.float32), 10)  # above the batch limit
     with pytest.raises((mv.MojoVecGPUError, KeyError)):
         srv.submit(cid + 5, np.zeros((1, 32), np.float32), 10)  # no such collection
     d, l, _ = srv.wait(srv.submit(cid, np.ones((3, 32), np.float32), 5))
     assert l.shape == (3, 5)
+    d, l, _ = srv.wait(srv.submit(cid, np.ones((150, 32), np.float32), 5))  # three parts
+    assert l.shape == (150, 5) and (l >= 0).all()
     srv.close()

@@ -214,6 +214,10 @@ def test_loader_rejections(mv, tmp_path):
     _expect_rejected(mv, path, _refresh(bytes(payload)), "version")
     bad_metric = S.write_collection_ivfpq(**dict(c, metric="dot"))
     _expect_rejected(mv, path, bad_metric, "metric must be")
+    # nprobe outside 1..nlist (io/serialization.mojo:1052-1055)
+    _expect_rejected(mv, path, S.write_collection_ivfpq(**dict(c, nprobe=0)), "nprobe")
+    _expect_rejected(mv, path, S.write_collection_ivfpq(**dict(c, nprobe=c["nlist"] + 1)),
+                     "out of valid range")
     ok = mv.IndexIVFPQ.load_snapshot(_write(path, good))
     assert ok.ntotal == 10 and ok.nprobe == 2
 
