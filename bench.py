@@ -421,8 +421,7 @@ def run_gpu(args, rank, world):
         "config": {
             "workload": workload,
             "form": ("fast: two-pass BF16 tcgen05 coarse GEMM + FP32 recheck, per-query table from the "
-                     "FP16 codebook, list pieces staged in shared memory by bulk copies, histogram "
-                     "select, certified rerank (the full FP32 rerank's results)"
+                     "FP16 codebook (codes read from L2), histogram select, certified rerank (the full FP32 rerank's results)"
                      + ("; batched: one plan (persistent scan, tuned launch shapes) replayed as a "
                         "CUDA graph" if batched else ""))
                     if fast_form else "plain FP32 (reference algorithm, bit-exact)",

@@ -637,6 +637,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ivfpq_scan_fast(FastScanArgs 
   __shared__ int s_fill;
   __shared__ int s_q;
   __shared__ unsigned s_amax;  // FP16 tables: largest |entry| (float bits)
+  __shared__ unsigned long long s_kth;  // the R-th smallest key of the last select
   __shared__ int s_e;          // rotated tables: entries are in units of 2^-s_e
   __shared__ int s_bad;        // rotated tables: non-finite query or codebook bound
   const int lane = threadIdx.x & 31;
@@ -752,23 +753,13 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ivfpq_scan_fast(FastScanArgs 
   for (int base = 0; base < total; base += chunk) {
     const int len = min(chunk, total - base);
     if (m + len > a.cap) {
-      const int r = block_radix_select_soa<FT>(khi, klo, m, a.R, outb, rs);
-      unsigned long long mx = 0ull;
+      const int r = block_hist_select<FT>(khi, klo, m, a.R, outb, rs, &s_kth);
       for (int j = threadIdx.x; j < r; j += FT) {
         const uint64_t k = outb[j];
         khi[j] = (uint32_t)(k >> 32);
         klo[j] = (uint32_t)k;
-        mx = k > mx ? k : mx;
       }
-      for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long t = __shfl_xor_sync(0xffffffffu, mx, o);
-        mx = t > mx ? t : mx;
-      }
-      if (threadIdx.x == 0) rs.lo = 0ull;
-      __syncthreads();
-      if (lane == 0) atomicMax(&rs.lo, mx);
-      __syncthreads();
-      if (r == a.R) bound = rs.lo;  // the R-th smallest key so far
+      if (r == a.R) bound = s_kth;  // the R-th smallest key so far
       m = r;
       if (threadIdx.x == 0) s_fill = m;
       __syncthreads();
@@ -853,7 +844,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ivfpq_scan_fast(FastScanArgs 
     m = s_fill;
     __syncthreads();
   }
-  const int r = block_radix_select_soa<FT>(khi, klo, m, a.R, outb, rs);
+  const int r = block_hist_select<FT>(khi, klo, m, a.R, outb, rs, &s_kth);
   if (a.sorted) {
     for (int j = r + threadIdx.x; j < a.Rp; j += FT) outb[j] = KEY_NONE;
     __syncthreads();

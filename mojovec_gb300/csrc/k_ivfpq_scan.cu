@@ -133,143 +133,6 @@ __device__ __forceinline__ void plan_round(const FastScanArgs& a, StageState& st
   }
 }
 
-// Ascending sort of the warp's 32 * RR keys, element r * 32 + lane in v[r].
-template <int RR>
-__device__ __forceinline__ void sort_side(const uint64_t* side, int h, int need, uint64_t* out,
-                                          unsigned long long* kth) {
-  const int lane = threadIdx.x & 31;
-  uint64_t v[RR];
-#pragma unroll
-  for (int r = 0; r < RR; ++r) {
-    const int e = r * 32 + lane;
-    v[r] = e < h ? side[e] : ~0ull;
-  }
-  warp_sort_regs<RR>(v);
-#pragma unroll
-  for (int r = 0; r < RR; ++r) {
-    const int e = r * 32 + lane;
-    if (e < need) out[e] = v[r];
-    if (e == need - 1) *kth = v[r];
-  }
-}
-
-// The R smallest of the n keys (khi[i] << 32 | klo[i]) into out[0, r),
-// unsorted, r = min(n, R); when n > R, st.kth holds the R-th smallest.
-// All threads call it; khi / klo are not modified.
-template <int NT>
-__device__ int block_hist_select(const uint32_t* khi, const uint32_t* klo, int n, int R,
-                                 uint64_t* out, RadixScratch& rs, StageState& st) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (n <= R) {
-    for (int i = tid; i < n; i += NT) out[i] = ((uint64_t)khi[i] << 32) | klo[i];
-    __syncthreads();
-    return n;
-  }
-  uint32_t lo = 0xffffffffu, hi = 0u;
-  for (int i = tid; i < n; i += NT) {
-    const uint32_t v = khi[i];
-    lo = min(lo, v);
-    hi = max(hi, v);
-  }
-  lo = __reduce_min_sync(0xffffffffu, lo);
-  hi = __reduce_max_sync(0xffffffffu, hi);
-  if (tid == 0) {
-    rs.lo = ~0ull;
-    rs.hi = 0ull;
-    rs.out_n = 0;
-  }
-  __syncthreads();
-  if (lane == 0) {
-    atomicMin(&rs.lo, (unsigned long long)lo);
-    atomicMax(&rs.hi, (unsigned long long)hi);
-  }
-  __syncthreads();
-  const uint32_t base = (uint32_t)rs.lo, span = (uint32_t)rs.hi - base;
-  const int sh = span < 2048u ? 0 : (32 - __clz((int)span)) - 11;  // (span >> sh) < 2048
-  const int nb = (int)(span >> sh) + 1;
-  for (int b = tid; b < nb; b += NT) rs.hist[b] = 0;
-  __syncthreads();
-  for (int i = tid; i < n; i += NT) atomicAdd(&rs.hist[(khi[i] - base) >> sh], 1u);
-  __syncthreads();
-  // the bin holding the R-th key: per-thread runs of bins, block prefix sums
-  const int per = (nb + NT - 1) / NT;
-  const int b0 = tid * per;
-  uint32_t local = 0;
-  for (int b = b0; b < b0 + per && b < nb; ++b) local += rs.hist[b];
-  uint32_t incl = local;
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += t;
-  }
-  if (lane == 31) rs.wsum[warp] = incl;
-  __syncthreads();
-  uint32_t wbase = 0;
-  for (int w = 0; w < warp; ++w) wbase += rs.wsum[w];
-  uint32_t run = wbase + incl - local;
-  for (int b = b0; b < b0 + per && b < nb; ++b) {
-    const uint32_t h = rs.hist[b];
-    if (run < (uint32_t)R && (uint32_t)R <= run + h) {
-      rs.bucket = (uint32_t)b;
-      rs.before = run;
-      rs.wsum[32 - 1] = h;  // read below, after the barrier (no warp reads wsum[31] again)
-    }
-    run += h;
-  }
-  __syncthreads();
-  const uint32_t bk = rs.bucket, before = rs.before, h = rs.wsum[31];
-  __syncthreads();  // every thread has the bin before the histogram is reused
-  if (h > 256u) {
-    // many keys share the boundary bin (equal distances): radix select
-    const int r = block_radix_select_soa<NT>(khi, klo, n, R, out, rs);
-    unsigned long long mx = 0ull;
-    for (int i = tid; i < r; i += NT) mx = out[i] > mx ? out[i] : mx;
-    for (int o = 16; o > 0; o >>= 1) {
-      const unsigned long long t = __shfl_xor_sync(0xffffffffu, mx, o);
-      mx = t > mx ? t : mx;
-    }
-    if (tid == 0) st.kth = 0ull;
-    __syncthreads();
-    if (lane == 0) atomicMax(&st.kth, mx);
-    __syncthreads();
-    return r;
-  }
-  uint64_t* side = reinterpret_cast<uint64_t*>(rs.hist);  // up to 256 keys of the boundary bin
-  if (tid == 0) rs.wsum[0] = 0;
-  __syncthreads();
-  for (int i0 = 0; i0 < n; i0 += NT) {
-    const int i = i0 + tid;
-    uint64_t v = ~0ull;
-    uint32_t bin = 0xffffffffu;
-    if (i < n) {
-      v = ((uint64_t)khi[i] << 32) | klo[i];
-      bin = (khi[i] - base) >> sh;
-    }
-    const bool below = bin < bk, at = bin == bk;
-    const unsigned mb = __ballot_sync(0xffffffffu, below);
-    const unsigned ma = __ballot_sync(0xffffffffu, at);
-    int ob = 0, oa = 0;
-    if (lane == 0) {
-      if (mb) ob = atomicAdd(&rs.out_n, __popc(mb));
-      if (ma) oa = atomicAdd(&rs.wsum[0], (uint32_t)__popc(ma));
-    }
-    ob = __shfl_sync(0xffffffffu, ob, 0);
-    oa = __shfl_sync(0xffffffffu, oa, 0);
-    const unsigned lt = (1u << lane) - 1u;
-    if (below) out[ob + __popc(mb & lt)] = v;
-    if (at) side[oa + __popc(ma & lt)] = v;
-  }
-  __syncthreads();
-  if (warp == 0) {
-    const int need = R - (int)before;
-    if (h <= 32u) sort_side<1>(side, (int)h, need, out + before, &st.kth);
-    else if (h <= 64u) sort_side<2>(side, (int)h, need, out + before, &st.kth);
-    else if (h <= 128u) sort_side<4>(side, (int)h, need, out + before, &st.kth);
-    else sort_side<8>(side, (int)h, need, out + before, &st.kth);
-  }
-  __syncthreads();
-  return R;
-}
-
 // Two CTAs per SM fit the shared memory at the default round size.
 template <int NT>
 __global__ void __launch_bounds__(NT, 2)
@@ -381,7 +244,7 @@ __global__ void __launch_bounds__(NT, 2)
       if (b) ph1 ^= 1u;
       else ph0 ^= 1u;
       if (m + len > a.cap) {  // keep the R smallest; later keys must beat the R-th
-        const int kept = block_hist_select<NT>(khi, klo, m, a.R, outb, rs, st);
+        const int kept = block_hist_select<NT>(khi, klo, m, a.R, outb, rs, &st.kth);
         for (int j = tid; j < kept; j += NT) {
           khi[j] = (uint32_t)(outb[j] >> 32);
           klo[j] = (uint32_t)outb[j];
@@ -457,7 +320,7 @@ __global__ void __launch_bounds__(NT, 2)
       if (warp == 0) plan_round(a, st, b, E, total, nprobe, pbeg, poff, cbuf(b), vbuf(b), b ? bar1 : bar0);
       __syncthreads();
     }
-    const int r = block_hist_select<NT>(khi, klo, m, a.R, outb, rs, st);
+    const int r = block_hist_select<NT>(khi, klo, m, a.R, outb, rs, &st.kth);
     if (a.sorted) {
       for (int j = r + tid; j < a.Rp; j += NT) outb[j] = KEY_NONE;
       __syncthreads();
