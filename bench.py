@@ -289,7 +289,7 @@ def run_gpu(args, rank, world):
     del flat
     setup_s = time.perf_counter() - t_setup
 
-    fast = dict(form=mv.FORM_FAST, nprobe=nprobe, rerank=args.rerank)
+    fast = dict(form=mv.FORM_FAST, nprobe=nprobe, rerank=args.rerank, lut=args.lut)
     plain = dict(form=mv.FORM_PLAIN, nprobe=nprobe)
     batched = args.form == "batched"
     headline = plain if args.form == "plain" else fast
@@ -297,7 +297,7 @@ def run_gpu(args, rank, world):
     if batched:
         # The batched form: one plan (device buffers, persistent scan, tuned
         # launch shapes) replayed as a CUDA graph, every query at this nprobe / k.
-        plan = mv.IVFPQBatchPlan(index, nq, nprobe, K, rerank=args.rerank)
+        plan = mv.IVFPQBatchPlan(index, nq, nprobe, K, rerank=args.rerank, lut=args.lut)
         npv = np.full(nq, nprobe, np.int32)
         kv = np.full(nq, K, np.int32)
         plan.set_queries(queries, npv, kv)
@@ -1577,6 +1577,8 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--form", default="fast", choices=["plain", "fast", "batched"])
     ap.add_argument("--nprobe", type=int, default=8)
+    ap.add_argument("--lut", type=int, default=None,
+                    help="ivfpq workload: fast-form scan variant (5 = list-major tensor-core scan)")
     ap.add_argument("--rerank", type=int, default=None,
                     help="shortlist depth (IVF-PQ default 256, flat default k * 4)")
     ap.add_argument("--nb", type=int, default=NB, help="base rows (profiling runs use fewer)")

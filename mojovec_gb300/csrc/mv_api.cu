@@ -705,6 +705,13 @@ void ensure_fast(mv_ivfpq* ix, cudaStream_t s) {
   if (ix->fast_ready) return;
   build_coarse_locked(ix, s);
   const int64_t total = ix->h_off[ix->nlist];
+  {
+    std::vector<int64_t> len(ix->nlist);
+    for (int L = 0; L < ix->nlist; ++L) len[L] = ix->h_off[L + 1] - ix->h_off[L];
+    std::sort(len.begin(), len.end(), std::greater<int64_t>());
+    ix->longest.assign(ix->nlist + 1, 0);
+    for (int L = 0; L < ix->nlist; ++L) ix->longest[L + 1] = ix->longest[L] + len[L];
+  }
   if (ix->metric == MV_METRIC_L2 && total > 0) {
     ix->d_vec_term.ensure((size_t)total * 4 + 16);  // staged scans copy 16-byte supersets
     launch_vec_terms(ix->d_off.as<int64_t>(), ix->nlist, ix->d_codes.as<uint8_t>(),
@@ -825,6 +832,18 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
     MV_REQUIRE(nq <= 65535ll * 64, MV_ERR_UNSUPPORTED, "batch too large for one launch");
     qb = nq;
   }
+  // lut 5: the list-major tensor-core scan, whose distance rows (smax words
+  // per query) must fit kTcRowBytes per chunk of queries
+  const int lut = p ? p->lut_fp16 : 0;
+  constexpr int64_t kTcRowBytes = 1ll << 31;
+  const int64_t smax = ix->longest.empty() ? 0 : ix->longest[std::min(nprobe, ix->nlist)];
+  bool tc = lut == 5 && ivfpq_tc_supported(ix->d, ix->M, ix->pq16_inv > 0.0f) && smax > 0;
+  if (tc) {
+    const int64_t fit = kTcRowBytes / (smax * 4);
+    if (batch ? fit < qb : fit < 1) tc = false;
+    else qb = std::min(qb, fit);
+  }
+  const int tc_qc = tc ? ivfpq_tc_qc(qb, nprobe, ix->nlist) : 0;
   const int nseg = fused ? umma_topk_nseg(qb, ix->nlist, ix->d, nc, ix->ctx->num_sms)
                  : twopass ? coarse_topk2_nseg(qb, ix->nlist, ix->d, nc, ix->ctx->num_sms) : 1;
   const int ncand = nseg * (fused ? umma_topk_groups(ix->d, nc) : 1) * next_pow2(nc);
@@ -834,7 +853,8 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
              : twopass ? ws_bytes((size_t)qb * nseg * lcap, 8) + ws_bytes((size_t)qb * nseg, 4) +
                             ws_bytes((size_t)qb, 4)
                        : ws_bytes((size_t)qb * ix->nlist, 4)) +
-            ws_bytes((size_t)qb * nprobe, 4) * 2 + ws_bytes((size_t)qb * R, 8));
+            ws_bytes((size_t)qb * nprobe, 4) * 2 + ws_bytes((size_t)qb * R, 8) +
+            (tc ? ws_bytes(ivfpq_tc_scratch_bytes(qb, nprobe, ix->nlist, ix->d, smax), 1) : 0));
   Arena ar(ws);
   __nv_bfloat16* xq = ar.take<__nv_bfloat16>((size_t)qb * kp);
   float* dmat = fused || twopass ? nullptr : ar.take<float>((size_t)qb * ix->nlist);
@@ -846,6 +866,8 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
   int32_t* probes = ar.take<int32_t>((size_t)qb * nprobe);
   float* term = ar.take<float>((size_t)qb * nprobe);
   uint64_t* skeys = ar.take<uint64_t>((size_t)qb * R);
+  void* tc_scratch =
+      tc ? ar.take<unsigned char>(ivfpq_tc_scratch_bytes(qb, nprobe, ix->nlist, ix->d, smax)) : nullptr;
   for (int64_t q0 = 0; q0 < nq; q0 += qb) {
     const int64_t nb = std::min(qb, nq - q0);
     const float* xb = d_x + q0 * ix->d;
@@ -922,7 +944,10 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
         a.filter_len = filter_len;
         a.ids = ix->d_ids.as<uint32_t>();
       }
-      if (batch) {
+      if (tc) {
+        a.nprobe_q = batch ? batch->nprobe_q : nullptr;
+        launch_ivfpq_scan_tc(a, smax, tc_qc, tc_scratch, ix->ctx->num_sms, current_wait_limit(), s);
+      } else if (batch) {
         a.nprobe_q = batch->nprobe_q;
         a.order = batch->order;
         a.counter = batch->scan_ctas_per_sm > 0 ? batch->counter : nullptr;

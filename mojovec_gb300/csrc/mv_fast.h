@@ -110,6 +110,20 @@ bool launch_ivfpq_scan_staged(FastScanArgs a, cudaStream_t s, int nt, int persis
 // that does not fit).
 void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s, int nt = 256, int persistent_ctas = 0,
                             int lut = 0);
+// List-major ADC on the tensor cores (k_ivfpq_tc.cu): FP16 queries times
+// FP16 reconstructions of the list rows, one decode per list row and batch;
+// writes the R smallest (distance, position) keys per query like the scan
+// above (a.q, nq, d, M, metric, pq16, pq16_inv, list_off, codes, vterm,
+// probes, term, nprobe, nprobe_q, R, sorted, out_keys, nlist, err, filter).
+// Shapes: FP16 codebook, M a multiple of 8, d / M = 4 or 8, d <= 128.
+bool ivfpq_tc_supported(int d, int M, bool has_pq16);
+// Queries per work item (32, 64 or 128) for a batch shape.
+int ivfpq_tc_qc(int64_t nq, int nprobe, int nlist);
+// smax: an upper bound on any query's candidate count (the nprobe longest
+// lists); the scratch holds nq distance rows of smax words.
+size_t ivfpq_tc_scratch_bytes(int64_t nq, int nprobe, int nlist, int d, int64_t smax);
+void launch_ivfpq_scan_tc(const FastScanArgs& a, int64_t smax, int qc, void* scratch, int num_sms,
+                          long long wait_limit, cudaStream_t s);
 // Flat fast form: merge nseg x ncp per-segment keys (kseg kept per segment)
 // into the R-key shortlist per query. With out_keys the shortlist is
 // written (unsorted) for the rerank; otherwise the k smallest become the

@@ -228,6 +228,9 @@ struct mv_ivfpq {
   bool has_pq_cn = false;
   mv::DevBuf d_cnorm;       // FP32 per centroid ||c||^2
   mv::DevBuf d_cent_bf16;   // nlist x d BF16
+  // longest[i]: total rows of the i longest lists (i = 0..nlist): bounds
+  // the candidate count of a query probing i lists
+  std::vector<int64_t> longest;
 };
 
 struct mv_ivfflat {
