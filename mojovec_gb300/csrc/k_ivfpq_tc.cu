@@ -130,6 +130,19 @@ __global__ void __launch_bounds__(256)
   const int64_t row = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
   if (row >= nq) return;
   const int np = nprobe_q ? min(max(nprobe_q[row], 1), P) : P;
+  // smax bounds the candidates of np distinct lists; a query over it (never
+  // expected) takes no part: seg -1 (the placement skips it), error site 106
+  int64_t tot = 0;
+  for (int p = lane; p < np; p += 32) {
+    const int L = probes[row * P + p];
+    if (L >= 0 && L < nlist) tot += list_off[L + 1] - list_off[L];
+  }
+  for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+  if (tot > smax) {
+    for (int p = lane; p < np; p += 32) seg[row * P + p] = -1;
+    if (lane == 0) atomicExch(err, 106);
+    return;
+  }
   int64_t carry = 0;
   for (int p0 = 0; p0 < np; p0 += 32) {
     const int p = p0 + lane;
@@ -154,7 +167,6 @@ __global__ void __launch_bounds__(256)
     }
     carry += __shfl_sync(0xffffffffu, incl, 31);
   }
-  if (lane == 0 && carry > smax) atomicExch(err, 106);  // never expected: smax bounds every row
 }
 
 // Exclusive scans over the lists of the pair counts (start) and of the
@@ -226,14 +238,14 @@ __global__ void __launch_bounds__(1024)
 
 __global__ void k_tc_place(const int32_t* __restrict__ probes, int64_t nq, int P,
                            const int32_t* __restrict__ nprobe_q, int nlist,
-                           const int64_t* __restrict__ start, int* __restrict__ cursor,
-                           int32_t* __restrict__ pairs) {
+                           const int64_t* __restrict__ seg, const int64_t* __restrict__ start,
+                           int* __restrict__ cursor, int32_t* __restrict__ pairs) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nq * P) return;
   const int64_t row = i / P;
   const int p = (int)(i - row * P);
   const int np = nprobe_q ? min(max(nprobe_q[row], 1), P) : P;
-  if (p >= np) return;
+  if (p >= np || seg[i] < 0) return;
   const int L = probes[i];
   if (L >= 0 && L < nlist) pairs[start[L] + atomicAdd(&cursor[L], 1)] = (int32_t)i;
 }
@@ -585,7 +597,8 @@ __global__ void __launch_bounds__(SEL_WARPS * 32) k_tc_select(SelArgs a) {
   }
   if (lane == 0) pbeg[np] = carry;
   __syncwarp();
-  const int n = carry;
+  // a row over smax was left unwritten (error site 106): no candidates
+  const int n = carry <= a.smax ? carry : 0;
   const uint32_t* src = a.dist + row * a.smax;
   uint64_t* out = a.out + row * a.R;
   const int R = a.R;
@@ -781,7 +794,7 @@ void launch_ivfpq_scan_tc(const FastScanArgs& f, int64_t smax, int qc, void* scr
                                 f.err);
   k_tc_items<<<1, 1024, 0, s>>>(cnt, f.list_off, nlist, qc, start, istart);
   k_tc_place<<<(unsigned)((nq * P + 255) / 256), 256, 0, s>>>(f.probes, nq, P, f.nprobe_q, nlist,
-                                                               start, cursor, pairs);
+                                                               seg, start, cursor, pairs);
   for (int i = 0; i < 4; ++i) count_launch();
   TcArgs t;
   t.q16 = q16;

@@ -837,7 +837,8 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
   const int lut = p ? p->lut_fp16 : 0;
   constexpr int64_t kTcRowBytes = 1ll << 31;
   const int64_t smax = ix->longest.empty() ? 0 : ix->longest[std::min(nprobe, ix->nlist)];
-  bool tc = lut == 5 && ivfpq_tc_supported(ix->d, ix->M, ix->pq16_inv > 0.0f) && smax > 0;
+  bool tc = lut == 5 && ivfpq_tc_supported(ix->d, ix->M, ix->pq16_inv > 0.0f) && smax > 0 &&
+            nprobe <= 1024;
   if (tc) {
     const int64_t fit = kTcRowBytes / (smax * 4);
     if (batch ? fit < qb : fit < 1) tc = false;
