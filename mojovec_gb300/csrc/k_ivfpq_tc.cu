@@ -603,19 +603,21 @@ __global__ void __launch_bounds__(SEL_WARPS * 32) k_tc_select(SelArgs a) {
   uint64_t* out = a.out + row * a.R;
   const int R = a.R;
   // Visits every key in a fixed order: f(valid, key) per element, per lane
-  // elements lane, lane + 32, ... (four loads in flight).
+  // elements lane, lane + 32, ... (four loads in flight). The loop bound is
+  // the same for every lane (f may hold warp votes); lanes past n pass
+  // valid = false.
   auto for_keys = [&](auto&& f) {
     int p = 0;
-    for (int i0 = lane; i0 < n; i0 += 128) {
+    for (int i0 = 0; i0 < n; i0 += 128) {
       uint32_t w[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const int i = i0 + 32 * u;
+        const int i = i0 + lane + 32 * u;
         w[u] = i < n ? __ldg(src + i) : TC_EXCLUDED;
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const int i = i0 + 32 * u;
+        const int i = i0 + lane + 32 * u;
         bool valid = false;
         uint64_t key = KEY_NONE;
         if (i < n) {
