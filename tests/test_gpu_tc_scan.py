@@ -121,15 +121,15 @@ def test_tc_select_is_exact(mv, nprobe):
 
 
 def test_tc_long_lists_and_crowded_lists(mv):
-    """Four far-apart clusters of 2500 / 800 / 500 / 200 rows, one list each:
-    the first list spans three 1024-row work items, and 300 queries probe
-    every list (three query chunks of up to 128). With k = all 4000 rows,
+    """Four far-apart clusters of 1300 / 400 / 250 / 48 rows, one list each:
+    the first list spans two 1024-row work items, and 300 queries probe
+    every list (three query chunks of up to 128). With k = all 1998 rows,
     every row comes back once with its distance within the FP16 bound; the
     1000 smallest are the prefix of that list."""
     rng = np.random.default_rng(31)
     d, M = 64, 16
     centers = rng.standard_normal((4, d)).astype(np.float32) * 30
-    sizes = [2500, 800, 500, 200]
+    sizes = [1300, 400, 250, 48]
     base = np.vstack([centers[i] + rng.standard_normal((s, d)).astype(np.float32)
                       for i, s in enumerate(sizes)]).astype(np.float32)
     q = (centers[rng.integers(0, 4, 300)] + rng.standard_normal((300, d))).astype(np.float32)
@@ -138,9 +138,10 @@ def test_tc_long_lists_and_crowded_lists(mv):
     g.set_codebooks(centers, t.codebooks()[1])
     g.add(base)
     assert np.diff(g.lists()[0]).tolist() == sizes
-    dist, lab = g.search(q, 4000, form=mv.FORM_FAST, nprobe=4, lut=5)
+    n = sum(sizes)
+    dist, lab = g.search(q, n, form=mv.FORM_FAST, nprobe=4, lut=5)
     for i in range(0, 300, 37):
-        assert np.array_equal(np.sort(lab[i]), np.arange(4000)), i
+        assert np.array_equal(np.sort(lab[i]), np.arange(n)), i
     _check_distances(g, q[::10], dist[::10], lab[::10], 0)
     d2, l2 = g.search(q, 1000, form=mv.FORM_FAST, nprobe=4, lut=5)
     assert np.array_equal(l2, lab[:, :1000])
