@@ -47,7 +47,6 @@ namespace {
 
 using namespace sm100;
 
-constexpr int TC_THREADS = 256;  // 8 warps: two per TMEM lane quarter
 constexpr int TC_BM = 128;       // list rows per tile (UMMA M)
 constexpr int TC_RS = 1024;      // list rows per work item
 constexpr uint32_t TC_EXCLUDED = 0xffffffffu;
@@ -169,77 +168,126 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// Exclusive scans over the lists of the pair counts (start) and of the
-// work items (istart): cnt[L] > 0 pairs give ceil(cnt / qc) query chunks
-// times ceil(len / TC_RS) row pieces. One block of 1024 threads.
+// One work item: rows [rbeg, rend) of list L (at CSR offset loff) against
+// query chunk `chunk` (nq queries, their FP16 rows and column data in the
+// chunk's images).
+struct TcItem {
+  int L, nq, chunk, pad;
+  long long loff, rbeg, rend;
+};
+
+// Per query column of a chunk: the distance-row offset of its probe of the
+// list, the coarse term and the scale of its accumulators.
+struct TcMeta {
+  long long seg;
+  float term, qmul;
+};
+
+// Exclusive scans over the lists of the pair counts (start), the query
+// chunks (cstart: ceil(cnt / qc)) and the work items (istart: chunks times
+// ceil(len / TC_RS) row pieces), then every list's item records. One block
+// of 1024 threads.
 __global__ void __launch_bounds__(1024)
     k_tc_items(const int* __restrict__ cnt, const int64_t* __restrict__ list_off, int nlist, int qc,
-               int64_t* __restrict__ start, int* __restrict__ istart) {
+               int64_t* __restrict__ start, int* __restrict__ cstart, int* __restrict__ istart,
+               TcItem* __restrict__ items) {
   __shared__ long long ws1[32];
-  __shared__ int ws2[32];
+  __shared__ int ws2[32], ws3[32];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const int per = (nlist + 1023) / 1024;
   const int b0 = min(nlist, t * per), b1 = min(nlist, b0 + per);
-  auto items = [&](int L) {
-    const int c = cnt[L];
+  auto chunks = [&](int L) { return (cnt[L] + qc - 1) / qc; };
+  auto pieces = [&](int L) {
     const int64_t len = list_off[L + 1] - list_off[L];
-    if (c == 0 || len == 0) return 0;
-    return ((c + qc - 1) / qc) * (int)((len + TC_RS - 1) / TC_RS);
+    return (int)((len + TC_RS - 1) / TC_RS);
   };
   long long s1 = 0;
-  int s2 = 0;
+  int s2 = 0, s3 = 0;
   for (int L = b0; L < b1; ++L) {
     s1 += cnt[L];
-    s2 += items(L);
+    s2 += chunks(L) * pieces(L);
+    s3 += chunks(L);
   }
   long long i1 = s1;
-  int i2 = s2;
+  int i2 = s2, i3 = s3;
   for (int o = 1; o < 32; o <<= 1) {
     const long long a = __shfl_up_sync(0xffffffffu, i1, o);
     const int b = __shfl_up_sync(0xffffffffu, i2, o);
+    const int c = __shfl_up_sync(0xffffffffu, i3, o);
     if (lane >= o) {
       i1 += a;
       i2 += b;
+      i3 += c;
     }
   }
   if (lane == 31) {
     ws1[w] = i1;
     ws2[w] = i2;
+    ws3[w] = i3;
   }
   __syncthreads();
   if (w == 0) {
     long long a = ws1[lane];
-    int b = ws2[lane];
+    int b = ws2[lane], c = ws3[lane];
     for (int o = 1; o < 32; o <<= 1) {
       const long long x = __shfl_up_sync(0xffffffffu, a, o);
       const int y = __shfl_up_sync(0xffffffffu, b, o);
+      const int z = __shfl_up_sync(0xffffffffu, c, o);
       if (lane >= o) {
         a += x;
         b += y;
+        c += z;
       }
     }
     ws1[lane] = a;
     ws2[lane] = b;
+    ws3[lane] = c;
   }
   __syncthreads();
   long long base1 = (w ? ws1[w - 1] : 0) + i1 - s1;
   int base2 = (w ? ws2[w - 1] : 0) + i2 - s2;
+  int base3 = (w ? ws3[w - 1] : 0) + i3 - s3;
   for (int L = b0; L < b1; ++L) {
     start[L] = base1;
     istart[L] = base2;
+    cstart[L] = base3;
+    const int nch = chunks(L), npc = pieces(L);
+    const int64_t loff = list_off[L], len = list_off[L + 1] - loff;
+    for (int c = 0; c < nch; ++c) {
+      for (int pc = 0; pc < npc; ++pc) {
+        TcItem it;
+        it.L = L;
+        it.nq = min(qc, cnt[L] - c * qc);
+        it.chunk = base3 + c;
+        it.pad = 0;
+        it.loff = loff;
+        it.rbeg = (long long)pc * TC_RS;
+        it.rend = min(len, (int64_t)(pc + 1) * TC_RS);
+        items[base2 + c * npc + pc] = it;
+      }
+    }
     base1 += cnt[L];
-    base2 += items(L);
+    base2 += nch * npc;
+    base3 += nch;
   }
   if (t == 1023) {
     start[nlist] = ws1[31];
     istart[nlist] = ws2[31];
+    cstart[nlist] = ws3[31];
   }
 }
 
+// Groups the pairs by list and writes each chunk's images: the FP16 query
+// rows in the MMA's B layout (K-major, 128-byte swizzle, k-block major:
+// image[kb][j][128 bytes]) and the column data. A pair's column j within
+// its list is taken by an atomic, so the order of the columns varies; every
+// column is computed the same way.
 __global__ void k_tc_place(const int32_t* __restrict__ probes, int64_t nq, int P,
                            const int32_t* __restrict__ nprobe_q, int nlist,
-                           const int64_t* __restrict__ seg, const int64_t* __restrict__ start,
-                           int* __restrict__ cursor, int32_t* __restrict__ pairs) {
+                           const int64_t* __restrict__ seg, const float* __restrict__ term,
+                           const __half* __restrict__ q16, const float* __restrict__ qmul, int kp,
+                           int qc, const int* __restrict__ cstart, int* __restrict__ cursor,
+                           uint8_t* __restrict__ bimg, TcMeta* __restrict__ meta) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nq * P) return;
   const int64_t row = i / P;
@@ -247,80 +295,125 @@ __global__ void k_tc_place(const int32_t* __restrict__ probes, int64_t nq, int P
   const int np = nprobe_q ? min(max(nprobe_q[row], 1), P) : P;
   if (p >= np || seg[i] < 0) return;
   const int L = probes[i];
-  if (L >= 0 && L < nlist) pairs[start[L] + atomicAdd(&cursor[L], 1)] = (int32_t)i;
+  if (L < 0 || L >= nlist) return;
+  const int c = atomicAdd(&cursor[L], 1);
+  const int64_t chunk = cstart[L] + c / qc;
+  const int j = c % qc;
+  TcMeta m;
+  m.seg = seg[i];
+  m.term = term[i];
+  m.qmul = qmul[row];
+  meta[chunk * qc + j] = m;
+  uint8_t* img = bimg + chunk * ((int64_t)qc * kp * 2);
+  const uint4* src = reinterpret_cast<const uint4*>(q16 + row * kp);
+  for (int cc = 0; cc < (kp >> 3); ++cc)
+    *reinterpret_cast<uint4*>(img + (cc >> 3) * (qc * 128) + sw128(j, cc & 7)) = src[cc];
+}
+
+// excl[pos] = 1 when the exclusion filter names the id of CSR row pos.
+__global__ void k_tc_excl(const uint32_t* __restrict__ ids, int64_t ntotal,
+                          const uint8_t* __restrict__ filter, int64_t filter_len,
+                          uint8_t* __restrict__ excl) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ntotal) return;
+  const uint32_t id = ids[i];
+  excl[i] = ((int64_t)id < filter_len && filter[id] != 0) ? 1 : 0;
 }
 
 // ---- the tensor-core scan -------------------------------------------------
+constexpr int TC_CONSUMERS = 256;                 // warps 0-7
+constexpr int TC_THREADS = TC_CONSUMERS + 32;     // + warp 8, the producer
+constexpr int TC_STAGES = 4;                      // tiles of codes in flight
+
 struct TcArgs {
-  const __half* q16;
-  const float* qmul;
-  const float* term;      // nq x P coarse terms
-  const int64_t* seg;     // nq x P distance-row offsets
-  const int* cnt;
-  const int64_t* start;
-  const int* istart;
-  const int32_t* pairs;
-  const int64_t* list_off;
-  const uint8_t* codes;
-  const float* vterm;     // per CSR row (L2), null for IP
-  const __half* pq16;     // M x 256 x dsub FP16 codebook (scaled)
-  const uint8_t* filter;
-  int64_t filter_len;
-  const uint32_t* ids;
-  uint32_t* dist;         // distance rows
-  int* counter;
+  const TcItem* items;
+  const int* total_items;  // device word: the item count
+  const uint8_t* bimg;     // chunk images of the B operand
+  const TcMeta* meta;      // chunk column data
+  const uint8_t* codes;    // CSR codes (16 bytes of slack at the end)
+  const float* vterm;      // per CSR row (L2; 16 bytes of slack), null for IP
+  const uint8_t* excl;     // per CSR row (16 bytes of slack), null without a filter
+  const __half* pq16;      // M x 256 x dsub FP16 codebook (scaled)
+  uint32_t* dist;          // distance rows
   int* err;
-  int nlist, P, M, dsub, d, kp, qc;
+  int M, dsub, d, kp, qc;
   long long wait_limit;
 };
 
 struct TcSmem {
-  int abytes, bbytes, cbbytes;
-  __host__ __device__ TcSmem(int kp, int qc, int d)
-      : abytes(TC_BM * kp * 2), bbytes(qc * kp * 2), cbbytes(d * 512) {}
+  int abytes, bbytes, mbytes, cbbytes, code_bytes, slot_bytes;
+  __host__ __device__ TcSmem(int kp, int qc, int d, int M)
+      : abytes(TC_BM * kp * 2), bbytes(qc * kp * 2), mbytes(qc * 16), cbbytes(d * 512),
+        code_bytes((TC_BM * M + 32 + 15) & ~15), slot_bytes(code_bytes + 544 + 160) {}
   __host__ __device__ int a_off(int b) const { return b * abytes; }
   __host__ __device__ int b_off(int b) const { return 2 * abytes + b * bbytes; }
-  __host__ __device__ int cb_off() const { return 2 * abytes + 2 * bbytes; }
-  __host__ __device__ int meta_off() const { return cb_off() + cbbytes; }
-  // per buffer and column: seg (8 bytes), term, qmul
-  __host__ __device__ int bars_off(int qc) const { return meta_off() + 2 * qc * 16; }
-  __host__ __device__ size_t total(int qc) const { return 1024 + (size_t)bars_off(qc) + 64; }
+  __host__ __device__ int m_off(int b) const { return 2 * abytes + 2 * bbytes + b * mbytes; }
+  __host__ __device__ int cb_off() const { return 2 * abytes + 2 * bbytes + 2 * mbytes; }
+  __host__ __device__ int slot_off(int s) const { return cb_off() + cbbytes + s * slot_bytes; }
+  __host__ __device__ int bars_off() const { return slot_off(TC_STAGES); }
+  __host__ __device__ size_t total() const { return 1024 + (size_t)bars_off() + 8 * (6 + 2 * TC_STAGES) + 16; }
 };
 
-// Persistent: one CTA per SM takes work items (list, query chunk, row
-// piece) from a counter. Per item the chunk's FP16 query rows go to B[item
-// parity]; per 128-row tile of the piece all eight warps decode the rows'
-// codes into A[tile parity] (thread r of a lane quarter owns row r, the two
-// warps of a quarter split the subspaces), one thread issues the d / 16
-// MMAs into accumulator (tile parity) and commits, and the warps then run
-// the epilogue of the PREVIOUS tile (its MMA overlaps this tile's decode):
-// distance = term + vterm + qmul * acc, one coalesced 128-byte store per
-// warp and query column.
+// Barrier among the consumer warps (id 1, 256 threads) that also returns
+// whether any of them passed v != 0: one answer for every consumer.
+__device__ __forceinline__ bool consumers_sync_or(int v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.s32 q, %1, 0;\n\t"
+      "bar.red.or.pred p, 1, 256, q;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(r)
+      : "r"(v)
+      : "memory");
+  return r != 0;
+}
+
+// Persistent: one CTA per SM walks the work items blockIdx.x, + gridDim.x,
+// ... Warp 8 (the producer, one lane) copies, with cp.async.bulk, each
+// item's query image and column data into B[item parity] and each 128-row
+// tile's codes, per-row terms and exclusion flags (16-byte aligned
+// supersets) into a ring of TC_STAGES slots. Warps 0-7 per tile: decode the
+// rows' codes into FP16 reconstructions in A[tile parity] (thread r of a
+// TMEM lane quarter owns row r, the two warps of a quarter split the
+// subspaces), one thread issues the d / 16 MMAs into accumulator (tile
+// parity), and then all run the epilogue of the PREVIOUS tile, whose MMAs
+// overlapped this tile's decode: distance = term + vterm + qmul * acc, one
+// 128-byte store per warp and query column.
 __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                            ~uintptr_t(1023));
-  const TcSmem L(a.kp, a.qc, a.d);
+  const TcSmem L(a.kp, a.qc, a.d, a.M);
   uint8_t* cb = sm + L.cb_off();
-  int64_t* mseg = reinterpret_cast<int64_t*>(sm + L.meta_off());  // [2][qc]
-  float* mterm = reinterpret_cast<float*>(mseg + 2 * a.qc);        // [2][qc]
-  float* mmul = mterm + 2 * a.qc;                                  // [2][qc]
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + L.bars_off(a.qc));
-  uint32_t* holder = reinterpret_cast<uint32_t*>(bars + 2);
-  __shared__ int s_item, s_L, s_nq, s_err;
-  __shared__ long long s_rbeg, s_rend, s_pb;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + L.bars_off());
+  uint32_t* holder = reinterpret_cast<uint32_t*>(bars + 6 + 2 * TC_STAGES);
+  __shared__ int s_err;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int qc = a.qc, kp = a.kp, M = a.M, dsub = a.dsub;
   const uint32_t bar0 = smem_u32(bars);
+  // bars: [0,1] B full, [2,3] B empty, [4,5] accumulator full,
+  // [6, 6+S) slot full, [6+S, 6+2S) slot empty
+  auto b_full = [&](int b) { return bar0 + 8u * b; };
+  auto b_empty = [&](int b) { return bar0 + 8u * (2 + b); };
+  auto acc_full = [&](int b) { return bar0 + 8u * (4 + b); };
+  auto s_full = [&](int s) { return bar0 + 8u * (6 + s); };
+  auto s_empty = [&](int s) { return bar0 + 8u * (6 + TC_STAGES + s); };
   if (tid == 0) {
     s_err = 0;
-    mbar_init(bar0, 1);
-    mbar_init(bar0 + 8, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(b_full(b), 1);
+      mbar_init(b_empty(b), TC_CONSUMERS);
+      mbar_init(acc_full(b), 1);
+    }
+    for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(s_full(s), 1);
+      mbar_init(s_empty(s), TC_CONSUMERS);
+    }
     fence_mbar_init();
   }
   if (warp == 0) tmem_alloc(smem_u32(holder), 2 * qc);
-  // the codebook, once per CTA
-  {
+  {  // the codebook, once per CTA
     const uint4* src = reinterpret_cast<const uint4*>(a.pq16);
     uint4* dst = reinterpret_cast<uint4*>(cb);
     for (int i = tid; i < L.cbbytes / 16; i += TC_THREADS) dst[i] = __ldg(src + i);
@@ -330,166 +423,200 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
   tc_fence_after();
   const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(holder);
   volatile int* verr = &s_err;
-  const int total_items = a.istart[a.nlist];
+  const int total = *a.total_items;
+  const int nkb = kp >> 6;
 
-  const int lq = warp & 3, half = warp >> 2;
-  const int r = lq * 32 + lane;  // this thread's tile row (decode and epilogue)
-  const int msplit = M >> 1;
-  const int m0 = half * msplit;
-  // the previous tile, waiting for its epilogue
-  bool have_prev = false;
-  int prev_g = 0, prev_ib = 0, prev_nq = 0, prev_nr = 0, prev_npad = 16;
-  int64_t prev_row0 = 0;
-  float prev_v = 0.0f;
-  bool prev_ex = false;
-  int g = 0, ic = 0;
-  int last_commit = -1;  // thread 0: index of the last committed tile
-
-  auto epilogue = [&]() {
-    const int buf = prev_g & 1;
-    bool ok = !*verr && mbar_wait(bar0 + 8u * buf, (uint32_t)(prev_g >> 1) & 1u, a.wait_limit);
-    if (!__all_sync(0xffffffffu, ok)) {
-      *verr = 1;
-      return;
-    }
-    tc_fence_after();
-    const int64_t* sg = mseg + prev_ib * qc;
-    const float* tm = mterm + prev_ib * qc;
-    const float* mu = mmul + prev_ib * qc;
-    const bool row_ok = r < prev_nr;
-    for (int cg = half; cg * 16 < prev_npad; cg += 2) {
-      float v[16];
-      tmem_ld16(tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(buf * qc + cg * 16), v);
-      if (row_ok) {
-#pragma unroll
-        for (int jj = 0; jj < 16; ++jj) {
-          const int j = cg * 16 + jj;
-          if (j < prev_nq) {
-            const float dd = fmaf(v[jj], mu[j], tm[j] + prev_v);
-            uint32_t o = float_to_ordered(dd);
-            o = o == TC_EXCLUDED ? TC_EXCLUDED - 1u : o;  // a NaN stays a candidate
-            a.dist[sg[j] + prev_row0 + r] = prev_ex ? TC_EXCLUDED : o;
+  if (warp == TC_CONSUMERS / 32) {
+    // ---- producer ----
+    if (lane == 0) {
+      int g = 0, i = 0;
+      for (int it = blockIdx.x; it < total; it += gridDim.x, ++i) {
+        const TcItem rec = a.items[it];
+        const int ib = i & 1;
+        if (*verr || !mbar_wait(b_empty(ib), ((uint32_t)(i >> 1) & 1u) ^ 1u, a.wait_limit)) {
+          *verr = 1;
+          break;
+        }
+        const int npad = max(16, (rec.nq + 15) & ~15);
+        mbar_arrive_expect_tx(b_full(ib), (uint32_t)(nkb * npad * 128 + npad * 16));
+        const uint8_t* img = a.bimg + (int64_t)rec.chunk * ((int64_t)qc * kp * 2);
+        for (int kb = 0; kb < nkb; ++kb)
+          bulk_load(smem_u32(sm + L.b_off(ib) + kb * qc * 128), img + kb * qc * 128,
+                    (uint32_t)(npad * 128), b_full(ib));
+        bulk_load(smem_u32(sm + L.m_off(ib)), a.meta + (int64_t)rec.chunk * qc, (uint32_t)(npad * 16),
+                  b_full(ib));
+        bool ok = true;
+        for (long long row0 = rec.rbeg; row0 < rec.rend; row0 += TC_BM, ++g) {
+          const int s = g % TC_STAGES;
+          if (*verr || !mbar_wait(s_empty(s), ((uint32_t)(g / TC_STAGES) & 1u) ^ 1u, a.wait_limit)) {
+            *verr = 1;
+            ok = false;
+            break;
           }
+          const int nr = (int)min((long long)TC_BM, rec.rend - row0);
+          const long long pos = rec.loff + row0;
+          const long long c0 = (pos * M) & ~15ll, c1 = (pos * M + (long long)nr * M + 15) & ~15ll;
+          uint32_t bytes = (uint32_t)(c1 - c0);
+          long long v0 = 0, v1 = 0, e0 = 0, e1 = 0;
+          if (a.vterm) {
+            v0 = (pos * 4) & ~15ll;
+            v1 = (pos * 4 + (long long)nr * 4 + 15) & ~15ll;
+            bytes += (uint32_t)(v1 - v0);
+          }
+          if (a.excl) {
+            e0 = pos & ~15ll;
+            e1 = (pos + nr + 15) & ~15ll;
+            bytes += (uint32_t)(e1 - e0);
+          }
+          uint8_t* slot = sm + L.slot_off(s);
+          mbar_arrive_expect_tx(s_full(s), bytes);
+          bulk_load(smem_u32(slot), a.codes + c0, (uint32_t)(c1 - c0), s_full(s));
+          if (a.vterm)
+            bulk_load(smem_u32(slot + L.code_bytes), reinterpret_cast<const uint8_t*>(a.vterm) + v0,
+                      (uint32_t)(v1 - v0), s_full(s));
+          if (a.excl)
+            bulk_load(smem_u32(slot + L.code_bytes + 544), a.excl + e0, (uint32_t)(e1 - e0), s_full(s));
+        }
+        if (!ok) {
+          ++i;
+          break;
         }
       }
+      // Unwind: every issued copy lands before the CTA may exit (full limit).
+      for (int j = (g > TC_STAGES ? g - TC_STAGES : 0); j < g; ++j)
+        if (!mbar_wait(s_full(j % TC_STAGES), (uint32_t)(j / TC_STAGES) & 1u)) *verr = 1;
+      for (int j = (i > 2 ? i - 2 : 0); j < i; ++j)
+        if (!mbar_wait(b_full(j & 1), (uint32_t)(j >> 1) & 1u)) *verr = 1;
     }
-    tc_fence_before();
-  };
+  } else {
+    // ---- consumers ----
+    const int lq = warp & 3, half = warp >> 2;
+    const int r = lq * 32 + lane;  // this thread's tile row (decode and epilogue)
+    const int msplit = M >> 1;
+    const int m0 = half * msplit;
+    bool have_prev = false, prev_last = false;
+    int prev_g = 0, prev_ib = 0, prev_nq = 0, prev_nr = 0, prev_npad = 16;
+    long long prev_row0 = 0;
+    float prev_v = 0.0f;
+    bool prev_ex = false;
+    int g = 0, i = 0;
+    int last_commit = -1;  // thread 0: the last committed tile
+    bool stop = false;
 
-  while (true) {
-    if (tid == 0) {
-      const int it = atomicAdd(a.counter, 1);
-      s_item = it;
-      if (it < total_items) {
-        int lo = 0, hi = a.nlist - 1;  // the list with istart[lo] <= it < istart[lo + 1]
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (a.istart[mid] <= it) lo = mid;
-          else hi = mid - 1;
-        }
-        const int64_t len = a.list_off[lo + 1] - a.list_off[lo];
-        const int nseg = (int)((len + TC_RS - 1) / TC_RS);
-        const int c = it - a.istart[lo];
-        const int chunk = c / nseg, piece = c - chunk * nseg;
-        s_L = lo;
-        s_rbeg = (int64_t)piece * TC_RS;
-        s_rend = min(len, (int64_t)(piece + 1) * TC_RS);
-        s_pb = a.start[lo] + (int64_t)chunk * qc;
-        s_nq = min(qc, a.cnt[lo] - chunk * qc);
+    auto epilogue = [&]() {
+      const int buf = prev_g & 1;
+      bool ok = !*verr && mbar_wait(acc_full(buf), (uint32_t)(prev_g >> 1) & 1u, a.wait_limit);
+      if (!__all_sync(0xffffffffu, ok)) {
+        *verr = 1;
+        return;
       }
-    }
-    const bool stop = __syncthreads_or(*verr);  // one answer for every thread
-    if (s_item >= total_items || stop) break;
-    const int ib = ic & 1;
-    const int Lst = s_L, nqi = s_nq;
-    const int64_t rbeg = s_rbeg, rend = s_rend, pb = s_pb;
-    const int64_t loff = a.list_off[Lst];
-    const int npad = max(16, (nqi + 15) & ~15);
-    // B[ib]: the chunk's query rows; meta[ib]: per column offset, term, scale
-    {
-      uint8_t* B = sm + L.b_off(ib);
-      const int cpr = kp >> 3;  // 16-byte chunks per row
-      for (int i = tid; i < nqi * cpr; i += TC_THREADS) {
-        const int j = i / cpr, c = i - j * cpr;
-        const int64_t pr = a.pairs[pb + j];
-        const int64_t qrow = pr / a.P;
-        const uint4 v = __ldg(reinterpret_cast<const uint4*>(a.q16 + qrow * kp) + c);
-        *reinterpret_cast<uint4*>(B + (c >> 3) * (qc * 128) + sw128(j, c & 7)) = v;
-      }
-      if (tid < nqi) {
-        const int64_t pr = a.pairs[pb + tid];
-        mseg[ib * qc + tid] = a.seg[pr];  // + row within the list = the row's slot
-        mterm[ib * qc + tid] = a.term[pr];
-        mmul[ib * qc + tid] = a.qmul[pr / a.P];
-      }
-    }
-    for (int64_t row0 = rbeg; row0 < rend; row0 += TC_BM) {
-      const int nr = (int)min((int64_t)TC_BM, rend - row0);
-      const int buf = g & 1;
-      uint8_t* A = sm + L.a_off(buf);
-      float cur_v = 0.0f;
-      bool cur_ex = false;
-      if (r < nr) {
-        const int64_t pos = loff + row0 + r;
-        const uint8_t* crow = a.codes + pos * M + m0;
-        for (int w0 = 0; w0 < msplit; w0 += 4) {
-          const uint32_t word = __ldg(reinterpret_cast<const uint32_t*>(crow + w0));
+      tc_fence_after();
+      const TcMeta* mt = reinterpret_cast<const TcMeta*>(sm + L.m_off(prev_ib));
+      const bool row_ok = r < prev_nr;
+      for (int cg = half; cg * 16 < prev_npad; cg += 2) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(buf * qc + cg * 16), v);
+        if (row_ok) {
 #pragma unroll
-          for (int b = 0; b < 4; ++b) {
-            const int m = m0 + w0 + b;
-            const uint32_t code = (word >> (8 * b)) & 255u;
-            if (dsub == 8) {
-              const uint4 cw = *reinterpret_cast<const uint4*>(cb + ((m << 8) + code) * 16);
-              *reinterpret_cast<uint4*>(A + (m >> 3) * (TC_BM * 128) + sw128(r, m & 7)) = cw;
-            } else {  // dsub 4: half a chunk per subspace
-              const uint2 cw = *reinterpret_cast<const uint2*>(cb + ((m << 8) + code) * 8);
-              *reinterpret_cast<uint2*>(A + (m >> 4) * (TC_BM * 128) + sw128(r, (m >> 1) & 7) +
-                                        (m & 1) * 8) = cw;
+          for (int jj = 0; jj < 16; ++jj) {
+            const int j = cg * 16 + jj;
+            if (j < prev_nq) {
+              const float dd = fmaf(v[jj], mt[j].qmul, mt[j].term + prev_v);
+              uint32_t o = float_to_ordered(dd);
+              o = o == TC_EXCLUDED ? TC_EXCLUDED - 1u : o;  // a NaN stays a candidate
+              a.dist[mt[j].seg + prev_row0 + r] = prev_ex ? TC_EXCLUDED : o;
             }
           }
         }
-        if (a.vterm) cur_v = __ldg(a.vterm + pos);
-        if (a.filter) {
-          const uint32_t id = a.ids[pos];
-          cur_ex = (int64_t)id < a.filter_len && a.filter[id] != 0;
-        }
       }
-      fence_proxy_async();
-      if (__syncthreads_or(*verr)) break;  // one answer for every thread
-      if (tid == 0) {
-        tc_fence_after();
-        const uint32_t dt = tmem + (uint32_t)(buf * qc);
-        const uint32_t idesc = idesc_f16_f32(TC_BM, npad);
-        const uint32_t abase = smem_u32(A), bbase = smem_u32(sm + L.b_off(ib));
-        const int ks = a.d >> 4;
-        for (int s = 0; s < ks; ++s) {
-          const int kb = s >> 2, kk = s & 3;
-          const uint64_t ad = desc_k_sw128(abase + kb * (TC_BM * 128)) + 2u * kk;
-          const uint64_t bd = desc_k_sw128(bbase + kb * (qc * 128)) + 2u * kk;
-          umma_f16(dt, ad, bd, idesc, s > 0 ? 1u : 0u);
+      tc_fence_before();
+    };
+
+    TcItem nrec;  // the next item's record, loaded one item ahead
+    if ((int)blockIdx.x < total) nrec = a.items[blockIdx.x];
+    for (int it = blockIdx.x; it < total && !stop; it += gridDim.x, ++i) {
+      const TcItem rec = nrec;
+      if (it + (int)gridDim.x < total) nrec = a.items[it + gridDim.x];
+      const int ib = i & 1;
+      const int nqi = rec.nq;
+      const int npad = max(16, (nqi + 15) & ~15);
+      bool okb = !*verr && mbar_wait(b_full(ib), (uint32_t)(i >> 1) & 1u, a.wait_limit);
+      if (!okb) *verr = 1;
+      for (long long row0 = rec.rbeg; row0 < rec.rend; row0 += TC_BM, ++g) {
+        const int nr = (int)min((long long)TC_BM, rec.rend - row0);
+        const int s = g % TC_STAGES;
+        const int buf = g & 1;
+        uint8_t* A = sm + L.a_off(buf);
+        float cur_v = 0.0f;
+        bool cur_ex = false;
+        bool oks = okb && !*verr && mbar_wait(s_full(s), (uint32_t)(g / TC_STAGES) & 1u, a.wait_limit);
+        if (!oks) *verr = 1;
+        if (oks && r < nr) {
+          const uint8_t* slot = sm + L.slot_off(s);
+          const long long pos = rec.loff + row0;
+          const int dc = (int)((pos * M) & 15), dv = (int)((pos * 4) & 15), de = (int)(pos & 15);
+          const uint8_t* crow = slot + dc + r * M + m0;
+          for (int w0 = 0; w0 < msplit; w0 += 4) {
+            const uint32_t word = *reinterpret_cast<const uint32_t*>(crow + w0);
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+              const int m = m0 + w0 + b;
+              const uint32_t code = (word >> (8 * b)) & 255u;
+              if (dsub == 8) {
+                const uint4 cw = *reinterpret_cast<const uint4*>(cb + ((m << 8) + code) * 16);
+                *reinterpret_cast<uint4*>(A + (m >> 3) * (TC_BM * 128) + sw128(r, m & 7)) = cw;
+              } else {  // dsub 4: half a chunk per subspace
+                const uint2 cw = *reinterpret_cast<const uint2*>(cb + ((m << 8) + code) * 8);
+                *reinterpret_cast<uint2*>(A + (m >> 4) * (TC_BM * 128) + sw128(r, (m >> 1) & 7) +
+                                          (m & 1) * 8) = cw;
+              }
+            }
+          }
+          if (a.vterm) cur_v = *reinterpret_cast<const float*>(slot + L.code_bytes + dv + r * 4);
+          if (a.excl) cur_ex = slot[L.code_bytes + 544 + de + r] != 0;
         }
-        umma_commit(bar0 + 8u * buf);
-        last_commit = g;
+        mbar_arrive(s_empty(s));
+        fence_proxy_async();
+        if (consumers_sync_or(*verr)) {  // one answer for every consumer
+          stop = true;
+          break;
+        }
+        if (tid == 0) {
+          tc_fence_after();
+          const uint32_t dt = tmem + (uint32_t)(buf * qc);
+          const uint32_t idesc = idesc_f16_f32(TC_BM, npad);
+          const uint32_t abase = smem_u32(A), bbase = smem_u32(sm + L.b_off(ib));
+          const int ks = a.d >> 4;
+          for (int k = 0; k < ks; ++k) {
+            const int kb = k >> 2, kk = k & 3;
+            const uint64_t ad = desc_k_sw128(abase + kb * (TC_BM * 128)) + 2u * kk;
+            const uint64_t bd = desc_k_sw128(bbase + kb * (qc * 128)) + 2u * kk;
+            umma_f16(dt, ad, bd, idesc, k > 0 ? 1u : 0u);
+          }
+          umma_commit(acc_full(buf));
+          last_commit = g;
+        }
+        if (have_prev) {
+          epilogue();
+          if (prev_last) mbar_arrive(b_empty(prev_ib));
+        }
+        have_prev = true;
+        prev_last = row0 + TC_BM >= rec.rend;
+        prev_g = g;
+        prev_ib = ib;
+        prev_nq = nqi;
+        prev_nr = nr;
+        prev_npad = npad;
+        prev_row0 = row0;
+        prev_v = cur_v;
+        prev_ex = cur_ex;
       }
-      if (have_prev) epilogue();
-      have_prev = true;
-      prev_g = g;
-      prev_ib = ib;
-      prev_nq = nqi;
-      prev_nr = nr;
-      prev_npad = npad;
-      prev_row0 = row0;
-      prev_v = cur_v;
-      prev_ex = cur_ex;
-      ++g;
     }
-    ++ic;
-  }
-  if (have_prev && !*verr) epilogue();
-  __syncthreads();
-  // Unwind: the last issued MMAs retire before TMEM is freed (full limit).
-  if (tid == 0 && last_commit >= 0) {
-    if (!mbar_wait(bar0 + 8u * (last_commit & 1), (uint32_t)(last_commit >> 1) & 1u)) *verr = 1;
+    if (have_prev && !*verr) epilogue();
+    // Unwind: the last issued MMAs retire before TMEM is freed (full limit).
+    if (tid == 0 && last_commit >= 0) {
+      if (!mbar_wait(acc_full(last_commit & 1), (uint32_t)(last_commit >> 1) & 1u)) *verr = 1;
+    }
   }
   __syncthreads();
   if (warp == 0) {
@@ -554,7 +681,8 @@ __device__ __forceinline__ void sel_sort_side(const uint64_t* side, int h, int n
   }
 }
 
-// One warp per query. The query's candidates are its distance row's first
+// Shortlists longer than SS_RMAX: one warp per query over its row in
+// global memory. The query's candidates are its distance row's first
 // n words, probe by probe; candidate i of probe p is CSR row
 // off[p] + (i - beg[p]) and its key is (word << 32) | row. Pass 1 finds the
 // valid keys' count, min and max; histogram passes over the keys still in
@@ -563,7 +691,7 @@ __device__ __forceinline__ void sel_sort_side(const uint64_t* side, int h, int n
 // every key below the bin and stages the bin's keys, which one warp sort
 // orders to fill the shortlist. The shortlist is written unsorted in a
 // fixed order (the row order of the passes).
-__global__ void __launch_bounds__(SEL_WARPS * 32) k_tc_select(SelArgs a) {
+__global__ void __launch_bounds__(SEL_WARPS * 32) k_tc_select_wide(SelArgs a) {
   extern __shared__ __align__(16) uint8_t smraw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t row = (int64_t)blockIdx.x * SEL_WARPS + warp;
@@ -728,6 +856,191 @@ __global__ void __launch_bounds__(SEL_WARPS * 32) k_tc_select(SelArgs a) {
   else sel_sort_side<8>(side, h, need, out + (R - need));
 }
 
+// ---- shortlists of up to SS_RMAX keys: one streaming pass ----------------
+constexpr int SS_WARPS = 4;
+constexpr int SS_RMAX = 256;
+constexpr int SS_CAP = 640;  // staged keys per warp: R kept + at least three rounds of 128
+
+__host__ __device__ inline size_t ss_warp_bytes(int P) {
+  return (size_t)SS_CAP * 8 + (size_t)SEL_SIDE * 8 + (size_t)SEL_BINS * 4 + (size_t)P * 8 +
+         (((size_t)P + 1) * 4 + 7) / 8 * 8;
+}
+
+// Keeps the R smallest of the m (> R) distinct keys buf[0, m) in buf[0, R),
+// unsorted, and returns the largest kept key. One warp: min and max, then
+// 256-bin histogram passes over [lo, hi] until the bin holding the R-th key
+// holds at most SEL_SIDE keys; the keys below that bin are compacted in
+// place (in order) and the bin's keys sorted to fill the rest.
+__device__ uint64_t warp_keep_smallest(uint64_t* buf, int m, int R, uint64_t* side, uint32_t* hist) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long kmin = ~0ull, kmax = 0ull;
+  for (int j = lane; j < m; j += 32) {
+    const unsigned long long k = buf[j];
+    kmin = k < kmin ? k : kmin;
+    kmax = k > kmax ? k : kmax;
+  }
+  uint64_t lo = shfl_min64(kmin), hi = shfl_max64(kmax);
+  int need = R, h = m;
+  for (int level = 0; level < 8; ++level) {
+    const uint64_t span = hi - lo;
+    const int sh = span < (uint64_t)SEL_BINS ? 0 : (64 - __clzll((long long)span)) - 8;
+    for (int b = lane; b < SEL_BINS; b += 32) hist[b] = 0u;
+    __syncwarp();
+    for (int j = lane; j < m; j += 32) {
+      const uint64_t k = buf[j];
+      if (k >= lo && k <= hi) atomicAdd(&hist[(k - lo) >> sh], 1u);
+    }
+    __syncwarp();
+    uint32_t c[8], local = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      c[j] = hist[lane * 8 + j];
+      local += c[j];
+    }
+    uint32_t incl = local;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    uint32_t run = incl - local;
+    int hit = -1;
+    uint32_t hb = 0, before = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      if (hit < 0 && run < (uint32_t)need && (uint32_t)need <= run + c[j]) {
+        hit = lane * 8 + j;
+        hb = c[j];
+        before = run;
+      }
+      run += c[j];
+    }
+    const int src_lane = __ffs(__ballot_sync(0xffffffffu, hit >= 0)) - 1;
+    const int b = __shfl_sync(0xffffffffu, hit, src_lane);
+    h = (int)__shfl_sync(0xffffffffu, hb, src_lane);
+    need -= (int)__shfl_sync(0xffffffffu, before, src_lane);
+    const uint64_t nlo = lo + ((uint64_t)b << sh);
+    const uint64_t wdt = (1ull << sh) - 1ull;  // sh <= 56
+    hi = hi - nlo <= wdt ? hi : nlo + wdt;
+    lo = nlo;
+    __syncwarp();
+    if (h <= SEL_SIDE) break;
+  }
+  // distinct keys: a one-key-wide bin holds one key, so h <= SEL_SIDE here
+  const unsigned lt = (1u << lane) - 1u;
+  int o = 0, so = 0;
+  for (int j0 = 0; j0 < m; j0 += 32) {
+    const int j = j0 + lane;
+    const uint64_t k = j < m ? buf[j] : KEY_NONE;
+    const bool below = j < m && k < lo;
+    const bool at = j < m && k >= lo && k <= hi;
+    const unsigned bb = __ballot_sync(0xffffffffu, below);  // every read of this round is done
+    const unsigned ba = __ballot_sync(0xffffffffu, at);
+    if (below) buf[o + __popc(bb & lt)] = k;  // o + rank <= j: never ahead of the reads
+    if (at) {
+      const int s = so + __popc(ba & lt);
+      if (s < SEL_SIDE) side[s] = k;
+    }
+    o += __popc(bb);
+    so += __popc(ba);
+  }
+  __syncwarp();
+  h = min(h, SEL_SIDE);
+  if (h <= 32) sel_sort_side<1>(side, h, need, buf + (R - need));
+  else if (h <= 64) sel_sort_side<2>(side, h, need, buf + (R - need));
+  else if (h <= 128) sel_sort_side<4>(side, h, need, buf + (R - need));
+  else sel_sort_side<8>(side, h, need, buf + (R - need));
+  __syncwarp();
+  return buf[R - 1];
+}
+
+// One warp per query, one pass over its distance row (16-byte loads, the
+// next round's load issued before this round's keys are built): keys below
+// the running bound T are staged in shared memory; when the staging area
+// could overflow, the R smallest are kept and T becomes the largest of
+// them (a later key at or above T cannot be among the R smallest). The
+// kept set is the R smallest keys whatever the order of arrival; it is
+// written unsorted, in a fixed order.
+__global__ void __launch_bounds__(SS_WARPS * 32) k_tc_select_stream(SelArgs a) {
+  extern __shared__ __align__(16) uint8_t smraw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * SS_WARPS + warp;
+  if (row >= a.nq) return;
+  uint8_t* base = smraw + (size_t)warp * ss_warp_bytes(a.P);
+  uint64_t* buf = reinterpret_cast<uint64_t*>(base);
+  uint64_t* side = buf + SS_CAP;
+  uint32_t* hist = reinterpret_cast<uint32_t*>(side + SEL_SIDE);
+  int64_t* poff = reinterpret_cast<int64_t*>(hist + SEL_BINS);
+  int* pbeg = reinterpret_cast<int*>(poff + a.P);
+  const int np = a.nprobe_q ? min(max(a.nprobe_q[row], 1), a.P) : a.P;
+  int carry = 0;
+  for (int p0 = 0; p0 < np; p0 += 32) {
+    const int p = p0 + lane;
+    int len = 0;
+    if (p < np) {
+      const int L = a.probes[row * a.P + p];
+      int64_t off = 0;
+      if (L >= 0 && L < a.nlist) {
+        off = a.list_off[L];
+        len = (int)(a.list_off[L + 1] - off);
+      }
+      poff[p] = off;
+    }
+    int incl = len;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    if (p < np) pbeg[p] = carry + incl - len;
+    carry += __shfl_sync(0xffffffffu, incl, 31);
+  }
+  if (lane == 0) pbeg[np] = carry;
+  __syncwarp();
+  const int n = carry <= a.smax ? carry : 0;  // a row over smax was left unwritten (site 106)
+  const uint32_t* src = a.dist + row * a.smax;  // smax is a multiple of 4: 16-byte rows
+  const int R = a.R;
+  const unsigned lt = (1u << lane) - 1u;
+  uint64_t T = KEY_NONE;
+  int m = 0, p = 0;
+  // words i0 + 4 lane .. + 3 of each 128-word round (the row holds smax
+  // >= roundup(n, 4) words, so the vector load stays in the row)
+  auto load4 = [&](int i0) {
+    const int i = i0 + 4 * lane;
+    return i < n ? __ldg(reinterpret_cast<const uint4*>(src + i))
+                 : make_uint4(TC_EXCLUDED, TC_EXCLUDED, TC_EXCLUDED, TC_EXCLUDED);
+  };
+  uint4 cur = load4(0);
+  for (int i0 = 0; i0 < n; i0 += 128) {
+    const uint4 nxt = load4(i0 + 128);
+    if (m + 128 > SS_CAP) {
+      T = warp_keep_smallest(buf, m, R, side, hist);
+      m = R;
+    }
+    const uint32_t w[4] = {cur.x, cur.y, cur.z, cur.w};
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + 4 * lane + u;
+      uint64_t key = KEY_NONE;
+      bool in = false;
+      if (i < n) {
+        while (pbeg[p + 1] <= i) ++p;
+        key = ((uint64_t)w[u] << 32) | (uint32_t)(poff[p] + (i - pbeg[p]));
+        in = w[u] != TC_EXCLUDED && key < T;
+      }
+      const unsigned b = __ballot_sync(0xffffffffu, in);
+      if (in) buf[m + __popc(b & lt)] = key;
+      m += __popc(b);
+    }
+    cur = nxt;
+  }
+  __syncwarp();
+  if (m > R) {
+    warp_keep_smallest(buf, m, R, side, hist);
+    m = R;
+  }
+  uint64_t* out = a.out + row * R;
+  for (int j = lane; j < R; j += 32) out[j] = j < m ? buf[j] : KEY_NONE;
+}
+
 // Rows of R keys sorted ascending in place (KEY_NONE padded to Rp in
 // shared memory).
 __global__ void __launch_bounds__(256) k_tc_sort(uint64_t* keys, int R, int Rp) {
@@ -749,14 +1062,40 @@ bool ivfpq_tc_supported(int d, int M, bool has_pq16) {
 
 int ivfpq_tc_qc(int64_t nq, int nprobe, int nlist) {
   const double per_list = (double)nq * nprobe / (nlist > 0 ? nlist : 1);
-  return per_list > 48.0 ? 128 : per_list > 20.0 ? 64 : 32;
+  return per_list > 48.0 ? 128 : 64;
 }
 
-size_t ivfpq_tc_scratch_bytes(int64_t nq, int nprobe, int nlist, int d, int64_t smax) {
-  const int kp = (d + 63) / 64 * 64;
-  return al((size_t)nq * kp * 2) + al((size_t)nq * 4) + al((size_t)nq * nprobe * 8) +
-         3 * al((size_t)(nlist + 1) * 4) + al((size_t)(nlist + 1) * 8) +
-         al((size_t)nq * nprobe * 4) + al(16) + al((size_t)nq * smax * 4);
+namespace {
+
+// Scratch layout of one launch (every part 256-byte aligned).
+struct TcLayout {
+  int64_t smax4, chunks, items;
+  size_t q16, qmul, seg, ints, start, items_b, bimg, meta, excl, dist, total;
+  TcLayout(int64_t nq, int P, int nlist, int d, int64_t smax, int qc, int64_t ntotal) {
+    const int kp = (d + 63) / 64 * 64;
+    const int64_t npairs = nq * P;
+    smax4 = (smax + 3) & ~3ll;
+    chunks = npairs / qc + nlist + 1;
+    items = nq * smax4 / ((int64_t)qc * TC_RS) + npairs / qc + ntotal / TC_RS + 2 * (int64_t)nlist + 4;
+    q16 = al((size_t)nq * kp * 2);
+    qmul = al((size_t)nq * 4);
+    seg = al((size_t)npairs * 8);
+    ints = 4 * al((size_t)(nlist + 1) * 4);  // cnt, cursor, cstart, istart
+    start = al((size_t)(nlist + 1) * 8);
+    items_b = al((size_t)items * sizeof(TcItem));
+    bimg = al((size_t)chunks * qc * kp * 2);
+    meta = al((size_t)chunks * qc * sizeof(TcMeta));
+    excl = al((size_t)ntotal + 16);
+    dist = al((size_t)nq * smax4 * 4);
+    total = q16 + qmul + seg + ints + start + items_b + bimg + meta + excl + dist;
+  }
+};
+
+}  // namespace
+
+size_t ivfpq_tc_scratch_bytes(int64_t nq, int nprobe, int nlist, int d, int64_t smax, int qc,
+                              int64_t ntotal) {
+  return TcLayout(nq, nprobe, nlist, d, smax, qc, ntotal).total;
 }
 
 void launch_ivfpq_scan_tc(const FastScanArgs& f, int64_t smax, int qc, void* scratch, int num_sms,
@@ -766,72 +1105,73 @@ void launch_ivfpq_scan_tc(const FastScanArgs& f, int64_t smax, int qc, void* scr
   const int d = f.d, M = f.M, P = f.nprobe, nlist = f.nlist;
   MV_REQUIRE(f.pq16 && ivfpq_tc_supported(d, M, true), MV_ERR_INTERNAL,
              "tensor-core ADC scan: unsupported shape");
-  MV_REQUIRE(qc == 32 || qc == 64 || qc == 128, MV_ERR_INTERNAL, "tensor-core ADC scan: bad chunk");
+  MV_REQUIRE(qc == 64 || qc == 128, MV_ERR_INTERNAL, "tensor-core ADC scan: bad chunk");
   MV_REQUIRE(nq * P < (1ll << 31) && smax < (1ll << 31), MV_ERR_UNSUPPORTED,
              "tensor-core ADC scan: batch too large");
   const int kp = (d + 63) / 64 * 64;
+  const TcLayout lay(nq, P, nlist, d, smax, qc, f.ntotal);
   unsigned char* p = static_cast<unsigned char*>(scratch);
   auto take = [&](size_t bytes) {
     unsigned char* r = p;
-    p += al(bytes);
+    p += bytes;
     return r;
   };
-  __half* q16 = reinterpret_cast<__half*>(take((size_t)nq * kp * 2));
-  float* qmul = reinterpret_cast<float*>(take((size_t)nq * 4));
-  int64_t* seg = reinterpret_cast<int64_t*>(take((size_t)nq * P * 8));
-  int* cnt = reinterpret_cast<int*>(take((size_t)(nlist + 1) * 4));
-  int* cursor = reinterpret_cast<int*>(take((size_t)(nlist + 1) * 4));
-  int* istart = reinterpret_cast<int*>(take((size_t)(nlist + 1) * 4));
-  int64_t* start = reinterpret_cast<int64_t*>(take((size_t)(nlist + 1) * 8));
-  int32_t* pairs = reinterpret_cast<int32_t*>(take((size_t)nq * P * 4));
-  int* counter = reinterpret_cast<int*>(take(16));
-  uint32_t* dist = reinterpret_cast<uint32_t*>(take((size_t)nq * smax * 4));
-  MV_CHECK_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (nlist + 1), s));
-  MV_CHECK_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * (nlist + 1), s));
-  MV_CHECK_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), s));
+  __half* q16 = reinterpret_cast<__half*>(take(lay.q16));
+  float* qmul = reinterpret_cast<float*>(take(lay.qmul));
+  int64_t* seg = reinterpret_cast<int64_t*>(take(lay.seg));
+  int* ints = reinterpret_cast<int*>(take(lay.ints));
+  const size_t ni = lay.ints / 16;  // ints per array (256-byte aligned parts)
+  int* cnt = ints;
+  int* cursor = ints + ni;
+  int* cstart = ints + 2 * ni;
+  int* istart = ints + 3 * ni;
+  int64_t* start = reinterpret_cast<int64_t*>(take(lay.start));
+  TcItem* items = reinterpret_cast<TcItem*>(take(lay.items_b));
+  uint8_t* bimg = take(lay.bimg);
+  TcMeta* meta = reinterpret_cast<TcMeta*>(take(lay.meta));
+  uint8_t* excl = take(lay.excl);
+  uint32_t* dist = reinterpret_cast<uint32_t*>(take(lay.dist));
+  MV_CHECK_CUDA(cudaMemsetAsync(cnt, 0, 2 * lay.ints / 4, s));  // cnt and cursor
   const float scale = f.metric == MV_METRIC_L2 ? -2.0f : -1.0f;
   const unsigned gw = (unsigned)((nq + 7) / 8);
   k_tc_q16<<<gw, 256, 0, s>>>(f.q, nq, d, kp, scale * f.pq16_inv, q16, qmul);
-  k_tc_pairs<<<gw, 256, 0, s>>>(f.probes, nq, P, f.nprobe_q, f.list_off, nlist, smax, seg, cnt,
-                                f.err);
-  k_tc_items<<<1, 1024, 0, s>>>(cnt, f.list_off, nlist, qc, start, istart);
+  k_tc_pairs<<<gw, 256, 0, s>>>(f.probes, nq, P, f.nprobe_q, f.list_off, nlist, lay.smax4, seg,
+                                cnt, f.err);
+  k_tc_items<<<1, 1024, 0, s>>>(cnt, f.list_off, nlist, qc, start, cstart, istart, items);
   k_tc_place<<<(unsigned)((nq * P + 255) / 256), 256, 0, s>>>(f.probes, nq, P, f.nprobe_q, nlist,
-                                                               seg, start, cursor, pairs);
+                                                               seg, f.term, q16, qmul, kp, qc,
+                                                               cstart, cursor, bimg, meta);
   for (int i = 0; i < 4; ++i) count_launch();
+  if (f.filter) {
+    k_tc_excl<<<(unsigned)((f.ntotal + 255) / 256), 256, 0, s>>>(f.ids, f.ntotal, f.filter,
+                                                                  f.filter_len, excl);
+    count_launch();
+  }
   TcArgs t;
-  t.q16 = q16;
-  t.qmul = qmul;
-  t.term = f.term;
-  t.seg = seg;
-  t.cnt = cnt;
-  t.start = start;
-  t.istart = istart;
-  t.pairs = pairs;
-  t.list_off = f.list_off;
+  t.items = items;
+  t.total_items = istart + nlist;
+  t.bimg = bimg;
+  t.meta = meta;
   t.codes = f.codes;
   t.vterm = f.vterm;
+  t.excl = f.filter ? excl : nullptr;
   t.pq16 = f.pq16;
-  t.filter = f.filter;
-  t.filter_len = f.filter_len;
-  t.ids = f.ids;
   t.dist = dist;
-  t.counter = counter;
   t.err = f.err;
-  t.nlist = nlist;
-  t.P = P;
   t.M = M;
   t.dsub = d / M;
   t.d = d;
   t.kp = kp;
   t.qc = qc;
   t.wait_limit = wait_limit;
-  const size_t smem = TcSmem(kp, qc, d).total(qc);
+  const size_t smem = TcSmem(kp, qc, d, M).total();
+  MV_REQUIRE(smem <= 227 * 1024, MV_ERR_INTERNAL, "tensor-core ADC scan: shared memory");
   smem_limit(k_tc_scan, smem);
   k_tc_scan<<<(unsigned)num_sms, TC_THREADS, smem, s>>>(t);
   count_launch();
   SelArgs sa;
   sa.dist = dist;
-  sa.smax = smax;
+  sa.smax = lay.smax4;
   sa.probes = f.probes;
   sa.nprobe_q = f.nprobe_q;
   sa.list_off = f.list_off;
@@ -841,10 +1181,17 @@ void launch_ivfpq_scan_tc(const FastScanArgs& f, int64_t smax, int qc, void* scr
   sa.nq = nq;
   sa.out = f.out_keys;
   sa.err = f.err;
-  const size_t ssm = sel_warp_bytes(P) * SEL_WARPS;
-  MV_REQUIRE(ssm <= 200 * 1024, MV_ERR_UNSUPPORTED, "tensor-core ADC scan: nprobe too large");
-  smem_limit(k_tc_select, ssm);
-  k_tc_select<<<(unsigned)((nq + SEL_WARPS - 1) / SEL_WARPS), SEL_WARPS * 32, ssm, s>>>(sa);
+  if (f.R <= SS_RMAX) {
+    const size_t ssm = ss_warp_bytes(P) * SS_WARPS;
+    MV_REQUIRE(ssm <= 200 * 1024, MV_ERR_UNSUPPORTED, "tensor-core ADC scan: nprobe too large");
+    smem_limit(k_tc_select_stream, ssm);
+    k_tc_select_stream<<<(unsigned)((nq + SS_WARPS - 1) / SS_WARPS), SS_WARPS * 32, ssm, s>>>(sa);
+  } else {
+    const size_t ssm = sel_warp_bytes(P) * SEL_WARPS;
+    MV_REQUIRE(ssm <= 200 * 1024, MV_ERR_UNSUPPORTED, "tensor-core ADC scan: nprobe too large");
+    smem_limit(k_tc_select_wide, ssm);
+    k_tc_select_wide<<<(unsigned)((nq + SEL_WARPS - 1) / SEL_WARPS), SEL_WARPS * 32, ssm, s>>>(sa);
+  }
   count_launch();
   if (f.sorted) {
     const int Rp = next_pow2(f.R);

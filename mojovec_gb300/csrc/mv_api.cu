@@ -855,7 +855,7 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
                             ws_bytes((size_t)qb, 4)
                        : ws_bytes((size_t)qb * ix->nlist, 4)) +
             ws_bytes((size_t)qb * nprobe, 4) * 2 + ws_bytes((size_t)qb * R, 8) +
-            (tc ? ws_bytes(ivfpq_tc_scratch_bytes(qb, nprobe, ix->nlist, ix->d, smax), 1) : 0));
+            (tc ? ws_bytes(ivfpq_tc_scratch_bytes(qb, nprobe, ix->nlist, ix->d, smax, tc_qc, ix->h_off[ix->nlist]), 1) : 0));
   Arena ar(ws);
   __nv_bfloat16* xq = ar.take<__nv_bfloat16>((size_t)qb * kp);
   float* dmat = fused || twopass ? nullptr : ar.take<float>((size_t)qb * ix->nlist);
@@ -868,7 +868,7 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
   float* term = ar.take<float>((size_t)qb * nprobe);
   uint64_t* skeys = ar.take<uint64_t>((size_t)qb * R);
   void* tc_scratch =
-      tc ? ar.take<unsigned char>(ivfpq_tc_scratch_bytes(qb, nprobe, ix->nlist, ix->d, smax)) : nullptr;
+      tc ? ar.take<unsigned char>(ivfpq_tc_scratch_bytes(qb, nprobe, ix->nlist, ix->d, smax, tc_qc, ix->h_off[ix->nlist])) : nullptr;
   for (int64_t q0 = 0; q0 < nq; q0 += qb) {
     const int64_t nb = std::min(qb, nq - q0);
     const float* xb = d_x + q0 * ix->d;

@@ -117,11 +117,13 @@ void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s, int nt = 256, int pe
 // probes, term, nprobe, nprobe_q, R, sorted, out_keys, nlist, err, filter).
 // Shapes: FP16 codebook, M a multiple of 8, d / M = 4 or 8, d <= 128.
 bool ivfpq_tc_supported(int d, int M, bool has_pq16);
-// Queries per work item (32, 64 or 128) for a batch shape.
+// Queries per work item (64 or 128) for a batch shape.
 int ivfpq_tc_qc(int64_t nq, int nprobe, int nlist);
 // smax: an upper bound on any query's candidate count (the nprobe longest
-// lists); the scratch holds nq distance rows of smax words.
-size_t ivfpq_tc_scratch_bytes(int64_t nq, int nprobe, int nlist, int d, int64_t smax);
+// lists); the scratch holds nq distance rows of smax words, the query
+// images of the work items and one flag per CSR row (ntotal).
+size_t ivfpq_tc_scratch_bytes(int64_t nq, int nprobe, int nlist, int d, int64_t smax, int qc,
+                              int64_t ntotal);
 void launch_ivfpq_scan_tc(const FastScanArgs& a, int64_t smax, int qc, void* scratch, int num_sms,
                           long long wait_limit, cudaStream_t s);
 // Flat fast form: merge nseg x ncp per-segment keys (kseg kept per segment)
