@@ -185,12 +185,10 @@ struct TcMeta {
 
 // Exclusive scans over the lists of the pair counts (start), the query
 // chunks (cstart: ceil(cnt / qc)) and the work items (istart: chunks times
-// ceil(len / TC_RS) row pieces), then every list's item records. One block
-// of 1024 threads.
+// ceil(len / TC_RS) row pieces). One block of 1024 threads.
 __global__ void __launch_bounds__(1024)
     k_tc_items(const int* __restrict__ cnt, const int64_t* __restrict__ list_off, int nlist, int qc,
-               int64_t* __restrict__ start, int* __restrict__ cstart, int* __restrict__ istart,
-               TcItem* __restrict__ items) {
+               int64_t* __restrict__ start, int* __restrict__ cstart, int* __restrict__ istart) {
   __shared__ long long ws1[32];
   __shared__ int ws2[32], ws3[32];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -251,29 +249,40 @@ __global__ void __launch_bounds__(1024)
     start[L] = base1;
     istart[L] = base2;
     cstart[L] = base3;
-    const int nch = chunks(L), npc = pieces(L);
-    const int64_t loff = list_off[L], len = list_off[L + 1] - loff;
-    for (int c = 0; c < nch; ++c) {
-      for (int pc = 0; pc < npc; ++pc) {
-        TcItem it;
-        it.L = L;
-        it.nq = min(qc, cnt[L] - c * qc);
-        it.chunk = base3 + c;
-        it.pad = 0;
-        it.loff = loff;
-        it.rbeg = (long long)pc * TC_RS;
-        it.rend = min(len, (int64_t)(pc + 1) * TC_RS);
-        items[base2 + c * npc + pc] = it;
-      }
-    }
     base1 += cnt[L];
-    base2 += nch * npc;
-    base3 += nch;
+    base2 += chunks(L) * pieces(L);
+    base3 += chunks(L);
   }
   if (t == 1023) {
     start[nlist] = ws1[31];
     istart[nlist] = ws2[31];
     cstart[nlist] = ws3[31];
+  }
+}
+
+// Every list's work-item records, one thread per list.
+__global__ void k_tc_fill(const int* __restrict__ cnt, const int64_t* __restrict__ list_off, int nlist,
+                          int qc, const int* __restrict__ cstart, const int* __restrict__ istart,
+                          TcItem* __restrict__ items) {
+  const int L = blockIdx.x * blockDim.x + threadIdx.x;
+  if (L >= nlist) return;
+  const int c = cnt[L];
+  const int64_t loff = list_off[L], len = list_off[L + 1] - loff;
+  if (c == 0 || len == 0) return;
+  const int nch = (c + qc - 1) / qc, npc = (int)((len + TC_RS - 1) / TC_RS);
+  const int i0 = istart[L], c0 = cstart[L];
+  for (int ch = 0; ch < nch; ++ch) {
+    for (int pc = 0; pc < npc; ++pc) {
+      TcItem it;
+      it.L = L;
+      it.nq = min(qc, c - ch * qc);
+      it.chunk = c0 + ch;
+      it.pad = 0;
+      it.loff = loff;
+      it.rbeg = (long long)pc * TC_RS;
+      it.rend = min(len, (int64_t)(pc + 1) * TC_RS);
+      items[i0 + ch * npc + pc] = it;
+    }
   }
 }
 
@@ -288,26 +297,41 @@ __global__ void k_tc_place(const int32_t* __restrict__ probes, int64_t nq, int P
                            const __half* __restrict__ q16, const float* __restrict__ qmul, int kp,
                            int qc, const int* __restrict__ cstart, int* __restrict__ cursor,
                            uint8_t* __restrict__ bimg, TcMeta* __restrict__ meta) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nq * P) return;
-  const int64_t row = i / P;
-  const int p = (int)(i - row * P);
-  const int np = nprobe_q ? min(max(nprobe_q[row], 1), P) : P;
-  if (p >= np || seg[i] < 0) return;
-  const int L = probes[i];
-  if (L < 0 || L >= nlist) return;
-  const int c = atomicAdd(&cursor[L], 1);
+  // 16 threads per pair: the group's first thread takes the column, each
+  // thread copies one 16-byte chunk of the query row (kp <= 128)
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i = gt >> 4;
+  const int cc = (int)(gt & 15);
+  const int lane = threadIdx.x & 31;
+  const unsigned gmask = 0xffffu << (lane & 16);
+  bool on = i < nq * P;
+  int64_t row = 0;
+  int L = -1;
+  if (on) {
+    row = i / P;
+    const int p = (int)(i - row * P);
+    const int np = nprobe_q ? min(max(nprobe_q[row], 1), P) : P;
+    L = probes[i];
+    on = p < np && seg[i] >= 0 && L >= 0 && L < nlist;
+  }
+  int c = 0;
+  if (on && cc == 0) c = atomicAdd(&cursor[L], 1);
+  c = __shfl_sync(gmask, c, lane & 16);
+  if (!on) return;
   const int64_t chunk = cstart[L] + c / qc;
   const int j = c % qc;
-  TcMeta m;
-  m.seg = seg[i];
-  m.term = term[i];
-  m.qmul = qmul[row];
-  meta[chunk * qc + j] = m;
-  uint8_t* img = bimg + chunk * ((int64_t)qc * kp * 2);
-  const uint4* src = reinterpret_cast<const uint4*>(q16 + row * kp);
-  for (int cc = 0; cc < (kp >> 3); ++cc)
-    *reinterpret_cast<uint4*>(img + (cc >> 3) * (qc * 128) + sw128(j, cc & 7)) = src[cc];
+  if (cc == 0) {
+    TcMeta m;
+    m.seg = seg[i];
+    m.term = term[i];
+    m.qmul = qmul[row];
+    meta[chunk * qc + j] = m;
+  }
+  if (cc < (kp >> 3)) {
+    uint8_t* img = bimg + chunk * ((int64_t)qc * kp * 2);
+    *reinterpret_cast<uint4*>(img + (cc >> 3) * (qc * 128) + sw128(j, cc & 7)) =
+        reinterpret_cast<const uint4*>(q16 + row * kp)[cc];
+  }
 }
 
 // excl[pos] = 1 when the exclusion filter names the id of CSR row pos.
@@ -324,6 +348,7 @@ __global__ void k_tc_excl(const uint32_t* __restrict__ ids, int64_t ntotal,
 constexpr int TC_CONSUMERS = 256;                 // warps 0-7
 constexpr int TC_THREADS = TC_CONSUMERS + 32;     // + warp 8, the producer
 constexpr int TC_STAGES = 4;                      // tiles of codes in flight
+constexpr int TC_NB = 4;                          // items in flight (query images), at most
 
 struct TcArgs {
   const TcItem* items;
@@ -337,21 +362,24 @@ struct TcArgs {
   uint32_t* dist;          // distance rows
   int* err;
   int M, dsub, d, kp, qc;
+  int nb;  // query-image buffers (2 .. TC_NB)
   long long wait_limit;
 };
 
 struct TcSmem {
-  int abytes, bbytes, mbytes, cbbytes, code_bytes, slot_bytes;
-  __host__ __device__ TcSmem(int kp, int qc, int d, int M)
-      : abytes(TC_BM * kp * 2), bbytes(qc * kp * 2), mbytes(qc * 16), cbbytes(d * 512),
+  int nb, abytes, bbytes, mbytes, cbbytes, code_bytes, slot_bytes;
+  __host__ __device__ TcSmem(int kp, int qc, int d, int M, int nb_)
+      : nb(nb_), abytes(TC_BM * kp * 2), bbytes(qc * kp * 2), mbytes(qc * 16), cbbytes(d * 512),
         code_bytes((TC_BM * M + 32 + 15) & ~15), slot_bytes(code_bytes + 544 + 160) {}
   __host__ __device__ int a_off(int b) const { return b * abytes; }
   __host__ __device__ int b_off(int b) const { return 2 * abytes + b * bbytes; }
-  __host__ __device__ int m_off(int b) const { return 2 * abytes + 2 * bbytes + b * mbytes; }
-  __host__ __device__ int cb_off() const { return 2 * abytes + 2 * bbytes + 2 * mbytes; }
+  __host__ __device__ int m_off(int b) const { return 2 * abytes + nb * bbytes + b * mbytes; }
+  __host__ __device__ int cb_off() const { return 2 * abytes + nb * bbytes + nb * mbytes; }
   __host__ __device__ int slot_off(int s) const { return cb_off() + cbbytes + s * slot_bytes; }
   __host__ __device__ int bars_off() const { return slot_off(TC_STAGES); }
-  __host__ __device__ size_t total() const { return 1024 + (size_t)bars_off() + 8 * (6 + 2 * TC_STAGES) + 16; }
+  __host__ __device__ size_t total() const {
+    return 1024 + (size_t)bars_off() + 8 * (2 * TC_NB + 2 + 2 * TC_STAGES) + 16;
+  }
 };
 
 // Barrier among the consumer warps (id 1, 256 threads) that also returns
@@ -384,28 +412,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                            ~uintptr_t(1023));
-  const TcSmem L(a.kp, a.qc, a.d, a.M);
+  const TcSmem L(a.kp, a.qc, a.d, a.M, a.nb);
   uint8_t* cb = sm + L.cb_off();
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + L.bars_off());
-  uint32_t* holder = reinterpret_cast<uint32_t*>(bars + 6 + 2 * TC_STAGES);
+  uint32_t* holder = reinterpret_cast<uint32_t*>(bars + 2 * TC_NB + 2 + 2 * TC_STAGES);
   __shared__ int s_err;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int qc = a.qc, kp = a.kp, M = a.M, dsub = a.dsub;
   const uint32_t bar0 = smem_u32(bars);
-  // bars: [0,1] B full, [2,3] B empty, [4,5] accumulator full,
-  // [6, 6+S) slot full, [6+S, 6+2S) slot empty
+  // bars: [0, NB) query image full, [NB, 2 NB) image empty, then two
+  // accumulator-full barriers, S slot-full and S slot-empty barriers
   auto b_full = [&](int b) { return bar0 + 8u * b; };
-  auto b_empty = [&](int b) { return bar0 + 8u * (2 + b); };
-  auto acc_full = [&](int b) { return bar0 + 8u * (4 + b); };
-  auto s_full = [&](int s) { return bar0 + 8u * (6 + s); };
-  auto s_empty = [&](int s) { return bar0 + 8u * (6 + TC_STAGES + s); };
+  auto b_empty = [&](int b) { return bar0 + 8u * (TC_NB + b); };
+  auto acc_full = [&](int b) { return bar0 + 8u * (2 * TC_NB + b); };
+  auto s_full = [&](int s) { return bar0 + 8u * (2 * TC_NB + 2 + s); };
+  auto s_empty = [&](int s) { return bar0 + 8u * (2 * TC_NB + 2 + TC_STAGES + s); };
+  const int nb = a.nb;
   if (tid == 0) {
     s_err = 0;
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < TC_NB; ++b) {
       mbar_init(b_full(b), 1);
       mbar_init(b_empty(b), TC_CONSUMERS);
-      mbar_init(acc_full(b), 1);
     }
+    for (int b = 0; b < 2; ++b) mbar_init(acc_full(b), 1);
     for (int s = 0; s < TC_STAGES; ++s) {
       mbar_init(s_full(s), 1);
       mbar_init(s_empty(s), TC_CONSUMERS);
@@ -430,10 +459,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
     // ---- producer ----
     if (lane == 0) {
       int g = 0, i = 0;
+      TcItem nrec;  // the next item's record, loaded one item ahead
+      if ((int)blockIdx.x < total) nrec = a.items[blockIdx.x];
       for (int it = blockIdx.x; it < total; it += gridDim.x, ++i) {
-        const TcItem rec = a.items[it];
-        const int ib = i & 1;
-        if (*verr || !mbar_wait(b_empty(ib), ((uint32_t)(i >> 1) & 1u) ^ 1u, a.wait_limit)) {
+        const TcItem rec = nrec;
+        if (it + (int)gridDim.x < total) nrec = a.items[it + gridDim.x];
+        const int ib = i % nb;
+        if (*verr || !mbar_wait(b_empty(ib), ((uint32_t)(i / nb) & 1u) ^ 1u, a.wait_limit)) {
           *verr = 1;
           break;
         }
@@ -485,8 +517,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
       // Unwind: every issued copy lands before the CTA may exit (full limit).
       for (int j = (g > TC_STAGES ? g - TC_STAGES : 0); j < g; ++j)
         if (!mbar_wait(s_full(j % TC_STAGES), (uint32_t)(j / TC_STAGES) & 1u)) *verr = 1;
-      for (int j = (i > 2 ? i - 2 : 0); j < i; ++j)
-        if (!mbar_wait(b_full(j & 1), (uint32_t)(j >> 1) & 1u)) *verr = 1;
+      for (int j = (i > nb ? i - nb : 0); j < i; ++j)
+        if (!mbar_wait(b_full(j % nb), (uint32_t)(j / nb) & 1u)) *verr = 1;
     }
   } else {
     // ---- consumers ----
@@ -521,10 +553,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
           for (int jj = 0; jj < 16; ++jj) {
             const int j = cg * 16 + jj;
             if (j < prev_nq) {
-              const float dd = fmaf(v[jj], mt[j].qmul, mt[j].term + prev_v);
+              const uint4 w = *reinterpret_cast<const uint4*>(mt + j);  // seg, term, qmul
+              const long long sg = (long long)(((uint64_t)w.y << 32) | w.x);
+              const float dd = fmaf(v[jj], __uint_as_float(w.w), __uint_as_float(w.z) + prev_v);
               uint32_t o = float_to_ordered(dd);
               o = o == TC_EXCLUDED ? TC_EXCLUDED - 1u : o;  // a NaN stays a candidate
-              a.dist[mt[j].seg + prev_row0 + r] = prev_ex ? TC_EXCLUDED : o;
+              a.dist[sg + prev_row0 + r] = prev_ex ? TC_EXCLUDED : o;
             }
           }
         }
@@ -537,10 +571,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
     for (int it = blockIdx.x; it < total && !stop; it += gridDim.x, ++i) {
       const TcItem rec = nrec;
       if (it + (int)gridDim.x < total) nrec = a.items[it + gridDim.x];
-      const int ib = i & 1;
+      const int ib = i % nb;
       const int nqi = rec.nq;
       const int npad = max(16, (nqi + 15) & ~15);
-      bool okb = !*verr && mbar_wait(b_full(ib), (uint32_t)(i >> 1) & 1u, a.wait_limit);
+      bool okb = !*verr && mbar_wait(b_full(ib), (uint32_t)(i / nb) & 1u, a.wait_limit);
       if (!okb) *verr = 1;
       for (long long row0 = rec.rbeg; row0 < rec.rend; row0 += TC_BM, ++g) {
         const int nr = (int)min((long long)TC_BM, rec.rend - row0);
@@ -1137,11 +1171,12 @@ void launch_ivfpq_scan_tc(const FastScanArgs& f, int64_t smax, int qc, void* scr
   k_tc_q16<<<gw, 256, 0, s>>>(f.q, nq, d, kp, scale * f.pq16_inv, q16, qmul);
   k_tc_pairs<<<gw, 256, 0, s>>>(f.probes, nq, P, f.nprobe_q, f.list_off, nlist, lay.smax4, seg,
                                 cnt, f.err);
-  k_tc_items<<<1, 1024, 0, s>>>(cnt, f.list_off, nlist, qc, start, cstart, istart, items);
-  k_tc_place<<<(unsigned)((nq * P + 255) / 256), 256, 0, s>>>(f.probes, nq, P, f.nprobe_q, nlist,
-                                                               seg, f.term, q16, qmul, kp, qc,
-                                                               cstart, cursor, bimg, meta);
-  for (int i = 0; i < 4; ++i) count_launch();
+  k_tc_items<<<1, 1024, 0, s>>>(cnt, f.list_off, nlist, qc, start, cstart, istart);
+  k_tc_fill<<<(unsigned)((nlist + 255) / 256), 256, 0, s>>>(cnt, f.list_off, nlist, qc, cstart,
+                                                            istart, items);
+  k_tc_place<<<(unsigned)((nq * P * 16 + 255) / 256), 256, 0, s>>>(
+      f.probes, nq, P, f.nprobe_q, nlist, seg, f.term, q16, qmul, kp, qc, cstart, cursor, bimg, meta);
+  for (int i = 0; i < 5; ++i) count_launch();
   if (f.filter) {
     k_tc_excl<<<(unsigned)((f.ntotal + 255) / 256), 256, 0, s>>>(f.ids, f.ntotal, f.filter,
                                                                   f.filter_len, excl);
@@ -1164,7 +1199,10 @@ void launch_ivfpq_scan_tc(const FastScanArgs& f, int64_t smax, int qc, void* scr
   t.kp = kp;
   t.qc = qc;
   t.wait_limit = wait_limit;
-  const size_t smem = TcSmem(kp, qc, d, M).total();
+  int nbuf = TC_NB;  // as many query images in flight as shared memory allows
+  while (nbuf > 2 && TcSmem(kp, qc, d, M, nbuf).total() > 227 * 1024) nbuf /= 2;
+  t.nb = nbuf;
+  const size_t smem = TcSmem(kp, qc, d, M, nbuf).total();
   MV_REQUIRE(smem <= 227 * 1024, MV_ERR_INTERNAL, "tensor-core ADC scan: shared memory");
   smem_limit(k_tc_scan, smem);
   k_tc_scan<<<(unsigned)num_sms, TC_THREADS, smem, s>>>(t);
