@@ -345,10 +345,15 @@ __global__ void k_tc_excl(const uint32_t* __restrict__ ids, int64_t ntotal,
 }
 
 // ---- the tensor-core scan -------------------------------------------------
-constexpr int TC_CONSUMERS = 256;                 // warps 0-7
-constexpr int TC_THREADS = TC_CONSUMERS + 32;     // + warp 8, the producer
-constexpr int TC_STAGES = 4;                      // tiles of codes in flight
-constexpr int TC_NB = 4;                          // items in flight (query images), at most
+// Warp roles of one CTA: 0-7 decode, 8-15 epilogue, 16 MMA (and TMEM
+// owner), 17 producer.
+constexpr int TC_DEC_WARPS = 8;
+constexpr int TC_EPI_WARPS = 8;
+constexpr int TC_MMA_WARP = 16;
+constexpr int TC_PROD_WARP = 17;
+constexpr int TC_THREADS = 18 * 32;
+constexpr int TC_STAGES = 5;  // tiles of codes in flight
+constexpr int TC_NB = 4;      // items in flight (query images), at most
 
 struct TcArgs {
   const TcItem* items;
@@ -377,37 +382,27 @@ struct TcSmem {
   __host__ __device__ int cb_off() const { return 2 * abytes + nb * bbytes + nb * mbytes; }
   __host__ __device__ int slot_off(int s) const { return cb_off() + cbbytes + s * slot_bytes; }
   __host__ __device__ int bars_off() const { return slot_off(TC_STAGES); }
-  __host__ __device__ size_t total() const {
-    return 1024 + (size_t)bars_off() + 8 * (2 * TC_NB + 2 + 2 * TC_STAGES) + 16;
-  }
+  static constexpr int kBars = 2 * TC_NB + 8 + 2 * TC_STAGES;
+  __host__ __device__ size_t total() const { return 1024 + (size_t)bars_off() + 8 * kBars + 16; }
 };
 
-// Barrier among the consumer warps (id 1, 256 threads) that also returns
-// whether any of them passed v != 0: one answer for every consumer.
-__device__ __forceinline__ bool consumers_sync_or(int v) {
-  uint32_t r;
-  asm volatile(
-      "{\n\t.reg .pred p, q;\n\t"
-      "setp.ne.s32 q, %1, 0;\n\t"
-      "bar.red.or.pred p, 1, 256, q;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(r)
-      : "r"(v)
-      : "memory");
-  return r != 0;
-}
-
 // Persistent: one CTA per SM walks the work items blockIdx.x, + gridDim.x,
-// ... Warp 8 (the producer, one lane) copies, with cp.async.bulk, each
-// item's query image and column data into B[item parity] and each 128-row
-// tile's codes, per-row terms and exclusion flags (16-byte aligned
-// supersets) into a ring of TC_STAGES slots. Warps 0-7 per tile: decode the
-// rows' codes into FP16 reconstructions in A[tile parity] (thread r of a
-// TMEM lane quarter owns row r, the two warps of a quarter split the
-// subspaces), one thread issues the d / 16 MMAs into accumulator (tile
-// parity), and then all run the epilogue of the PREVIOUS tile, whose MMAs
-// overlapped this tile's decode: distance = term + vterm + qmul * acc, one
-// 128-byte store per warp and query column.
+// ... and every role walks the same items and 128-row tiles in the same
+// order, handing them on through mbarriers:
+//   producer  cp.async.bulk of each item's query image and column data into
+//             B[item % nb] and of each tile's codes, per-row terms and
+//             exclusion flags (16-byte aligned supersets) into slot
+//             (tile % S);
+//   decode    (two threads per row, each half of the subspaces) the FP16
+//             reconstructions of the tile's rows into A[tile & 1];
+//   MMA       d / 16 tcgen05.mma into accumulator (tile & 1), committed to
+//             the epilogue and back to the decoders;
+//   epilogue  (a row per thread, half of the query columns per warp)
+//             distance = term + vterm + qmul * acc, one 128-byte store per
+//             warp and column.
+// Decode, MMA and epilogue of consecutive tiles overlap. Every wait is
+// bounded; on expiry the role stops, the others stop at their next wait,
+// issued copies and MMAs retire before the CTA frees TMEM and exits.
 __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -415,33 +410,38 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
   const TcSmem L(a.kp, a.qc, a.d, a.M, a.nb);
   uint8_t* cb = sm + L.cb_off();
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + L.bars_off());
-  uint32_t* holder = reinterpret_cast<uint32_t*>(bars + 2 * TC_NB + 2 + 2 * TC_STAGES);
+  uint32_t* holder = reinterpret_cast<uint32_t*>(bars + TcSmem::kBars);
   __shared__ int s_err;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int qc = a.qc, kp = a.kp, M = a.M, dsub = a.dsub;
+  const int qc = a.qc, kp = a.kp, M = a.M, dsub = a.dsub, nb = a.nb;
   const uint32_t bar0 = smem_u32(bars);
-  // bars: [0, NB) query image full, [NB, 2 NB) image empty, then two
-  // accumulator-full barriers, S slot-full and S slot-empty barriers
   auto b_full = [&](int b) { return bar0 + 8u * b; };
   auto b_empty = [&](int b) { return bar0 + 8u * (TC_NB + b); };
-  auto acc_full = [&](int b) { return bar0 + 8u * (2 * TC_NB + b); };
-  auto s_full = [&](int s) { return bar0 + 8u * (2 * TC_NB + 2 + s); };
-  auto s_empty = [&](int s) { return bar0 + 8u * (2 * TC_NB + 2 + TC_STAGES + s); };
-  const int nb = a.nb;
+  auto a_full = [&](int b) { return bar0 + 8u * (2 * TC_NB + b); };
+  auto a_empty = [&](int b) { return bar0 + 8u * (2 * TC_NB + 2 + b); };
+  auto acc_full = [&](int b) { return bar0 + 8u * (2 * TC_NB + 4 + b); };
+  auto acc_empty = [&](int b) { return bar0 + 8u * (2 * TC_NB + 6 + b); };
+  auto s_full = [&](int s) { return bar0 + 8u * (2 * TC_NB + 8 + s); };
+  auto s_empty = [&](int s) { return bar0 + 8u * (2 * TC_NB + 8 + TC_STAGES + s); };
   if (tid == 0) {
     s_err = 0;
     for (int b = 0; b < TC_NB; ++b) {
       mbar_init(b_full(b), 1);
-      mbar_init(b_empty(b), TC_CONSUMERS);
+      mbar_init(b_empty(b), TC_EPI_WARPS);
     }
-    for (int b = 0; b < 2; ++b) mbar_init(acc_full(b), 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(a_full(b), TC_DEC_WARPS);
+      mbar_init(a_empty(b), 1);
+      mbar_init(acc_full(b), 1);
+      mbar_init(acc_empty(b), TC_EPI_WARPS);
+    }
     for (int s = 0; s < TC_STAGES; ++s) {
       mbar_init(s_full(s), 1);
-      mbar_init(s_empty(s), TC_CONSUMERS);
+      mbar_init(s_empty(s), TC_DEC_WARPS + TC_EPI_WARPS);
     }
     fence_mbar_init();
   }
-  if (warp == 0) tmem_alloc(smem_u32(holder), 2 * qc);
+  if (warp == TC_MMA_WARP) tmem_alloc(smem_u32(holder), 2 * qc);
   {  // the codebook, once per CTA
     const uint4* src = reinterpret_cast<const uint4*>(a.pq16);
     uint4* dst = reinterpret_cast<uint4*>(cb);
@@ -454,21 +454,30 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
   volatile int* verr = &s_err;
   const int total = *a.total_items;
   const int nkb = kp >> 6;
+  const long long lim = a.wait_limit;
+  auto wait = [&](uint32_t bar, uint32_t parity) {
+    if (*verr) return false;
+    if (mbar_wait(bar, parity, lim)) return true;
+    *verr = 1;
+    return false;
+  };
+  // the record of item it, one item ahead
+  TcItem nrec;
+  if ((int)blockIdx.x < total) nrec = a.items[blockIdx.x];
+  auto next_item = [&](int it) {
+    const TcItem rec = nrec;
+    if (it + (int)gridDim.x < total) nrec = a.items[it + gridDim.x];
+    return rec;
+  };
 
-  if (warp == TC_CONSUMERS / 32) {
-    // ---- producer ----
+  if (warp == TC_PROD_WARP) {
     if (lane == 0) {
       int g = 0, i = 0;
-      TcItem nrec;  // the next item's record, loaded one item ahead
-      if ((int)blockIdx.x < total) nrec = a.items[blockIdx.x];
-      for (int it = blockIdx.x; it < total; it += gridDim.x, ++i) {
-        const TcItem rec = nrec;
-        if (it + (int)gridDim.x < total) nrec = a.items[it + gridDim.x];
+      bool ok = true;
+      for (int it = blockIdx.x; it < total && ok; it += gridDim.x, ++i) {
+        const TcItem rec = next_item(it);
         const int ib = i % nb;
-        if (*verr || !mbar_wait(b_empty(ib), ((uint32_t)(i / nb) & 1u) ^ 1u, a.wait_limit)) {
-          *verr = 1;
-          break;
-        }
+        if (!wait(b_empty(ib), ((uint32_t)(i / nb) & 1u) ^ 1u)) break;
         const int npad = max(16, (rec.nq + 15) & ~15);
         mbar_arrive_expect_tx(b_full(ib), (uint32_t)(nkb * npad * 128 + npad * 16));
         const uint8_t* img = a.bimg + (int64_t)rec.chunk * ((int64_t)qc * kp * 2);
@@ -477,11 +486,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
                     (uint32_t)(npad * 128), b_full(ib));
         bulk_load(smem_u32(sm + L.m_off(ib)), a.meta + (int64_t)rec.chunk * qc, (uint32_t)(npad * 16),
                   b_full(ib));
-        bool ok = true;
         for (long long row0 = rec.rbeg; row0 < rec.rend; row0 += TC_BM, ++g) {
           const int s = g % TC_STAGES;
-          if (*verr || !mbar_wait(s_empty(s), ((uint32_t)(g / TC_STAGES) & 1u) ^ 1u, a.wait_limit)) {
-            *verr = 1;
+          if (!wait(s_empty(s), ((uint32_t)(g / TC_STAGES) & 1u) ^ 1u)) {
             ok = false;
             break;
           }
@@ -509,10 +516,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
           if (a.excl)
             bulk_load(smem_u32(slot + L.code_bytes + 544), a.excl + e0, (uint32_t)(e1 - e0), s_full(s));
         }
-        if (!ok) {
-          ++i;
-          break;
-        }
       }
       // Unwind: every issued copy lands before the CTA may exit (full limit).
       for (int j = (g > TC_STAGES ? g - TC_STAGES : 0); j < g; ++j)
@@ -520,76 +523,64 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
       for (int j = (i > nb ? i - nb : 0); j < i; ++j)
         if (!mbar_wait(b_full(j % nb), (uint32_t)(j / nb) & 1u)) *verr = 1;
     }
-  } else {
-    // ---- consumers ----
-    const int lq = warp & 3, half = warp >> 2;
-    const int r = lq * 32 + lane;  // this thread's tile row (decode and epilogue)
-    const int msplit = M >> 1;
-    const int m0 = half * msplit;
-    bool have_prev = false, prev_last = false;
-    int prev_g = 0, prev_ib = 0, prev_nq = 0, prev_nr = 0, prev_npad = 16;
-    long long prev_row0 = 0;
-    float prev_v = 0.0f;
-    bool prev_ex = false;
-    int g = 0, i = 0;
-    int last_commit = -1;  // thread 0: the last committed tile
-    bool stop = false;
-
-    auto epilogue = [&]() {
-      const int buf = prev_g & 1;
-      bool ok = !*verr && mbar_wait(acc_full(buf), (uint32_t)(prev_g >> 1) & 1u, a.wait_limit);
-      if (!__all_sync(0xffffffffu, ok)) {
-        *verr = 1;
-        return;
-      }
-      tc_fence_after();
-      const TcMeta* mt = reinterpret_cast<const TcMeta*>(sm + L.m_off(prev_ib));
-      const bool row_ok = r < prev_nr;
-      for (int cg = half; cg * 16 < prev_npad; cg += 2) {
-        float v[16];
-        tmem_ld16(tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(buf * qc + cg * 16), v);
-        if (row_ok) {
-#pragma unroll
-          for (int jj = 0; jj < 16; ++jj) {
-            const int j = cg * 16 + jj;
-            if (j < prev_nq) {
-              const uint4 w = *reinterpret_cast<const uint4*>(mt + j);  // seg, term, qmul
-              const long long sg = (long long)(((uint64_t)w.y << 32) | w.x);
-              const float dd = fmaf(v[jj], __uint_as_float(w.w), __uint_as_float(w.z) + prev_v);
-              uint32_t o = float_to_ordered(dd);
-              o = o == TC_EXCLUDED ? TC_EXCLUDED - 1u : o;  // a NaN stays a candidate
-              a.dist[sg + prev_row0 + r] = prev_ex ? TC_EXCLUDED : o;
-            }
+  } else if (warp == TC_MMA_WARP) {
+    if (lane == 0) {
+      int g = 0, i = 0, last_commit = -1;
+      bool ok = true;
+      for (int it = blockIdx.x; it < total && ok; it += gridDim.x, ++i) {
+        const TcItem rec = next_item(it);
+        const int ib = i % nb;
+        if (!wait(b_full(ib), (uint32_t)(i / nb) & 1u)) break;
+        const int npad = max(16, (rec.nq + 15) & ~15);
+        const uint32_t idesc = idesc_f16_f32(TC_BM, npad);
+        const uint32_t bbase = smem_u32(sm + L.b_off(ib));
+        for (long long row0 = rec.rbeg; row0 < rec.rend; row0 += TC_BM, ++g) {
+          const int buf = g & 1;
+          const uint32_t ph = (uint32_t)(g >> 1) & 1u;
+          if (!wait(a_full(buf), ph) || !wait(acc_empty(buf), ph ^ 1u)) {
+            ok = false;
+            break;
           }
+          tc_fence_after();
+          const uint32_t dt = tmem + (uint32_t)(buf * qc);
+          const uint32_t abase = smem_u32(sm + L.a_off(buf));
+          const int ks = a.d >> 4;
+          for (int k = 0; k < ks; ++k) {
+            const int kb = k >> 2, kk = k & 3;
+            const uint64_t ad = desc_k_sw128(abase + kb * (TC_BM * 128)) + 2u * kk;
+            const uint64_t bd = desc_k_sw128(bbase + kb * (qc * 128)) + 2u * kk;
+            umma_f16(dt, ad, bd, idesc, k > 0 ? 1u : 0u);
+          }
+          umma_commit(acc_full(buf));
+          umma_commit(a_empty(buf));
+          last_commit = g;
         }
       }
-      tc_fence_before();
-    };
-
-    TcItem nrec;  // the next item's record, loaded one item ahead
-    if ((int)blockIdx.x < total) nrec = a.items[blockIdx.x];
-    for (int it = blockIdx.x; it < total && !stop; it += gridDim.x, ++i) {
-      const TcItem rec = nrec;
-      if (it + (int)gridDim.x < total) nrec = a.items[it + gridDim.x];
-      const int ib = i % nb;
-      const int nqi = rec.nq;
-      const int npad = max(16, (nqi + 15) & ~15);
-      bool okb = !*verr && mbar_wait(b_full(ib), (uint32_t)(i / nb) & 1u, a.wait_limit);
-      if (!okb) *verr = 1;
+      // Unwind: the issued MMAs retire before TMEM is freed (full limit).
+      if (last_commit >= 0 &&
+          !mbar_wait(acc_full(last_commit & 1), (uint32_t)(last_commit >> 1) & 1u))
+        *verr = 1;
+    }
+  } else if (warp < TC_DEC_WARPS) {
+    // ---- decode: thread (quarter, lane) owns row r, half of the subspaces
+    const int r = (warp & 3) * 32 + lane;
+    const int msplit = M >> 1, m0 = (warp >> 2) * msplit;
+    int g = 0;
+    bool ok = true;
+    for (int it = blockIdx.x; it < total && ok; it += gridDim.x) {
+      const TcItem rec = next_item(it);
       for (long long row0 = rec.rbeg; row0 < rec.rend; row0 += TC_BM, ++g) {
+        const int s = g % TC_STAGES, buf = g & 1;
+        if (!wait(s_full(s), (uint32_t)(g / TC_STAGES) & 1u) ||
+            !wait(a_empty(buf), ((uint32_t)(g >> 1) & 1u) ^ 1u)) {
+          ok = false;
+          break;
+        }
         const int nr = (int)min((long long)TC_BM, rec.rend - row0);
-        const int s = g % TC_STAGES;
-        const int buf = g & 1;
-        uint8_t* A = sm + L.a_off(buf);
-        float cur_v = 0.0f;
-        bool cur_ex = false;
-        bool oks = okb && !*verr && mbar_wait(s_full(s), (uint32_t)(g / TC_STAGES) & 1u, a.wait_limit);
-        if (!oks) *verr = 1;
-        if (oks && r < nr) {
-          const uint8_t* slot = sm + L.slot_off(s);
+        if (r < nr) {
+          uint8_t* A = sm + L.a_off(buf);
           const long long pos = rec.loff + row0;
-          const int dc = (int)((pos * M) & 15), dv = (int)((pos * 4) & 15), de = (int)(pos & 15);
-          const uint8_t* crow = slot + dc + r * M + m0;
+          const uint8_t* crow = sm + L.slot_off(s) + (int)((pos * M) & 15) + r * M + m0;
           for (int w0 = 0; w0 < msplit; w0 += 4) {
             const uint32_t word = *reinterpret_cast<const uint32_t*>(crow + w0);
 #pragma unroll
@@ -606,54 +597,80 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
               }
             }
           }
-          if (a.vterm) cur_v = *reinterpret_cast<const float*>(slot + L.code_bytes + dv + r * 4);
-          if (a.excl) cur_ex = slot[L.code_bytes + 544 + de + r] != 0;
         }
-        mbar_arrive(s_empty(s));
         fence_proxy_async();
-        if (consumers_sync_or(*verr)) {  // one answer for every consumer
-          stop = true;
-          break;
+        __syncwarp();
+        if (lane == 0) {
+          mbar_arrive(a_full(buf));
+          mbar_arrive(s_empty(s));
         }
-        if (tid == 0) {
-          tc_fence_after();
-          const uint32_t dt = tmem + (uint32_t)(buf * qc);
-          const uint32_t idesc = idesc_f16_f32(TC_BM, npad);
-          const uint32_t abase = smem_u32(A), bbase = smem_u32(sm + L.b_off(ib));
-          const int ks = a.d >> 4;
-          for (int k = 0; k < ks; ++k) {
-            const int kb = k >> 2, kk = k & 3;
-            const uint64_t ad = desc_k_sw128(abase + kb * (TC_BM * 128)) + 2u * kk;
-            const uint64_t bd = desc_k_sw128(bbase + kb * (qc * 128)) + 2u * kk;
-            umma_f16(dt, ad, bd, idesc, k > 0 ? 1u : 0u);
-          }
-          umma_commit(acc_full(buf));
-          last_commit = g;
-        }
-        if (have_prev) {
-          epilogue();
-          if (prev_last) mbar_arrive(b_empty(prev_ib));
-        }
-        have_prev = true;
-        prev_last = row0 + TC_BM >= rec.rend;
-        prev_g = g;
-        prev_ib = ib;
-        prev_nq = nqi;
-        prev_nr = nr;
-        prev_npad = npad;
-        prev_row0 = row0;
-        prev_v = cur_v;
-        prev_ex = cur_ex;
       }
     }
-    if (have_prev && !*verr) epilogue();
-    // Unwind: the last issued MMAs retire before TMEM is freed (full limit).
-    if (tid == 0 && last_commit >= 0) {
-      if (!mbar_wait(acc_full(last_commit & 1), (uint32_t)(last_commit >> 1) & 1u)) *verr = 1;
+  } else {
+    // ---- epilogue: thread (quarter, lane) owns row r, warp half h takes
+    // the column groups h, h + 2, ...
+    const int ew = warp - TC_DEC_WARPS;
+    const int lq = ew & 3, half = ew >> 2;  // warp % 4 == lq: this warp's TMEM lanes
+    const int r = lq * 32 + lane;
+    int g = 0, i = 0;
+    bool ok = true;
+    for (int it = blockIdx.x; it < total && ok; it += gridDim.x, ++i) {
+      const TcItem rec = next_item(it);
+      const int ib = i % nb;
+      if (!wait(b_full(ib), (uint32_t)(i / nb) & 1u)) break;
+      const int nqi = rec.nq, npad = max(16, (nqi + 15) & ~15);
+      const TcMeta* mt = reinterpret_cast<const TcMeta*>(sm + L.m_off(ib));
+      for (long long row0 = rec.rbeg; row0 < rec.rend; row0 += TC_BM, ++g) {
+        const int s = g % TC_STAGES, buf = g & 1;
+        if (!wait(s_full(s), (uint32_t)(g / TC_STAGES) & 1u) ||
+            !wait(acc_full(buf), (uint32_t)(g >> 1) & 1u)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const int nr = (int)min((long long)TC_BM, rec.rend - row0);
+        const long long pos = rec.loff + row0;
+        const uint8_t* slot = sm + L.slot_off(s);
+        const bool row_ok = r < nr;
+        float vr = 0.0f;
+        bool ex = false;
+        if (row_ok && a.vterm)
+          vr = *reinterpret_cast<const float*>(slot + L.code_bytes + (int)((pos * 4) & 15) + r * 4);
+        if (row_ok && a.excl) ex = slot[L.code_bytes + 544 + (int)(pos & 15) + r] != 0;
+        for (int cg = half; cg * 16 < npad; cg += 2) {
+          // lane jj < 16 holds column cg * 16 + jj's data; broadcast by shuffles
+          uint4 mw = make_uint4(0u, 0u, 0u, 0u);
+          if (lane < 16 && cg * 16 + lane < nqi) mw = *reinterpret_cast<const uint4*>(mt + cg * 16 + lane);
+          float v[16];
+          tmem_ld16(tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(buf * qc + cg * 16), v);
+#pragma unroll
+          for (int jj = 0; jj < 16; ++jj) {
+            if (cg * 16 + jj < nqi) {  // the same for every lane
+              const uint32_t slo = __shfl_sync(0xffffffffu, mw.x, jj);
+              const uint32_t shi = __shfl_sync(0xffffffffu, mw.y, jj);
+              const float tq = __uint_as_float(__shfl_sync(0xffffffffu, mw.z, jj));
+              const float mq = __uint_as_float(__shfl_sync(0xffffffffu, mw.w, jj));
+              if (row_ok) {
+                uint32_t o = float_to_ordered(fmaf(v[jj], mq, tq + vr));
+                o = o == TC_EXCLUDED ? TC_EXCLUDED - 1u : o;  // a NaN stays a candidate
+                const long long sg = (long long)(((uint64_t)shi << 32) | slo);
+                a.dist[sg + row0 + r] = ex ? TC_EXCLUDED : o;
+              }
+            }
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) {
+          mbar_arrive(acc_empty(buf));
+          mbar_arrive(s_empty(s));
+          if (row0 + TC_BM >= rec.rend) mbar_arrive(b_empty(ib));
+        }
+      }
     }
   }
   __syncthreads();
-  if (warp == 0) {
+  if (warp == TC_MMA_WARP) {
     tc_fence_after();
     tmem_dealloc(tmem, 2 * qc);
   }
