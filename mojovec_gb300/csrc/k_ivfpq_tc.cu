@@ -404,9 +404,10 @@ struct TcSmem {
 // bounded; on expiry the role stops, the others stop at their next wait,
 // issued copies and MMAs retire before the CTA frees TMEM and exits.
 __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
-                                           ~uintptr_t(1023));
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  // 1024-byte aligned, and kept a pointer into the shared array (not an
+  // integer round trip) so that every access compiles to a shared-memory one
+  uint8_t* sm = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   const TcSmem L(a.kp, a.qc, a.d, a.M, a.nb);
   uint8_t* cb = sm + L.cb_off();
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + L.bars_off());
@@ -638,23 +639,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
           vr = *reinterpret_cast<const float*>(slot + L.code_bytes + (int)((pos * 4) & 15) + r * 4);
         if (row_ok && a.excl) ex = slot[L.code_bytes + 544 + (int)(pos & 15) + r] != 0;
         for (int cg = half; cg * 16 < npad; cg += 2) {
-          // lane jj < 16 holds column cg * 16 + jj's data; broadcast by shuffles
-          uint4 mw = make_uint4(0u, 0u, 0u, 0u);
-          if (lane < 16 && cg * 16 + lane < nqi) mw = *reinterpret_cast<const uint4*>(mt + cg * 16 + lane);
           float v[16];
           tmem_ld16(tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(buf * qc + cg * 16), v);
+          if (row_ok) {
+            uint32_t* drow = a.dist + row0 + r;
 #pragma unroll
-          for (int jj = 0; jj < 16; ++jj) {
-            if (cg * 16 + jj < nqi) {  // the same for every lane
-              const uint32_t slo = __shfl_sync(0xffffffffu, mw.x, jj);
-              const uint32_t shi = __shfl_sync(0xffffffffu, mw.y, jj);
-              const float tq = __uint_as_float(__shfl_sync(0xffffffffu, mw.z, jj));
-              const float mq = __uint_as_float(__shfl_sync(0xffffffffu, mw.w, jj));
-              if (row_ok) {
-                uint32_t o = float_to_ordered(fmaf(v[jj], mq, tq + vr));
+            for (int jj = 0; jj < 16; ++jj) {
+              if (cg * 16 + jj < nqi) {
+                const TcMeta m = mt[cg * 16 + jj];  // one broadcast shared load per column
+                uint32_t o = float_to_ordered(fmaf(v[jj], m.qmul, m.term + vr));
                 o = o == TC_EXCLUDED ? TC_EXCLUDED - 1u : o;  // a NaN stays a candidate
-                const long long sg = (long long)(((uint64_t)shi << 32) | slo);
-                a.dist[sg + row0 + r] = ex ? TC_EXCLUDED : o;
+                drow[m.seg] = ex ? TC_EXCLUDED : o;
               }
             }
           }
