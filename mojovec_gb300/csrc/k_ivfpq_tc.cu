@@ -403,6 +403,7 @@ struct TcSmem {
 // Decode, MMA and epilogue of consecutive tiles overlap. Every wait is
 // bounded; on expiry the role stops, the others stop at their next wait,
 // issued copies and MMAs retire before the CTA frees TMEM and exits.
+template <int DSUB>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   // 1024-byte aligned, and kept a pointer into the shared array (not an
@@ -414,7 +415,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
   uint32_t* holder = reinterpret_cast<uint32_t*>(bars + TcSmem::kBars);
   __shared__ int s_err;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int qc = a.qc, kp = a.kp, M = a.M, dsub = a.dsub, nb = a.nb;
+  const int qc = a.qc, kp = a.kp, M = a.M, nb = a.nb;
   const uint32_t bar0 = smem_u32(bars);
   auto b_full = [&](int b) { return bar0 + 8u * b; };
   auto b_empty = [&](int b) { return bar0 + 8u * (TC_NB + b); };
@@ -588,7 +589,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
             for (int b = 0; b < 4; ++b) {
               const int m = m0 + w0 + b;
               const uint32_t code = (word >> (8 * b)) & 255u;
-              if (dsub == 8) {
+              if (DSUB == 8) {
                 const uint4 cw = *reinterpret_cast<const uint4*>(cb + ((m << 8) + code) * 16);
                 *reinterpret_cast<uint4*>(A + (m >> 3) * (TC_BM * 128) + sw128(r, m & 7)) = cw;
               } else {  // dsub 4: half a chunk per subspace
@@ -641,17 +642,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_scan(TcArgs a) {
         for (int cg = half; cg * 16 < npad; cg += 2) {
           float v[16];
           tmem_ld16(tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(buf * qc + cg * 16), v);
-          if (row_ok) {
-            uint32_t* drow = a.dist + row0 + r;
+          // Straight-line over the 16 columns (the loads of padding columns
+          // read the image's unused entries; only their stores are off), so
+          // the columns' load-compute-store chains interleave.
+          uint32_t* drow = a.dist + row0 + r;
+          const int jmax = row_ok ? nqi - cg * 16 : 0;
 #pragma unroll
-            for (int jj = 0; jj < 16; ++jj) {
-              if (cg * 16 + jj < nqi) {
-                const TcMeta m = mt[cg * 16 + jj];  // one broadcast shared load per column
-                uint32_t o = float_to_ordered(fmaf(v[jj], m.qmul, m.term + vr));
-                o = o == TC_EXCLUDED ? TC_EXCLUDED - 1u : o;  // a NaN stays a candidate
-                drow[m.seg] = ex ? TC_EXCLUDED : o;
-              }
-            }
+          for (int jj = 0; jj < 16; ++jj) {
+            const TcMeta m = mt[cg * 16 + jj];  // one broadcast shared load per column
+            uint32_t o = float_to_ordered(fmaf(v[jj], m.qmul, m.term + vr));
+            o = o == TC_EXCLUDED ? TC_EXCLUDED - 1u : o;  // a NaN stays a candidate
+            if (jj < jmax) drow[m.seg] = ex ? TC_EXCLUDED : o;
           }
         }
         tc_fence_before();
@@ -1216,8 +1217,13 @@ void launch_ivfpq_scan_tc(const FastScanArgs& f, int64_t smax, int qc, void* scr
   t.nb = nbuf;
   const size_t smem = TcSmem(kp, qc, d, M, nbuf).total();
   MV_REQUIRE(smem <= 227 * 1024, MV_ERR_INTERNAL, "tensor-core ADC scan: shared memory");
-  smem_limit(k_tc_scan, smem);
-  k_tc_scan<<<(unsigned)num_sms, TC_THREADS, smem, s>>>(t);
+  if (t.dsub == 8) {
+    smem_limit(k_tc_scan<8>, smem);
+    k_tc_scan<8><<<(unsigned)num_sms, TC_THREADS, smem, s>>>(t);
+  } else {
+    smem_limit(k_tc_scan<4>, smem);
+    k_tc_scan<4><<<(unsigned)num_sms, TC_THREADS, smem, s>>>(t);
+  }
   count_launch();
   SelArgs sa;
   sa.dist = dist;
