@@ -396,10 +396,13 @@ def run_gpu(args, rank, world):
     achieved = code_bytes / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
     fast_form = args.form in ("fast", "batched")
     workload = f"ivfpq_{nb}x128_nlist4096_M16_nq{nq}_k10"
+    # the fast scan's kernel: the bank-rotated table scan unless a variant is named
+    scan_kernel = ("k_ivfpq_scan_rt" if args.lut == 6 else "k_ivfpq_scan_fast") \
+        if fast_form else "k_ivfpq_scan_plain"
     traffic = None  # DRAM bytes per launch from the committed ncu capture of this config
     try:
         t = json.load(open(os.path.join(ROOT, "profiles", "dram_traffic.json"))).get(
-            "k_ivfpq_scan_fast", {})
+            scan_kernel, {})
         if fast_form and t.get("workload") == workload and t.get("nprobe") == nprobe:
             traffic = int(t["dram_bytes_per_launch"])
     except (OSError, ValueError, KeyError):
@@ -421,7 +424,8 @@ def run_gpu(args, rank, world):
         "config": {
             "workload": workload,
             "form": ("fast: two-pass BF16 tcgen05 coarse GEMM + FP32 recheck, per-query table from the "
-                     "FP16 codebook (codes read from L2), histogram select, certified rerank (the full FP32 rerank's results)"
+                     "FP16 codebook (codes read from L2), histogram select, certified rerank from an "
+                     "8-bit row copy (the full FP32 rerank's results)"
                      + ("; batched: one plan (persistent scan, tuned launch shapes) replayed as a "
                         "CUDA graph" if batched else ""))
                     if fast_form else "plain FP32 (reference algorithm, bit-exact)",
@@ -447,7 +451,7 @@ def run_gpu(args, rank, world):
         "gpu_launches": int(launches),
         "roofline": {
             "bound": "hbm",
-            "kernel": "k_ivfpq_scan_fast" if fast_form else "k_ivfpq_scan_plain",
+            "kernel": scan_kernel,
             "achieved": round(achieved, 1),
             "peak": hbm_peak,
             "peak_source": peak_src,
@@ -1578,7 +1582,8 @@ def main():
     ap.add_argument("--form", default="fast", choices=["plain", "fast", "batched"])
     ap.add_argument("--nprobe", type=int, default=8)
     ap.add_argument("--lut", type=int, default=None,
-                    help="ivfpq workload: fast-form scan variant (5 = list-major tensor-core scan)")
+                    help="ivfpq workload: fast-form scan variant (default FP32 tables; 6 = bank-rotated "
+                         "fixed-point tables with per-candidate slots)")
     ap.add_argument("--rerank", type=int, default=None,
                     help="shortlist depth (IVF-PQ default 256, flat default k * 4)")
     ap.add_argument("--nb", type=int, default=NB, help="base rows (profiling runs use fewer)")

@@ -1001,114 +1001,156 @@ __global__ void __launch_bounds__(FT) k_rerank_fast(RerankArgs a) {
 }
 
 // Certified rerank (k <= 32), one warp per query. Every shortlisted row's
-// distance is first computed from its BF16 copy (half the bytes; 32 rows
-// per warp in flight, lane-owned partial sums reduced by a transposing
-// butterfly) and turned into an interval that provably holds the FP32
-// distance the exact pass computes: the BF16 value's own summation error,
-// the triangle inequality with the row's rounding radius r >=
-// ||y - bf16(y)|| (L2), or Cauchy-Schwarz with ||q|| and ||bf16(y)|| (IP),
-// and the exact pass's summation error (both bounded by
-// gamma = (d + 64) * 2^-24 relative to the sum of |terms|), with 2^-20 of
-// slack for the bound arithmetic. The k-th smallest upper end of any group
-// of candidates bounds the query's k-th smallest key; a candidate whose
-// lower end exceeds it has k candidates strictly closer and is dropped. The
-// survivors are computed in FP32 with k_rerank_fast's arithmetic, so the
-// results are the ones the full FP32 pass gives.
-constexpr int RC_WARPS = 8;
-__global__ void __launch_bounds__(RC_WARPS * 32, 2) k_rerank_cert(RerankArgs a) {
+// distance is first computed from its 8-bit copy (a quarter of the FP32
+// bytes, one 128-byte line per row at d = 128) and turned into an interval
+// that provably holds the FP32 distance the exact pass computes. With y8 the
+// row the copy decodes to (y8_j = fmaf(s_j, 2^23 + u_j, a'_j), the FP32
+// expression the copy was made with) and r >= ||y - y8||: the prescreen
+// value's own summation error, the triangle inequality with r (L2) or
+// Cauchy-Schwarz with ||q|| and ||y8|| (IP), and the exact pass's summation
+// error (both bounded by gamma = (d + 64) * 2^-24 relative to the sum of
+// |terms|), with 2^-20 of slack for the bound arithmetic. The k-th smallest
+// upper end of any group of candidates bounds the query's k-th smallest
+// key; a candidate whose lower end exceeds it has k candidates strictly
+// closer and is dropped. The survivors are computed in FP32 with
+// k_rerank_fast's arithmetic, so the results are the ones the full FP32
+// pass gives.
+//
+// The 8-bit rows are gathered 32 at a time into a two-round ring in shared
+// memory with asynchronous 16-byte copies: round i + 2's copies are issued
+// as soon as round i is decoded, so every warp keeps two rounds of row
+// bytes in flight. Decoding reads one 4-byte word of every row per lane
+// (bank-conflict free), and a transposing butterfly gives lane l row l's sum.
+constexpr int RC_ROWS = 32;
+
+__host__ __device__ constexpr size_t rerank_cert_warp_bytes(int d, int R) {
+  // query | 2 x 32 rows of d8 bytes | survivors' keys (R) | lower ends |
+  // positions | upper ends / survivor list
+  return ((((size_t)d * 4 + 15) & ~size_t(15)) + 2 * RC_ROWS * (size_t)(((d + 15) & ~15)) +
+          (size_t)R * 20 + 15) & ~size_t(15);
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+__global__ void __launch_bounds__(128, 4) k_rerank_cert(RerankArgs a) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int d = a.d;
+  const int d = a.d, d8 = a.d8;
+  const int nwarps = blockDim.x >> 5;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t row = (int64_t)blockIdx.x * RC_WARPS + warp;
+  const int64_t row = (int64_t)blockIdx.x * nwarps + warp;
   if (row >= a.nq) return;  // warps are independent: no block-wide barrier below
   const size_t qbytes = ((size_t)d * 4 + 15) & ~size_t(15);
-  unsigned char* base = smraw + (size_t)warp * (qbytes + (size_t)a.R * 24);
+  unsigned char* base = smraw + (size_t)warp * rerank_cert_warp_bytes(d, a.R);
   float* qv = reinterpret_cast<float*>(base);
-  uint64_t* sk = reinterpret_cast<uint64_t*>(base + qbytes);  // R: survivors' keys
-  float* blo = reinterpret_cast<float*>(sk + a.R);             // R lower ends
-  uint32_t* spos = reinterpret_cast<uint32_t*>(blo + a.R);     // R positions
-  uint32_t* sid = spos + a.R;                                  // R ids
-  int* slist = reinterpret_cast<int*>(sid + a.R);              // R survivors
+  unsigned char* ring = base + qbytes;                       // 2 x RC_ROWS rows of d8 bytes
+  const size_t rbytes = (size_t)RC_ROWS * d8;
+  uint64_t* sk = reinterpret_cast<uint64_t*>(ring + 2 * rbytes);  // R: survivors' keys
+  float* blo = reinterpret_cast<float*>(sk + a.R);                // R lower ends
+  uint32_t* spos = reinterpret_cast<uint32_t*>(blo + a.R);        // R positions
+  uint32_t* bhi = spos + a.R;                                     // R upper ends (ordered)
+  int* slist = reinterpret_cast<int*>(bhi);                       // R survivors (after bhi)
   const float INF = __int_as_float(0x7f800000);
   const float gam = (float)(d + 64) * 5.9604645e-08f;  // (d + 64) * 2^-24
   const float up = 1.0f + 9.5367432e-07f, dn = 1.0f - 9.5367432e-07f;  // 1 +- 2^-20
   for (int j = lane; j < d; j += 32) qv[j] = a.q[row * d + j];
+  const uint64_t* cand = a.cand + row * a.R;
+  constexpr int KU = 8;  // shortlist keys in flight per lane
+  for (int c0 = 0; c0 < a.R; c0 += 32 * KU) {
+    uint64_t kk[KU];
+#pragma unroll
+    for (int u = 0; u < KU; ++u) {
+      const int c = c0 + u * 32 + lane;
+      kk[u] = c < a.R ? __ldg(cand + c) : KEY_NONE;
+    }
+#pragma unroll
+    for (int u = 0; u < KU; ++u) {
+      const int c = c0 + u * 32 + lane;
+      uint32_t mpos = 0xffffffffu;
+      if (kk[u] != KEY_NONE) {
+        mpos = key_id(kk[u]);
+        if ((int64_t)mpos >= a.ntotal) {
+          atomicExch(a.err, 105);
+          mpos = 0xffffffffu;
+        }
+      }
+      if (c < a.R) spos[c] = mpos;
+    }
+  }
   __syncwarp();
+  const int nrounds = (a.R + RC_ROWS - 1) / RC_ROWS;
+  const int chunks = d8 >> 4;  // 16-byte pieces per row
+  // issue round t's row copies into ring slot t & 1 (empty slots copy nothing)
+  auto issue = [&](int t) {
+    if (t < nrounds) {
+      const uint32_t dst0 = (uint32_t)__cvta_generic_to_shared(ring + (size_t)(t & 1) * rbytes);
+      for (int e = lane; e < RC_ROWS * chunks; e += 32) {
+        const int u = e / chunks, ch = e - u * chunks;
+        const int c = t * RC_ROWS + u;
+        const uint32_t p = c < a.R ? spos[c] : 0xffffffffu;
+        if (p != 0xffffffffu)
+          cp_async16(dst0 + (uint32_t)(u * d8 + ch * 16), a.raw8 + (int64_t)p * d8 + ch * 16);
+      }
+    }
+    cp_async_commit();  // one group per round, empty or not
+  };
+  issue(0);
+  issue(1);
   float qn = 0.0f;  // IP: upper bound on ||q||
   if (a.metric != MV_METRIC_L2) {
     for (int j = lane; j < d; j += 32) qn = fmaf(qv[j], qv[j], qn);
     for (int o = 16; o > 0; o >>= 1) qn += __shfl_xor_sync(0xffffffffu, qn, o);
     qn = sqrtf(qn * (1.0f + 2.0f * gam)) * up;
   }
-  const uint64_t* cand = a.cand + row * a.R;
-  uint32_t hk = 0xffffffffu;  // ordered bits of the smallest group bound so far
-  for (int c0 = 0; c0 < a.R; c0 += 32) {
+  for (int t = 0; t < nrounds; ++t) {
+    const int c0 = t * RC_ROWS;
     const int c = c0 + lane;
-    uint32_t mpos = 0xffffffffu, mid = 0;
-    if (c < a.R) {
-      const uint64_t key = cand[c];
-      if (key != KEY_NONE) {
-        mpos = key_id(key);
-        if ((int64_t)mpos >= a.ntotal) {
-          atomicExch(a.err, 105);
-          mpos = 0xffffffffu;
+    const uint32_t mine = c < a.R ? spos[c] : 0xffffffffu;
+    const float2 meta = mine != 0xffffffffu ? __ldg(a.rmeta + mine) : make_float2(0.0f, 0.0f);
+    cp_async_wait<1>();  // round t's group has landed (round t + 1's may be in flight)
+    __syncwarp();
+    const unsigned char* buf = ring + (size_t)(t & 1) * rbytes;
+    float acc[RC_ROWS];
+#pragma unroll
+    for (int u = 0; u < RC_ROWS; ++u) acc[u] = 0.0f;
+    // lane: elements j .. j + 3 of every row (one 4-byte word); elements
+    // past d decode to 0 against a query element of 0
+    for (int j0 = 0; j0 < d; j0 += 128) {
+      const int j = j0 + lane * 4;
+      const bool jin = j < d;
+      float qj[4], aj[4], sj[4];
+#pragma unroll
+      for (int tt = 0; tt < 4; ++tt) {
+        const bool in = j + tt < d;
+        const float2 ds = in ? a.dim8[j + tt] : make_float2(-8388608.0f, 1.0f);
+        qj[tt] = in ? qv[j + tt] : 0.0f;
+        aj[tt] = ds.x;
+        sj[tt] = ds.y;
+      }
+#pragma unroll
+      for (int u = 0; u < RC_ROWS; ++u) {
+        const uint32_t w = jin ? *reinterpret_cast<const uint32_t*>(buf + u * d8 + j) : 0u;
+        float y[4];
+#pragma unroll
+        for (int tt = 0; tt < 4; ++tt)
+          y[tt] = fmaf(sj[tt], __uint_as_float(__byte_perm(w, 0x4B00u, 0x5440u + tt)), aj[tt]);
+        if (a.metric == MV_METRIC_L2) {
+          const float d0 = qj[0] - y[0], d1 = qj[1] - y[1], d2 = qj[2] - y[2], d3 = qj[3] - y[3];
+          acc[u] = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, acc[u]))));
+        } else {
+          acc[u] = fmaf(qj[0], y[0], fmaf(qj[1], y[1], fmaf(qj[2], y[2], fmaf(qj[3], y[3], acc[u]))));
         }
       }
     }
-    float mrad = 0.0f, mn16 = 0.0f;
-    if (mpos != 0xffffffffu) {
-      mid = a.ids ? a.ids[mpos] : mpos;
-      mrad = a.rad[mpos];
-      if (a.metric != MV_METRIC_L2) mn16 = a.n16[mpos];
-    }
-    float acc[32];
-#pragma unroll
-    for (int u = 0; u < 32; ++u) acc[u] = 0.0f;
-    if ((d & 3) == 0) {
-      for (int j0 = 0; j0 < d; j0 += 128) {
-        const int j = j0 + lane * 4;
-        const bool jin = j < d;
-        uint2 v[32];
-#pragma unroll
-        for (int u = 0; u < 32; ++u) {
-          const uint32_t p = __shfl_sync(0xffffffffu, mpos, u);
-          v[u] = jin && p != 0xffffffffu ? *reinterpret_cast<const uint2*>(a.raw16 + (int64_t)p * d + j)
-                                         : make_uint2(0u, 0u);
-        }
-        const float q0 = jin ? qv[j] : 0.0f, q1 = jin ? qv[j + 1] : 0.0f;
-        const float q2 = jin ? qv[j + 2] : 0.0f, q3 = jin ? qv[j + 3] : 0.0f;
-#pragma unroll
-        for (int u = 0; u < 32; ++u) {
-          const float y0 = __uint_as_float(v[u].x << 16), y1 = __uint_as_float(v[u].x & 0xffff0000u);
-          const float y2 = __uint_as_float(v[u].y << 16), y3 = __uint_as_float(v[u].y & 0xffff0000u);
-          if (a.metric == MV_METRIC_L2) {
-            const float d0 = jin ? q0 - y0 : 0.0f, d1 = jin ? q1 - y1 : 0.0f;
-            const float d2 = jin ? q2 - y2 : 0.0f, d3 = jin ? q3 - y3 : 0.0f;
-            acc[u] = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, acc[u]))));
-          } else {
-            acc[u] = fmaf(q0, y0, fmaf(q1, y1, fmaf(q2, y2, fmaf(q3, y3, acc[u]))));
-          }
-        }
-      }
-    } else {
-      for (int j0 = 0; j0 < d; j0 += 32) {  // every lane runs the same trips
-        const int j = j0 + lane;
-        const bool jin = j < d;
-        const float qj = jin ? qv[j] : 0.0f;
-#pragma unroll
-        for (int u = 0; u < 32; ++u) {
-          const uint32_t p = __shfl_sync(0xffffffffu, mpos, u);
-          const float y = jin && p != 0xffffffffu ? __bfloat162float(a.raw16[(int64_t)p * d + j]) : 0.0f;
-          if (a.metric == MV_METRIC_L2) {
-            const float df = jin ? qj - y : 0.0f;
-            acc[u] = fmaf(df, df, acc[u]);
-          } else {
-            acc[u] = fmaf(qj, y, acc[u]);
-          }
-        }
-      }
-    }
-    // transposing butterfly: lane l ends with candidate l's sum
+    __syncwarp();  // every lane has read the slot before it is refilled
+    issue(t + 2);
+    // transposing butterfly: lane l ends with row c0 + l's sum
 #pragma unroll
     for (int w = 16; w >= 1; w >>= 1) {
       const bool upper = (lane & w) != 0;
@@ -1119,36 +1161,42 @@ __global__ void __launch_bounds__(RC_WARPS * 32, 2) k_rerank_cert(RerankArgs a) 
         acc[i] = keep + __shfl_xor_sync(0xffffffffu, send, w);
       }
     }
-    float lo = INF, hi = INF;  // empty slots never survive
-    if (mpos != 0xffffffffu) {
-      const float t = acc[0];
-      const float r = mrad, yn = mn16;
-      if (!(fabsf(t) < INF)) {  // not finite: always computed exactly
-        lo = -INF;
-        hi = INF;
-      } else if (a.metric == MV_METRIC_L2) {
-        const float slo = sqrtf(t * (1.0f - 2.0f * gam)) * dn - r * up;
-        const float shi = sqrtf(t * (1.0f + 2.0f * gam)) * up + r * up;
-        const float m = fmaxf(slo, 0.0f);
-        lo = m * m * (1.0f - 2.0f * gam) * dn;
-        hi = shi * shi * (1.0f + 2.0f * gam) * up;
-      } else {
-        const float e = qn * (gam * yn + r + gam * (yn + r)) * up;
-        lo = (-t - e) * (-t - e < 0.0f ? up : dn);
-        hi = (-t + e) * (-t + e < 0.0f ? dn : up);
-      }
-    }
     if (c < a.R) {
+      float lo = INF, hi = INF;  // empty slots never survive
+      if (mine != 0xffffffffu) {
+        const float tv = acc[0];
+        const float r = meta.x, yn = meta.y;
+        if (!(fabsf(tv) < INF) || !(r < INF) || !(yn < INF)) {  // not finite: computed exactly
+          lo = -INF;
+          hi = INF;
+        } else if (a.metric == MV_METRIC_L2) {
+          const float slo = sqrtf(tv * (1.0f - 2.0f * gam)) * dn - r * up;
+          const float shi = sqrtf(tv * (1.0f + 2.0f * gam)) * up + r * up;
+          const float m = fmaxf(slo, 0.0f);
+          lo = m * m * (1.0f - 2.0f * gam) * dn;
+          hi = shi * shi * (1.0f + 2.0f * gam) * up;
+        } else {
+          const float e = qn * (gam * yn + r + gam * (yn + r)) * up;
+          lo = (-tv - e) * (-tv - e < 0.0f ? up : dn);
+          hi = (-tv + e) * (-tv + e < 0.0f ? dn : up);
+        }
+      }
       blo[c] = lo;
-      spos[c] = mpos;
-      sid[c] = mid;
+      bhi[c] = float_to_ordered(hi);
     }
-    uint64_t hv[1] = {c < a.R ? ((uint64_t)float_to_ordered(hi) << 32) | (uint32_t)lane : KEY_NONE};
+  }
+  cp_async_wait<0>();
+  __syncwarp();
+  // the k-th smallest upper end of each group of 32 candidates
+  uint32_t hk = 0xffffffffu;  // ordered bits of the smallest group bound
+  for (int g0 = 0; g0 < a.R; g0 += 32) {
+    const int c = g0 + lane;
+    uint64_t hv[1] = {c < a.R ? ((uint64_t)bhi[c] << 32) | (uint32_t)lane : KEY_NONE};
     warp_sort_regs<1>(hv);
     const uint64_t kth = __shfl_sync(0xffffffffu, hv[0], a.k - 1);
     if (kth != KEY_NONE) hk = min(hk, (uint32_t)(kth >> 32));
   }
-  __syncwarp();
+  __syncwarp();  // bhi is read by every lane before slist overwrites it
   const float hkf = hk == 0xffffffffu ? INF : ordered_to_float(hk);
   int ns = 0;
   for (int c0 = 0; c0 < a.R; c0 += 32) {
@@ -1169,15 +1217,22 @@ __global__ void __launch_bounds__(RC_WARPS * 32, 2) k_rerank_cert(RerankArgs a) 
       pos[u] = i0 + u < ns ? spos[slist[i0 + u]] : 0xffffffffu;
       acc[u] = 0.0f;
     }
+    // the survivors' ids: lane u of the group loads survivor u's beside the rows
+    uint32_t myid = 0;
+    {
+      const uint32_t pp = lane < U && i0 + lane < ns ? spos[slist[i0 + lane]] : 0xffffffffu;
+      if (pp != 0xffffffffu) myid = a.ids ? a.ids[pp] : pp;
+    }
     rerank_rows_fp32<U>(a, qv, pos, acc);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      float t = acc[u];
-      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      float tv = acc[u];
+      for (int o = 16; o > 0; o >>= 1) tv += __shfl_xor_sync(0xffffffffu, tv, o);
+      const uint32_t id = __shfl_sync(0xffffffffu, myid, u);
       if (lane == 0 && i0 + u < ns) {
         const int c = slist[i0 + u];
         sk[i0 + u] = pos[u] == 0xffffffffu ? KEY_NONE - (uint64_t)c
-                                           : make_key(a.metric == MV_METRIC_L2 ? t : -t, sid[c]);
+                                           : make_key(a.metric == MV_METRIC_L2 ? tv : -tv, id);
       }
     }
   }
@@ -1194,35 +1249,96 @@ __global__ void __launch_bounds__(RC_WARPS * 32, 2) k_rerank_cert(RerankArgs a) 
   rerank_write(a, row, outb, lane, 32);
 }
 
-// BF16 copy of each row, an upper bound on ||y - bf16(y)|| and on
-// ||bf16(y)||, one warp per row. The squared sums carry a relative error of
-// at most (d + 2) 2^-24 (non-negative terms), covered by the (d + 64) 2^-23
+// Per-dimension minimum and maximum of the rows (ordered words, combined
+// with atomics into dimord[0, d) and dimord[d, 2d)); a block walks a range
+// of rows with one thread per dimension.
+__global__ void k_dim_minmax(const float* __restrict__ raw, int64_t n, int d, int64_t rows_per_block,
+                             uint32_t* __restrict__ dimord) {
+  const int64_t r0 = (int64_t)blockIdx.x * rows_per_block;
+  const int64_t r1 = min(n, r0 + rows_per_block);
+  for (int j = threadIdx.x; j < d; j += blockDim.x) {
+    uint32_t lo = 0xffffffffu, hi = 0u;
+    for (int64_t r = r0; r < r1; ++r) {
+      const uint32_t o = float_to_ordered(raw[r * d + j]);
+      lo = min(lo, o);
+      hi = max(hi, o);
+    }
+    if (r0 < r1) {
+      atomicMin(&dimord[j], lo);
+      atomicMax(&dimord[d + j], hi);
+    }
+  }
+}
+
+__global__ void k_dim_init(uint32_t* dimord, int d) {
+  for (int j = threadIdx.x; j < d; j += blockDim.x) {
+    dimord[j] = 0xffffffffu;
+    dimord[d + j] = 0u;
+  }
+}
+
+// Per dimension (a'_j, s_j) of the 8-bit copy: s_j a power of two and
+// a_j = floor(min_j / s_j) s_j with 255 s_j >= max_j - a_j (s_j = 1 for a
+// constant or non-finite dimension), stored as a'_j = a_j - 2^23 s_j so that
+// y8 = fmaf(s_j, 2^23 + u, a'_j) decodes a code from its float bits
+// 0x4B000000 | u. a'_j is exact while |a_j / s_j| < 2^23; every row bound is
+// computed from the decoded values, so the copy stays certified either way.
+__global__ void k_dim_steps(const uint32_t* __restrict__ dimord, int d, float2* __restrict__ dim8) {
+  for (int j = threadIdx.x; j < d; j += blockDim.x) {
+    const float lo = ordered_to_float(dimord[j]), hi = ordered_to_float(dimord[d + j]);
+    float s = 1.0f, a = 0.0f;
+    if (isfinite(lo) && isfinite(hi)) {
+      const float range = hi - lo;
+      if (range > 0.0f && range < __int_as_float(0x7f800000)) {
+        s = ldexpf(1.0f, ilogbf(range) - 7);
+        if (255.0f * s < range) s *= 2.0f;
+        if (hi - floorf(lo / s) * s > 255.0f * s) s *= 2.0f;
+      }
+      a = floorf(lo / s) * s;
+    }
+    dim8[j] = make_float2(a - 8388608.0f * s, s);
+  }
+}
+
+// 8-bit copy of each row, an upper bound on ||y - y8|| and on ||y8||, one
+// warp per row. The squared sums carry a relative error of at most
+// (d + 2) 2^-24 (non-negative terms), covered by the (d + 64) 2^-23
 // inflation, and 2^-21 more covers the square root.
-__global__ void k_rerank_rows(const float* __restrict__ raw, int64_t n, int d,
-                              __nv_bfloat16* __restrict__ raw16, float* __restrict__ rad,
-                              float* __restrict__ n16) {
+__global__ void k_rerank_rows8(const float* __restrict__ raw, int64_t n, int d, int d8,
+                               const float2* __restrict__ dim8, uint8_t* __restrict__ raw8,
+                               float2* __restrict__ rmeta) {
   const int lane = threadIdx.x & 31;
   const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (r >= n) return;
   float e2 = 0.0f, y2 = 0.0f;
-  for (int j = lane; j < d; j += 32) {
-    const float y = raw[r * d + j];
-    const __nv_bfloat16 b = __float2bfloat16_rn(y);
-    const float yb = __bfloat162float(b);
-    raw16[r * d + j] = b;
-    const float df = y - yb;  // exact
-    e2 = fmaf(df, df, e2);
-    y2 = fmaf(yb, yb, y2);
+  bool finite = true;
+  for (int j = lane; j < d8; j += 32) {
+    uint32_t code = 0;
+    if (j < d) {
+      const float y = raw[r * d + j];
+      const float2 as = dim8[j];
+      const float a = fmaf(8388608.0f, as.y, as.x);  // a_j (exact when a'_j is)
+      const float t = rintf((y - a) / as.y);
+      code = (uint32_t)(int)fminf(fmaxf(t, 0.0f), 255.0f);  // NaN -> 0
+      const float y8 = fmaf(as.y, __uint_as_float(0x4B000000u | code), as.x);
+      const float df = y - y8;
+      finite = finite && isfinite(y) && isfinite(y8);
+      e2 = fmaf(df, df, e2);
+      y2 = fmaf(y8, y8, y2);
+    }
+    raw8[r * d8 + j] = (uint8_t)code;
   }
   for (int o = 16; o > 0; o >>= 1) {
     e2 += __shfl_xor_sync(0xffffffffu, e2, o);
     y2 += __shfl_xor_sync(0xffffffffu, y2, o);
   }
+  finite = __all_sync(0xffffffffu, finite);
   if (lane == 0) {
+    const float INF = __int_as_float(0x7f800000);
     const float infl = 1.0f + (float)(d + 64) * 1.1920929e-07f;
     const float up = 1.0f + 4.7683716e-07f;  // 1 + 2^-21
-    rad[r] = sqrtf(e2 * infl) * up;
-    n16[r] = sqrtf(y2 * infl) * up;
+    const float rr = sqrtf(e2 * infl) * up, yn = sqrtf(y2 * infl) * up;
+    rmeta[r] = finite && rr < INF && yn < INF ? make_float2(rr, yn) : make_float2(INF, INF);
   }
 }
 
@@ -1347,6 +1463,12 @@ size_t fast_scan_smem(const FastScanArgs& a) {
 void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s, int nt, int persistent_ctas,
                             int lut) {
   if (a.nq == 0) return;
+  // lut 6: the bank-rotated fixed-point table scan with per-candidate slots
+  if (lut == 6 && ivfpq_rt_supported(a)) {
+    launch_ivfpq_scan_rt(a, s, nt, persistent_ctas);
+    return;
+  }
+  MV_REQUIRE(lut != 6, MV_ERR_UNSUPPORTED, "rotated-table scan: unsupported M, d or codebook");
   if (lut == 4 && launch_ivfpq_scan_staged(a, s, nt, persistent_ctas, a.stage_entries)) return;
   a.cap = fast_scan_cap(a.R);
   a.Rp = next_pow2(a.R);
@@ -1378,10 +1500,13 @@ void launch_rerank_fast(RerankArgs a, cudaStream_t s) {
   if (a.nq == 0) return;
   a.kp = next_pow2(a.k);
   const size_t qbytes = ((size_t)a.d * 4 + 15) & ~size_t(15);
-  const size_t csmem = (size_t)RC_WARPS * (qbytes + (size_t)a.R * 24);
-  if (a.raw16 && a.rad && a.n16 && a.k <= 32 && a.R >= 32 && csmem <= 100 * 1024) {
+  const size_t wbytes = rerank_cert_warp_bytes(a.d, a.R);
+  const int cw = (int)std::min<size_t>(4, (96 * 1024) / wbytes);  // warps per CTA
+  if (a.raw8 && a.rmeta && a.dim8 && a.d8 == rerank8_row_bytes(a.d) && a.k <= 32 && a.R >= 32 &&
+      cw >= 1) {
+    const size_t csmem = (size_t)cw * wbytes;
     smem_attr(k_rerank_cert, csmem);
-    k_rerank_cert<<<(unsigned)((a.nq + RC_WARPS - 1) / RC_WARPS), RC_WARPS * 32, csmem, s>>>(a);
+    k_rerank_cert<<<(unsigned)((a.nq + cw - 1) / cw), cw * 32, csmem, s>>>(a);
     count_launch();
     MV_CHECK_CUDA(cudaGetLastError());
     return;
@@ -1394,10 +1519,18 @@ void launch_rerank_fast(RerankArgs a, cudaStream_t s) {
   MV_CHECK_CUDA(cudaGetLastError());
 }
 
-void launch_rerank_rows(const float* raw, int64_t n, int d, __nv_bfloat16* raw16, float* rad,
-                        float* n16, cudaStream_t s) {
+void launch_rerank_rows8(const float* raw, int64_t n, int d, uint32_t* dimord, float2* dim8,
+                         uint8_t* raw8, float2* rmeta, cudaStream_t s) {
   if (n == 0) return;
-  k_rerank_rows<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(raw, n, d, raw16, rad, n16);
+  const int d8 = rerank8_row_bytes(d);
+  k_dim_init<<<1, 256, 0, s>>>(dimord, d);
+  count_launch();
+  const int64_t per = 256;
+  k_dim_minmax<<<(unsigned)((n + per - 1) / per), 128, 0, s>>>(raw, n, d, per, dimord);
+  count_launch();
+  k_dim_steps<<<1, 256, 0, s>>>(dimord, d, dim8);
+  count_launch();
+  k_rerank_rows8<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(raw, n, d, d8, dim8, raw8, rmeta);
   count_launch();
   MV_CHECK_CUDA(cudaGetLastError());
 }

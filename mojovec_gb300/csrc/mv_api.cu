@@ -777,11 +777,13 @@ void ensure_fast(mv_ivfpq* ix, cudaStream_t s) {
     }
   }
   if (ix->has_raw && total > 0) {
-    ix->d_raw16.ensure((size_t)total * ix->d * 2);
-    ix->d_rad.ensure((size_t)total * 4);
-    ix->d_n16.ensure((size_t)total * 4);
-    launch_rerank_rows(ix->d_raw.as<float>(), total, ix->d, ix->d_raw16.as<__nv_bfloat16>(),
-                       ix->d_rad.as<float>(), ix->d_n16.as<float>(), s);
+    ix->d_raw8.ensure((size_t)total * rerank8_row_bytes(ix->d));
+    ix->d_rmeta.ensure((size_t)total * sizeof(float2));
+    ix->d_dim8.ensure((size_t)ix->d * sizeof(float2));
+    ix->d_dimord.ensure((size_t)ix->d * 8);
+    launch_rerank_rows8(ix->d_raw.as<float>(), total, ix->d, ix->d_dimord.as<uint32_t>(),
+                        ix->d_dim8.as<float2>(), ix->d_raw8.as<uint8_t>(),
+                        ix->d_rmeta.as<float2>(), s);
   }
   sync(s);
   ix->fast_ready = true;
@@ -832,19 +834,6 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
     MV_REQUIRE(nq <= 65535ll * 64, MV_ERR_UNSUPPORTED, "batch too large for one launch");
     qb = nq;
   }
-  // lut 5: the list-major tensor-core scan, whose distance rows (smax words
-  // per query) must fit kTcRowBytes per chunk of queries
-  const int lut = p ? p->lut_fp16 : 0;
-  constexpr int64_t kTcRowBytes = 1ll << 31;
-  const int64_t smax = ix->longest.empty() ? 0 : ix->longest[std::min(nprobe, ix->nlist)];
-  bool tc = lut == 5 && ivfpq_tc_supported(ix->d, ix->M, ix->pq16_inv > 0.0f) && smax > 0 &&
-            nprobe <= 1024;
-  if (tc) {
-    const int64_t fit = kTcRowBytes / (smax * 4);
-    if (batch ? fit < qb : fit < 1) tc = false;
-    else qb = std::min(qb, fit);
-  }
-  const int tc_qc = tc ? ivfpq_tc_qc(qb, nprobe, ix->nlist) : 0;
   const int nseg = fused ? umma_topk_nseg(qb, ix->nlist, ix->d, nc, ix->ctx->num_sms)
                  : twopass ? coarse_topk2_nseg(qb, ix->nlist, ix->d, nc, ix->ctx->num_sms) : 1;
   const int ncand = nseg * (fused ? umma_topk_groups(ix->d, nc) : 1) * next_pow2(nc);
@@ -854,8 +843,7 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
              : twopass ? ws_bytes((size_t)qb * nseg * lcap, 8) + ws_bytes((size_t)qb * nseg, 4) +
                             ws_bytes((size_t)qb, 4)
                        : ws_bytes((size_t)qb * ix->nlist, 4)) +
-            ws_bytes((size_t)qb * nprobe, 4) * 2 + ws_bytes((size_t)qb * R, 8) +
-            (tc ? ws_bytes(ivfpq_tc_scratch_bytes(qb, nprobe, ix->nlist, ix->d, smax, tc_qc, ix->h_off[ix->nlist]), 1) : 0));
+            ws_bytes((size_t)qb * nprobe, 4) * 2 + ws_bytes((size_t)qb * R, 8));
   Arena ar(ws);
   __nv_bfloat16* xq = ar.take<__nv_bfloat16>((size_t)qb * kp);
   float* dmat = fused || twopass ? nullptr : ar.take<float>((size_t)qb * ix->nlist);
@@ -867,8 +855,6 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
   int32_t* probes = ar.take<int32_t>((size_t)qb * nprobe);
   float* term = ar.take<float>((size_t)qb * nprobe);
   uint64_t* skeys = ar.take<uint64_t>((size_t)qb * R);
-  void* tc_scratch =
-      tc ? ar.take<unsigned char>(ivfpq_tc_scratch_bytes(qb, nprobe, ix->nlist, ix->d, smax, tc_qc, ix->h_off[ix->nlist])) : nullptr;
   for (int64_t q0 = 0; q0 < nq; q0 += qb) {
     const int64_t nb = std::min(qb, nq - q0);
     const float* xb = d_x + q0 * ix->d;
@@ -945,10 +931,7 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
         a.filter_len = filter_len;
         a.ids = ix->d_ids.as<uint32_t>();
       }
-      if (tc) {
-        a.nprobe_q = batch ? batch->nprobe_q : nullptr;
-        launch_ivfpq_scan_tc(a, smax, tc_qc, tc_scratch, ix->ctx->num_sms, current_wait_limit(), s);
-      } else if (batch) {
+      if (batch) {
         a.nprobe_q = batch->nprobe_q;
         a.order = batch->order;
         a.counter = batch->scan_ctas_per_sm > 0 ? batch->counter : nullptr;
@@ -976,10 +959,11 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
       r.ntotal = ix->h_off[ix->nlist];
       r.err = ix->ctx->d_err.as<int>();
       r.k_q = batch ? batch->k_q : nullptr;
-      if (!(p && p->rerank_fp32) && ix->d_raw16.p) {
-        r.raw16 = ix->d_raw16.as<__nv_bfloat16>();
-        r.rad = ix->d_rad.as<float>();
-        r.n16 = ix->d_n16.as<float>();
+      if (!(p && p->rerank_fp32) && ix->d_raw8.p) {
+        r.raw8 = ix->d_raw8.as<uint8_t>();
+        r.rmeta = ix->d_rmeta.as<float2>();
+        r.dim8 = ix->d_dim8.as<float2>();
+        r.d8 = rerank8_row_bytes(ix->d);
       }
       launch_rerank_fast(r, s);
     } else {

@@ -48,6 +48,13 @@ struct FastScanArgs {
   int stage_entries = 0;  // staged scan: candidates per staged round (0: automatic)
 };
 
+// Bank-rotated fixed-point table scan (k_ivfpq_rt.cu): M a multiple of 4
+// up to 32, dsub 4 or 8 with the FP16 codebook and its subspace norm bounds.
+bool ivfpq_rt_supported(const FastScanArgs& a);
+// One CTA (nt threads: 256 or 512) per query, or with a.counter a
+// persistent grid of persistent_ctas CTAs.
+void launch_ivfpq_scan_rt(FastScanArgs a, cudaStream_t s, int nt, int persistent_ctas);
+
 struct RerankArgs {
   const float* q;
   int64_t nq;
@@ -64,17 +71,25 @@ struct RerankArgs {
   const int32_t* k_q = nullptr;  // per-query k (<= k; the row keeps k slots), may be null
   int kp;                 // set by the launcher
   // Certified prescreen (k <= 32; all null: every candidate is computed in
-  // FP32): BF16 copies of the rows, per row an upper bound on
-  // ||y - bf16(y)|| and (IP) on ||bf16(y)||.
-  const __nv_bfloat16* raw16 = nullptr;
-  const float* rad = nullptr;
-  const float* n16 = nullptr;
+  // FP32): 8-bit copies of the rows (d8 bytes each) with y8_j =
+  // fmaf(s_j, u_j, a_j) from the per-dimension (a_j, s_j) in dim8, and per
+  // row upper bounds on ||y - y8|| and (IP) on ||y8|| in rmeta.
+  const uint8_t* raw8 = nullptr;
+  const float2* rmeta = nullptr;
+  const float2* dim8 = nullptr;
+  int d8 = 0;
 };
 
-// BF16 copies of FP32 rows (CSR order) for the certified rerank prescreen,
-// with per row upper bounds on ||y - bf16(y)|| and ||bf16(y)||.
-void launch_rerank_rows(const float* raw, int64_t n, int d, __nv_bfloat16* raw16, float* rad,
-                        float* n16, cudaStream_t s);
+// Row bytes of the 8-bit prescreen copy of d-element rows.
+inline int rerank8_row_bytes(int d) { return (d + 15) & ~15; }
+
+// 8-bit copies of FP32 rows (CSR order) for the certified rerank prescreen:
+// per dimension j an offset a_j (the minimum over the rows) and a step s_j
+// (the smallest power of two with 255 s_j >= max_j - min_j), codes
+// u = round((y_j - a_j) / s_j), and per row upper bounds on ||y - y8|| and
+// ||y8|| with y8_j = fmaf(s_j, u_j, a_j). dimord holds 2 d words of scratch.
+void launch_rerank_rows8(const float* raw, int64_t n, int d, uint32_t* dimord, float2* dim8,
+                         uint8_t* raw8, float2* rmeta, cudaStream_t s);
 
 // Two-pass coarse GEMM lists (launch_coarse_topk2) -> the nprobe nearest
 // lists, as launch_coarse_rows (one warp per query; nseg * cap <= 256).
@@ -103,29 +118,15 @@ size_t fast_scan_smem(const FastScanArgs& a);
 // The staged scan (k_ivfpq_scan.cu); returns false, launching nothing, when
 // its shared memory would not fit (the caller runs the unstaged kernel).
 bool launch_ivfpq_scan_staged(FastScanArgs a, cudaStream_t s, int nt, int persistent_ctas, int E);
-// lut: 0 or 2 = FP32 tables read with codes from global memory, 1 = FP16
-// tables with a per-query power-of-two scale (FP32 sums), 3 = bank-rotated
-// fixed-point tables where M allows (else FP32), 4 = FP32 tables with codes
-// and terms staged in shared memory by bulk copies (the unstaged kernel when
-// that does not fit).
+// lut: 0 or 2 = FP32 tables read with codes from global memory; 6 = the
+// bank-rotated fixed-point table scan with per-candidate slots
+// (k_ivfpq_rt.cu) or an error; 1 = FP16 tables with a per-query
+// power-of-two scale (FP32 sums), 3 = bank-rotated fixed-point tables in
+// the per-candidate layout where M allows (else FP32), 4 = FP32 tables with
+// codes and terms staged in shared memory by bulk copies (the unstaged
+// kernel when that does not fit).
 void launch_ivfpq_scan_fast(FastScanArgs a, cudaStream_t s, int nt = 256, int persistent_ctas = 0,
                             int lut = 0);
-// List-major ADC on the tensor cores (k_ivfpq_tc.cu): FP16 queries times
-// FP16 reconstructions of the list rows, one decode per list row and batch;
-// writes the R smallest (distance, position) keys per query like the scan
-// above (a.q, nq, d, M, metric, pq16, pq16_inv, list_off, codes, vterm,
-// probes, term, nprobe, nprobe_q, R, sorted, out_keys, nlist, err, filter).
-// Shapes: FP16 codebook, M a multiple of 8, d / M = 4 or 8, d <= 128.
-bool ivfpq_tc_supported(int d, int M, bool has_pq16);
-// Queries per work item (64 or 128) for a batch shape.
-int ivfpq_tc_qc(int64_t nq, int nprobe, int nlist);
-// smax: an upper bound on any query's candidate count (the nprobe longest
-// lists); the scratch holds nq distance rows of smax words, the query
-// images of the work items and one flag per CSR row (ntotal).
-size_t ivfpq_tc_scratch_bytes(int64_t nq, int nprobe, int nlist, int d, int64_t smax, int qc,
-                              int64_t ntotal);
-void launch_ivfpq_scan_tc(const FastScanArgs& a, int64_t smax, int qc, void* scratch, int num_sms,
-                          long long wait_limit, cudaStream_t s);
 // Flat fast form: merge nseg x ncp per-segment keys (kseg kept per segment)
 // into the R-key shortlist per query. With out_keys the shortlist is
 // written (unsorted) for the rerank; otherwise the k smallest become the

@@ -219,9 +219,10 @@ struct mv_ivfpq {
   bool coarse_ready = false;  // d_cent_bf16, d_cnorm, d_ccert (centroid-only state)
   mv::DevBuf d_ccert;       // 2 floats: bound on ||bf16(c)||^2, max ||c - bf16(c)||
   mv::DevBuf d_vec_term;    // FP32 per vector: ||y||^2 + 2<c, y> (y = PQ reconstruction)
-  mv::DevBuf d_raw16;       // BF16 rows per entry (certified rerank prescreen)
-  mv::DevBuf d_rad;         // FP32 per entry: bound on ||y - bf16(y)||
-  mv::DevBuf d_n16;         // FP32 per entry: bound on ||bf16(y)||
+  mv::DevBuf d_raw8;        // 8-bit rows per entry, d8 bytes (certified rerank prescreen)
+  mv::DevBuf d_rmeta;       // float2 per entry: bounds on ||y - y8|| and ||y8||
+  mv::DevBuf d_dim8;        // float2 per dimension: offset a_j, power-of-two step s_j
+  mv::DevBuf d_dimord;      // 2 x d ordered words: per-dimension minimum and maximum
   mv::DevBuf d_pq16;        // FP16 codebook * pq16_scale (fast-form tables; dsub 4 or 8)
   float pq16_inv = 0.0f;    // 1 / scale; 0 = no FP16 codebook
   mv::DevBuf d_pq_cn;       // FP32 per subspace: bound on its largest codeword norm

@@ -422,3 +422,84 @@ def recall(gt_labels, labels):
     for i in range(gt.shape[0]):
         hits += len(set(gt[i].tolist()) & set(got[i].tolist()))
     return hits / gt.size
+
+
+class CollectionIVFPQ:
+    """Restatement of the managed IVF-PQ collection's query path over the
+    oracle index (api/collection_ivfpq.mojo): training validation and
+    cosine normalisation (:170-185), id validation and auto-train on the
+    first add (:187-242), query validation and preparation (:254-285), and
+    the id map with 1 - d for the cosine and inner-product metrics
+    (:287-333). Test infrastructure only."""
+
+    MAX_QUERY_RESULTS = 2048
+    PQ_CENTROIDS = 256
+
+    def __init__(self, d, nlist, M, nprobe, metric="l2"):
+        if metric not in ("l2", "cosine", "ip"):
+            raise ValueError('metric must be "l2", "cosine", or "ip".')
+        self.d, self.metric, self.nprobe = d, metric, nprobe
+        self.index = IVFPQ(d, nlist, M, METRIC_L2 if metric == "l2" else METRIC_IP)
+        self.nlist = nlist
+        self.trained = False
+        self.user_ids = []
+        self.id_to_internal = {}
+
+    def _prepare(self, rows):
+        rows = _f32(rows).reshape(-1, self.d)
+        if self.metric == "cosine":  # collection_vector_query.mojo:24-46
+            return normalize(rows)
+        if rows.size and not np.isfinite(rows).all():
+            raise ValueError("Vector components must be finite.")
+        return rows
+
+    def train(self, rows):
+        rows = _f32(rows).reshape(-1, self.d)
+        if rows.shape[0] < max(self.nlist, self.PQ_CENTROIDS):
+            raise ValueError("IVF-PQ training requires at least max(nlist, 256) vectors.")
+        if self.trained:
+            return
+        self.index.train(self._prepare(rows))
+        self.trained = True
+
+    def add(self, ids, rows):
+        rows = _f32(rows).reshape(-1, self.d)
+        if rows.shape[0] != len(ids):
+            raise ValueError("Embeddings length must equal len(ids) * dimension.")
+        if len(ids) == 0:
+            return
+        seen = set()
+        for rid in ids:
+            if rid in seen:
+                raise ValueError("Duplicate IDs are not allowed within an add batch.")
+            if rid in self.id_to_internal:
+                raise ValueError("Cannot add an ID that already exists.")
+            seen.add(rid)
+        if not self.trained:
+            self.train(rows)
+        self.index.add(self._prepare(rows))
+        for rid in ids:
+            self.id_to_internal[int(rid)] = len(self.user_ids)
+            self.user_ids.append(int(rid))
+
+    def query(self, rows, n_results=10):
+        """(ids, distances) as lists of rows, collection_ivfpq.mojo:287-333."""
+        rows = _f32(rows).reshape(-1, self.d)
+        if n_results <= 0 or n_results > self.MAX_QUERY_RESULTS:
+            raise ValueError("n_results must be between 1 and 2048.")
+        if rows.shape[0] == 0:
+            return [], []
+        dist, lab = self.index.search(self._prepare(rows), n_results, self.nprobe)
+        all_ids, all_dist = [], []
+        for drow, lrow in zip(dist, lab):
+            ids, ds = [], []
+            for dv, iv in zip(drow, lrow):
+                if 0 <= iv < len(self.user_ids):
+                    ids.append(self.user_ids[iv])
+                    ds.append(np.float32(1.0) - dv if self.metric != "l2" else dv)
+                else:
+                    ids.append(-1)
+                    ds.append(dv)
+            all_ids.append(ids)
+            all_dist.append(np.array(ds, np.float32))
+        return all_ids, all_dist
