@@ -1086,12 +1086,15 @@ __global__ void __launch_bounds__(128, 4) k_rerank_cert(RerankArgs a) {
   __syncwarp();
   const int nrounds = (a.R + RC_ROWS - 1) / RC_ROWS;
   const int chunks = d8 >> 4;  // 16-byte pieces per row
+  const bool pow2c = (chunks & (chunks - 1)) == 0;
+  const int csh = 31 - __clz(chunks);
   // issue round t's row copies into ring slot t & 1 (empty slots copy nothing)
   auto issue = [&](int t) {
     if (t < nrounds) {
       const uint32_t dst0 = (uint32_t)__cvta_generic_to_shared(ring + (size_t)(t & 1) * rbytes);
       for (int e = lane; e < RC_ROWS * chunks; e += 32) {
-        const int u = e / chunks, ch = e - u * chunks;
+        // (row, piece) of copy e: shifts when the piece count is a power of two
+        const int u = pow2c ? e >> csh : e / chunks, ch = e - u * chunks;
         const int c = t * RC_ROWS + u;
         const uint32_t p = c < a.R ? spos[c] : 0xffffffffu;
         if (p != 0xffffffffu)
@@ -1107,6 +1110,16 @@ __global__ void __launch_bounds__(128, 4) k_rerank_cert(RerankArgs a) {
     for (int j = lane; j < d; j += 32) qn = fmaf(qv[j], qv[j], qn);
     for (int o = 16; o > 0; o >>= 1) qn += __shfl_xor_sync(0xffffffffu, qn, o);
     qn = sqrtf(qn * (1.0f + 2.0f * gam)) * up;
+  }
+  float q0[4], a0[4], s0[4];
+#pragma unroll
+  for (int tt = 0; tt < 4; ++tt) {
+    const int j = lane * 4 + tt;
+    const bool in = j < d;
+    const float2 ds = in ? a.dim8[j] : make_float2(-8388608.0f, 1.0f);
+    q0[tt] = in ? qv[j] : 0.0f;
+    a0[tt] = ds.x;
+    s0[tt] = ds.y;
   }
   for (int t = 0; t < nrounds; ++t) {
     const int c0 = t * RC_ROWS;
@@ -1127,15 +1140,22 @@ __global__ void __launch_bounds__(128, 4) k_rerank_cert(RerankArgs a) {
       float qj[4], aj[4], sj[4];
 #pragma unroll
       for (int tt = 0; tt < 4; ++tt) {
-        const bool in = j + tt < d;
-        const float2 ds = in ? a.dim8[j + tt] : make_float2(-8388608.0f, 1.0f);
-        qj[tt] = in ? qv[j + tt] : 0.0f;
-        aj[tt] = ds.x;
-        sj[tt] = ds.y;
+        if (j0 == 0) {  // the first 128 elements' query and steps stay in registers
+          qj[tt] = q0[tt];
+          aj[tt] = a0[tt];
+          sj[tt] = s0[tt];
+        } else {
+          const bool in = j + tt < d;
+          const float2 ds = in ? a.dim8[j + tt] : make_float2(-8388608.0f, 1.0f);
+          qj[tt] = in ? qv[j + tt] : 0.0f;
+          aj[tt] = ds.x;
+          sj[tt] = ds.y;
+        }
       }
+      const unsigned char* rowp = buf + j;
 #pragma unroll
-      for (int u = 0; u < RC_ROWS; ++u) {
-        const uint32_t w = jin ? *reinterpret_cast<const uint32_t*>(buf + u * d8 + j) : 0u;
+      for (int u = 0; u < RC_ROWS; ++u, rowp += d8) {
+        const uint32_t w = jin ? *reinterpret_cast<const uint32_t*>(rowp) : 0u;
         float y[4];
 #pragma unroll
         for (int tt = 0; tt < 4; ++tt)
@@ -1187,15 +1207,17 @@ __global__ void __launch_bounds__(128, 4) k_rerank_cert(RerankArgs a) {
   }
   cp_async_wait<0>();
   __syncwarp();
-  // the k-th smallest upper end of each group of 32 candidates
-  uint32_t hk = 0xffffffffu;  // ordered bits of the smallest group bound
+  // the k-th smallest upper end over the whole shortlist: the 32 smallest
+  // (upper end, candidate) keys merged group by group (k <= 32). Bounding
+  // by each group's own k-th smallest instead leaves several times more
+  // survivors, as a query's k nearest rows spread over the groups.
+  uint64_t best = KEY_NONE;
   for (int g0 = 0; g0 < a.R; g0 += 32) {
     const int c = g0 + lane;
-    uint64_t hv[1] = {c < a.R ? ((uint64_t)bhi[c] << 32) | (uint32_t)lane : KEY_NONE};
-    warp_sort_regs<1>(hv);
-    const uint64_t kth = __shfl_sync(0xffffffffu, hv[0], a.k - 1);
-    if (kth != KEY_NONE) hk = min(hk, (uint32_t)(kth >> 32));
+    best = warp_merge_smallest32(best, c < a.R ? ((uint64_t)bhi[c] << 32) | (uint32_t)c : KEY_NONE);
   }
+  const uint64_t kth = __shfl_sync(0xffffffffu, best, a.k - 1);
+  const uint32_t hk = kth != KEY_NONE ? (uint32_t)(kth >> 32) : 0xffffffffu;
   __syncwarp();  // bhi is read by every lane before slist overwrites it
   const float hkf = hk == 0xffffffffu ? INF : ordered_to_float(hk);
   int ns = 0;
@@ -1239,7 +1261,7 @@ __global__ void __launch_bounds__(128, 4) k_rerank_cert(RerankArgs a) {
   __syncwarp();
   // the k smallest keys are the survivors' smallest (every other key is
   // padding, above all real keys)
-  uint64_t best = KEY_NONE;
+  best = KEY_NONE;
   for (int i0 = 0; i0 < ns; i0 += 32)
     best = warp_merge_smallest32(best, i0 + lane < ns ? sk[i0 + lane] : KEY_NONE);
   uint64_t* outb = sk;  // reuse: 32 sorted keys
