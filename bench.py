@@ -1034,7 +1034,7 @@ def run_serve(args, rank, world):
     forms = {
         "plain": [dict(form=mv.FORM_PLAIN, nprobe=8), dict(form=mv.FORM_PLAIN, rerank_factor=2),
                   dict(form=mv.FORM_PLAIN)],
-        "fast": [dict(form=mv.FORM_FAST, nprobe=8, rerank=256),
+        "fast": [dict(form=mv.FORM_FAST, nprobe=8, rerank=224),
                  dict(form=mv.FORM_FAST, rerank_factor=2), dict(form=mv.FORM_FAST, rerank=40)],
     }
     rng = np.random.default_rng(np.random.SeedSequence(20261203).spawn(8)[6])
@@ -1137,7 +1137,7 @@ def run_serve(args, rank, world):
             "forms": {"plain": "IVF-PQ plain nprobe 8; SQ8 integer keys from the tensor cores "
                                "(exact for s8 codes at d <= 1040) + FP32 rerank of 2k; Flat exact "
                                "FP32 (certified tensor-core shortlist)",
-                      "fast": "IVF-PQ fast nprobe 8 rerank 256; SQ8 as plain; Flat BF16 + FP32 "
+                      "fast": "IVF-PQ fast nprobe 8 rerank 224; SQ8 as plain; Flat BF16 + FP32 "
                               "rerank of max(k, 40)"},
             "results": results,
             "setup_s": round(setup_s, 1),
@@ -1609,7 +1609,7 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.rerank is None:
-        args.rerank = 256 if args.workload == "ivfpq" else 4 * args.k
+        args.rerank = 224 if args.workload == "ivfpq" else 4 * args.k
     world = _env_int("WORLD_SIZE", 1)
     rank = _env_int("RANK", 0)
 

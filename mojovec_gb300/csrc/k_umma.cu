@@ -258,10 +258,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 // with the smallest published one, which can only drop keys that are not
 // among the row's K smallest over all segments. At the end each thread writes its heap (unsorted,
 // KEY_NONE padded to ncp) to out[(row * nseg + seg) * ncp + j].
-// Pending slots per row: at least 32, up to 64 when shared memory allows.
-// The warp drains when any row has more than pend - 32 (a 32-column chunk
-// per check), so a larger buffer means fewer, fuller drains.
-constexpr int TOPK_PEND_MIN = 32, TOPK_PEND_MAX = 64;
+// Pending slots per row: at least 16, up to 64 when shared memory allows.
+// The warp drains when any row has more than pend - 4 (a check after every
+// group of 4 columns), so a larger buffer means fewer, fuller drains.
+constexpr int TOPK_PEND_MIN = 16, TOPK_PEND_MAX = 64;
 
 __device__ __forceinline__ void heap_replace_top(uint64_t* h, int K, uint64_t key) {
   int i = 0;
@@ -643,9 +643,9 @@ __global__ void __launch_bounds__(64 + 128 * EG, 1)
                                        (uint32_t)(col0 + j);
                 pc += pass ? 1 : 0;
               }
+              if (__any_sync(0xffffffffu, pc > g.pend - 4)) drain();
             }
           }
-          if (__any_sync(0xffffffffu, pc > g.pend - 32)) drain();
         }
       }
       tc_fence_before();
@@ -1202,6 +1202,13 @@ TopkCfg topk_cfg(int nkb, int nc, bool f8 = false) {
     return {64, 1, topk_pend_fit(nkb, 64, nc, 1, f8)};
   }
   const int bn = nkb <= 2 ? 128 : 64;
+  // Two epilogue groups (8 warps, each group half of every tile's columns
+  // with heaps of its own) when they fit beside the tiles: the per-row heap
+  // epilogue, not the MMAs, bounds this kernel.
+  if (bn == 128 && !f8) {
+    const int p2 = topk_pend_fit(nkb, bn, nc, 2, f8);
+    if (p2 >= TOPK_PEND_MIN) return {bn, 2, p2};
+  }
   return {bn, 1, topk_pend_fit(nkb, bn, nc, 1, f8)};
 }
 size_t topk_smem(int nkb, const TopkCfg& c, int nc, bool f8 = false) {
@@ -1289,6 +1296,8 @@ void launch_umma_topk(const __nv_bfloat16* X, int64_t nx, const __nv_bfloat16* Y
       l2m ? go(k_umma_topk<64, true, 1, false, true>, 192)
           : go(k_umma_topk<64, false, 1, false, true>, 192);
     }
+  } else if (c.bn == 128 && c.eg == 2) {
+    l2m ? go(k_umma_topk<128, true, 2>, 320) : go(k_umma_topk<128, false, 2>, 320);
   } else if (c.bn == 128) {
     l2m ? go(k_umma_topk<128, true, 1>, 192) : go(k_umma_topk<128, false, 1>, 192);
   } else {
