@@ -70,7 +70,10 @@ typedef struct mv_search_params {
                           1 = FP16 tables, 3 = bank-rotated 32-bit fixed-point tables
                           (M a multiple of 4 and at least 8; else FP32), 4 = FP32
                           tables with the probed lists staged in shared memory by
-                          bulk copies. 0, 2 and 4 return the same bits */
+                          bulk copies, 6 = bank-rotated fixed-point tables with one
+                          staging slot per candidate and a range select (M a
+                          multiple of 4 up to 32, d / M = 4 or 8; else an error).
+                          0, 2 and 4 return the same bits */
   int32_t coarse_path; /* fast form, BF16 coarse step: 0 = automatic, 1 = GEMM with a
                           per-row top-k epilogue, 2 = distance matrix then one warp
                           per query selecting its lists, 3 = two-pass GEMM (bucket
@@ -83,8 +86,9 @@ typedef struct mv_search_params {
   int32_t flat_e4m3;   /* fast form, Flat: 1 = shortlist from an E4M3 (FP8) GEMM with
                           per-row scales instead of BF16 (exact FP32 rerank either way) */
   int32_t rerank_fp32; /* fast form, IVF-PQ: 1 = every shortlisted row reranked from its FP32
-                          copy; 0 (default) = a certified BF16 prescreen first, which
-                          provably leaves the results unchanged */
+                          copy; 0 (default, k <= 32) = a certified prescreen from an
+                          8-bit copy of the rows first, which provably leaves the
+                          results unchanged */
 } mv_search_params;
 
 /* ---- library / context ---------------------------------------------- */
