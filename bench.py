@@ -799,7 +799,7 @@ def run_batch(args, rank, world):
     nprobe = rng.integers(8, 257, size=nq).astype(np.int32)
     k = rng.choice(np.array([1, 10, 100], np.int32), size=nq)
     rerank = 200
-    plan = mv.IVFPQBatchPlan(ix, nq, 256, 100, rerank=rerank)
+    plan = mv.IVFPQBatchPlan(ix, nq, 256, 100, rerank=rerank, lut=args.lut)
     plan.set_queries(queries, nprobe, k)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
@@ -827,7 +827,7 @@ def run_batch(args, rank, world):
     t0 = time.perf_counter()
     e2e_steps = max(2, min(args.steps, 5))
     for _ in range(e2e_steps):
-        ix.search_batch(queries, nprobe, k, rerank=rerank)
+        ix.search_batch(queries, nprobe, k, rerank=rerank, lut=args.lut)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     # recall@10 on a sample of the k >= 10 queries against the fast flat
     # search with a deep exact rerank (BF16 shortlist of 400, FP32 distances)

@@ -1016,14 +1016,13 @@ __global__ void __launch_bounds__(FT) k_rerank_fast(RerankArgs a) {
 // k_rerank_fast's arithmetic, so the results are the ones the full FP32
 // pass gives.
 //
-// The 8-bit rows are gathered 32 at a time into a two-round ring in shared
-// memory with asynchronous 16-byte copies: round i + 2's copies are issued
-// as soon as round i is decoded, so every warp keeps two rounds of row
-// bytes in flight. Decoding reads one 4-byte word of every row per lane
-// (bank-conflict free), and a transposing butterfly gives lane l row l's sum.
-constexpr int RC_ROWS = 32;
-
-__host__ __device__ constexpr size_t rerank_cert_warp_bytes(int d, int R) {
+// The 8-bit rows are gathered RC_ROWS at a time into a two-round ring in
+// shared memory with asynchronous 16-byte copies: round i + 2's copies are
+// issued as soon as round i is decoded, so every warp keeps two rounds of
+// row bytes in flight. Decoding reads one 4-byte word of every row per lane
+// (bank-conflict free), and a transposing butterfly gives each lane a row's
+// sum.
+__host__ __device__ constexpr size_t rerank_cert_warp_bytes(int d, int R, int RC_ROWS) {
   // query | 2 x 32 rows of d8 bytes | survivors' keys (R) | lower ends |
   // positions | upper ends / survivor list
   return ((((size_t)d * 4 + 15) & ~size_t(15)) + 2 * RC_ROWS * (size_t)(((d + 15) & ~15)) +
@@ -1039,7 +1038,10 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-__global__ void __launch_bounds__(128, 4) k_rerank_cert(RerankArgs a) {
+// RC_ROWS rows per round (32, or 16 with half the accumulators, registers
+// and ring for more warps per SM).
+template <int RC_ROWS>
+__global__ void __launch_bounds__(128, RC_ROWS == 32 ? 4 : 6) k_rerank_cert(RerankArgs a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int d = a.d, d8 = a.d8;
   const int nwarps = blockDim.x >> 5;
@@ -1047,7 +1049,7 @@ __global__ void __launch_bounds__(128, 4) k_rerank_cert(RerankArgs a) {
   const int64_t row = (int64_t)blockIdx.x * nwarps + warp;
   if (row >= a.nq) return;  // warps are independent: no block-wide barrier below
   const size_t qbytes = ((size_t)d * 4 + 15) & ~size_t(15);
-  unsigned char* base = smraw + (size_t)warp * rerank_cert_warp_bytes(d, a.R);
+  unsigned char* base = smraw + (size_t)warp * rerank_cert_warp_bytes(d, a.R, RC_ROWS);
   float* qv = reinterpret_cast<float*>(base);
   unsigned char* ring = base + qbytes;                       // 2 x RC_ROWS rows of d8 bytes
   const size_t rbytes = (size_t)RC_ROWS * d8;
@@ -1123,7 +1125,7 @@ __global__ void __launch_bounds__(128, 4) k_rerank_cert(RerankArgs a) {
   }
   for (int t = 0; t < nrounds; ++t) {
     const int c0 = t * RC_ROWS;
-    const int c = c0 + lane;
+    const int c = c0 + (lane & (RC_ROWS - 1));
     const uint32_t mine = c < a.R ? spos[c] : 0xffffffffu;
     const float2 meta = mine != 0xffffffffu ? __ldg(a.rmeta + mine) : make_float2(0.0f, 0.0f);
     cp_async_wait<1>();  // round t's group has landed (round t + 1's may be in flight)
@@ -1170,9 +1172,10 @@ __global__ void __launch_bounds__(128, 4) k_rerank_cert(RerankArgs a) {
     }
     __syncwarp();  // every lane has read the slot before it is refilled
     issue(t + 2);
-    // transposing butterfly: lane l ends with row c0 + l's sum
+    // transposing butterfly: lane l ends with row c0 + (l mod RC_ROWS)'s sum
+    // (with 16 rows, lanes l and l + 16 add their halves at the end)
 #pragma unroll
-    for (int w = 16; w >= 1; w >>= 1) {
+    for (int w = RC_ROWS / 2; w >= 1; w >>= 1) {
       const bool upper = (lane & w) != 0;
 #pragma unroll
       for (int i = 0; i < w; ++i) {
@@ -1181,7 +1184,8 @@ __global__ void __launch_bounds__(128, 4) k_rerank_cert(RerankArgs a) {
         acc[i] = keep + __shfl_xor_sync(0xffffffffu, send, w);
       }
     }
-    if (c < a.R) {
+    if constexpr (RC_ROWS == 16) acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], 16);
+    if (lane < RC_ROWS && c < a.R) {
       float lo = INF, hi = INF;  // empty slots never survive
       if (mine != 0xffffffffu) {
         const float tv = acc[0];
@@ -1522,13 +1526,17 @@ void launch_rerank_fast(RerankArgs a, cudaStream_t s) {
   if (a.nq == 0) return;
   a.kp = next_pow2(a.k);
   const size_t qbytes = ((size_t)a.d * 4 + 15) & ~size_t(15);
-  const size_t wbytes = rerank_cert_warp_bytes(a.d, a.R);
+  // rows per round of the certified rerank: 16 (80 registers, six CTAs of
+  // four warps per SM) measured 0.161 ms against 0.168 ms for 32 at the
+  // 1M x 128 headline shape
+  constexpr int kRows = 16;
+  const size_t wbytes = rerank_cert_warp_bytes(a.d, a.R, kRows);
   const int cw = (int)std::min<size_t>(4, (96 * 1024) / wbytes);  // warps per CTA
   if (a.raw8 && a.rmeta && a.dim8 && a.d8 == rerank8_row_bytes(a.d) && a.k <= 32 && a.R >= 32 &&
       cw >= 1) {
     const size_t csmem = (size_t)cw * wbytes;
-    smem_attr(k_rerank_cert, csmem);
-    k_rerank_cert<<<(unsigned)((a.nq + cw - 1) / cw), cw * 32, csmem, s>>>(a);
+    smem_attr(k_rerank_cert<kRows>, csmem);
+    k_rerank_cert<kRows><<<(unsigned)((a.nq + cw - 1) / cw), cw * 32, csmem, s>>>(a);
     count_launch();
     MV_CHECK_CUDA(cudaGetLastError());
     return;

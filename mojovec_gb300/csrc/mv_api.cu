@@ -1346,24 +1346,36 @@ int32_t mv_ivfpq_search(mv_ivfpq* ix, const float* x, int64_t nq, int32_t k,
   return guard(ix->ctx, [&] {
     check_search_args(nq, k);
     if (nq == 0) return;
-    SlotLease lease(ix->ctx);
-    cudaStream_t s = lease.stream();
-    DevBuf& io = lease.slot->io;
+    // Large batches run as two halves on two streams (each with its own
+    // scratch), so that the second half's query copy and the first half's
+    // result copy overlap the other half's kernels. A query's results do not
+    // depend on the batch it is searched in.
+    constexpr int64_t kOverlapMin = 8192;
+    const int parts = nq >= kOverlapMin ? 2 : 1;
+    std::unique_ptr<SlotLease> leases[2];
+    for (int h = 0; h < parts; ++h) leases[h].reset(new SlotLease(ix->ctx));
     const size_t fl = filter ? (size_t)filter_len : 0;
-    io.ensure(ws_bytes((size_t)nq * ix->d, 4) + ws_bytes((size_t)nq * k, 4) +
-              ws_bytes((size_t)nq * k, 8) + ws_bytes(fl + 1, 1));
-    Arena ar(io);
-    float* dx = ar.take<float>((size_t)nq * ix->d);
-    float* dd = ar.take<float>((size_t)nq * k);
-    int64_t* dl = ar.take<int64_t>((size_t)nq * k);
-    uint8_t* df = ar.take<uint8_t>(fl + 1);
-    h2d(dx, x, sizeof(float) * nq * ix->d, s);
-    if (fl) h2d(df, filter, fl, s);
-    ivfpq_search_any(ix, dx, nq, k, fl ? df : nullptr, (int64_t)fl, params, dd, dl,
-                     lease.slot->ws, s);
-    d2h(distances, dd, sizeof(float) * nq * k, s);
-    d2h(labels, dl, sizeof(int64_t) * nq * k, s);
-    check_kernel_errors(ix->ctx, s);
+    const int64_t per = (nq + parts - 1) / parts;
+    for (int h = 0; h < parts; ++h) {
+      const int64_t q0 = h * per, nh = std::min(per, nq - q0);
+      cudaStream_t s = leases[h]->stream();
+      DevBuf& io = leases[h]->slot->io;
+      io.ensure(ws_bytes((size_t)nh * ix->d, 4) + ws_bytes((size_t)nh * k, 4) +
+                ws_bytes((size_t)nh * k, 8) + ws_bytes(fl + 1, 1));
+      Arena ar(io);
+      float* dx = ar.take<float>((size_t)nh * ix->d);
+      float* dd = ar.take<float>((size_t)nh * k);
+      int64_t* dl = ar.take<int64_t>((size_t)nh * k);
+      uint8_t* df = ar.take<uint8_t>(fl + 1);
+      h2d(dx, x + q0 * ix->d, sizeof(float) * nh * ix->d, s);
+      if (fl) h2d(df, filter, fl, s);
+      ivfpq_search_any(ix, dx, nh, k, fl ? df : nullptr, (int64_t)fl, params, dd, dl,
+                       leases[h]->slot->ws, s);
+      d2h(distances + q0 * k, dd, sizeof(float) * nh * k, s);
+      d2h(labels + q0 * k, dl, sizeof(int64_t) * nh * k, s);
+    }
+    for (int h = 0; h + 1 < parts; ++h) sync(leases[h]->stream());
+    check_kernel_errors(ix->ctx, leases[parts - 1]->stream());
   });
 }
 

@@ -303,7 +303,7 @@ class IndexIVFPQ:
                                           _p(lab)))
         return dist, lab
 
-    def search_batch(self, x, nprobe, k, rerank: int = 0, coarse_fp32: bool = False):
+    def search_batch(self, x, nprobe, k, rerank: int = 0, coarse_fp32: bool = False, lut=None):
         """Fast-form search with per-query nprobe and k (mv_ivfpq_search_batch).
         Returns (distances, labels) of shape (n, max(k)); slots past a
         query's k read 1e38 / -1."""
@@ -314,7 +314,7 @@ class IndexIVFPQ:
         kmax = int(k.max()) if n else 1
         dist = np.empty((n, kmax), np.float32)
         lab = np.empty((n, kmax), np.int64)
-        p = _params(FORM_FAST, 0, rerank, coarse_fp32)
+        p = _params(FORM_FAST, 0, rerank, coarse_fp32, lut=lut)
         check(_lib.load().mv_ivfpq_search_batch(self._h, _p(x), n, _p(nprobe), _p(k), kmax,
                                                 C.byref(p), _p(dist), _p(lab)))
         return dist, lab
