@@ -397,8 +397,10 @@ def run_gpu(args, rank, world):
     fast_form = args.form in ("fast", "batched")
     workload = f"ivfpq_{nb}x128_nlist4096_M16_nq{nq}_k10"
     # the fast scan's kernel: the bank-rotated table scan unless a variant is named
-    scan_kernel = ("k_ivfpq_scan_rt" if args.lut == 6 else "k_ivfpq_scan_fast") \
-        if fast_form else "k_ivfpq_scan_plain"
+    # the fast scan's ADC kernel: by default (and lut 7) the two-kernel scan's
+    # k_ivfpq_rows, whose per-query select is timed with it in the scan stage
+    scan_kernel = ({6: "k_ivfpq_scan_rt", None: "k_ivfpq_rows", 0: "k_ivfpq_rows", 7: "k_ivfpq_rows"}
+                   .get(args.lut, "k_ivfpq_scan_fast")) if fast_form else "k_ivfpq_scan_plain"
     traffic = None  # DRAM bytes per launch from the committed ncu capture of this config
     try:
         t = json.load(open(os.path.join(ROOT, "profiles", "dram_traffic.json"))).get(
@@ -424,8 +426,9 @@ def run_gpu(args, rank, world):
         "config": {
             "workload": workload,
             "form": ("fast: two-pass BF16 tcgen05 coarse GEMM + FP32 recheck, per-query table from the "
-                     "FP16 codebook (codes read from L2), histogram select, certified rerank from an "
-                     "8-bit row copy (the full FP32 rerank's results)"
+                     "FP16 codebook (codes read from L2) writing per-candidate distance rows, warp-per-query "
+                     "streaming select, certified rerank from an 8-bit row copy (the full FP32 rerank's "
+                     "results)"
                      + ("; batched: one plan (persistent scan, tuned launch shapes) replayed as a "
                         "CUDA graph" if batched else ""))
                     if fast_form else "plain FP32 (reference algorithm, bit-exact)",
@@ -459,8 +462,10 @@ def run_gpu(args, rank, world):
             "frac": round(achieved / hbm_peak, 4),
             "traffic": traffic,
             "algorithmic_bytes_per_launch": code_bytes,
-            "note": "codes (16 MB) are L2-resident at this size: DRAM traffic is far below the "
-                    "algorithmic bytes; the limiter is the shared-memory table (smem_lookups)",
+            "note": "codes (16 MB) are L2-resident at this size: DRAM traffic (codes, and the "
+                    "distance rows of the two-kernel scan) is far below the algorithmic bytes; the "
+                    "scan is instruction-issue-bound (table lookups and the candidate walk), see "
+                    "smem_lookups for the shared-memory table's own bound",
             "launch_ms": round(per_launch_ms, 4),
             "smem_lookups": smem_roofline(code_bytes, per_launch_ms, peaks, clk),
         },
@@ -1582,8 +1587,9 @@ def main():
     ap.add_argument("--form", default="fast", choices=["plain", "fast", "batched"])
     ap.add_argument("--nprobe", type=int, default=8)
     ap.add_argument("--lut", type=int, default=None,
-                    help="ivfpq workload: fast-form scan variant (default FP32 tables; 6 = bank-rotated "
-                         "fixed-point tables with per-candidate slots)")
+                    help="ivfpq workload: fast-form scan variant (default: FP32 tables, two-kernel "
+                         "scan where it pays; 2 = single-kernel; 6 = bank-rotated fixed-point tables "
+                         "with per-candidate slots; 7 = two-kernel always)")
     ap.add_argument("--rerank", type=int, default=None,
                     help="shortlist depth (IVF-PQ default 256, flat default k * 4)")
     ap.add_argument("--nb", type=int, default=NB, help="base rows (profiling runs use fewer)")

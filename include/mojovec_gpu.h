@@ -66,14 +66,16 @@ typedef struct mv_search_params {
   int32_t rerank;      /* fast form: shortlist depth for the exact FP32 rerank
                           (0 = no rerank) */
   int32_t coarse_fp32; /* fast form: 1 = FP32 SIMT coarse instead of BF16 */
-  int32_t lut_fp16;    /* fast form, table and scan variant: 0 or 2 = FP32 tables,
+  int32_t lut_fp16;    /* fast form, table and scan variant: 0 or 2 = FP32 tables (0 may
+                          run them as two kernels, per-candidate distance rows then a
+                          per-query select, where that pays; 7 always does),
                           1 = FP16 tables, 3 = bank-rotated 32-bit fixed-point tables
                           (M a multiple of 4 and at least 8; else FP32), 4 = FP32
                           tables with the probed lists staged in shared memory by
                           bulk copies, 6 = bank-rotated fixed-point tables with one
                           staging slot per candidate and a range select (M a
                           multiple of 4 up to 32, d / M = 4 or 8; else an error).
-                          0, 2 and 4 return the same bits */
+                          0, 2, 4 and 7 return the same bits */
   int32_t coarse_path; /* fast form, BF16 coarse step: 0 = automatic, 1 = GEMM with a
                           per-row top-k epilogue, 2 = distance matrix then one warp
                           per query selecting its lists, 3 = two-pass GEMM (bucket

@@ -55,6 +55,13 @@ bool ivfpq_rt_supported(const FastScanArgs& a);
 // persistent grid of persistent_ctas CTAs.
 void launch_ivfpq_scan_rt(FastScanArgs a, cudaStream_t s, int nt, int persistent_ctas);
 
+// Two-kernel scan (k_ivfpq_rows.cu): per-candidate distance rows, then a
+// per-query select; the same shortlist as the single-kernel FP32-table scan.
+// smax bounds every query's candidate count (the nprobe longest lists); the
+// rows take nq * ivfpq_rows_stride(smax) words of scratch.
+int64_t ivfpq_rows_stride(int64_t smax);
+void launch_ivfpq_scan_rows(FastScanArgs f, uint32_t* dist, int64_t smax, cudaStream_t s, int nt);
+
 struct RerankArgs {
   const float* q;
   int64_t nq;
@@ -118,9 +125,11 @@ size_t fast_scan_smem(const FastScanArgs& a);
 // The staged scan (k_ivfpq_scan.cu); returns false, launching nothing, when
 // its shared memory would not fit (the caller runs the unstaged kernel).
 bool launch_ivfpq_scan_staged(FastScanArgs a, cudaStream_t s, int nt, int persistent_ctas, int E);
-// lut: 0 or 2 = FP32 tables read with codes from global memory; 6 = the
+// lut: 0 or 2 = FP32 tables read with codes from global memory (with 0 the
+// search itself may take the two-kernel scan instead, same results); 6 = the
 // bank-rotated fixed-point table scan with per-candidate slots
-// (k_ivfpq_rt.cu) or an error; 1 = FP16 tables with a per-query
+// (k_ivfpq_rt.cu) or an error; 7 = the two-kernel scan (distance rows and a
+// per-query select, launched by the search itself); 1 = FP16 tables with a per-query
 // power-of-two scale (FP32 sums), 3 = bank-rotated fixed-point tables in
 // the per-candidate layout where M allows (else FP32), 4 = FP32 tables with
 // codes and terms staged in shared memory by bulk copies (the unstaged

@@ -142,9 +142,11 @@ class Context:
 
 def _params(form=None, nprobe=0, rerank=0, coarse_fp32=False, lut_fp16=False, coarse_path=0,
             plain_scan=False, e4m3=False, rerank_fp32=False, lut=None):
-    """lut: fast-form table / scan variant (0 or 2 FP32, 1 FP16, 3 bank-rotated
-    fixed point, 4 FP32 with staged lists, 6 bank-rotated fixed point with
-    per-candidate slots and a range select); None takes it from lut_fp16."""
+    """lut: fast-form table / scan variant (0 FP32 tables, with the two-kernel
+    scan where it pays; 2 FP32 in one kernel; 1 FP16; 3 bank-rotated fixed
+    point; 4 FP32 with staged lists; 6 bank-rotated fixed point with
+    per-candidate slots and a range select; 7 the two-kernel scan: distance
+    rows then a per-query select); None takes it from lut_fp16."""
     p = SearchParams()
     p.rerank_fp32 = 1 if rerank_fp32 else 0
     p.coarse_path = int(coarse_path)
