@@ -30,7 +30,7 @@ namespace {
 
 constexpr uint32_t ROW_EXCLUDED = 0xffffffffu;
 
-template <int NT>
+template <int NT, int CPT>
 __global__ void __launch_bounds__(NT, 1024 / NT)
     k_ivfpq_rows(FastScanArgs a, uint32_t* __restrict__ dist, int64_t smax) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -85,42 +85,51 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
   }
   uint32_t* drow = dist + row * smax;
   int p = 0;  // per-thread probe cursor (candidate indices only grow)
-  // Two candidates per thread per step: both rows' loads are issued before
-  // either table walk.
-  for (int j0 = 0; j0 < total; j0 += 2 * NT) {
-    const int c0 = j0 + tid, c1 = c0 + NT;
-    const bool has0 = c0 < total, has1 = c1 < total;
-    // Lanes without a candidate keep their cursor and use position 0 (a
-    // valid entry: the index is not empty), so no load leaves the lists.
-    if (has0)
-      while (pbeg[p + 1] <= c0) ++p;
-    int64_t pos0 = has0 ? poff[p] + (c0 - pbeg[p]) : 0;
-    const float t0 = has0 ? pterm[p] : 0.0f;
-    int p1 = p;
-    if (has1)
-      while (pbeg[p1 + 1] <= c1) ++p1;
-    int64_t pos1 = has1 ? poff[p1] + (c1 - pbeg[p1]) : 0;
-    const float t1 = has1 ? pterm[p1] : 0.0f;
-    bool keep0 = has0, keep1 = has1;
-    if ((has0 && (pos0 < 0 || pos0 >= a.ntotal)) || (has1 && (pos1 < 0 || pos1 >= a.ntotal))) {
-      atomicExch(a.err, 109);  // never expected: skip both, stay warp-uniform
-      pos0 = 0;
-      pos1 = 0;
-      keep0 = keep1 = false;
+  // CPT candidates per thread per step: every row's loads are issued before
+  // any table walk.
+  for (int j0 = 0; j0 < total; j0 += CPT * NT) {
+    int64_t pos[CPT];
+    float t[CPT];
+    bool has[CPT], keep[CPT];
+    bool bad = false;
+#pragma unroll
+    for (int u = 0; u < CPT; ++u) {
+      const int c = j0 + tid + u * NT;
+      has[u] = c < total;
+      // Lanes without a candidate keep their cursor and use position 0 (a
+      // valid entry: the index is not empty), so no load leaves the lists.
+      if (has[u])
+        while (pbeg[p + 1] <= c) ++p;
+      pos[u] = has[u] ? poff[p] + (c - pbeg[p]) : 0;
+      t[u] = has[u] ? pterm[p] : 0.0f;
+      keep[u] = has[u];
+      bad = bad || (has[u] && (pos[u] < 0 || pos[u] >= a.ntotal));
+    }
+    if (bad) {
+      atomicExch(a.err, 109);  // never expected: skip the step, stay warp-uniform
+#pragma unroll
+      for (int u = 0; u < CPT; ++u) {
+        pos[u] = 0;
+        keep[u] = false;
+      }
     }
     if (a.filter) {  // filtered ids never enter the shortlist
-      const uint32_t id0 = a.ids[pos0], id1 = a.ids[pos1];
-      if ((int64_t)id0 < a.filter_len && a.filter[id0] != 0) keep0 = false;
-      if ((int64_t)id1 < a.filter_len && a.filter[id1] != 0) keep1 = false;
+#pragma unroll
+      for (int u = 0; u < CPT; ++u) {
+        const uint32_t id = a.ids[pos[u]];
+        if ((int64_t)id < a.filter_len && a.filter[id] != 0) keep[u] = false;
+      }
     }
-    const float v0 = a.vterm ? a.vterm[pos0] : 0.0f;
-    const float v1 = a.vterm ? a.vterm[pos1] : 0.0f;
-    const float d0 = adc_fast(lut, a.codes + pos0 * M, M, t0 + v0);
-    const float d1 = adc_fast(lut, a.codes + pos1 * M, M, t1 + v1);
-    // ROW_EXCLUDED marks no key: a NaN distance keeps the word below it
-    if (has0) drow[c0] = keep0 ? min(float_to_ordered(d0), ROW_EXCLUDED - 1u) : ROW_EXCLUDED;
-    if (has1) drow[c1] = keep1 ? min(float_to_ordered(d1), ROW_EXCLUDED - 1u) : ROW_EXCLUDED;
-    if (has0) p = p1;
+    float v[CPT];
+#pragma unroll
+    for (int u = 0; u < CPT; ++u) v[u] = a.vterm ? a.vterm[pos[u]] : 0.0f;
+#pragma unroll
+    for (int u = 0; u < CPT; ++u) {
+      const float dd = adc_fast(lut, a.codes + pos[u] * M, M, t[u] + v[u]);
+      // ROW_EXCLUDED marks no key: a NaN distance keeps the word below it
+      if (has[u]) drow[j0 + tid + u * NT] = keep[u] ? min(float_to_ordered(dd), ROW_EXCLUDED - 1u)
+                                                   : ROW_EXCLUDED;
+    }
   }
 }
 
@@ -573,10 +582,10 @@ void launch_ivfpq_scan_rows(FastScanArgs f, uint32_t* dist, int64_t smax, cudaSt
     smem_limit(kernel, smem);
     kernel<<<(unsigned)nq, threads, smem, s>>>(f, dist, stride);
   };
-  if (nt == 64) go(k_ivfpq_rows<64>, 64);
-  else if (nt == 128) go(k_ivfpq_rows<128>, 128);
-  else if (nt == 512) go(k_ivfpq_rows<512>, 512);
-  else go(k_ivfpq_rows<256>, 256);
+  if (nt == 64) go(k_ivfpq_rows<64, 2>, 64);
+  else if (nt == 128) go(k_ivfpq_rows<128, 2>, 128);
+  else if (nt == 512) go(k_ivfpq_rows<512, 2>, 512);
+  else go(k_ivfpq_rows<256, 2>, 256);
   count_launch();
   SelArgs sa;
   sa.dist = dist;
