@@ -8,11 +8,11 @@ top-k with global ids; one gather and this k-way merge give the unsharded
 result, with the canonical tie rule of every search here: ascending
 (distance, id) for L2, descending inner product then ascending id for IP
 (index/index_flat.mojo:260-325 and index/index_ivf_pq.mojo:326-360 keep the
-k smallest keys; the tie rule is this build's canonical order). Empty slots
+k smallest keys; the tie rule is the library's canonical order). Empty slots
 (label -1) sort after every result.
 
-The GPU build runs replicas only (one GPU per process); this merge is the
-exchange step a sharded deployment adds, tested on CPU-split inputs.
+The library runs one index per GPU process (replicas); this merge is the
+exchange step a sharded deployment adds on the host.
 """
 
 from __future__ import annotations
