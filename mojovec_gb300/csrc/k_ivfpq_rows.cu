@@ -507,7 +507,8 @@ __global__ void __launch_bounds__(SS_WARPS * 32) k_row_select_stream(SelArgs a) 
   const int R = a.R;
   const unsigned lt = (1u << lane) - 1u;
   uint64_t T = KEY_NONE;
-  int m = 0, p = 0;
+  uint32_t Tw = 0xffffffffu;  // T's distance word
+  int m = 0, p = 0;           // p: probe cursor, advanced only for words that may enter
   // words i0 + 4 lane .. + 3 of each 128-word round (the row holds smax
   // >= roundup(n, 4) words, so the vector load stays in the row)
   auto load4 = [&](int i0) {
@@ -522,6 +523,7 @@ __global__ void __launch_bounds__(SS_WARPS * 32) k_row_select_stream(SelArgs a) 
     const uint4 n3 = load4(i0 + 384);
     if (m + 128 > SS_CAP) {
       T = warp_keep_smallest(buf, m, R, side, hist);
+      Tw = (uint32_t)(T >> 32);
       m = R;
     }
     const uint32_t w[4] = {cur.x, cur.y, cur.z, cur.w};
@@ -529,11 +531,12 @@ __global__ void __launch_bounds__(SS_WARPS * 32) k_row_select_stream(SelArgs a) 
     for (int u = 0; u < 4; ++u) {
       const int i = i0 + 4 * lane + u;
       uint64_t key = KEY_NONE;
-      bool in = false;
-      if (i < n) {
+      // a key below T has a word at or below T's; only those build the key
+      bool in = i < n && w[u] != ROW_EXCLUDED && w[u] <= Tw;
+      if (in) {
         while (pbeg[p + 1] <= i) ++p;
         key = ((uint64_t)w[u] << 32) | (uint32_t)(poff[p] + (i - pbeg[p]));
-        in = w[u] != ROW_EXCLUDED && key < T;
+        in = key < T;
       }
       const unsigned b = __ballot_sync(0xffffffffu, in);
       if (in) buf[m + __popc(b & lt)] = key;
