@@ -1029,6 +1029,34 @@ __host__ __device__ constexpr size_t rerank_cert_warp_bytes(int d, int R, int RC
           (size_t)R * 20 + 15) & ~size_t(15);
 }
 
+// The k-th smallest (1 <= k <= 64) of the warp's 64 values v0, v1 (value
+// r * 32 + lane in v_r): bitonic sort of the 64, then position k - 1.
+__device__ __forceinline__ uint32_t warp_kth_smallest64(uint32_t v0, uint32_t v1, int k) {
+  const int lane = threadIdx.x & 31;
+  uint32_t v[2] = {v0, v1};
+#pragma unroll
+  for (int size = 2; size <= 64; size <<= 1) {
+#pragma unroll
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      if (stride == 32) {  // size 64, ascending: the pair is (v0, v1) of one lane
+        const uint32_t lo = min(v[0], v[1]), hi = max(v[0], v[1]);
+        v[0] = lo;
+        v[1] = hi;
+      } else {
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          const int e = r * 32 + lane;
+          const uint32_t o = __shfl_xor_sync(0xffffffffu, v[r], stride);
+          const bool asc = (e & size) == 0, lower = (e & stride) == 0;
+          v[r] = lower == asc ? min(v[r], o) : max(v[r], o);
+        }
+      }
+    }
+  }
+  const int pos = k - 1;
+  return __shfl_sync(0xffffffffu, pos < 32 ? v[0] : v[1], pos & 31);
+}
+
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }
@@ -1211,17 +1239,20 @@ __global__ void __launch_bounds__(128, RC_ROWS == 32 ? 4 : 6) k_rerank_cert(Rera
   }
   cp_async_wait<0>();
   __syncwarp();
-  // the k-th smallest upper end over the whole shortlist: the 32 smallest
-  // (upper end, candidate) keys merged group by group (k <= 32). Bounding
-  // by each group's own k-th smallest instead leaves several times more
-  // survivors, as a query's k nearest rows spread over the groups.
-  uint64_t best = KEY_NONE;
-  for (int g0 = 0; g0 < a.R; g0 += 32) {
-    const int c = g0 + lane;
-    best = warp_merge_smallest32(best, c < a.R ? ((uint64_t)bhi[c] << 32) | (uint32_t)c : KEY_NONE);
+  // The bound: the k-th smallest upper end of a subset of the shortlist (k
+  // distinct candidates have upper ends at or below it, so it bounds the
+  // k-th smallest key; k <= 32). The subset is each lane's two smallest
+  // upper ends (64 values): it holds the whole shortlist's k smallest unless
+  // one lane holds three of them. Bounding by each group of 32's own k-th
+  // smallest instead leaves several times more survivors, as a query's k
+  // nearest rows spread over the groups.
+  uint32_t m1 = 0xffffffffu, m2 = 0xffffffffu;  // (ordered INF is below 0xffffffff)
+  for (int c = lane; c < a.R; c += 32) {
+    const uint32_t x = bhi[c];
+    m2 = min(m2, max(m1, x));
+    m1 = min(m1, x);
   }
-  const uint64_t kth = __shfl_sync(0xffffffffu, best, a.k - 1);
-  const uint32_t hk = kth != KEY_NONE ? (uint32_t)(kth >> 32) : 0xffffffffu;
+  const uint32_t hk = warp_kth_smallest64(m1, m2, a.k);
   __syncwarp();  // bhi is read by every lane before slist overwrites it
   const float hkf = hk == 0xffffffffu ? INF : ordered_to_float(hk);
   int ns = 0;
@@ -1265,7 +1296,7 @@ __global__ void __launch_bounds__(128, RC_ROWS == 32 ? 4 : 6) k_rerank_cert(Rera
   __syncwarp();
   // the k smallest keys are the survivors' smallest (every other key is
   // padding, above all real keys)
-  best = KEY_NONE;
+  uint64_t best = KEY_NONE;
   for (int i0 = 0; i0 < ns; i0 += 32)
     best = warp_merge_smallest32(best, i0 + lane < ns ? sk[i0 + lane] : KEY_NONE);
   uint64_t* outb = sk;  // reuse: 32 sorted keys
