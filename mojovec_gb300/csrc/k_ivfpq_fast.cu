@@ -1004,15 +1004,16 @@ __global__ void __launch_bounds__(FT) k_rerank_fast(RerankArgs a) {
 // distance is first computed from its 8-bit copy (a quarter of the FP32
 // bytes, one 128-byte line per row at d = 128) and turned into an interval
 // that provably holds the FP32 distance the exact pass computes. With y8 the
-// row the copy decodes to (y8_j = fmaf(s_j, 2^23 + u_j, a'_j), the FP32
+// row the copy decodes to (y8_j = fmaf(S_j, 1 + u_j 2^-15, a''_j), the FP32
 // expression the copy was made with) and r >= ||y - y8||: the prescreen
-// value's own summation error, the triangle inequality with r (L2) or
-// Cauchy-Schwarz with ||q|| and ||y8|| (IP), and the exact pass's summation
-// error (both bounded by gamma = (d + 64) * 2^-24 relative to the sum of
-// |terms|), with 2^-20 of slack for the bound arithmetic. The k-th smallest
-// upper end of any group of candidates bounds the query's k-th smallest
-// key; a candidate whose lower end exceeds it has k candidates strictly
-// closer and is dropped. The survivors are computed in FP32 with
+// value's own summation error, the triangle inequality with r (L2; widened
+// by the rounding of the per-query constants its one-FMA differences use)
+// or Cauchy-Schwarz with ||q|| and ||y8|| (IP), and the exact pass's
+// summation error (both bounded by gamma = (d + 64) * 2^-24 relative to the
+// sum of |terms|), with 2^-20 of slack for the bound arithmetic. The k-th
+// smallest upper end of any k or more candidates bounds the query's k-th
+// smallest key; a candidate whose lower end exceeds it has k candidates
+// strictly closer and is dropped. The survivors are computed in FP32 with
 // k_rerank_fast's arithmetic, so the results are the ones the full FP32
 // pass gives.
 //
@@ -1135,21 +1136,38 @@ __global__ void __launch_bounds__(128, RC_ROWS == 32 ? 4 : 6) k_rerank_cert(Rera
   };
   issue(0);
   issue(1);
+  const bool l2 = a.metric == MV_METRIC_L2;
   float qn = 0.0f;  // IP: upper bound on ||q||
-  if (a.metric != MV_METRIC_L2) {
+  float eq = 0.0f;  // L2: upper bound on ||t||, t_j = (q_j - a''_j) - fl(q_j - a''_j)
+  if (!l2) {
     for (int j = lane; j < d; j += 32) qn = fmaf(qv[j], qv[j], qn);
     for (int o = 16; o > 0; o >>= 1) qn += __shfl_xor_sync(0xffffffffu, qn, o);
     qn = sqrtf(qn * (1.0f + 2.0f * gam)) * up;
+  } else {
+    for (int j = lane; j < d; j += 32) {
+      const float x = qv[j], b = -a.dim8[j].x;
+      const float sm = x + b, bp = sm - x;
+      const float t = (x - (sm - bp)) + (b - bp);  // two-sum: x + b - sm exactly
+      eq = fmaf(t, t, eq);
+    }
+    for (int o = 16; o > 0; o >>= 1) eq += __shfl_xor_sync(0xffffffffu, eq, o);
+    eq = sqrtf(eq * (1.0f + 2.0f * gam)) * up;
   }
-  float q0[4], a0[4], s0[4];
+  // Element constants of the lane's first 128 elements. L2 computes each
+  // difference in one rounding as fma(-S, V, c) with c = fl(q - a''), which
+  // is (q - y8) + eta, |eta_j| <= |t_j| + 2^-24 |y8_j| (y8_j = fl(S V + a''),
+  // one rounding): the bound below widens r by eq + 2^-24 ||y8||. IP decodes
+  // y8 = fma(S, V, a''). Elements past d decode to 0 against a query
+  // element of 0 (byte 0 gives V = 1).
+  float q0[4], k0[4], m0[4];  // query; L2: (c, -S), IP: (a'', S)
 #pragma unroll
   for (int tt = 0; tt < 4; ++tt) {
     const int j = lane * 4 + tt;
     const bool in = j < d;
-    const float2 ds = in ? a.dim8[j] : make_float2(-8388608.0f, 1.0f);
+    const float2 ds = in ? a.dim8[j] : make_float2(-1.0f, 1.0f);
     q0[tt] = in ? qv[j] : 0.0f;
-    a0[tt] = ds.x;
-    s0[tt] = ds.y;
+    k0[tt] = l2 ? q0[tt] - ds.x : ds.x;
+    m0[tt] = l2 ? -ds.y : ds.y;
   }
   for (int t = 0; t < nrounds; ++t) {
     const int c0 = t * RC_ROWS;
@@ -1162,39 +1180,37 @@ __global__ void __launch_bounds__(128, RC_ROWS == 32 ? 4 : 6) k_rerank_cert(Rera
     float acc[RC_ROWS];
 #pragma unroll
     for (int u = 0; u < RC_ROWS; ++u) acc[u] = 0.0f;
-    // lane: elements j .. j + 3 of every row (one 4-byte word); elements
-    // past d decode to 0 against a query element of 0
+    // lane: elements j .. j + 3 of every row (one 4-byte word)
     for (int j0 = 0; j0 < d; j0 += 128) {
       const int j = j0 + lane * 4;
       const bool jin = j < d;
-      float qj[4], aj[4], sj[4];
+      float qj[4], kj[4], mj[4];
 #pragma unroll
       for (int tt = 0; tt < 4; ++tt) {
-        if (j0 == 0) {  // the first 128 elements' query and steps stay in registers
+        if (j0 == 0) {  // the first 128 elements' constants stay in registers
           qj[tt] = q0[tt];
-          aj[tt] = a0[tt];
-          sj[tt] = s0[tt];
+          kj[tt] = k0[tt];
+          mj[tt] = m0[tt];
         } else {
           const bool in = j + tt < d;
-          const float2 ds = in ? a.dim8[j + tt] : make_float2(-8388608.0f, 1.0f);
+          const float2 ds = in ? a.dim8[j + tt] : make_float2(-1.0f, 1.0f);
           qj[tt] = in ? qv[j + tt] : 0.0f;
-          aj[tt] = ds.x;
-          sj[tt] = ds.y;
+          kj[tt] = l2 ? qj[tt] - ds.x : ds.x;
+          mj[tt] = l2 ? -ds.y : ds.y;
         }
       }
       const unsigned char* rowp = buf + j;
 #pragma unroll
       for (int u = 0; u < RC_ROWS; ++u, rowp += d8) {
         const uint32_t w = jin ? *reinterpret_cast<const uint32_t*>(rowp) : 0u;
-        float y[4];
+        float e[4];  // L2: c - S V; IP: y8
 #pragma unroll
         for (int tt = 0; tt < 4; ++tt)
-          y[tt] = fmaf(sj[tt], __uint_as_float(__byte_perm(w, 0x4B00u, 0x5440u + tt)), aj[tt]);
-        if (a.metric == MV_METRIC_L2) {
-          const float d0 = qj[0] - y[0], d1 = qj[1] - y[1], d2 = qj[2] - y[2], d3 = qj[3] - y[3];
-          acc[u] = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, acc[u]))));
+          e[tt] = fmaf(mj[tt], __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u + 16u * tt)), kj[tt]);
+        if (l2) {
+          acc[u] = fmaf(e[0], e[0], fmaf(e[1], e[1], fmaf(e[2], e[2], fmaf(e[3], e[3], acc[u]))));
         } else {
-          acc[u] = fmaf(qj[0], y[0], fmaf(qj[1], y[1], fmaf(qj[2], y[2], fmaf(qj[3], y[3], acc[u]))));
+          acc[u] = fmaf(qj[0], e[0], fmaf(qj[1], e[1], fmaf(qj[2], e[2], fmaf(qj[3], e[3], acc[u]))));
         }
       }
     }
@@ -1218,12 +1234,13 @@ __global__ void __launch_bounds__(128, RC_ROWS == 32 ? 4 : 6) k_rerank_cert(Rera
       if (mine != 0xffffffffu) {
         const float tv = acc[0];
         const float r = meta.x, yn = meta.y;
-        if (!(fabsf(tv) < INF) || !(r < INF) || !(yn < INF)) {  // not finite: computed exactly
+        if (!(fabsf(tv) < INF) || !(r < INF) || !(yn < INF) || !(eq < INF)) {  // computed exactly
           lo = -INF;
           hi = INF;
-        } else if (a.metric == MV_METRIC_L2) {
-          const float slo = sqrtf(tv * (1.0f - 2.0f * gam)) * dn - r * up;
-          const float shi = sqrtf(tv * (1.0f + 2.0f * gam)) * up + r * up;
+        } else if (l2) {
+          const float rr = (r + eq + yn * 5.9604645e-08f) * up;  // r + ||eta||
+          const float slo = sqrtf(tv * (1.0f - 2.0f * gam)) * dn - rr * up;
+          const float shi = sqrtf(tv * (1.0f + 2.0f * gam)) * up + rr * up;
           const float m = fmaxf(slo, 0.0f);
           lo = m * m * (1.0f - 2.0f * gam) * dn;
           hi = shi * shi * (1.0f + 2.0f * gam) * up;
@@ -1334,12 +1351,14 @@ __global__ void k_dim_init(uint32_t* dimord, int d) {
   }
 }
 
-// Per dimension (a'_j, s_j) of the 8-bit copy: s_j a power of two and
+// Per dimension (a''_j, S_j) of the 8-bit copy: s_j a power of two and
 // a_j = floor(min_j / s_j) s_j with 255 s_j >= max_j - a_j (s_j = 1 for a
-// constant or non-finite dimension), stored as a'_j = a_j - 2^23 s_j so that
-// y8 = fmaf(s_j, 2^23 + u, a'_j) decodes a code from its float bits
-// 0x4B000000 | u. a'_j is exact while |a_j / s_j| < 2^23; every row bound is
-// computed from the decoded values, so the copy stays certified either way.
+// constant or non-finite dimension), stored as S_j = 2^15 s_j and
+// a''_j = a_j - S_j, so that y8 = fmaf(S_j, V, a''_j) decodes code u from
+// the float V = 1 + u 2^-15, whose bits are 0x3F800000 | (u << 8) (one
+// byte permute). a''_j is exact while |a_j / s_j| < 2^24 - 2^15; every row
+// bound is computed from the decoded values, so the copy stays certified
+// either way.
 __global__ void k_dim_steps(const uint32_t* __restrict__ dimord, int d, float2* __restrict__ dim8) {
   for (int j = threadIdx.x; j < d; j += blockDim.x) {
     const float lo = ordered_to_float(dimord[j]), hi = ordered_to_float(dimord[d + j]);
@@ -1353,7 +1372,7 @@ __global__ void k_dim_steps(const uint32_t* __restrict__ dimord, int d, float2* 
       }
       a = floorf(lo / s) * s;
     }
-    dim8[j] = make_float2(a - 8388608.0f * s, s);
+    dim8[j] = make_float2(a - 32768.0f * s, 32768.0f * s);
   }
 }
 
@@ -1374,10 +1393,11 @@ __global__ void k_rerank_rows8(const float* __restrict__ raw, int64_t n, int d, 
     if (j < d) {
       const float y = raw[r * d + j];
       const float2 as = dim8[j];
-      const float a = fmaf(8388608.0f, as.y, as.x);  // a_j (exact when a'_j is)
-      const float t = rintf((y - a) / as.y);
+      const float a = as.x + as.y;               // a_j (exact when a''_j is)
+      const float st = as.y * 3.0517578125e-05f;  // s_j = S_j 2^-15
+      const float t = rintf((y - a) / st);
       code = (uint32_t)(int)fminf(fmaxf(t, 0.0f), 255.0f);  // NaN -> 0
-      const float y8 = fmaf(as.y, __uint_as_float(0x4B000000u | code), as.x);
+      const float y8 = fmaf(as.y, __uint_as_float(0x3F800000u | (code << 8)), as.x);
       const float df = y - y8;
       finite = finite && isfinite(y) && isfinite(y8);
       e2 = fmaf(df, df, e2);

@@ -79,8 +79,9 @@ struct RerankArgs {
   int kp;                 // set by the launcher
   // Certified prescreen (k <= 32; all null: every candidate is computed in
   // FP32): 8-bit copies of the rows (d8 bytes each) with y8_j =
-  // fmaf(s_j, u_j, a_j) from the per-dimension (a_j, s_j) in dim8, and per
-  // row upper bounds on ||y - y8|| and (IP) on ||y8|| in rmeta.
+  // fmaf(S_j, 1 + u_j 2^-15, a''_j) from the per-dimension (a''_j, S_j) in
+  // dim8 (S_j = 2^15 s_j, a''_j = a_j - S_j), and per row upper bounds on
+  // ||y - y8|| and on ||y8|| in rmeta.
   const uint8_t* raw8 = nullptr;
   const float2* rmeta = nullptr;
   const float2* dim8 = nullptr;
@@ -94,7 +95,8 @@ inline int rerank8_row_bytes(int d) { return (d + 15) & ~15; }
 // per dimension j an offset a_j (the minimum over the rows) and a step s_j
 // (the smallest power of two with 255 s_j >= max_j - min_j), codes
 // u = round((y_j - a_j) / s_j), and per row upper bounds on ||y - y8|| and
-// ||y8|| with y8_j = fmaf(s_j, u_j, a_j). dimord holds 2 d words of scratch.
+// ||y8|| with y8_j = fmaf(S_j, 1 + u_j 2^-15, a_j - S_j), S_j = 2^15 s_j.
+// dimord holds 2 d words of scratch.
 void launch_rerank_rows8(const float* raw, int64_t n, int d, uint32_t* dimord, float2* dim8,
                          uint8_t* raw8, float2* rmeta, cudaStream_t s);
 

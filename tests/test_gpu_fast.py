@@ -279,7 +279,7 @@ def test_fast_filter_equals_index_without_filtered_rows(mv, rerank):
 @pytest.mark.parametrize("metric", [0, 1])
 @pytest.mark.parametrize("d", [64, 96, 130])
 def test_certified_rerank_prescreen_is_exact(mv, metric, d):
-    """The BF16 prescreen of the rerank (default) must return the bits of the
+    """The 8-bit prescreen of the rerank (default) must return the bits of the
     rerank that computes every shortlisted row in FP32 (rerank_fp32): on
     real-valued rows, on SIFT-like integer rows, with duplicated rows (exact
     ties across the k-th boundary) and with k from 1 to 32."""
@@ -297,6 +297,28 @@ def test_certified_rerank_prescreen_is_exact(mv, metric, d):
     for k, R in ((1, 16), (10, 256), (32, 100)):
         a = g.search(q, k, form=mv.FORM_FAST, nprobe=6, rerank=R)
         b = g.search(q, k, form=mv.FORM_FAST, nprobe=6, rerank=R, rerank_fp32=True)
+        assert np.array_equal(a[1], b[1]), (k, R)
+        assert np.array_equal(a[0].view(np.uint32), b[0].view(np.uint32)), (k, R)
+
+
+@pytest.mark.parametrize("metric", [0, 1])
+def test_certified_rerank_offset_rows(mv, metric):
+    """Rows and queries far from the origin against their spread (4096 plus
+    noise of 1e-3, and a second cluster at -3e5): the 8-bit copy's
+    per-dimension offsets and the per-query constants of the prescreen
+    round, and the certified rerank must still return the full FP32
+    rerank's bits."""
+    rng = np.random.default_rng(39)
+    d = 64
+    base = (4096.0 + 1e-3 * rng.standard_normal((12000, d))).astype(np.float32)
+    base[6000:] = (-3e5 + 0.25 * rng.standard_normal((6000, d))).astype(np.float32)
+    base[100:140] = base[100]  # exact ties
+    q = np.vstack([base[rng.integers(0, 12000, 60)] + 1e-4 * rng.standard_normal((60, d)),
+                   base[100:104]]).astype(np.float32)
+    g = _index(mv, base, d, 32, 8, metric)
+    for k, R in ((1, 32), (10, 128), (32, 64)):
+        a = g.search(q, k, form=mv.FORM_FAST, nprobe=8, rerank=R)
+        b = g.search(q, k, form=mv.FORM_FAST, nprobe=8, rerank=R, rerank_fp32=True)
         assert np.array_equal(a[1], b[1]), (k, R)
         assert np.array_equal(a[0].view(np.uint32), b[0].view(np.uint32)), (k, R)
 
