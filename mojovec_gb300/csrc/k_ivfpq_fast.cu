@@ -227,17 +227,43 @@ __device__ void coarse_recheck_warp(uint64_t* B, int64_t row, const float* __res
       if (key != KEY_NONE && !ok[u] && lane == 0) atomicExch(err, 106);
       acc[u] = 0.0f;
     }
-    for (int j = lane; j < d; j += 32) {
-      const float qj = qr[j];
+    if (d <= 128) {
+      // every element of the round loaded before any is summed (one load
+      // latency per round); the sums run in the same order as below
+      float qv[4], cv[CU][4];
 #pragma unroll
-      for (int u = 0; u < CU; ++u) {
-        if (!ok[u]) continue;
-        const float v = cent[(int64_t)list[u] * d + j];
-        if (metric == MV_METRIC_L2) {
-          const float df = qj - v;
-          acc[u] = fmaf(df, df, acc[u]);
-        } else {
-          acc[u] = fmaf(qj, v, acc[u]);
+      for (int jj = 0; jj < 4; ++jj) {
+        const int j = lane + 32 * jj;
+        qv[jj] = j < d ? qr[j] : 0.0f;
+#pragma unroll
+        for (int u = 0; u < CU; ++u) cv[u][jj] = ok[u] && j < d ? cent[(int64_t)list[u] * d + j] : 0.0f;
+      }
+#pragma unroll
+      for (int jj = 0; jj < 4; ++jj) {
+        if (lane + 32 * jj >= d) break;
+#pragma unroll
+        for (int u = 0; u < CU; ++u) {
+          if (metric == MV_METRIC_L2) {
+            const float df = qv[jj] - cv[u][jj];
+            acc[u] = fmaf(df, df, acc[u]);
+          } else {
+            acc[u] = fmaf(qv[jj], cv[u][jj], acc[u]);
+          }
+        }
+      }
+    } else {
+      for (int j = lane; j < d; j += 32) {
+        const float qj = qr[j];
+#pragma unroll
+        for (int u = 0; u < CU; ++u) {
+          if (!ok[u]) continue;
+          const float v = cent[(int64_t)list[u] * d + j];
+          if (metric == MV_METRIC_L2) {
+            const float df = qj - v;
+            acc[u] = fmaf(df, df, acc[u]);
+          } else {
+            acc[u] = fmaf(qj, v, acc[u]);
+          }
         }
       }
     }
