@@ -84,7 +84,11 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
     return;
   }
   uint32_t* drow = dist + row * smax;
-  int p = 0;  // per-thread probe cursor (candidate indices only grow)
+  // per-thread probe cursor (candidate indices only grow) with the probe's
+  // end, CSR base (offset - first index) and term kept in registers
+  int p = 0, pend = pbeg[1];
+  int64_t pbase = poff[0];  // pbeg[0] = 0
+  float pt = pterm[0];
   // CPT candidates per thread per step: every row's loads are issued before
   // any table walk.
   for (int j0 = 0; j0 < total; j0 += CPT * NT) {
@@ -98,10 +102,16 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
       has[u] = c < total;
       // Lanes without a candidate keep their cursor and use position 0 (a
       // valid entry: the index is not empty), so no load leaves the lists.
-      if (has[u])
-        while (pbeg[p + 1] <= c) ++p;
-      pos[u] = has[u] ? poff[p] + (c - pbeg[p]) : 0;
-      t[u] = has[u] ? pterm[p] : 0.0f;
+      if (has[u] && c >= pend) {  // c < pbeg[nprobe]: p stops below nprobe
+        do {
+          ++p;
+        } while (pbeg[p + 1] <= c);
+        pend = pbeg[p + 1];
+        pbase = poff[p] - pbeg[p];
+        pt = pterm[p];
+      }
+      pos[u] = has[u] ? pbase + c : 0;
+      t[u] = has[u] ? pt : 0.0f;
       keep[u] = has[u];
       bad = bad || (has[u] && (pos[u] < 0 || pos[u] >= a.ntotal));
     }
