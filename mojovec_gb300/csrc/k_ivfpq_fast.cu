@@ -772,7 +772,15 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ivfpq_scan_fast(FastScanArgs 
   const int total = pbeg[nprobe];
   const int chunk = a.cap - a.R;
   int m = 0;
-  int p = 0;  // per-thread probe cursor (candidate indices only grow)
+  // Per-thread probe cursors of the thread's first and second candidates
+  // (each one's indices only grow), with the probe's end, CSR base (offset
+  // - first index) and term kept in registers.
+  int p = 0, pend = pbeg[1];
+  int64_t pbase = poff[0];  // pbeg[0] = 0
+  float pt = pterm[0];
+  int p1 = 0, pend1 = pend;
+  int64_t pbase1 = pbase;
+  float pt1 = pt;
   // Keys at or above `bound` cannot enter the shortlist once R keys below
   // it have been seen; it tightens after every intermediate select.
   unsigned long long bound = ~0ull;
@@ -799,15 +807,26 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ivfpq_scan_fast(FastScanArgs 
       const int c0 = base + j, c1 = c0 + FT;
       // Lanes without a candidate keep their cursor and use position 0 (a
       // valid entry: the index is not empty), so no load leaves the lists.
-      if (has0)
-        while (pbeg[p + 1] <= c0) ++p;
-      int64_t pos0c = has0 ? poff[p] + (c0 - pbeg[p]) : 0;
-      const float t0 = has0 ? pterm[p] : 0.0f;
-      int p1 = p;
-      if (has1)
-        while (pbeg[p1 + 1] <= c1) ++p1;
-      int64_t pos1 = has1 ? poff[p1] + (c1 - pbeg[p1]) : 0;
-      const float t1 = has1 ? pterm[p1] : 0.0f;
+      if (has0 && c0 >= pend) {  // c0 < pbeg[nprobe]: p stops below nprobe
+        do {
+          ++p;
+        } while (pbeg[p + 1] <= c0);
+        pend = pbeg[p + 1];
+        pbase = poff[p] - pbeg[p];
+        pt = pterm[p];
+      }
+      int64_t pos0c = has0 ? pbase + c0 : 0;
+      const float t0 = has0 ? pt : 0.0f;
+      if (has1 && c1 >= pend1) {
+        do {
+          ++p1;
+        } while (pbeg[p1 + 1] <= c1);
+        pend1 = pbeg[p1 + 1];
+        pbase1 = poff[p1] - pbeg[p1];
+        pt1 = pterm[p1];
+      }
+      int64_t pos1 = has1 ? pbase1 + c1 : 0;
+      const float t1 = has1 ? pt1 : 0.0f;
       bool keep0 = has0, keep1 = has1;
       if ((has0 && (pos0c < 0 || pos0c >= a.ntotal)) || (has1 && (pos1 < 0 || pos1 >= a.ntotal))) {
         atomicExch(a.err, 104);  // never expected: skip both, stay warp-uniform
@@ -864,7 +883,6 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_ivfpq_scan_fast(FastScanArgs 
         khi[slot] = (uint32_t)(k1 >> 32);
         klo[slot] = (uint32_t)k1;
       }
-      if (has0) p = p1;
     }
     __syncthreads();
     m = s_fill;
