@@ -128,7 +128,8 @@ int32_t mv_ctx_set_wait_limit(mv_ctx* ctx, int64_t cycles);
 #define MV_STAGE_FLAT 5     /* Flat / SQ8 distance tiles */
 #define MV_STAGE_ENCODE 6   /* residuals + PQ codes of added rows */
 #define MV_STAGE_APPEND 7   /* list append: CSR layout + scatter */
-#define MV_STAGE_COUNT 8
+#define MV_STAGE_ADC 8      /* table + ADC kernel of the two-kernel fast scan (inside SCAN) */
+#define MV_STAGE_COUNT 9
 int32_t mv_ctx_profile(mv_ctx* ctx, int32_t enable);
 /* Plain-form selections run on the tensor cores with an exact FP32 recheck
  * and an error bound that proves the result equals the exact scan's;

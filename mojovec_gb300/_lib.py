@@ -28,7 +28,7 @@ METRIC_IP = 1
 FORM_PLAIN = 0
 FORM_FAST = 1
 
-STAGES = ("coarse", "select", "scan", "lut", "rerank", "flat", "encode", "append")
+STAGES = ("coarse", "select", "scan", "lut", "rerank", "flat", "encode", "append", "adc")
 
 _ERR_NAMES = {
     MV_ERR_ARG: "MV_ERR_ARG",

@@ -585,7 +585,8 @@ size_t ivfpq_rows_smem(int M, int d, int nprobe) {
 
 int64_t ivfpq_rows_stride(int64_t smax) { return std::max<int64_t>(4, (smax + 3) & ~int64_t(3)); }
 
-void launch_ivfpq_scan_rows(FastScanArgs f, uint32_t* dist, int64_t smax, cudaStream_t s, int nt) {
+void launch_ivfpq_scan_rows(FastScanArgs f, uint32_t* dist, int64_t smax, cudaStream_t s, int nt,
+                            mv_ctx* prof) {
   const int64_t nq = f.nq;
   if (nq == 0) return;
   const int64_t stride = ivfpq_rows_stride(smax);
@@ -593,6 +594,7 @@ void launch_ivfpq_scan_rows(FastScanArgs f, uint32_t* dist, int64_t smax, cudaSt
   MV_REQUIRE(smem <= 200 * 1024, MV_ERR_UNSUPPORTED, "two-kernel ADC scan: M, d or nprobe too large");
   auto go = [&](auto kernel, int threads) {
     smem_limit(kernel, smem);
+    StageTimer t(prof, MV_STAGE_ADC, s);
     kernel<<<(unsigned)nq, threads, smem, s>>>(f, dist, stride);
   };
   if (nt == 64) go(k_ivfpq_rows<64, 2>, 64);

@@ -949,7 +949,7 @@ void ivfpq_search_fast(mv_ivfpq* ix, const float* d_x, int64_t nq, int k, int np
         a.nprobe_q = batch ? batch->nprobe_q : nullptr;
         // 128 threads per query (eight queries per SM) measured 0.309 ms
         // for the scan stage at 1M x 128, nprobe 8; 256: 0.326, 512: 0.381
-        launch_ivfpq_scan_rows(a, drows, smax, s, batch ? batch->scan_threads : 128);
+        launch_ivfpq_scan_rows(a, drows, smax, s, batch ? batch->scan_threads : 128, ix->ctx);
       } else if (batch) {
         a.nprobe_q = batch->nprobe_q;
         a.order = batch->order;

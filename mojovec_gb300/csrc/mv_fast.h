@@ -8,6 +8,8 @@
 
 #include <cstdint>
 
+struct mv_ctx;  // the C interface's context (stage profiler)
+
 namespace mv {
 
 struct FastScanArgs {
@@ -60,7 +62,9 @@ void launch_ivfpq_scan_rt(FastScanArgs a, cudaStream_t s, int nt, int persistent
 // smax bounds every query's candidate count (the nprobe longest lists); the
 // rows take nq * ivfpq_rows_stride(smax) words of scratch.
 int64_t ivfpq_rows_stride(int64_t smax);
-void launch_ivfpq_scan_rows(FastScanArgs f, uint32_t* dist, int64_t smax, cudaStream_t s, int nt);
+// prof: context whose stage profiler times the ADC kernel alone (MV_STAGE_ADC), or null.
+void launch_ivfpq_scan_rows(FastScanArgs f, uint32_t* dist, int64_t smax, cudaStream_t s, int nt,
+                            mv_ctx* prof = nullptr);
 
 struct RerankArgs {
   const float* q;
