@@ -1074,34 +1074,6 @@ __host__ __device__ constexpr size_t rerank_cert_warp_bytes(int d, int R, int RC
           (size_t)R * 20 + 15) & ~size_t(15);
 }
 
-// The k-th smallest (1 <= k <= 64) of the warp's 64 values v0, v1 (value
-// r * 32 + lane in v_r): bitonic sort of the 64, then position k - 1.
-__device__ __forceinline__ uint32_t warp_kth_smallest64(uint32_t v0, uint32_t v1, int k) {
-  const int lane = threadIdx.x & 31;
-  uint32_t v[2] = {v0, v1};
-#pragma unroll
-  for (int size = 2; size <= 64; size <<= 1) {
-#pragma unroll
-    for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      if (stride == 32) {  // size 64, ascending: the pair is (v0, v1) of one lane
-        const uint32_t lo = min(v[0], v[1]), hi = max(v[0], v[1]);
-        v[0] = lo;
-        v[1] = hi;
-      } else {
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-          const int e = r * 32 + lane;
-          const uint32_t o = __shfl_xor_sync(0xffffffffu, v[r], stride);
-          const bool asc = (e & size) == 0, lower = (e & stride) == 0;
-          v[r] = lower == asc ? min(v[r], o) : max(v[r], o);
-        }
-      }
-    }
-  }
-  const int pos = k - 1;
-  return __shfl_sync(0xffffffffu, pos < 32 ? v[0] : v[1], pos & 31);
-}
-
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }

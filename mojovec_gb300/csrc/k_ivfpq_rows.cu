@@ -79,11 +79,12 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
   else build_lut<NT>([&](int i, float v) { lut[i] = v; }, qv, a.pq, M, dsub, scale);
   __syncthreads();
   const int total = pbeg[nprobe];
-  if (total > smax) {  // never expected: smax bounds every query's candidates
+  if (total > smax - 1) {  // never expected: smax - 1 bounds every query's candidates
     if (tid == 0) atomicExch(a.err, 106);
     return;
   }
   uint32_t* drow = dist + row * smax;
+  uint32_t m1 = 0xffffffffu, m2 = 0xffffffffu;  // the thread's two smallest kept words
   // per-thread probe cursor (candidate indices only grow) with the probe's
   // end, CSR base (offset - first index) and term kept in registers
   int p = 0, pend = pbeg[1];
@@ -137,9 +138,29 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
     for (int u = 0; u < CPT; ++u) {
       const float dd = adc_fast(lut, a.codes + pos[u] * M, M, t[u] + v[u]);
       // ROW_EXCLUDED marks no key: a NaN distance keeps the word below it
-      if (has[u]) drow[j0 + tid + u * NT] = keep[u] ? min(float_to_ordered(dd), ROW_EXCLUDED - 1u)
-                                                   : ROW_EXCLUDED;
+      const uint32_t wd = keep[u] ? min(float_to_ordered(dd), ROW_EXCLUDED - 1u) : ROW_EXCLUDED;
+      if (has[u]) drow[j0 + tid + u * NT] = wd;
+      const uint32_t x = has[u] ? wd : 0xffffffffu;
+      m2 = min(m2, max(m1, x));
+      m1 = min(m1, x);
     }
+  }
+  // Starting bound for the select, in the row's last word: each warp's kw-th
+  // smallest of its threads' two smallest words, kw = ceil(R / warps), and
+  // the largest of those. NW * kw >= R distinct candidates have words at or
+  // below it, so the R-th smallest word is too; 0xffffffff (no bound) when
+  // kw > 64 or a warp lacks kw kept candidates.
+  constexpr int NW = NT / 32;
+  __shared__ uint32_t wb[NW];
+  const int kw = (a.R + NW - 1) / NW;
+  const uint32_t b = kw >= 1 && kw <= 64 ? warp_kth_smallest64(m1, m2, kw) : 0xffffffffu;
+  if (lane == 0) wb[tid >> 5] = b;
+  __syncthreads();
+  if (tid == 0) {
+    uint32_t tmax = 0u;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) tmax = max(tmax, wb[w]);
+    drow[smax - 1] = tmax;
   }
 }
 
@@ -512,12 +533,14 @@ __global__ void __launch_bounds__(SS_WARPS * 32) k_row_select_stream(SelArgs a) 
   }
   if (lane == 0) pbeg[np] = carry;
   __syncwarp();
-  const int n = carry <= a.smax ? carry : 0;  // a row over smax was left unwritten (site 106)
+  const int n = carry <= a.smax - 1 ? carry : 0;  // a row over smax - 1 was left unwritten (106)
   const uint32_t* src = a.dist + row * a.smax;  // smax is a multiple of 4: 16-byte rows
   const int R = a.R;
   const unsigned lt = (1u << lane) - 1u;
   uint64_t T = KEY_NONE;
-  uint32_t Tw = 0xffffffffu;  // T's distance word
+  // T's distance word; it starts at the rows kernel's bound on the R-th
+  // smallest word (the row's last word)
+  uint32_t Tw = n > 0 ? __ldg(src + a.smax - 1) : 0xffffffffu;
   int m = 0, p = 0;           // p: probe cursor, advanced only for words that may enter
   // words i0 + 4 lane .. + 3 of each 128-word round (the row holds smax
   // >= roundup(n, 4) words, so the vector load stays in the row)
@@ -583,7 +606,9 @@ size_t ivfpq_rows_smem(int M, int d, int nprobe) {
          (size_t)(nprobe + 1) * 4 + (size_t)nprobe * 4;
 }
 
-int64_t ivfpq_rows_stride(int64_t smax) { return std::max<int64_t>(4, (smax + 3) & ~int64_t(3)); }
+// A row holds smax candidate words and, in its last word, the select's
+// starting bound (16-byte aligned rows).
+int64_t ivfpq_rows_stride(int64_t smax) { return std::max<int64_t>(4, (smax + 4) & ~int64_t(3)); }
 
 void launch_ivfpq_scan_rows(FastScanArgs f, uint32_t* dist, int64_t smax, cudaStream_t s, int nt,
                             mv_ctx* prof) {
