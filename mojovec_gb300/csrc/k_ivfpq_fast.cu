@@ -1139,13 +1139,25 @@ __global__ void __launch_bounds__(128, RC_ROWS == 32 ? 4 : 6) k_rerank_cert(Rera
   auto issue = [&](int t) {
     if (t < nrounds) {
       const uint32_t dst0 = (uint32_t)__cvta_generic_to_shared(ring + (size_t)(t & 1) * rbytes);
-      for (int e = lane; e < RC_ROWS * chunks; e += 32) {
-        // (row, piece) of copy e: shifts when the piece count is a power of two
-        const int u = pow2c ? e >> csh : e / chunks, ch = e - u * chunks;
-        const int c = t * RC_ROWS + u;
-        const uint32_t p = c < a.R ? spos[c] : 0xffffffffu;
-        if (p != 0xffffffffu)
-          cp_async16(dst0 + (uint32_t)(u * d8 + ch * 16), a.raw8 + (int64_t)p * d8 + ch * 16);
+      if (chunks == 8) {  // 128-byte rows: the lane copies piece lane % 8 of rows lane / 8 + 4 i
+        const int ch = lane & 7;
+#pragma unroll
+        for (int i = 0; i < RC_ROWS / 4; ++i) {
+          const int u = (lane >> 3) + 4 * i;
+          const int c = t * RC_ROWS + u;
+          const uint32_t p = c < a.R ? spos[c] : 0xffffffffu;
+          if (p != 0xffffffffu)
+            cp_async16(dst0 + (uint32_t)(u * 128 + ch * 16), a.raw8 + (int64_t)p * 128 + ch * 16);
+        }
+      } else {
+        for (int e = lane; e < RC_ROWS * chunks; e += 32) {
+          // (row, piece) of copy e: shifts when the piece count is a power of two
+          const int u = pow2c ? e >> csh : e / chunks, ch = e - u * chunks;
+          const int c = t * RC_ROWS + u;
+          const uint32_t p = c < a.R ? spos[c] : 0xffffffffu;
+          if (p != 0xffffffffu)
+            cp_async16(dst0 + (uint32_t)(u * d8 + ch * 16), a.raw8 + (int64_t)p * d8 + ch * 16);
+        }
       }
     }
     cp_async_commit();  // one group per round, empty or not
