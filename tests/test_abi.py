@@ -36,6 +36,18 @@ def test_binding_covers_header():
     assert sorted(_lib.SIGNATURES) == _declared()
 
 
+def test_stage_names_follow_header_stage_ids():
+    """The binding's stage names index mv_ctx_stage_times' arrays, so their
+    order must be the header's MV_STAGE_* ids."""
+    from mojovec_gb300 import _lib
+
+    text = open(os.path.join(ROOT, "include", "mojovec_gpu.h")).read()
+    ids = {name.lower(): int(v) for name, v in re.findall(r"#define MV_STAGE_([A-Z]+) (\d+)", text)}
+    count = ids.pop("count")
+    assert count == len(_lib.STAGES) == len(ids)
+    assert all(ids[name] == i for i, name in enumerate(_lib.STAGES))
+
+
 def test_version_and_error_without_gpu(mv):
     from mojovec_gb300 import _lib
 
