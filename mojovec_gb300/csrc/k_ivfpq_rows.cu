@@ -86,10 +86,13 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
   uint32_t* drow = dist + row * smax;
   uint32_t m1 = 0xffffffffu, m2 = 0xffffffffu;  // the thread's two smallest kept words
   // per-thread probe cursor (candidate indices only grow) with the probe's
-  // end, CSR base (offset - first index) and term kept in registers
+  // end, CSR base (offset - first index) and term kept in registers, and
+  // whether the probe's CSR range lies in the index (then so does every
+  // candidate position of it)
   int p = 0, pend = pbeg[1];
   int64_t pbase = poff[0];  // pbeg[0] = 0
   float pt = pterm[0];
+  bool pok = poff[0] >= 0 && poff[0] + pend <= a.ntotal;
   // CPT candidates per thread per step: every row's loads are issued before
   // any table walk.
   for (int j0 = 0; j0 < total; j0 += CPT * NT) {
@@ -110,11 +113,12 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
         pend = pbeg[p + 1];
         pbase = poff[p] - pbeg[p];
         pt = pterm[p];
+        pok = poff[p] >= 0 && poff[p] + (pend - pbeg[p]) <= a.ntotal;
       }
       pos[u] = has[u] ? pbase + c : 0;
       t[u] = has[u] ? pt : 0.0f;
       keep[u] = has[u];
-      bad = bad || (has[u] && (pos[u] < 0 || pos[u] >= a.ntotal));
+      bad = bad || (has[u] && !pok);
     }
     if (bad) {
       atomicExch(a.err, 109);  // never expected: skip the step, stay warp-uniform
