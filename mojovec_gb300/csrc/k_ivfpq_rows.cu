@@ -7,11 +7,12 @@
 // lists laid end to end and writes every candidate's distance as an
 // order-preserving word into the query's row of a distance matrix (word i
 // is candidate i; ROW_EXCLUDED marks a row the exclusion filter names,
-// index_ivf_pq.mojo:328-334). There is no staging area, compaction or
-// barrier after the table build.
+// index_ivf_pq.mojo:328-334). There is no staging area or compaction; the
+// row's last word gets a bound on the R-th smallest word (from each
+// thread's two smallest), the select's starting bound.
 // k_row_select_stream (one warp per query, shortlists up to 256) streams
-// its row once, staging keys below a running bound and keeping the R
-// smallest whenever its staging area could overflow; k_row_select_wide
+// its row once from that bound, staging keys below a running bound and
+// keeping the R smallest whenever its staging area could overflow; k_row_select_wide
 // (longer shortlists) narrows the key range of the R-th key with 256-bin
 // histogram passes. Keys are (distance word, CSR position), the same keys
 // the single-kernel scan selects from, so both return the same shortlist.
@@ -496,12 +497,13 @@ __device__ uint64_t warp_keep_smallest(uint64_t* buf, int m, int R, uint64_t* si
 }
 
 // One warp per query, one pass over its distance row (16-byte loads, three
-// rounds ahead of the keys being built): keys below
-// the running bound T are staged in shared memory; when the staging area
-// could overflow, the R smallest are kept and T becomes the largest of
-// them (a later key at or above T cannot be among the R smallest). The
-// kept set is the R smallest keys whatever the order of arrival; it is
-// written unsorted, in a fixed order.
+// rounds ahead of the keys being built): keys below the running bound T
+// (whose word starts at the rows kernel's bound on the R-th smallest word)
+// are staged in shared memory; when the staging area could overflow, the R
+// smallest are kept and T becomes the largest of them (a later key at or
+// above T cannot be among the R smallest). The kept set is the R smallest
+// keys whatever the order of arrival; it is written unsorted, in a fixed
+// order.
 __global__ void __launch_bounds__(SS_WARPS * 32) k_row_select_stream(SelArgs a) {
   extern __shared__ __align__(16) uint8_t smraw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
