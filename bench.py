@@ -681,7 +681,7 @@ def run_flat(args, rank, world):
     if rank == 0 and not args.no_cpu and sq8:
         from oracle import oracle as orc
 
-        sample = min(args.cpu_sample // 10, nq)
+        sample = min(args.cpu_sample // 100, nq)
         threads = os.cpu_count() or 1
         ref = orc.SQ8(dim, metric)
         ref.add(base)
@@ -697,7 +697,7 @@ def run_flat(args, rank, world):
     elif rank == 0 and not args.no_cpu:
         from oracle import oracle as orc
 
-        sample = min(args.cpu_sample // 10, nq)
+        sample = min(args.cpu_sample // 100, nq)
         threads = os.cpu_count() or 1
         orc.flat_search(base, queries[:4], k, metric=metric, nthreads=threads)
         t0 = time.perf_counter()
@@ -1546,7 +1546,7 @@ def run_reference_flat(args):
     threads = os.cpu_count() or 1
     base, queries = build_workload(args.nb, args.nq, args.dim)
     metric = 0 if args.metric == "l2" else 1
-    sample = min(max(args.cpu_sample // 10, 1), args.nq)
+    sample = min(max(args.cpu_sample // 100, 1), args.nq)
     q = queries[:sample]
     if args.workload == "sq8":
         ref = orc.SQ8(args.dim, metric)
@@ -1596,7 +1596,7 @@ def main():
                     help="shortlist depth (IVF-PQ default 256, flat default k * 4)")
     ap.add_argument("--nb", type=int, default=NB, help="base rows (profiling runs use fewer)")
     ap.add_argument("--nq", type=int, default=NQ, help="queries per step")
-    ap.add_argument("--cpu-sample", type=int, default=500)
+    ap.add_argument("--cpu-sample", type=int, default=10000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="ivfpq",
                     choices=["ivfpq", "flat", "sq8", "kmeans", "batch", "serve", "curve", "ivfflat",
